@@ -1,0 +1,196 @@
+/*
+ * seidart_gpu.h -- C ABI of the GB300 (sm_103a) CPML-FDTD solvers.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (SEIDART_OK = 0, negative SEIDART_ERR_* on failure;
+ * seidart_last_error() gives the message of the calling thread's last error).
+ *
+ * Grid layout everywhere: Fortran column-major on the PADDED grid, x fastest:
+ *   2D / 2.5D : a(i,k)   -> a[i + nx*k]              (0-based i < nx, k < nz)
+ *   3D        : a(i,j,k) -> a[i + nx*(j + ny*k)]
+ * Padded means n = n_interior + 2*cpml, exactly as the reference pads the grid
+ * before calling a solver (src/fortran/main.f08:69-71).  Complex (2.5D) arrays
+ * are interleaved (re, im) doubles, the memory layout of Fortran complex(real64).
+ *
+ * Reference interfaces these calls replace:
+ *   seismic2      src/fortran/cpmlfdtd.f08:57-597    (subroutine seismic2)
+ *   seismic25     src/fortran/cpmlfdtd.f08:600-1337  (subroutine seismic25)
+ *   seismic3      src/fortran/cpmlfdtd.f08:1341-2313 (subroutine seismic3)
+ *   electromag2   src/fortran/cpmlfdtd.f08:2317-2760 (subroutine electromag2)
+ *   electromag25  src/fortran/cpmlfdtd.f08:2764-3350 (subroutine electromag25)
+ *   legacy names  legacy/cpmlfdtd_wrapper.c:7-16     (seismic2_ ... electromag25c_)
+ */
+#ifndef SEIDART_GPU_H
+#define SEIDART_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define SEIDART_OK               0
+#define SEIDART_ERR_ARG         -1  /* bad argument (sizes, indices, NULL)        */
+#define SEIDART_ERR_CUDA        -2  /* CUDA runtime error                         */
+#define SEIDART_ERR_UNSTABLE    -3  /* max |v| exceeded 1e25 (reference: stop)    */
+#define SEIDART_ERR_IO          -4  /* file contract: missing / malformed record  */
+#define SEIDART_ERR_NOMEM       -5  /* device allocation failed                   */
+#define SEIDART_ERR_TIMEOUT     -6  /* a bounded device wait gave up              */
+#define SEIDART_ERR_UNSUPPORTED -7  /* e.g. plane-wave source, missing GPU        */
+
+/* ------------------------------------------------------- solver families */
+#define SEIDART_SEISMIC2      1
+#define SEIDART_SEISMIC25     2
+#define SEIDART_SEISMIC3      3
+#define SEIDART_ELECTROMAG2   4
+#define SEIDART_ELECTROMAG25  5
+
+/* precision of the field arrays and stencil arithmetic */
+#define SEIDART_FP64 0   /* drop-in path: same operation order as the reference */
+#define SEIDART_FP32 1   /* fast path: FP32 fields, FP64 set-up of coefficients */
+
+/* density face averaging, src/fortran/averaging.f08:5-25 (scalar_mean codes) */
+#define SEIDART_DENSITY_HARMONIC   1
+#define SEIDART_DENSITY_GEOMETRIC  2
+#define SEIDART_DENSITY_ARITHMETIC 3
+#define SEIDART_DENSITY_NONE       4
+
+/* Domain_Type (src/fortran/seidart_types.f08:13-20); nx/ny/nz already padded. */
+typedef struct SeidartDomain {
+    double dim;            /* 2, 2.5 or 3 */
+    int nx, ny, nz;        /* padded sizes; ny is ignored in 2D/2.5D */
+    double dx, dy, dz;
+    int cpml;              /* CPML thickness in cells */
+} SeidartDomain;
+
+/* Source_Type (src/fortran/seidart_types.f08:23-33), point sources only. */
+typedef struct SeidartSource {
+    double dt;
+    int time_steps;        /* length of every source time series */
+    int xind, yind, zind;  /* interior indices; source cell = ind + cpml (1-based) */
+    double ky;             /* 2.5D wavenumber (reference reads env KY) */
+} SeidartSource;
+
+/* ---------------------------------------------------------- array slots
+ * Host arrays are passed as `const double* const* arrays` in these orders.
+ * Model arrays are read-only grids; source series have time_steps entries
+ * (NULL = all zeros); field / memory arrays are grids of state.              */
+
+/* C_ij order shared by seismic25 / seismic3 */
+enum { SEIDART_C11, SEIDART_C12, SEIDART_C13, SEIDART_C14, SEIDART_C15, SEIDART_C16,
+       SEIDART_C22, SEIDART_C23, SEIDART_C24, SEIDART_C25, SEIDART_C26,
+       SEIDART_C33, SEIDART_C34, SEIDART_C35, SEIDART_C36,
+       SEIDART_C44, SEIDART_C45, SEIDART_C46, SEIDART_C55, SEIDART_C56, SEIDART_C66,
+       SEIDART_RHO3,                                   /* 21 */
+       SEIDART_GX3, SEIDART_GY3, SEIDART_GZ3,          /* gamma_x, gamma_y, gamma_z    */
+       SEIDART_GXY3, SEIDART_GYZ3, SEIDART_GXZ3,       /* gamma_xy, gamma_yz, gamma_xz */
+       SEIDART_KAPPA3, SEIDART_KAPPAH3, SEIDART_ACOEF3, SEIDART_ACOEFH3,
+       SEIDART_BCOEF3, SEIDART_BCOEFH3,
+       SEIDART_NMODEL3 };                              /* 34 */
+
+/* seismic2 model (src/fortran/cpmlfdtd.f08:159-174, :253-261) */
+enum { S2_C11, S2_C13, S2_C15, S2_C33, S2_C35, S2_C55, S2_RHO,
+       S2_GX, S2_GZ, S2_GXZ,
+       S2_KAPPA, S2_KAPPAH, S2_ACOEF, S2_ACOEFH, S2_BCOEF, S2_BCOEFH,
+       S2_NMODEL };                                    /* 16 */
+enum { S2_SRCX, S2_SRCZ, S2_SRCXX, S2_SRCXZ, S2_SRCZZ, S2_NSRC };
+enum { S2_VX, S2_VZ, S2_SXX, S2_SZZ, S2_SXZ, S2_NFIELD };
+enum { S2_M_DVX_DX1, S2_M_DVX_DZ1, S2_M_DVZ_DX1, S2_M_DVZ_DZ1,
+       S2_M_DVX_DX2, S2_M_DVX_DZ2, S2_M_DVZ_DX2, S2_M_DVZ_DZ2,
+       S2_M_DSXX_DX, S2_M_DSZZ_DZ, S2_M_DSXZ_DX, S2_M_DSXZ_DZ, S2_NMEM };
+
+/* seismic25 / seismic3 sources and fields */
+enum { S3_SRCX, S3_SRCY, S3_SRCZ, S3_SRCXX, S3_SRCXY, S3_SRCXZ,
+       S3_SRCYY, S3_SRCYZ, S3_SRCZZ, S3_NSRC };
+enum { S3_VX, S3_VY, S3_VZ, S3_SXX, S3_SXY, S3_SXZ, S3_SYY, S3_SYZ, S3_SZZ, S3_NFIELD };
+/* seismic25 memories: 4 stress loops x {dvx,dvy,dvz} x {dx,dz}, then 6 velocity
+ * memories (src/fortran/cpmlfdtd.f08:650-664).  Loop L (1..4) occupies slots
+ * 6*(L-1) + {dvx_dx, dvy_dx, dvz_dx, dvx_dz, dvy_dz, dvz_dz}.               */
+enum { S25_M_DSXX_DX = 24, S25_M_DSXZ_DZ, S25_M_DSXY_DX, S25_M_DSYZ_DZ,
+       S25_M_DSXZ_DX, S25_M_DSZZ_DZ, S25_NMEM };       /* 30 complex */
+/* seismic3 memories: 4 stress loops x 9 (dvx_dx,dvx_dy,dvx_dz, dvy_dx,..,dvz_dz)
+ * at slot 9*(L-1) + 3*comp + dir, then 9 velocity memories.                 */
+enum { S3_M_DSXX_DX = 36, S3_M_DSYY_DY, S3_M_DSZZ_DZ, S3_M_DSXY_DX, S3_M_DSXY_DY,
+       S3_M_DSXZ_DX, S3_M_DSXZ_DZ, S3_M_DSYZ_DY, S3_M_DSYZ_DZ, S3_NMEM };  /* 45 */
+
+/* electromag2 (src/fortran/cpmlfdtd.f08:2409-2414, :2484-2491) */
+enum { E2_E11, E2_E13, E2_E33, E2_S11, E2_S13, E2_S33,
+       E2_KAPPA, E2_KAPPAH, E2_ACOEF, E2_ACOEFH, E2_BCOEF, E2_BCOEFH, E2_NMODEL };
+enum { E2_SRCX, E2_SRCZ, E2_NSRC };
+enum { E2_EX, E2_EZ, E2_HY, E2_NFIELD };
+enum { E2_M_DEX_DZ, E2_M_DEZ_DX, E2_M_DHY_DX, E2_M_DHY_DZ, E2_NMEM };
+
+/* electromag25 (src/fortran/cpmlfdtd.f08:2886-2900) */
+enum { E25_E11, E25_E12, E25_E13, E25_E22, E25_E23, E25_E33,
+       E25_S11, E25_S12, E25_S13, E25_S22, E25_S23, E25_S33,
+       E25_KAPPA, E25_KAPPAH, E25_ACOEF, E25_ACOEFH, E25_BCOEF, E25_BCOEFH,
+       E25_NMODEL };
+enum { E25_SRCX, E25_SRCY, E25_SRCZ, E25_NSRC };
+enum { E25_EX, E25_EY, E25_EZ, E25_HX, E25_HY, E25_HZ, E25_NFIELD };
+enum { E25_M_DEY_DX, E25_M_DEY_DZ, E25_M_DEX_DZ, E25_M_DEZ_DX,
+       E25_M_DHZ_DX, E25_M_DHX_DZ, E25_M_DHY_DZ, E25_M_DHY_DX, E25_NMEM };
+
+/* Number of slots of each kind for a solver family; *is_complex = 1 for 2.5D.
+ * *nrec_comp = number of receiver components recorded per receiver and step. */
+int seidart_layout(int family, int* nmodel, int* nsrc, int* nfield, int* nmem,
+                   int* is_complex, int* nrec_comp);
+
+/* ------------------------------------------------------- one-call runs
+ * Run `src->time_steps` steps of a solver from the given initial fields, all
+ * buffers on the HOST (copies are done inside).  Mirrors one call of the
+ * reference subroutine, minus its file I/O:
+ *   fields  in: initial fields (velocity / E initial conditions, the rest
+ *               usually zero);  out: fields after the last step.
+ *   rec_cells   nrec 0-based linear cell indices (may be 0 / NULL).
+ *   traces      out, [time_steps][nrec_comp][nrec] doubles (complex: 2x).
+ *   norms       out, [time_steps] max-norm series (3D: [2][time_steps],
+ *               velocity then stress norm), may be NULL.
+ * Returns SEIDART_ERR_UNSTABLE when the norm exceeds 1e25 (the step is
+ * reported by seidart_last_error()), as the reference's `stop` does.        */
+int seidart_run(int family, int precision, const SeidartDomain* dom,
+                const SeidartSource* src, int density_code,
+                const double* const* model, const double* const* srcfn,
+                double* const* fields, int nrec, const int* rec_cells,
+                double* traces, double* norms);
+
+/* ------------------------------------------------------- solver handles
+ * A handle owns the device copy of one model and its state on one CUDA
+ * stream; steps are asynchronous on that stream.                           */
+typedef struct SeidartSolver SeidartSolver;
+
+int seidart_solver_create(SeidartSolver** out, int family, int precision,
+                          const SeidartDomain* dom, const SeidartSource* src,
+                          int density_code, const double* const* model,
+                          const double* const* srcfn, int nrec,
+                          const int* rec_cells);
+/* Use a caller-owned cudaStream_t (passed as void*; NULL = the handle's own). */
+int seidart_solver_set_stream(SeidartSolver* s, void* stream);
+int seidart_solver_set_fields(SeidartSolver* s, const double* const* fields);
+int seidart_solver_get_fields(SeidartSolver* s, double* const* fields);
+/* CPML memory variables expanded to full grids (zeros where not stored). */
+int seidart_solver_get_memory(SeidartSolver* s, double* const* mem);
+/* Advance nsteps steps (asynchronous). */
+int seidart_solver_step(SeidartSolver* s, int nsteps);
+/* Wait for the stream; returns SEIDART_ERR_UNSTABLE if any step blew up. */
+int seidart_solver_sync(SeidartSolver* s);
+/* Copy traces / norms of steps [0, steps_done) to the host. */
+int seidart_solver_traces(SeidartSolver* s, double* traces, double* norms);
+int seidart_solver_steps_done(const SeidartSolver* s);
+/* Device pointer of field slot `slot` (FP64 or FP32 per precision). */
+void* seidart_solver_field_ptr(SeidartSolver* s, int slot);
+/* Advance nsteps steps launching kernels one by one (no CUDA graph) with a
+ * CUDA event after each kernel, then wait.  Outputs, per kernel slot k of a
+ * step (at most 8): kernel_ms[k] summed milliseconds, kernel_launches[k]
+ * launches, names + k*names_len its kernel name; *total_ms = elapsed time of
+ * the whole run.  Any output pointer may be NULL. */
+int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, double* kernel_ms,
+                           int* kernel_launches, char* names, int names_len);
+/* Number of kernel launches the last seidart_solver_step call issued. */
+long long seidart_solver_launches(const SeidartSolver* s);
+int seidart_solver_destroy(SeidartSolver* s);
+
+const char* seidart_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEIDART_GPU_H */

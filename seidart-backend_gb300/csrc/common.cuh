@@ -1,0 +1,89 @@
+// common.cuh -- shared device helpers for the CPML-FDTD kernels.
+//
+// Each solver .cu file is compiled twice: with SEIDART_REAL=double and
+// --fmad=false (the drop-in FP64 path, which keeps the reference's expression
+// trees so results are reproducible operation by operation), and with
+// SEIDART_REAL=float and FMA contraction on (the fast FP32 path).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef SEIDART_REAL
+#define SEIDART_REAL double
+#endif
+typedef SEIDART_REAL real;
+
+#define SD_CAT2(a, b) a##b
+#define SD_CAT(a, b) SD_CAT2(a, b)
+#if defined(SEIDART_FP32)
+#define SD_SUFFIX _f32
+#define SD_EXACT 0
+#else
+#define SD_SUFFIX _f64
+#define SD_EXACT 1
+#endif
+// launcher names carry the precision suffix so both builds link into one library
+#define SD_NAME(n) SD_CAT(n, SD_SUFFIX)
+
+// Axis-aligned box [lo, hi) per axis (0-based) inside which the CPML
+// coefficients are inert (acoef = acoef_half = 0, kappa = kappa_half = 1):
+// there the memory variables stay zero and the derivative passes through
+// unchanged, so kernels skip the CPML arithmetic and its memory traffic.
+struct Box {
+    int i0, i1, j0, j1, k0, k1;
+};
+
+__device__ __forceinline__ bool in_box2(const Box& b, int i, int k) {
+    return i >= b.i0 && i < b.i1 && k >= b.k0 && k < b.k1;
+}
+__device__ __forceinline__ bool in_box3(const Box& b, int i, int j, int k) {
+    return i >= b.i0 && i < b.i1 && j >= b.j0 && j < b.j1 && k >= b.k0 && k < b.k1;
+}
+
+// scalar_mean, src/fortran/averaging.f08:5-25 (FP64 path: same operations)
+__device__ __forceinline__ double scalar_mean_d(double a, double b, int code) {
+    switch (code) {
+    case 1: return 2.0 * a * b / (a + b);
+    case 2: return sqrt(a * b);
+    case 3: return 0.5 * (a + b);
+    default: return a;
+    }
+}
+// FP32 path: reciprocal of the face density (buoyancy) directly
+__device__ __forceinline__ float inv_mean_f(float a, float b, int code) {
+    switch (code) {
+    case 1: return __fdividef(a + b, 2.0f * a * b);
+    case 2: return rsqrtf(a * b);
+    case 3: return __fdividef(2.0f, a + b);
+    default: return __frcp_rn(a);
+    }
+}
+
+// Max-norm accumulation: non-negative doubles order like their bit patterns,
+// so an unsigned 64-bit atomicMax gives the exact maximum.  NaN (bit pattern
+// above +inf) also wins, which flags a NaN blow-up as unstable.
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+    atomicMax(reinterpret_cast<unsigned long long*>(addr),
+              static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+// max that lets a NaN win (fmax would drop it)
+__device__ __forceinline__ double nanmax(double a, double b) {
+    return (a != a) ? a : ((b != b) ? b : fmax(a, b));
+}
+
+// Block-wide max of v over NW warps; every thread of the block must call it.
+// The result is valid in warp 0.
+template <int NW>
+__device__ __forceinline__ double block_max(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < NW) ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}

@@ -1,0 +1,136 @@
+// kernels.h -- argument blocks and launchers shared by the solver runtime
+// (solver.cu) and the per-family kernel files.  Each launcher exists twice,
+// suffixed _f64 (drop-in FP64 build) and _f32 (fast FP32 build).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+struct BoxH {
+    int i0, i1, j0, j1, k0, k1;
+};
+
+// Optional callback after each kernel launch of a step (used by the
+// profiling entry point to record CUDA events between kernels).
+struct LaunchHook {
+    void (*fn)(void* ctx, int kernel, const char* name);
+    void* ctx;
+};
+
+// Per-step scalars common to all families.  The 1-based step number lives in
+// device memory (*step) and the last kernel of every step increments it, so
+// one captured CUDA graph of G steps replays from any starting step.
+struct StepInfo {
+    int* step;       // device: 1-based number of the step being computed
+    int nrec;        // receivers
+    const int* rec;  // receiver cell indices (device)
+};
+
+// ------------------------------------------------------------- seismic2
+// model slots follow S2_* of seidart_gpu.h.  In the FP32 build the gamma
+// slots hold 1/(1+gamma dt) and the kappa slots hold 1/kappa.
+template <typename T>
+struct S2Args {
+    int nx, nz, density_code;
+    T dx, dz, dt;
+    BoxH box;
+    const T* m[16];
+    T* f[5];
+    T* mem[12];
+    const double* src[5];  // source series (device, FP64), NULL = zero
+    int isrc, jsrc;        // 0-based source cell
+    int stress_src;        // 1 if any stress-source series is non-zero
+    T* traces;             // [nt][2][nrec]
+    double* norms;         // [nt]
+};
+void launch_seismic2_f64(const S2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic2_f32(const S2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
+// ----------------------------------------------------------- electromag2
+// Derived coefficient arrays (aEx..eEz, eps11*eps0, eps33*eps0) are built on
+// the host in FP64 from the reference's formulas, then cast.
+template <typename T>
+struct E2Args {
+    int nx, nz;
+    T dx, dz, dt, dbHy;
+    BoxH box;
+    const T* c[10];   // aEx bEx dEx eEx aEz bEz dEz eEz e11abs e33abs
+    const T* cpml[6]; // kappa kappa_half acoef acoef_half bcoef bcoef_half
+    T* f[3];          // Ex Ez Hy
+    T* mem[4];
+    const double* src[2];
+    int isrc, jsrc;
+    T* traces;        // [nt][2][nrec]
+    double* norms;
+};
+void launch_electromag2_f64(const E2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag2_f32(const E2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
+// ------------------------------------------------------------- seismic25
+// Complex fields are interleaved (re, im) arrays of T.  The nine face
+// densities are pre-averaged on the host exactly as the reference does
+// (array_averaging2d, running averages included).
+template <typename T>
+struct S25Args {
+    int nx, nz;
+    T dx, dz, dt, ky;
+    BoxH box;
+    const T* C[21];
+    const T* g[6];     // gamma_x y z xy yz xz (FP32: 1/(1+gamma dt))
+    const T* cpml[6];  // kappa kappa_half acoef acoef_half bcoef bcoef_half (FP32: 1/kappa)
+    const T* rho9[9];  // rhoxx rhoyx rhozx rhoxy rhoyy rhozy rhoxz rhoyz rhozz (FP32: 1/rho)
+    const T* rho;      // raw density for the source terms (FP64 path), 1/rho in FP32
+    T* f[9];           // complex
+    T* mem[30];        // complex
+    const double* src[9];
+    int isrc, ksrc;
+    int stress_src;
+    T* traces;         // [nt][3][nrec] complex
+    double* norms;
+};
+void launch_seismic25_f64(const S25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic25_f32(const S25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
+// ----------------------------------------------------------- electromag25
+template <typename T>
+struct E25Args {
+    int nx, nz;
+    T dx, dz, dt, ky, dtmu;
+    BoxH box;
+    const T* sig[6];   // s11 s12 s13 s22 s23 s33
+    const T* inv[9];   // aEx bEx cEx aEy bEy cEy aEz bEz cEz
+    const T* eabs[3];  // eps11, eps22, eps33 times eps0
+    const T* cpml[6];
+    T* f[6];           // Ex Ey Ez Hx Hy Hz (complex)
+    T* mem[8];
+    const double* src[3];
+    int isrc, ksrc;
+    T* traces;         // [nt][3][nrec] complex
+    double* norms;
+};
+void launch_electromag25_f64(const E25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag25_f32(const E25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
+// -------------------------------------------------------------- seismic3
+template <typename T>
+struct S3Args {
+    int nx, ny, nz, density_code;
+    T dx, dy, dz, dt;
+    BoxH box;
+    const T* C[21];
+    const T* rho;     // FP64: rho;   FP32: rho (buoyancy computed per face)
+    const T* g[6];    // gamma_x y z xy yz xz (FP32: 1/(1+gamma dt))
+    const T* cpml[6]; // FP32: kappa slots hold 1/kappa
+    T* f[9];
+    T* mem[45];
+    const double* src[9];
+    int isrc, jsrc, ksrc;
+    int stress_src;
+    T* traces;        // [nt][3][nrec]
+    double* norms;    // [2][nt]: velocity norm, stress norm
+    int nt;
+};
+void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
+// Number of kernel launches one step of each family issues (for accounting).
+int seidart_step_launches(int family, int stress_src);

@@ -1,0 +1,819 @@
+// solver.cu -- host runtime behind the C ABI (include/seidart_gpu.h).
+//
+// A SeidartSolver owns, for one model, a single device arena holding the
+// model arrays (converted once to the field precision, with FP64-derived
+// coefficients such as 1/(1+gamma dt), 1/kappa or the EM tensor inverses),
+// the fields, the full-grid CPML memory arrays, the source series, the
+// receiver traces and the per-step norms.  Steps run asynchronously on the
+// solver's stream; chunks of steps are captured once into a CUDA graph and
+// replayed (the step number lives in device memory, so one graph serves
+// every starting step).
+//
+// Host-side coefficient set-up follows the reference formulas statement by
+// statement (this file is compiled with -ffp-contract=off so the FP64 values
+// match the CPU restatement exactly).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/seidart_gpu.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (expr);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return set_err(SEIDART_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
+    } while (0)
+
+const double kPi = 3.141592653589793238462643;
+const double kEps0 = 8.85418782e-12;
+const double kMu0 = 4.0 * kPi * 1.0e-7;  // constants.f08:9
+
+struct Layout {
+    int nmodel, nsrc, nfield, nmem, cplx, ncomp;
+};
+bool layout_of(int fam, Layout* L) {
+    switch (fam) {
+    case SEIDART_SEISMIC2: *L = {S2_NMODEL, S2_NSRC, S2_NFIELD, S2_NMEM, 0, 2}; return true;
+    case SEIDART_SEISMIC25: *L = {SEIDART_NMODEL3, S3_NSRC, S3_NFIELD, S25_NMEM, 1, 3}; return true;
+    case SEIDART_SEISMIC3: *L = {SEIDART_NMODEL3, S3_NSRC, S3_NFIELD, S3_NMEM, 0, 3}; return true;
+    case SEIDART_ELECTROMAG2: *L = {E2_NMODEL, E2_NSRC, E2_NFIELD, E2_NMEM, 0, 2}; return true;
+    case SEIDART_ELECTROMAG25: *L = {E25_NMODEL, E25_NSRC, E25_NFIELD, E25_NMEM, 1, 3}; return true;
+    default: return false;
+    }
+}
+
+// CPML slot offsets inside each family's model list (kappa, kappa_half,
+// acoef, acoef_half, bcoef, bcoef_half are always consecutive).
+int cpml_slot(int fam) {
+    switch (fam) {
+    case SEIDART_SEISMIC2: return S2_KAPPA;
+    case SEIDART_ELECTROMAG2: return E2_KAPPA;
+    case SEIDART_ELECTROMAG25: return E25_KAPPA;
+    default: return SEIDART_KAPPA3;
+    }
+}
+
+// array_averaging2d, averaging.f08:27-80 (in place, ascending: '+i'/'+j'
+// are running averages)
+double scalar_mean_h(double a, double b, int code) {
+    switch (code) {
+    case 1: return 2.0 * a * b / (a + b);
+    case 2: return sqrt(a * b);
+    case 3: return 0.5 * (a + b);
+    default: return a;
+    }
+}
+void averaging2d(double* a, int ni, int nj, int code, int dir) {
+    auto ix = [ni](int i, int j) { return (size_t)(i - 1) + (size_t)ni * (size_t)(j - 1); };
+    switch (dir) {
+    case 0: for (int j = 1; j <= nj; ++j) for (int i = 2; i <= ni; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i - 1, j)], code); break;
+    case 1: for (int j = 1; j <= nj; ++j) for (int i = 1; i <= ni - 1; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i + 1, j)], code); break;
+    case 2: for (int j = 2; j <= nj; ++j) for (int i = 1; i <= ni; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i, j - 1)], code); break;
+    default: for (int j = 1; j <= nj - 1; ++j) for (int i = 1; i <= ni; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i, j + 1)], code); break;
+    }
+}
+
+template <typename T>
+__global__ void zero_ring2d(T* f, int nx, int nz, int ncomp_per_cell) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int per = 2 * nx + 2 * nz;
+    if (t >= per) return;
+    int i, k;
+    if (t < nx) { i = t; k = 0; }
+    else if (t < 2 * nx) { i = t - nx; k = nz - 1; }
+    else if (t < 2 * nx + nz) { i = 0; k = t - 2 * nx; }
+    else { i = nx - 1; k = t - 2 * nx - nz; }
+    const size_t c = (size_t)i + (size_t)nx * k;
+    for (int q = 0; q < ncomp_per_cell; ++q) f[c * ncomp_per_cell + q] = 0;
+}
+
+}  // namespace
+
+struct SeidartSolver {
+    int family = 0, precision = 0, density = 1;
+    SeidartDomain dom{};
+    SeidartSource src{};
+    Layout L{};
+    size_t ncell = 0, esize = 8;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    char* arena = nullptr;
+    size_t arena_bytes = 0, arena_used = 0;
+    std::vector<void*> fields, mem;
+    int* step_dev = nullptr;
+    int* rec_dev = nullptr;
+    int nrec = 0;
+    void* traces = nullptr;
+    double* norms = nullptr;
+    int nnorm = 1;
+    int steps_done = 0;
+    int stress_src = 0;
+    BoxH box{};
+    long long launches = 0;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    int graph_len[2] = {0, 0};
+    bool graphs_ok = true;
+    // precision-specific launch argument blocks
+    S2Args<double> s2d; S2Args<float> s2f;
+    E2Args<double> e2d; E2Args<float> e2f;
+    S25Args<double> s25d; S25Args<float> s25f;
+    E25Args<double> e25d; E25Args<float> e25f;
+    S3Args<double> s3d; S3Args<float> s3f;
+
+    void* carve(size_t bytes) {
+        const size_t off = (arena_used + 255) & ~(size_t)255;
+        arena_used = off + bytes;
+        return arena ? arena + off : nullptr;
+    }
+};
+
+namespace {
+
+// Upload n values of `h` (FP64) as T into device memory d.
+template <typename T>
+int upload(void* d, const double* h, size_t n, cudaStream_t st) {
+    if (sizeof(T) == sizeof(double)) {
+        CUDA_TRY(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return SEIDART_OK;
+    }
+    std::vector<float> tmp(n);
+    for (size_t q = 0; q < n; ++q) tmp[q] = (float)h[q];
+    CUDA_TRY(cudaMemcpyAsync(d, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SEIDART_OK;
+}
+template <typename T>
+int download(double* h, const void* d, size_t n, cudaStream_t st) {
+    if (sizeof(T) == sizeof(double)) {
+        CUDA_TRY(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return SEIDART_OK;
+    }
+    std::vector<float> tmp(n);
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (size_t q = 0; q < n; ++q) h[q] = tmp[q];
+    return SEIDART_OK;
+}
+
+// Interior box: the largest box found inside [cpml, n-cpml) per axis whose
+// cells all have inert CPML coefficients (acoef = acoef_half = 0,
+// kappa = kappa_half = 1, finite b).  Starting from the nominal box, faces
+// that still hold active cells (e.g. the half-grid profile reaching one cell
+// further on the high side) are peeled off a few times; the result is then
+// verified cell by cell.  If verification fails the box is empty and the
+// CPML arithmetic runs on every cell, as in the reference.
+BoxH interior_box(const SeidartSolver& s, const double* const* model) {
+    const int cs = cpml_slot(s.family);
+    const double *kap = model[cs], *kaph = model[cs + 1], *ac = model[cs + 2], *ach = model[cs + 3],
+                 *bc = model[cs + 4], *bch = model[cs + 5];
+    const int nx = s.dom.nx, nz = s.dom.nz, c = s.dom.cpml;
+    const bool is3 = s.family == SEIDART_SEISMIC3;
+    const int ny = is3 ? s.dom.ny : 1;
+    BoxH b{c, nx - c, is3 ? c : 0, is3 ? ny - c : 1, c, nz - c};
+    const BoxH empty{0, 0, 0, 0, 0, 0};
+    auto active = [&](int i, int j, int k) {
+        const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+        return ac[q] != 0.0 || ach[q] != 0.0 || kap[q] != 1.0 || kaph[q] != 1.0 || !isfinite(bc[q]) ||
+               !isfinite(bch[q]);
+    };
+    auto nonempty = [&]() { return b.i0 < b.i1 && b.j0 < b.j1 && b.k0 < b.k1; };
+    // face test on plane `axis` = idx of the current box
+    auto face = [&](int axis, int idx) {
+        const int lo[3] = {b.i0, b.j0, b.k0}, hi[3] = {b.i1, b.j1, b.k1};
+        int l[3] = {lo[0], lo[1], lo[2]}, h[3] = {hi[0], hi[1], hi[2]};
+        l[axis] = idx; h[axis] = idx + 1;
+        for (int k = l[2]; k < h[2]; ++k)
+            for (int j = l[1]; j < h[1]; ++j)
+                for (int i = l[0]; i < h[0]; ++i)
+                    if (active(i, j, k)) return true;
+        return false;
+    };
+    for (int it = 0; it < 4 && nonempty(); ++it) {
+        bool changed = false;
+        if (face(0, b.i0)) { ++b.i0; changed = true; }
+        if (nonempty() && face(0, b.i1 - 1)) { --b.i1; changed = true; }
+        if (is3 && nonempty() && face(1, b.j0)) { ++b.j0; changed = true; }
+        if (is3 && nonempty() && face(1, b.j1 - 1)) { --b.j1; changed = true; }
+        if (nonempty() && face(2, b.k0)) { ++b.k0; changed = true; }
+        if (nonempty() && face(2, b.k1 - 1)) { --b.k1; changed = true; }
+        if (!changed) break;
+    }
+    if (!nonempty()) return empty;
+    for (int k = b.k0; k < b.k1; ++k)
+        for (int j = b.j0; j < b.j1; ++j)
+            for (int i = b.i0; i < b.i1; ++i)
+                if (active(i, j, k)) return empty;
+    return b;
+}
+
+// Model set-up per family; `T` is the field precision.
+template <typename T>
+int setup_model(SeidartSolver& s, const double* const* model, const double* const* srcfn,
+                const double** dev_src, std::vector<std::vector<double>>& derived) {
+    const size_t N = s.ncell;
+    const bool f32 = sizeof(T) == sizeof(float);
+    const double dt = s.src.dt;
+    auto arr = [&](const double* h) -> const T* {
+        T* d = (T*)s.carve(N * sizeof(T));
+        if (d && upload<T>(d, h, N, s.stream) != SEIDART_OK) return nullptr;
+        return d;
+    };
+    // while measuring (no arena yet) only sizes matter: skip the arithmetic
+    static const double dummy = 0.0;
+    auto derive = [&](auto fn) -> const double* {
+        if (!s.arena) return &dummy;
+        derived.emplace_back(N);
+        std::vector<double>& v = derived.back();
+        for (size_t q = 0; q < N; ++q) v[q] = fn(q);
+        return v.data();
+    };
+    // FP32: gamma -> 1/(1+gamma dt), kappa -> 1/kappa (same memory traffic)
+    auto gam = [&](const double* g) { return f32 ? arr(derive([&](size_t q) { return 1.0 / (1.0 + g[q] * dt); })) : arr(g); };
+    auto kap = [&](const double* k) { return f32 ? arr(derive([&](size_t q) { return 1.0 / k[q]; })) : arr(k); };
+    const int cs = cpml_slot(s.family);
+    const T* cp[6];
+    cp[0] = kap(model[cs]);
+    cp[1] = kap(model[cs + 1]);
+    for (int q = 2; q < 6; ++q) cp[q] = arr(model[cs + q]);
+
+    switch (s.family) {
+    case SEIDART_SEISMIC2: {
+        S2Args<T> a{};
+        for (int q = 0; q < 7; ++q) a.m[q] = arr(model[q]);
+        for (int q = 7; q < 10; ++q) a.m[q] = gam(model[q]);
+        for (int q = 0; q < 6; ++q) a.m[10 + q] = cp[q];
+        for (int q = 0; q < 5; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.s2d = a; else s.s2f = a;
+        break;
+    }
+    case SEIDART_ELECTROMAG2: {
+        // cpmlfdtd.f08:2519-2540
+        const double *e11 = model[E2_E11], *e13 = model[E2_E13], *e33 = model[E2_E33], *s11 = model[E2_S11],
+                     *s13 = model[E2_S13], *s33 = model[E2_S33];
+        std::vector<double> det(s.arena ? N : 0);
+        for (size_t q = 0; q < det.size(); ++q) {
+            const double a11 = e11[q] * kEps0, a13 = e13[q] * kEps0, a33 = e33[q] * kEps0;
+            double d = a11 * a33 - a13 * a13;
+            if (d <= 1.0e-18 * kEps0 * kEps0) d = 1.0e-18 * kEps0 * kEps0;
+            det[q] = d;
+        }
+        auto A = [&](size_t q, int which) {
+            const double a11 = e11[q] * kEps0, a13 = e13[q] * kEps0, a33 = e33[q] * kEps0, d = det[q];
+            switch (which) {
+            case 0: return a33 / d;
+            case 1: return -a13 / d;
+            case 2: return (a33 * s11[q] - a13 * s13[q]) / d;
+            case 3: return (a33 * s13[q] - a13 * s33[q]) / d;
+            case 4: return -a13 / d;
+            case 5: return a11 / d;
+            case 6: return (a11 * s13[q] - a13 * s11[q]) / d;
+            case 7: return (a11 * s33[q] - a13 * s13[q]) / d;
+            case 8: return a11;
+            default: return a33;
+            }
+        };
+        E2Args<T> a{};
+        for (int w = 0; w < 10; ++w) a.c[w] = arr(derive([&](size_t q) { return A(q, w); }));
+        for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
+        for (int q = 0; q < 2; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.e2d = a; else s.e2f = a;
+        break;
+    }
+    case SEIDART_SEISMIC25: {
+        S25Args<T> a{};
+        for (int q = 0; q < 21; ++q) a.C[q] = arr(model[q]);
+        for (int q = 0; q < 6; ++q) a.g[q] = gam(model[SEIDART_GX3 + q]);
+        for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
+        // density averaging, cpmlfdtd.f08:889-898 (FP32: stored as 1/rho)
+        const double* rho = model[SEIDART_RHO3];
+        const int dirs[9] = {0, -1, 2, 1, -1, 2, 1, -1, 3};  // -1: plain rho
+        for (int q = 0; q < 9; ++q) {
+            if (!s.arena) { a.rho9[q] = arr(rho); continue; }
+            derived.emplace_back(rho, rho + N);
+            if (dirs[q] >= 0) averaging2d(derived.back().data(), s.dom.nx, s.dom.nz, s.density, dirs[q]);
+            if (f32) for (double& v : derived.back()) v = 1.0 / v;
+            a.rho9[q] = arr(derived.back().data());
+        }
+        a.rho = f32 ? arr(derive([&](size_t q) { return 1.0 / rho[q]; })) : arr(rho);
+        for (int q = 0; q < 9; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.s25d = a; else s.s25f = a;
+        break;
+    }
+    case SEIDART_ELECTROMAG25: {
+        // cpmlfdtd.f08:3046-3067
+        std::vector<double> det(s.arena ? N : 0);
+        const double* E[6];
+        for (int q = 0; q < 6; ++q) E[q] = model[E25_E11 + q];
+        auto ee = [&](int w, size_t q) { return E[w][q] * kEps0; };  // 0 e11 1 e12 2 e13 3 e22 4 e23 5 e33
+        for (size_t q = 0; q < det.size(); ++q) {
+            const double a11 = ee(0, q), a12 = ee(1, q), a13 = ee(2, q), a22 = ee(3, q), a23 = ee(4, q), a33 = ee(5, q);
+            det[q] = a11 * (a22 * a33 - a23 * a23) - a12 * (a12 * a33 - a23 * a13) + a13 * (a12 * a23 - a22 * a13);
+        }
+        auto inv = [&](size_t q, int w) {
+            const double a11 = ee(0, q), a12 = ee(1, q), a13 = ee(2, q), a22 = ee(3, q), a23 = ee(4, q), a33 = ee(5, q);
+            const double d = det[q];
+            const double aEx = (a22 * a33 - a23 * a23) / d, bEx = -((a12 * a33 - a23 * a13) / d),
+                         cEx = (a12 * a23 - a22 * a13) / d, bEy = (a11 * a33 - a13 * a13) / d,
+                         cEy = -((a11 * a23 - a12 * a13) / d), cEz = (a11 * a22 - a12 * a12) / d;
+            const double v[9] = {aEx, bEx, cEx, bEx, bEy, cEy, cEx, cEy, cEz};
+            return v[w];
+        };
+        E25Args<T> a{};
+        for (int w = 0; w < 9; ++w) a.inv[w] = arr(derive([&](size_t q) { return inv(q, w); }));
+        for (int w = 0; w < 6; ++w) a.sig[w] = arr(model[E25_S11 + w]);
+        const int ed[3] = {0, 3, 5};
+        for (int w = 0; w < 3; ++w) a.eabs[w] = arr(derive([&](size_t q) { return ee(ed[w], q); }));
+        for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
+        for (int q = 0; q < 3; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.e25d = a; else s.e25f = a;
+        break;
+    }
+    case SEIDART_SEISMIC3: {
+        S3Args<T> a{};
+        for (int q = 0; q < 21; ++q) a.C[q] = arr(model[q]);
+        a.rho = arr(model[SEIDART_RHO3]);
+        for (int q = 0; q < 6; ++q) a.g[q] = gam(model[SEIDART_GX3 + q]);
+        for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
+        for (int q = 0; q < 9; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.s3d = a; else s.s3f = a;
+        break;
+    }
+    }
+    (void)srcfn;
+    return SEIDART_OK;
+}
+
+// Fill the per-family scalar fields and state pointers of the arg blocks.
+template <typename T, typename A>
+void fill_common2(SeidartSolver& s, A& a) {
+    a.nx = s.dom.nx; a.nz = s.dom.nz;
+    a.dt = (T)s.src.dt;
+    a.box = s.box;
+    a.traces = (T*)s.traces;
+    a.norms = s.norms;
+    for (size_t q = 0; q < s.fields.size(); ++q) a.f[q] = (T*)s.fields[q];
+    for (size_t q = 0; q < s.mem.size(); ++q) a.mem[q] = (T*)s.mem[q];
+}
+
+template <typename T>
+void finish_args(SeidartSolver& s) {
+    const int is = s.src.xind + s.dom.cpml - 1, js = s.src.yind + s.dom.cpml - 1, ks = s.src.zind + s.dom.cpml - 1;
+    const bool f32 = sizeof(T) == sizeof(float);
+    switch (s.family) {
+    case SEIDART_SEISMIC2: {
+        S2Args<T>& a = *(S2Args<T>*)(f32 ? (void*)&s.s2f : (void*)&s.s2d);
+        fill_common2<T>(s, a);
+        a.dx = (T)s.dom.dx; a.dz = (T)s.dom.dz; a.density_code = s.density;
+        a.isrc = is; a.jsrc = ks; a.stress_src = s.stress_src;
+        break;
+    }
+    case SEIDART_ELECTROMAG2: {
+        E2Args<T>& a = *(E2Args<T>*)(f32 ? (void*)&s.e2f : (void*)&s.e2d);
+        fill_common2<T>(s, a);
+        // the FP32 build multiplies by 1/dx, 1/dz
+        a.dx = f32 ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
+        a.dz = f32 ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
+        a.dbHy = (T)(s.src.dt / kMu0);
+        a.isrc = is; a.jsrc = ks;
+        break;
+    }
+    case SEIDART_SEISMIC25: {
+        S25Args<T>& a = *(S25Args<T>*)(f32 ? (void*)&s.s25f : (void*)&s.s25d);
+        fill_common2<T>(s, a);
+        a.dx = (T)s.dom.dx; a.dz = (T)s.dom.dz; a.ky = (T)s.src.ky;
+        a.isrc = is; a.ksrc = ks; a.stress_src = s.stress_src;
+        break;
+    }
+    case SEIDART_ELECTROMAG25: {
+        E25Args<T>& a = *(E25Args<T>*)(f32 ? (void*)&s.e25f : (void*)&s.e25d);
+        fill_common2<T>(s, a);
+        a.dx = (T)s.dom.dx; a.dz = (T)s.dom.dz; a.ky = (T)s.src.ky;
+        a.dtmu = (T)(s.src.dt / kMu0);
+        a.isrc = is; a.ksrc = ks;
+        break;
+    }
+    case SEIDART_SEISMIC3: {
+        S3Args<T>& a = *(S3Args<T>*)(f32 ? (void*)&s.s3f : (void*)&s.s3d);
+        fill_common2<T>(s, a);
+        a.ny = s.dom.ny;
+        a.dx = (T)s.dom.dx; a.dy = (T)s.dom.dy; a.dz = (T)s.dom.dz; a.density_code = s.density;
+        a.isrc = is; a.jsrc = js; a.ksrc = ks; a.stress_src = s.stress_src;
+        a.nt = s.src.time_steps;
+        break;
+    }
+    }
+}
+
+int launches_per_step(const SeidartSolver& s) { return 3 + (s.stress_src ? 1 : 0); }
+
+void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nullptr) {
+    StepInfo si{s.step_dev, s.nrec, s.rec_dev};
+    const bool f32 = s.precision == SEIDART_FP32;
+    switch (s.family) {
+    case SEIDART_SEISMIC2: f32 ? launch_seismic2_f32(s.s2f, si, st, h) : launch_seismic2_f64(s.s2d, si, st, h); break;
+    case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : launch_electromag2_f64(s.e2d, si, st, h); break;
+    case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : launch_seismic25_f64(s.s25d, si, st, h); break;
+    case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
+    case SEIDART_SEISMIC3: f32 ? launch_seismic3_f32(s.s3f, si, st, h) : launch_seismic3_f64(s.s3d, si, st, h); break;
+    }
+}
+
+// Event recorder for seidart_solver_profile: one event after every kernel.
+struct EventLog {
+    cudaStream_t st;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kid;
+    std::vector<std::string> names;
+    size_t next = 0;
+    bool failed = false;
+    static void on_launch(void* ctx, int k, const char* name) {
+        EventLog* L = (EventLog*)ctx;
+        if (L->next >= L->ev.size()) { L->failed = true; return; }
+        if (cudaEventRecord(L->ev[L->next], L->st) != cudaSuccess) L->failed = true;
+        L->kid[L->next] = k;
+        if ((int)L->names.size() <= k) L->names.resize(k + 1);
+        L->names[k] = name;
+        ++L->next;
+    }
+};
+
+int graph_for(SeidartSolver& s, int len, cudaGraphExec_t* out) {
+    for (int q = 0; q < 2; ++q)
+        if (s.graph_exec[q] && s.graph_len[q] == len) { *out = s.graph_exec[q]; return SEIDART_OK; }
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+    for (int t = 0; t < len; ++t) launch_one_step(s, s.stream);
+    CUDA_TRY(cudaStreamEndCapture(s.stream, &g));
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(SEIDART_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    // keep at most two cached lengths (the chunk and a tail)
+    int slot = s.graph_exec[0] == nullptr ? 0 : 1;
+    if (s.graph_exec[slot]) cudaGraphExecDestroy(s.graph_exec[slot]);
+    s.graph_exec[slot] = ex;
+    s.graph_len[slot] = len;
+    *out = ex;
+    return SEIDART_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* seidart_last_error(void) { return g_err.c_str(); }
+
+int seidart_layout(int family, int* nmodel, int* nsrc, int* nfield, int* nmem, int* is_complex, int* nrec_comp) {
+    Layout L;
+    if (!layout_of(family, &L)) return set_err(SEIDART_ERR_ARG, "unknown solver family %d", family);
+    if (nmodel) *nmodel = L.nmodel;
+    if (nsrc) *nsrc = L.nsrc;
+    if (nfield) *nfield = L.nfield;
+    if (nmem) *nmem = L.nmem;
+    if (is_complex) *is_complex = L.cplx;
+    if (nrec_comp) *nrec_comp = L.ncomp;
+    return SEIDART_OK;
+}
+
+int seidart_solver_create(SeidartSolver** out, int family, int precision, const SeidartDomain* dom,
+                          const SeidartSource* src, int density_code, const double* const* model,
+                          const double* const* srcfn, int nrec, const int* rec_cells) {
+    if (!out || !dom || !src || !model) return set_err(SEIDART_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    Layout L;
+    if (!layout_of(family, &L)) return set_err(SEIDART_ERR_ARG, "unknown solver family %d", family);
+    if (precision != SEIDART_FP64 && precision != SEIDART_FP32)
+        return set_err(SEIDART_ERR_ARG, "precision must be SEIDART_FP64 or SEIDART_FP32");
+    if (density_code < 1 || density_code > 4)
+        return set_err(SEIDART_ERR_ARG, "density_code %d: must be 1 harmonic, 2 geometric, 3 arithmetic, 4 none",
+                       density_code);
+    const bool is3 = family == SEIDART_SEISMIC3;
+    const int nx = dom->nx, nz = dom->nz, ny = is3 ? dom->ny : 1;
+    if (nx < 6 || nz < 6 || (is3 && ny < 6)) return set_err(SEIDART_ERR_ARG, "grid too small (need >= 6 cells per axis)");
+    if (src->time_steps < 1) return set_err(SEIDART_ERR_ARG, "time_steps must be >= 1");
+    if (!(src->dt > 0)) return set_err(SEIDART_ERR_ARG, "dt must be > 0");
+    if (!(dom->dx > 0) || !(dom->dz > 0) || (is3 && !(dom->dy > 0))) return set_err(SEIDART_ERR_ARG, "grid spacing must be > 0");
+    // the source cell and its staggered neighbours (+1) must lie inside the grid
+    const int is = src->xind + dom->cpml - 1, js = src->yind + dom->cpml - 1, ks = src->zind + dom->cpml - 1;
+    if (is < 0 || is + 1 >= nx || ks < 0 || ks + 1 >= nz || (is3 && (js < 0 || js + 1 >= ny)))
+        return set_err(SEIDART_ERR_ARG, "source index (%d,%d,%d)+cpml outside the padded grid", src->xind, src->yind, src->zind);
+    for (int q = 0; q < L.nmodel; ++q)
+        if (!model[q]) return set_err(SEIDART_ERR_ARG, "model array %d is NULL", q);
+    const size_t N = (size_t)nx * ny * nz;
+    for (int r = 0; r < nrec; ++r)
+        if (!rec_cells || rec_cells[r] < 0 || (size_t)rec_cells[r] >= N)
+            return set_err(SEIDART_ERR_ARG, "receiver %d cell index out of range", r);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return set_err(SEIDART_ERR_UNSUPPORTED, "no CUDA device: the solvers run only on the GPU");
+
+    SeidartSolver* s = new SeidartSolver();
+    s->family = family; s->precision = precision; s->density = density_code;
+    s->dom = *dom; s->src = *src; s->L = L;
+    if (!is3) s->dom.ny = 1;
+    s->ncell = N;
+    s->esize = precision == SEIDART_FP32 ? 4 : 8;
+    s->nrec = nrec;
+    s->nnorm = is3 ? 2 : 1;
+    s->box = interior_box(*s, model);
+    for (int q = 0; q < L.nsrc; ++q) {
+        // stress-source series are every slot after the force components
+        const int first_stress = (family == SEIDART_SEISMIC2) ? S2_SRCXX : ((family == SEIDART_SEISMIC3 || family == SEIDART_SEISMIC25) ? S3_SRCXX : 1 << 20);
+        if (q >= first_stress && srcfn && srcfn[q])
+            for (int t = 0; t < src->time_steps; ++t)
+                if (srcfn[q][t] != 0.0) { s->stress_src = 1; break; }
+    }
+    const int cf = L.cplx ? 2 : 1;
+    // two passes: measure, then allocate and carve for real
+    std::vector<std::vector<double>> derived;
+    for (int pass = 0; pass < 2; ++pass) {
+        s->arena_used = 0;
+        s->fields.assign(L.nfield, nullptr);
+        s->mem.assign(L.nmem, nullptr);
+        for (int q = 0; q < L.nfield; ++q) s->fields[q] = s->carve(N * cf * s->esize);
+        for (int q = 0; q < L.nmem; ++q) s->mem[q] = s->carve(N * cf * s->esize);
+        const double* dsrc[9] = {nullptr};
+        std::vector<std::pair<double*, int>> src_up;
+        for (int q = 0; q < L.nsrc; ++q) {
+            if (srcfn && srcfn[q]) {
+                dsrc[q] = (const double*)s->carve(sizeof(double) * src->time_steps);
+                src_up.push_back({(double*)dsrc[q], q});
+            }
+        }
+        s->step_dev = (int*)s->carve(sizeof(int));
+        s->rec_dev = (int*)s->carve(sizeof(int) * (nrec > 0 ? nrec : 1));
+        s->traces = s->carve((size_t)src->time_steps * L.ncomp * (nrec > 0 ? nrec : 1) * cf * s->esize);
+        s->norms = (double*)s->carve(sizeof(double) * src->time_steps * s->nnorm);
+        if (pass == 0) {
+            // model arrays: measured by running the set-up against a null arena
+            derived.clear();
+            int rc = precision == SEIDART_FP32 ? setup_model<float>(*s, model, srcfn, dsrc, derived)
+                                               : setup_model<double>(*s, model, srcfn, dsrc, derived);
+            if (rc != SEIDART_OK) { delete s; return rc; }
+            s->arena_bytes = s->arena_used;
+            cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) { delete s; return set_err(SEIDART_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+            s->own_stream = true;
+            e = cudaMalloc((void**)&s->arena, s->arena_bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                cudaStreamDestroy(s->stream);
+                const size_t mb = s->arena_bytes >> 20;
+                delete s;
+                return set_err(SEIDART_ERR_NOMEM, "device allocation of %zu MiB failed: %s", mb, cudaGetErrorString(e));
+            }
+        } else {
+            int rc = SEIDART_OK;
+            if (cudaMemsetAsync(s->arena, 0, s->arena_bytes, s->stream) != cudaSuccess) rc = SEIDART_ERR_CUDA;
+            for (auto& p : src_up)
+                if (rc == SEIDART_OK &&
+                    cudaMemcpyAsync(p.first, srcfn[p.second], sizeof(double) * src->time_steps, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+                    rc = SEIDART_ERR_CUDA;
+            if (rc == SEIDART_OK && nrec > 0 &&
+                cudaMemcpyAsync(s->rec_dev, rec_cells, sizeof(int) * nrec, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+                rc = SEIDART_ERR_CUDA;
+            const int one = 1;
+            if (rc == SEIDART_OK && cudaMemcpyAsync(s->step_dev, &one, sizeof(int), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+                rc = SEIDART_ERR_CUDA;
+            if (rc == SEIDART_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = SEIDART_ERR_CUDA;
+            derived.clear();
+            if (rc == SEIDART_OK)
+                rc = precision == SEIDART_FP32 ? setup_model<float>(*s, model, srcfn, dsrc, derived)
+                                               : setup_model<double>(*s, model, srcfn, dsrc, derived);
+            if (rc != SEIDART_OK) {
+                seidart_solver_destroy(s);
+                return rc == SEIDART_ERR_CUDA ? set_err(rc, "device set-up failed: %s", cudaGetErrorString(cudaGetLastError())) : rc;
+            }
+        }
+    }
+    if (precision == SEIDART_FP32) finish_args<float>(*s); else finish_args<double>(*s);
+    *out = s;
+    return SEIDART_OK;
+}
+
+int seidart_solver_set_stream(SeidartSolver* s, void* stream) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (s->own_stream) cudaStreamDestroy(s->stream);
+    for (int q = 0; q < 2; ++q)
+        if (s->graph_exec[q]) { cudaGraphExecDestroy(s->graph_exec[q]); s->graph_exec[q] = nullptr; s->graph_len[q] = 0; }
+    if (stream) { s->stream = (cudaStream_t)stream; s->own_stream = false; }
+    else { CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)); s->own_stream = true; }
+    return SEIDART_OK;
+}
+
+int seidart_solver_set_fields(SeidartSolver* s, const double* const* fields) {
+    if (!s || !fields) return set_err(SEIDART_ERR_ARG, "NULL argument");
+    const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
+    for (int q = 0; q < s->L.nfield; ++q) {
+        if (!fields[q]) continue;  // NULL keeps the current values
+        const int rc = s->precision == SEIDART_FP32 ? upload<float>(s->fields[q], fields[q], n, s->stream)
+                                                    : upload<double>(s->fields[q], fields[q], n, s->stream);
+        if (rc != SEIDART_OK) return rc;
+    }
+    return SEIDART_OK;
+}
+
+static int zero_rings(SeidartSolver* s) {
+    // electromag2: the Hy ring is zeroed lazily by the next H update
+    if (s->family == SEIDART_ELECTROMAG2) {
+        const int per = 2 * s->dom.nx + 2 * s->dom.nz;
+        if (s->precision == SEIDART_FP32)
+            zero_ring2d<float><<<(per + 255) / 256, 256, 0, s->stream>>>((float*)s->fields[E2_HY], s->dom.nx, s->dom.nz, 1);
+        else
+            zero_ring2d<double><<<(per + 255) / 256, 256, 0, s->stream>>>((double*)s->fields[E2_HY], s->dom.nx, s->dom.nz, 1);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return SEIDART_OK;
+}
+
+int seidart_solver_get_fields(SeidartSolver* s, double* const* fields) {
+    if (!s || !fields) return set_err(SEIDART_ERR_ARG, "NULL argument");
+    int rc = zero_rings(s);
+    if (rc != SEIDART_OK) return rc;
+    const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
+    for (int q = 0; q < s->L.nfield; ++q) {
+        if (!fields[q]) continue;
+        rc = s->precision == SEIDART_FP32 ? download<float>(fields[q], s->fields[q], n, s->stream)
+                                          : download<double>(fields[q], s->fields[q], n, s->stream);
+        if (rc != SEIDART_OK) return rc;
+    }
+    return SEIDART_OK;
+}
+
+int seidart_solver_get_memory(SeidartSolver* s, double* const* mem) {
+    if (!s || !mem) return set_err(SEIDART_ERR_ARG, "NULL argument");
+    const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
+    for (int q = 0; q < s->L.nmem; ++q) {
+        if (!mem[q]) continue;
+        const int rc = s->precision == SEIDART_FP32 ? download<float>(mem[q], s->mem[q], n, s->stream)
+                                                    : download<double>(mem[q], s->mem[q], n, s->stream);
+        if (rc != SEIDART_OK) return rc;
+    }
+    return SEIDART_OK;
+}
+
+int seidart_solver_step(SeidartSolver* s, int nsteps) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    if (nsteps < 0 || s->steps_done + nsteps > s->src.time_steps)
+        return set_err(SEIDART_ERR_ARG, "stepping %d steps from step %d exceeds time_steps = %d", nsteps,
+                       s->steps_done, s->src.time_steps);
+    const int chunk = s->family == SEIDART_SEISMIC3 ? 16 : 64;
+    int left = nsteps;
+    while (left > 0) {
+        const int len = left >= chunk ? chunk : left;
+        cudaGraphExec_t ex = nullptr;
+        if (s->graphs_ok && graph_for(*s, len, &ex) == SEIDART_OK) {
+            CUDA_TRY(cudaGraphLaunch(ex, s->stream));
+        } else {
+            // streams that cannot be captured (the legacy default stream) launch directly
+            cudaGetLastError();
+            s->graphs_ok = false;
+            for (int t = 0; t < len; ++t) launch_one_step(*s, s->stream);
+            CUDA_TRY(cudaGetLastError());
+        }
+        left -= len;
+    }
+    s->steps_done += nsteps;
+    s->launches = (long long)nsteps * launches_per_step(*s);
+    return SEIDART_OK;
+}
+
+int seidart_solver_sync(SeidartSolver* s) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    CUDA_TRY(cudaGetLastError());
+    if (s->steps_done == 0) return SEIDART_OK;
+    std::vector<double> nrm(s->steps_done);
+    CUDA_TRY(cudaMemcpy(nrm.data(), s->norms, sizeof(double) * s->steps_done, cudaMemcpyDeviceToHost));
+    for (int t = 0; t < s->steps_done; ++t)
+        if (!(nrm[t] <= 1.0e25))  // > threshold, or NaN
+            return set_err(SEIDART_ERR_UNSTABLE, "code became unstable and blew up at step %d (max |v| = %g)", t + 1, nrm[t]);
+    return SEIDART_OK;
+}
+
+int seidart_solver_traces(SeidartSolver* s, double* traces, double* norms) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const size_t per = (size_t)s->L.ncomp * s->nrec * (s->L.cplx ? 2 : 1);
+    if (traces && s->nrec > 0) {
+        const int rc = s->precision == SEIDART_FP32 ? download<float>(traces, s->traces, per * s->steps_done, s->stream)
+                                                    : download<double>(traces, s->traces, per * s->steps_done, s->stream);
+        if (rc != SEIDART_OK) return rc;
+    }
+    if (norms) {
+        for (int q = 0; q < s->nnorm; ++q)
+            CUDA_TRY(cudaMemcpy(norms + (size_t)q * s->steps_done, s->norms + (size_t)q * s->src.time_steps,
+                                sizeof(double) * s->steps_done, cudaMemcpyDeviceToHost));
+    }
+    return SEIDART_OK;
+}
+
+int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, double* kernel_ms, int* kernel_launches,
+                           char* names, int names_len) {
+    if (!s || nsteps < 1) return set_err(SEIDART_ERR_ARG, "bad arguments");
+    if (s->steps_done + nsteps > s->src.time_steps)
+        return set_err(SEIDART_ERR_ARG, "stepping %d steps from step %d exceeds time_steps = %d", nsteps,
+                       s->steps_done, s->src.time_steps);
+    const int per = 8;
+    EventLog L;
+    L.st = s->stream;
+    L.ev.resize((size_t)nsteps * per + 1);
+    L.kid.assign(L.ev.size(), -1);
+    for (auto& e : L.ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaEventRecord(L.ev[0], s->stream));
+    L.next = 1;
+    LaunchHook h{&EventLog::on_launch, &L};
+    for (int t = 0; t < nsteps; ++t) launch_one_step(*s, s->stream, &h);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    double km[per] = {0}; int kl[per] = {0};
+    float tot = 0.f;
+    if (e == cudaSuccess && !L.failed) {
+        for (size_t q = 1; q < L.next; ++q) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, L.ev[q - 1], L.ev[q]);
+            const int k = L.kid[q];
+            if (k >= 0 && k < per) { km[k] += ms; kl[k] += 1; }
+        }
+        cudaEventElapsedTime(&tot, L.ev[0], L.ev[L.next - 1]);
+    }
+    for (auto& ev : L.ev) cudaEventDestroy(ev);
+    if (e != cudaSuccess) return set_err(SEIDART_ERR_CUDA, "profile run failed: %s", cudaGetErrorString(e));
+    if (L.failed) return set_err(SEIDART_ERR_CUDA, "profile event recording failed");
+    s->steps_done += nsteps;
+    s->launches = 0;
+    for (int k = 0; k < per; ++k) s->launches += kl[k];
+    if (total_ms) *total_ms = tot;
+    for (int k = 0; k < per; ++k) {
+        if (kernel_ms) kernel_ms[k] = km[k];
+        if (kernel_launches) kernel_launches[k] = kl[k];
+        if (names && names_len > 0) {
+            const std::string nm = k < (int)L.names.size() ? L.names[k] : std::string();
+            snprintf(names + (size_t)k * names_len, names_len, "%s", nm.c_str());
+        }
+    }
+    return SEIDART_OK;
+}
+
+int seidart_solver_steps_done(const SeidartSolver* s) { return s ? s->steps_done : -1; }
+
+void* seidart_solver_field_ptr(SeidartSolver* s, int slot) {
+    if (!s || slot < 0 || slot >= (int)s->fields.size()) return nullptr;
+    return s->fields[slot];
+}
+
+long long seidart_solver_launches(const SeidartSolver* s) { return s ? s->launches : -1; }
+
+int seidart_solver_destroy(SeidartSolver* s) {
+    if (!s) return SEIDART_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int q = 0; q < 2; ++q)
+        if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
+    if (s->arena) cudaFree(s->arena);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return SEIDART_OK;
+}
+
+int seidart_run(int family, int precision, const SeidartDomain* dom, const SeidartSource* src, int density_code,
+                const double* const* model, const double* const* srcfn, double* const* fields, int nrec,
+                const int* rec_cells, double* traces, double* norms) {
+    SeidartSolver* s = nullptr;
+    int rc = seidart_solver_create(&s, family, precision, dom, src, density_code, model, srcfn, nrec, rec_cells);
+    if (rc != SEIDART_OK) return rc;
+    if (fields) rc = seidart_solver_set_fields(s, fields);
+    if (rc == SEIDART_OK) rc = seidart_solver_step(s, src->time_steps);
+    int sync_rc = rc == SEIDART_OK ? seidart_solver_sync(s) : rc;
+    std::string err = g_err;
+    if (rc == SEIDART_OK && fields) rc = seidart_solver_get_fields(s, fields);
+    if (rc == SEIDART_OK) rc = seidart_solver_traces(s, traces, norms);
+    seidart_solver_destroy(s);
+    if (rc != SEIDART_OK) return rc;
+    if (sync_rc != SEIDART_OK) { g_err = err; return sync_rc; }
+    return SEIDART_OK;
+}
+
+}  // extern "C"

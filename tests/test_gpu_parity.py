@@ -1,0 +1,128 @@
+"""GPU solvers (through the C ABI) against the CPU restatement of the reference.
+
+FP64 path: every field, CPML memory array, receiver sample and max-norm must
+equal the oracle's exactly (the kernels keep the reference's expression
+trees, --fmad=false).  FP32 path: relative L2 error against the FP64 oracle
+at most FP32_TOL on fields and traces.
+"""
+import numpy as np
+import pytest
+
+import seidart_gpu as sg
+from seidart_gpu import models
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4  # relative L2 of FP32 results against the FP64 oracle
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    nb = np.linalg.norm(b.ravel())
+    return np.linalg.norm((a - b).ravel()) / (nb if nb > 0 else 1.0)
+
+
+def assert_exact(g, o):
+    for name in ("fields", "memory"):
+        for q, (a, b) in enumerate(zip(g[name], o[name])):
+            assert np.array_equal(a, b), f"{name}[{q}] max |diff| {np.max(np.abs(a - b))}"
+    assert np.array_equal(g["traces"], o["traces"]), f"traces max |diff| {np.max(np.abs(g['traces'] - o['traces']))}"
+    assert np.array_equal(g["norms"], o["norms"]), "norms differ"
+
+
+def small_problems():
+    p1 = models.seismic2_two_layer(n=64, cpml=10, nt=150, src=(32, 12), nrec=16, rec_z=6, gamma=5.0)
+    p2 = models.electromag2_blocks(n=64, cpml=10, nt=200, src=(32, 12), nrec=16, rec_z=6, nblocks=5)
+    p2.model["e13"][:] = 0.4
+    p2.model["s13"][:] = 2e-4
+    p3 = models.seismic25_two_layer(n=48, cpml=8, nt=120, nrec=12)
+    p4 = models.electromag25_blocks(n=48, cpml=8, nt=150, nrec=12)
+    p5 = models.seismic3_layers(n=24, cpml=6, nt=40, nlayers=3, nrec_side=4, rec_z=3, src_z=6)
+    return {"seismic2": p1, "electromag2": p2, "seismic25": p3, "electromag25": p4, "seismic3": p5}
+
+
+PROBLEMS = small_problems()
+
+
+@pytest.mark.parametrize("name", list(PROBLEMS))
+def test_fp64_bit_exact(oracle, name):
+    p = PROBLEMS[name]
+    o = oracle.run_oracle(p)
+    g = sg.run(p, sg.FP64)
+    assert_exact(g, o)
+
+
+@pytest.mark.parametrize("name", list(PROBLEMS))
+def test_fp32_rel_l2(oracle, name):
+    p = PROBLEMS[name]
+    o = oracle.run_oracle(p)
+    g = sg.run(p, sg.FP32)
+    assert rel_l2(g["traces"], o["traces"]) <= FP32_TOL
+    for q in range(len(o["fields"])):
+        if np.linalg.norm(o["fields"][q]) > 0:
+            assert rel_l2(g["fields"][q], o["fields"][q]) <= FP32_TOL, f"field {q}"
+
+
+@pytest.mark.parametrize("density", ["harmonic", "geometric", "arithmetic", "none"])
+def test_seismic2_density_and_stress_source(oracle, density):
+    p = models.seismic2_two_layer(n=48, cpml=8, nt=100, src=(24, 10), nrec=8, rec_z=4, density=density, gamma=3.0)
+    p.src["xx"] = 0.2 * p.src["z"]
+    p.src["xz"] = -0.3 * p.src["z"]
+    p.src["zz"] = 0.1 * p.src["z"]
+    assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
+
+
+def test_seismic3_stress_source_and_norms(oracle):
+    p = models.seismic3_layers(n=20, cpml=5, nt=30, nlayers=2, nrec_side=3, rec_z=2, src_z=5, density="harmonic")
+    for k in ("xx", "xy", "xz", "yy", "yz", "zz"):
+        p.src[k] = 0.05 * p.src["z"]
+    p.src["x"] = 0.5 * p.src["z"]
+    p.src["y"] = -0.5 * p.src["z"]
+    assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
+
+
+@pytest.mark.parametrize("name", ["seismic2", "electromag2", "seismic3"])
+def test_chunked_stepping_matches_one_shot(name):
+    """Graph chunks of different lengths (and a tail) give the same state."""
+    p = PROBLEMS[name]
+    ref = sg.run(p, sg.FP64)
+    with sg.Solver(p, sg.FP64) as s:
+        for n in (1, 7, 64, 13):
+            if s.steps_done + n <= p.time_steps:
+                s.step(n)
+        s.step(p.time_steps - s.steps_done)
+        s.sync()
+        tr, nrm = s.traces()
+        f = s.get_fields()
+    assert np.array_equal(tr, ref["traces"])
+    for a, b in zip(f, ref["fields"]):
+        assert np.array_equal(a, b)
+
+
+def test_no_cpml_and_no_receivers(oracle):
+    """cpml = 0 (empty PML) and zero receivers."""
+    p = models.seismic2_two_layer(n=32, cpml=0, nt=40, src=(16, 10), nrec=4, rec_z=4)
+    p.receivers = None
+    g = sg.run(p, sg.FP64)
+    o = oracle.run_oracle(p)
+    for a, b in zip(g["fields"], o["fields"]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(g["norms"], o["norms"])
+
+
+def test_source_on_edge_is_zeroed(oracle):
+    """A source on the Dirichlet ring is injected and then zeroed, as in the reference."""
+    p = models.seismic2_two_layer(n=24, cpml=4, nt=30, src=(-3, 10), nrec=4, rec_z=4)
+    assert p.source_cell() % p.nx == 0
+    assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
+
+
+def test_unstable_reports_error(oracle):
+    """dt far above the CFL limit blows up; the solver returns SEIDART_ERR_UNSTABLE."""
+    p = models.seismic2_two_layer(n=32, cpml=4, nt=400, src=(16, 10), nrec=4, rec_z=4)
+    p.dt *= 4.0
+    o = oracle.run_oracle(p)
+    assert o["blowup"] is not None
+    with pytest.raises(sg.UnstableError) as e:
+        sg.run(p, sg.FP64)
+    assert f"step {o['blowup']}" in str(e.value)
