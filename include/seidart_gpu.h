@@ -22,6 +22,7 @@
  */
 #ifndef SEIDART_GPU_H
 #define SEIDART_GPU_H
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -187,8 +188,47 @@ int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, doubl
 /* Number of kernel launches the last seidart_solver_step call issued. */
 long long seidart_solver_launches(const SeidartSolver* s);
 int seidart_solver_destroy(SeidartSolver* s);
+/* Device pointer, element type and stream of field slot `slot` (for callers
+ * that read the live fields on the device, e.g. snapshot writers). */
+int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex,
+                                   int* is_fp32, size_t* ncell, void** stream);
 
 const char* seidart_last_error(void);
+
+/* ------------------------------------------------------- file contract
+ * The body of the reference subroutines with their file I/O: read every
+ * input record from directory `dir` (c11.dat ..., *_cpml.dat,
+ * initialcondition*.dat, seismicsource*.dat / electromagneticsource*.dat;
+ * src/fortran/seidartio.f08:161-292), run all time steps and write the
+ * per-step snapshots Vx|Vy|Vz|Ex|Ey|Ez.<it:06d>.<xind>[.<yind>].<zind>.dat
+ * (float32 records if single_output, else float64; seidartio.f08:366-426)
+ * and, for 3D, velocity_norm.dat / stress_norm.dat.  source_type "ac" loads
+ * the force components, any other the stress components (seismic); "pw"
+ * (plane wave) returns SEIDART_ERR_UNSUPPORTED.
+ * Replaces: seismic2/25/3, electromag2/25 in src/fortran/cpmlfdtd.f08. */
+int seidart_run_files(const char* dir, int family, int precision, const SeidartDomain* dom,
+                      const SeidartSource* src, int density_code, const char* source_type,
+                      int single_output, int write_snapshots);
+const char* seidart_io_last_error(void);
+
+/* Legacy entry points with the argument layout of legacy/cpmlfdtd_wrapper.c:7-16
+ * (padded nx[,ny],nz; spacings; PML thickness; src = interior source indices;
+ * number of steps; single-precision output flag).  They read the .dat inputs
+ * from the working directory and write the snapshots there; dt follows the
+ * legacy rule (legacy/cpmlfdtd_cbindings.f95:867-868 for the elastic case). */
+void seismic2_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output);
+void seismic25_(int nx, int ny, int nz, double dx, double dy, double dz, int npoints_pml, int* src,
+                int nstep, int single_output);
+void electromag2_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output);
+void electromag25_(int nx, int ny, int nz, double dx, double dy, double dz, int npoints_pml, int* src,
+                   int nstep, int single_output);
+void electromag2c_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output);
+void electromag25c_(int nx, int ny, int nz, double dx, double dy, double dz, int npoints_pml, int* src,
+                    int nstep, int single_output);
+
+/* `seidartfdtd <input.json> [seismic=true|false] [density_method=...]`
+ * (src/fortran/main.f08:31-119); returns the process exit status. */
+int seidart_cli_main(int argc, char** argv);
 
 #ifdef __cplusplus
 }

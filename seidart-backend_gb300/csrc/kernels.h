@@ -128,7 +128,11 @@ struct S3Args {
     T* traces;        // [nt][3][nrec]
     double* norms;    // [2][nt]: velocity norm, stress norm
     int nt;
+    double* norms_part;  // [2][64] per-step partial maxima (FP32 z-marching kernels)
 };
+// FP32 z-marching kernels of seismic3_fast.cu (the FP32 path of seismic3)
+void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+int seismic3_fast_norm_slots();
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 

@@ -126,6 +126,7 @@ struct SeidartSolver {
     int nrec = 0;
     void* traces = nullptr;
     double* norms = nullptr;
+    double* norms_part = nullptr;  // per-step partial maxima of the FP32 3D kernels
     int nnorm = 1;
     int steps_done = 0;
     int stress_src = 0;
@@ -422,6 +423,7 @@ void finish_args(SeidartSolver& s) {
         a.dx = (T)s.dom.dx; a.dy = (T)s.dom.dy; a.dz = (T)s.dom.dz; a.density_code = s.density;
         a.isrc = is; a.jsrc = js; a.ksrc = ks; a.stress_src = s.stress_src;
         a.nt = s.src.time_steps;
+        a.norms_part = s.norms_part;
         break;
     }
     }
@@ -437,7 +439,7 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : launch_electromag2_f64(s.e2d, si, st, h); break;
     case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : launch_seismic25_f64(s.s25d, si, st, h); break;
     case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
-    case SEIDART_SEISMIC3: f32 ? launch_seismic3_f32(s.s3f, si, st, h) : launch_seismic3_f64(s.s3d, si, st, h); break;
+    case SEIDART_SEISMIC3: f32 ? launch_seismic3_fast(s.s3f, si, st, h) : launch_seismic3_f64(s.s3d, si, st, h); break;
     }
 }
 
@@ -567,6 +569,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->rec_dev = (int*)s->carve(sizeof(int) * (nrec > 0 ? nrec : 1));
         s->traces = s->carve((size_t)src->time_steps * L.ncomp * (nrec > 0 ? nrec : 1) * cf * s->esize);
         s->norms = (double*)s->carve(sizeof(double) * src->time_steps * s->nnorm);
+        s->norms_part = (double*)s->carve(sizeof(double) * 2 * 64);
         if (pass == 0) {
             // model arrays: measured by running the set-up against a null arena
             derived.clear();
@@ -779,6 +782,17 @@ int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, doubl
 }
 
 int seidart_solver_steps_done(const SeidartSolver* s) { return s ? s->steps_done : -1; }
+
+int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex, int* is_fp32,
+                                   size_t* ncell, void** stream) {
+    if (!s || slot < 0 || slot >= (int)s->fields.size()) return set_err(SEIDART_ERR_ARG, "bad field slot");
+    if (dev) *dev = s->fields[slot];
+    if (is_complex) *is_complex = s->L.cplx;
+    if (is_fp32) *is_fp32 = s->precision == SEIDART_FP32;
+    if (ncell) *ncell = s->ncell;
+    if (stream) *stream = (void*)s->stream;
+    return SEIDART_OK;
+}
 
 void* seidart_solver_field_ptr(SeidartSolver* s, int slot) {
     if (!s || slot < 0 || slot >= (int)s->fields.size()) return nullptr;

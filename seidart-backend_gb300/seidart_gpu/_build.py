@@ -92,6 +92,14 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    exe = PKG / "seidartfdtd"
+    main_c = CSRC / "seidartfdtd_main.c"
+    if main_c.exists() and (force or not exe.exists() or _stale(exe, [LIB, main_c])):
+        cmd = [_nvcc(), *ARCH, "-o", str(exe), str(main_c), "-L", str(PKG), "-lseidart_gpu",
+               "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"seidartfdtd link failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

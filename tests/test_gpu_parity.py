@@ -81,6 +81,25 @@ def test_seismic3_stress_source_and_norms(oracle):
     assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
 
 
+@pytest.mark.parametrize("density", ["harmonic", "geometric", "arithmetic", "none"])
+def test_seismic3_fp32_stress_source_density(oracle, density):
+    """FP32 z-marching kernels: every source term, density rule and norm."""
+    p = models.seismic3_layers(n=30, cpml=6, nt=40, nlayers=3, nrec_side=4, rec_z=3, src_z=7, density=density)
+    for k in ("xx", "xy", "xz", "yy", "yz", "zz"):
+        p.src[k] = 0.05 * p.src["z"]
+    p.src["x"] = 0.5 * p.src["z"]
+    p.src["y"] = -0.5 * p.src["z"]
+    o = oracle.run_oracle(p)
+    g = sg.run(p, sg.FP32)
+    assert rel_l2(g["traces"], o["traces"]) <= FP32_TOL
+    for q in range(9):
+        assert rel_l2(g["fields"][q], o["fields"][q]) <= FP32_TOL, f"field {q}"
+    assert rel_l2(g["norms"], o["norms"]) <= FP32_TOL
+    for q in range(45):
+        if np.linalg.norm(o["memory"][q]) > 0:
+            assert rel_l2(g["memory"][q], o["memory"][q]) <= 10 * FP32_TOL, f"memory {q}"
+
+
 @pytest.mark.parametrize("name", ["seismic2", "electromag2", "seismic3"])
 def test_chunked_stepping_matches_one_shot(name):
     """Graph chunks of different lengths (and a tail) give the same state."""
