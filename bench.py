@@ -114,12 +114,10 @@ def kernel_bytes(p, box_cells: int) -> dict:
     shell (outside the inert interior box)."""
     n = p.ncell
     shell = n - box_cells
-    return {
-        # v(3) + C(21) + gamma(6) + sigma read(6) + sigma write(6); shell: 36 memories R+W + 6 coefficients
-        "s3f_stress": WORD * (42 * n + 78 * shell),
-        # sigma(6) + rho(1) + v R+W(6); shell: 9 memories R+W + 6 coefficients
-        "s3f_velocity": WORD * (13 * n + 24 * shell),
-    }
+    stress = WORD * (42 * n + 78 * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12; shell: 36 memories R+W + 6 coefficients
+    velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
+    # z-marching kernels (default) and one-thread-per-cell kernels
+    return {"s3f_stress": stress, "s3f_velocity": velocity, "s3_stress": stress, "s3_velocity": velocity}
 
 
 def step_bytes(p, box_cells: int) -> int:

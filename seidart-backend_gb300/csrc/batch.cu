@@ -1,0 +1,555 @@
+// batch.cu -- many 2D elastic models of uneven sizes in one persistent launch.
+//
+// Each model is a seismic2 problem (src/fortran/cpmlfdtd.f08:311-576) in the
+// FP32 arithmetic of seismic2.cu.  All models' tiles form one flattened work
+// list; a cooperative, persistent grid (co-resident CTAs, one per slot the
+// occupancy calculator allows) walks it three times per step:
+//   phase 1  stress half-step of every tile of every model
+//   phase 2  velocity half-step, force source, Dirichlet ring, norms
+//   phase 3  per model: stress source (non-'ac' sources), receiver gather
+// separated by a grid barrier whose spin is bounded: a barrier that does not
+// complete within its iteration budget sets an error word, every CTA returns,
+// and the host reports SEIDART_ERR_TIMEOUT.  Tile shape and CTAs per SM come
+// from an autotuner that times the candidates on the batch itself.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/seidart_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+struct BModel {
+    int nx, nz, density_code, isrc, jsrc, stress_src, nrec;
+    float dt, hx, hz;  // hx = 1/(24 dx), hz = 1/(24 dz)
+    BoxH box;
+    const float* m[16];  // S2_* slots; gamma -> 1/(1+gamma dt), kappa -> 1/kappa
+    float* f[5];
+    float* mem[12];
+    const double* src[5];
+    const int* rec;
+    float* traces;   // [nt][2][nrec]
+    double* norms;   // [nt]
+    int tile0, tiles_x, tiles;
+};
+
+struct BatchArgs {
+    const BModel* models;
+    const int* tile_model;  // flattened tile -> model
+    int nmodels, ntiles;
+    int* step;              // device step counter (1-based)
+    unsigned* bar_count;    // grid barrier arrival count
+    unsigned* bar_gen;      // grid barrier generation
+    int* status;            // 0 ok, 1 barrier timeout
+    long long spin_limit;   // barrier spin budget (iterations)
+    int force_timeout;      // test hook: expect one more arrival than exists
+};
+
+// Grid-wide barrier for a cooperative (co-resident) grid with a bounded wait.
+__device__ bool grid_barrier(const BatchArgs& B) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        volatile unsigned* gen = B.bar_gen;
+        volatile int* st = B.status;
+        const unsigned g = *gen;
+        __threadfence();
+        const unsigned expect = gridDim.x + (B.force_timeout ? 1u : 0u);
+        const unsigned arrived = atomicAdd(B.bar_count, 1u) + 1u;
+        int good = 1;
+        if (arrived == expect) {
+            *B.bar_count = 0;
+            __threadfence();
+            atomicAdd(B.bar_gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (*st != 0 || ++spins > B.spin_limit) {
+                    atomicExch(B.status, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good && (*st == 0);
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int TX, int TY>
+__device__ __forceinline__ bool tile_cell(const BatchArgs& B, int t, const BModel*& M, int& i, int& j) {
+    M = &B.models[B.tile_model[t]];
+    const int lt = t - M->tile0;
+    const int tx = lt % M->tiles_x, tz = lt / M->tiles_x;
+    i = tx * TX + threadIdx.x + 1;  // Fortran indices
+    j = tz * TY + threadIdx.y + 1;
+    return i <= M->nx && j <= M->nz;
+}
+
+#define IXM(fi, fk) ((size_t)((fi) - 1) + (size_t)nx * (size_t)((fk) - 1))
+
+// stress half-step of one cell (seismic2.cu FP32 arithmetic)
+__device__ __forceinline__ void cell_stress(const BModel& a, int i, int j) {
+    const int nx = a.nx, nz = a.nz;
+    const bool normal = (j >= 3 && j <= nz - 1 && i >= 2 && i <= nx - 2);
+    const bool shear = (j >= 2 && j <= nz - 2 && i >= 3 && i <= nx - 1);
+    if (!normal && !shear) return;
+    const size_t c = IXM(i, j);
+    const float* __restrict__ vx = a.f[0];
+    const float* __restrict__ vz = a.f[1];
+    const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
+    const float dt = a.dt, hx = a.hx, hz = a.hz;
+#define D4(p1, p0, p2, m1, h) ((27.0f * ((p1) - (p0)) - ((p2) - (m1))) * (h))
+    if (normal) {
+        float dvx_dx = D4(vx[IXM(i + 1, j)], vx[c], vx[IXM(i + 2, j)], vx[IXM(i - 1, j)], hx);
+        float dvz_dz = D4(vz[c], vz[IXM(i, j - 1)], vz[IXM(i, j + 1)], vz[IXM(i, j - 2)], hz);
+        float dvz_dx = D4(vz[IXM(i + 1, j)], vz[c], vz[IXM(i + 2, j)], vz[IXM(i - 1, j)], hx);
+        float dvx_dz = D4(vx[c], vx[IXM(i, j - 1)], vx[IXM(i, j + 1)], vx[IXM(i, j - 2)], hz);
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], b = a.m[14][c], aa = a.m[12][c];
+            const float M0 = bh * a.mem[0][c] + ah * dvx_dx, M1 = bh * a.mem[1][c] + ah * dvx_dz;
+            const float M3 = b * a.mem[3][c] + aa * dvz_dz, M2 = b * a.mem[2][c] + aa * dvz_dx;
+            a.mem[0][c] = M0; a.mem[1][c] = M1; a.mem[2][c] = M2; a.mem[3][c] = M3;
+            dvx_dx = dvx_dx * a.m[11][c] + M0;
+            dvx_dz = dvx_dz * a.m[11][c] + M1;
+            dvz_dz = dvz_dz * a.m[10][c] + M3;
+            dvz_dx = dvz_dx * a.m[10][c] + M2;
+        }
+        const float c11 = a.m[0][c], c13 = a.m[1][c], c15 = a.m[2][c], c33 = a.m[3][c], c35 = a.m[4][c];
+        a.f[2][c] = (a.f[2][c] + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * a.m[7][c];
+        a.f[3][c] = (a.f[3][c] + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * a.m[8][c];
+    }
+    if (shear) {
+        float dvx_dx = D4(vx[c], vx[IXM(i - 1, j)], vx[IXM(i + 1, j)], vx[IXM(i - 2, j)], hx);
+        float dvz_dz = D4(vz[IXM(i, j + 1)], vz[c], vz[IXM(i, j + 2)], vz[IXM(i, j - 1)], hz);
+        float dvz_dx = D4(vz[c], vz[IXM(i - 1, j)], vz[IXM(i + 1, j)], vz[IXM(i - 2, j)], hx);
+        float dvx_dz = D4(vx[IXM(i, j + 1)], vx[c], vx[IXM(i, j + 2)], vx[IXM(i, j - 1)], hz);
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
+            const float M4 = bh * a.mem[4][c] + ah * dvx_dx, M5 = bh * a.mem[5][c] + ah * dvx_dz;
+            const float M7 = bh * a.mem[7][c] + ah * dvz_dz, M6 = bh * a.mem[6][c] + ah * dvz_dx;
+            a.mem[4][c] = M4; a.mem[5][c] = M5; a.mem[6][c] = M6; a.mem[7][c] = M7;
+            dvx_dx = dvx_dx * kh + M4;
+            dvx_dz = dvx_dz * kh + M5;
+            dvz_dz = dvz_dz * kh + M7;
+            dvz_dx = dvz_dx * kh + M6;
+        }
+        const float c15 = a.m[2][c], c35 = a.m[4][c], c55 = a.m[5][c];
+        a.f[4][c] = (a.f[4][c] + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * a.m[9][c];
+    }
+#undef D4
+}
+
+// velocity half-step, force source, Dirichlet ring; returns the cell's |v|
+__device__ __forceinline__ double cell_velocity(const BModel& a, int i, int j, int it) {
+    const int nx = a.nx, nz = a.nz;
+    const size_t c = IXM(i, j);
+    const float *sxx = a.f[2], *szz = a.f[3], *sxz = a.f[4], *rho = a.m[6];
+    const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
+    const float dt = a.dt, hx = a.hx, hz = a.hz;
+    float vx = a.f[0][c], vz = a.f[1][c];
+    if (j >= 3 && j <= nz - 1 && i >= 3 && i <= nx - 1) {
+        const float bxx = inv_mean_f(rho[c], rho[IXM(i - 1, j)], a.density_code);
+        const float bzx = inv_mean_f(rho[c], rho[IXM(i, j - 1)], a.density_code);
+        float d1 = (27.0f * (sxx[c] - sxx[IXM(i - 1, j)]) + sxx[IXM(i - 2, j)]) * hx;
+        float d2 = (27.0f * (sxz[c] - sxz[IXM(i, j - 1)]) + sxz[IXM(i, j - 2)]) * hz;
+        if (pml) {
+            const float b = a.m[14][c], aa = a.m[12][c], k = a.m[10][c];
+            const float M8 = b * a.mem[8][c] + aa * d1, M11 = b * a.mem[11][c] + aa * d2;
+            a.mem[8][c] = M8; a.mem[11][c] = M11;
+            d1 = d1 * k + M8;
+            d2 = d2 * k + M11;
+        }
+        vx = vx + dt * (d1 * bxx + d2 * bzx);
+    }
+    if (j >= 2 && j <= nz - 2 && i >= 2 && i <= nx - 2) {
+        const float bxz = inv_mean_f(rho[c], rho[IXM(i + 1, j)], a.density_code);
+        const float bzz = inv_mean_f(rho[c], rho[IXM(i, j + 1)], a.density_code);
+        float d1 = (27.0f * (sxz[IXM(i + 1, j)] - sxz[c]) - sxz[IXM(i + 2, j)]) * hx;
+        float d2 = (27.0f * (szz[IXM(i, j + 1)] - szz[c]) - szz[IXM(i, j + 2)]) * hz;
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
+            const float M10 = bh * a.mem[10][c] + ah * d1, M9 = bh * a.mem[9][c] + ah * d2;
+            a.mem[10][c] = M10; a.mem[9][c] = M9;
+            d1 = d1 * kh + M10;
+            d2 = d2 * kh + M9;
+        }
+        vz = vz + dt * (d1 * bxz + d2 * bzz);
+    }
+    if (i - 1 == a.isrc && j - 1 == a.jsrc) {
+        if (a.src[0]) vx = vx + (float)a.src[0][it - 1] / rho[c];
+        if (a.src[1]) vz = vz + (float)a.src[1][it - 1] / rho[c];
+    }
+    if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0.f; vz = 0.f; }
+    a.f[0][c] = vx;
+    a.f[1][c] = vz;
+    return sqrt((double)vx * vx + (double)vz * vz);
+}
+
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) s2b_persistent(BatchArgs B, int nsteps) {
+    __shared__ double red[TX * TY / 32];
+    const int it0 = *B.step;
+    for (int s = 0; s < nsteps; ++s) {
+        const int it = it0 + s;
+        // phase 1: stress
+        for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
+            const BModel* M;
+            int i, j;
+            if (tile_cell<TX, TY>(B, t, M, i, j)) cell_stress(*M, i, j);
+        }
+        if (!grid_barrier(B)) return;
+        // phase 2: velocity, force source, Dirichlet, norms
+        for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
+            const BModel* M;
+            int i, j;
+            double n = 0.0;
+            if (tile_cell<TX, TY>(B, t, M, i, j)) n = cell_velocity(*M, i, j, it);
+            n = block_max<TX * TY / 32>(n, red);
+            if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&M->norms[it - 1], n);
+            __syncthreads();
+        }
+        if (!grid_barrier(B)) return;
+        // phase 3: per-model stress source and receivers
+        for (int m = blockIdx.x; m < B.nmodels; m += gridDim.x) {
+            const BModel& a = B.models[m];
+            const int tid = threadIdx.x + TX * threadIdx.y;
+            if (a.stress_src && tid == 0) {
+                const int nx = a.nx;
+                const size_t c = IXM(a.isrc + 1, a.jsrc + 1), c1 = IXM(a.isrc + 2, a.jsrc + 2);
+                const float* rho = a.m[6];
+                if (a.src[2]) a.f[2][c] = a.f[2][c] + (float)a.src[2][it - 1] / rho[c];
+                if (a.src[3]) a.f[4][c1] = a.f[4][c1] + (float)a.src[3][it - 1] / rho[c1];
+                if (a.src[4]) a.f[3][c] = a.f[3][c] + (float)a.src[4][it - 1] / rho[c];
+            }
+            for (int r = tid; r < a.nrec; r += TX * TY) {
+                const size_t base = (size_t)(it - 1) * 2 * a.nrec;
+                a.traces[base + r] = a.f[0][a.rec[r]];
+                a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
+            }
+        }
+        if (!grid_barrier(B)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) *B.step = it0 + nsteps;
+}
+
+struct Variant {
+    int tx, ty;
+    const void* fn;
+};
+const Variant kVariants[] = {
+    {32, 4, (const void*)s2b_persistent<32, 4>},
+    {32, 8, (const void*)s2b_persistent<32, 8>},
+    {64, 4, (const void*)s2b_persistent<64, 4>},
+    {32, 16, (const void*)s2b_persistent<32, 16>},
+    {64, 8, (const void*)s2b_persistent<64, 8>},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
+extern "C" int seidart_solver_internal_reset(SeidartSolver* s);
+extern "C" int seidart_solver_internal_advance(SeidartSolver* s, int nsteps);
+
+struct SeidartBatch {
+    int nmodels = 0;
+    std::vector<SeidartSolver*> solvers;  // each model's arena and state
+    BModel* dev_models[kNumVariants] = {nullptr};  // descriptors per tile-shape variant
+    int* dev_tile_model[kNumVariants] = {nullptr};
+    int ntiles[kNumVariants] = {0};
+    int* ctl = nullptr;  // step, barrier count, barrier generation, status
+    cudaStream_t stream = nullptr;
+    int variant = 1, bps = 1, nsm = 0;
+    int steps_done = 0, time_steps = 0;
+    long long spin_limit = 20000000;  // about a second of 64 ns sleeps
+    double tune_ms[kNumVariants][2] = {{0}};
+    int tune_bps[kNumVariants][2] = {{0}};
+    long long launches = 0;
+};
+
+namespace {
+std::string g_berr;
+int berr(int code, const std::string& m) {
+    g_berr = m;
+    return code;
+}
+
+int max_bps(int var) {
+    int n = 0;
+    const Variant& V = kVariants[var];
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, V.fn, V.tx * V.ty, 0) != cudaSuccess) return 0;
+    return n;
+}
+
+int launch_chunk(SeidartBatch* b, int var, int bps, int nsteps, int force_timeout) {
+    BatchArgs A{};
+    A.models = b->dev_models[var];
+    A.tile_model = b->dev_tile_model[var];
+    A.nmodels = b->nmodels;
+    A.ntiles = b->ntiles[var];
+    A.step = b->ctl;
+    A.bar_count = (unsigned*)(b->ctl + 1);
+    A.bar_gen = (unsigned*)(b->ctl + 2);
+    A.status = b->ctl + 3;
+    A.spin_limit = b->spin_limit;
+    A.force_timeout = force_timeout;
+    const Variant& V = kVariants[var];
+    if (bps < 1 || bps > max_bps(var)) return berr(SEIDART_ERR_ARG, "CTAs per SM outside the occupancy limit");
+    dim3 blk(V.tx, V.ty), grd(b->nsm * bps);
+    void* args[] = {&A, &nsteps};
+    const cudaError_t e = cudaLaunchCooperativeKernel(V.fn, grd, blk, args, 0, b->stream);
+    if (e != cudaSuccess) return berr(SEIDART_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
+    ++b->launches;
+    return SEIDART_OK;
+}
+
+int read_status(SeidartBatch* b, int* status) {
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return berr(SEIDART_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    int st = 0;
+    if (cudaMemcpy(&st, b->ctl + 3, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return berr(SEIDART_ERR_CUDA, "status read");
+    *status = st;
+    return SEIDART_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char* seidart_batch_last_error(void) { return g_berr.c_str(); }
+
+int seidart_batch_destroy(SeidartBatch* b) {
+    if (!b) return SEIDART_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (auto* s : b->solvers) seidart_solver_destroy(s);
+    for (int v = 0; v < kNumVariants; ++v) {
+        if (b->dev_models[v]) cudaFree(b->dev_models[v]);
+        if (b->dev_tile_model[v]) cudaFree(b->dev_tile_model[v]);
+    }
+    if (b->ctl) cudaFree(b->ctl);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SEIDART_OK;
+}
+
+int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* doms, const SeidartSource* srcs,
+                         const int* density_codes, const double* const* const* models,
+                         const double* const* const* srcfn, const int* nrec, const int* const* rec_cells) {
+    if (!out || nmodels < 1 || !doms || !srcs || !models) return berr(SEIDART_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    SeidartBatch* b = new SeidartBatch();
+    b->nmodels = nmodels;
+    b->time_steps = srcs[0].time_steps;
+    std::vector<BModel> hm;
+    for (int m = 0; m < nmodels; ++m) {
+        if (srcs[m].time_steps != b->time_steps) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_ARG, "all models of a batch advance together: time_steps must match");
+        }
+        SeidartSolver* s = nullptr;
+        const int rc = seidart_solver_create(&s, SEIDART_SEISMIC2, SEIDART_FP32, &doms[m], &srcs[m],
+                                             density_codes ? density_codes[m] : SEIDART_DENSITY_ARITHMETIC,
+                                             models[m], srcfn ? srcfn[m] : nullptr, nrec ? nrec[m] : 0,
+                                             rec_cells ? rec_cells[m] : nullptr);
+        if (rc != SEIDART_OK) {
+            seidart_batch_destroy(b);
+            return berr(rc, std::string("model ") + std::to_string(m) + ": " + seidart_last_error());
+        }
+        b->solvers.push_back(s);
+        S2Args<float> a;
+        const int* rec = nullptr;
+        seidart_solver_internal_s2f(s, &a, &rec);
+        BModel M{};
+        M.nx = a.nx; M.nz = a.nz; M.density_code = a.density_code; M.isrc = a.isrc; M.jsrc = a.jsrc;
+        M.stress_src = a.stress_src; M.nrec = nrec ? nrec[m] : 0;
+        M.dt = a.dt; M.hx = 1.0f / (24.0f * a.dx); M.hz = 1.0f / (24.0f * a.dz);
+        M.box = a.box;
+        for (int q = 0; q < 16; ++q) M.m[q] = a.m[q];
+        for (int q = 0; q < 5; ++q) M.f[q] = a.f[q];
+        for (int q = 0; q < 12; ++q) M.mem[q] = a.mem[q];
+        for (int q = 0; q < 5; ++q) M.src[q] = a.src[q];
+        M.rec = rec; M.traces = a.traces; M.norms = a.norms;
+        hm.push_back(M);
+    }
+    cudaDeviceProp prop;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaGetDeviceProperties(&prop, dev);
+    b->nsm = prop.multiProcessorCount;
+    if (!prop.cooperativeLaunch) { seidart_batch_destroy(b); return berr(SEIDART_ERR_UNSUPPORTED, "device lacks cooperative launch"); }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void**)&b->ctl, 4 * sizeof(int)) != cudaSuccess) {
+        seidart_batch_destroy(b);
+        return berr(SEIDART_ERR_NOMEM, "batch control allocation failed");
+    }
+    const int ctl0[4] = {1, 0, 0, 0};
+    cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    for (int v = 0; v < kNumVariants; ++v) {
+        std::vector<int> tm;
+        std::vector<BModel> mv = hm;
+        for (int m = 0; m < nmodels; ++m) {
+            mv[m].tiles_x = (mv[m].nx + kVariants[v].tx - 1) / kVariants[v].tx;
+            const int tz = (mv[m].nz + kVariants[v].ty - 1) / kVariants[v].ty;
+            mv[m].tile0 = (int)tm.size();
+            mv[m].tiles = mv[m].tiles_x * tz;
+            for (int q = 0; q < mv[m].tiles; ++q) tm.push_back(m);
+        }
+        b->ntiles[v] = (int)tm.size();
+        if (cudaMalloc((void**)&b->dev_tile_model[v], sizeof(int) * tm.size()) != cudaSuccess ||
+            cudaMalloc((void**)&b->dev_models[v], sizeof(BModel) * nmodels) != cudaSuccess) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_NOMEM, "tile table allocation failed");
+        }
+        cudaMemcpy(b->dev_tile_model[v], tm.data(), sizeof(int) * tm.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(b->dev_models[v], mv.data(), sizeof(BModel) * nmodels, cudaMemcpyHostToDevice);
+    }
+    b->variant = 1;
+    b->bps = std::max(1, max_bps(1));
+    *out = b;
+    return SEIDART_OK;
+}
+
+// Time every (tile shape, CTAs per SM) candidate on `trial_steps` steps of
+// the batch itself, keep the fastest, then reset every model to zero state
+// and step 1 (set the initial fields afterwards).
+int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, int* best_bps) {
+    if (!b || trial_steps < 1 || trial_steps > b->time_steps) return berr(SEIDART_ERR_ARG, "bad trial length");
+    double best = 1e300;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int v = 0; v < kNumVariants; ++v) {
+        const int mx = max_bps(v);
+        const int cand[2] = {mx, std::max(1, mx / 2)};
+        for (int q = 0; q < 2; ++q) {
+            const int bps = cand[q];
+            b->tune_bps[v][q] = bps;
+            b->tune_ms[v][q] = -1;
+            if (bps < 1 || (q == 1 && cand[1] == cand[0])) continue;
+            const int ctl0[4] = {1, 0, 0, 0};
+            cudaMemcpyAsync(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice, b->stream);
+            cudaEventRecord(e0, b->stream);
+            int rc = launch_chunk(b, v, bps, trial_steps, 0);
+            cudaEventRecord(e1, b->stream);
+            int st = 0;
+            if (rc == SEIDART_OK) rc = read_status(b, &st);
+            if (rc != SEIDART_OK || st != 0) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc != SEIDART_OK ? rc : berr(SEIDART_ERR_TIMEOUT, "grid barrier timed out during autotuning"); }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            b->tune_ms[v][q] = ms;
+            if (ms < best) { best = ms; b->variant = v; b->bps = bps; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto* s : b->solvers) {
+        const int rc = seidart_solver_internal_reset(s);
+        if (rc != SEIDART_OK) return berr(rc, seidart_last_error());
+    }
+    const int ctl0[4] = {1, 0, 0, 0};
+    cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    b->steps_done = 0;
+    if (best_variant) *best_variant = b->variant;
+    if (best_bps) *best_bps = b->bps;
+    return SEIDART_OK;
+}
+
+int seidart_batch_tuning(const SeidartBatch* b, int variant, int* tx, int* ty, int* bps, double* ms) {
+    if (!b || variant < 0 || variant >= kNumVariants) return berr(SEIDART_ERR_ARG, "bad variant");
+    if (tx) *tx = kVariants[variant].tx;
+    if (ty) *ty = kVariants[variant].ty;
+    for (int q = 0; q < 2; ++q) {
+        if (bps) bps[q] = b->tune_bps[variant][q];
+        if (ms) ms[q] = b->tune_ms[variant][q];
+    }
+    return SEIDART_OK;
+}
+
+int seidart_batch_set_config(SeidartBatch* b, int variant, int bps) {
+    if (!b || variant < 0 || variant >= kNumVariants || bps < 1 || bps > max_bps(variant))
+        return berr(SEIDART_ERR_ARG, "bad batch configuration");
+    b->variant = variant;
+    b->bps = bps;
+    return SEIDART_OK;
+}
+
+// Advance every model `nsteps` steps: one persistent cooperative launch per
+// chunk of steps.
+int seidart_batch_step(SeidartBatch* b, int nsteps, int chunk) {
+    if (!b || nsteps < 0 || b->steps_done + nsteps > b->time_steps) return berr(SEIDART_ERR_ARG, "steps exceed time_steps");
+    if (chunk < 1) chunk = nsteps > 0 ? nsteps : 1;
+    b->launches = 0;
+    for (int left = nsteps; left > 0;) {
+        const int n = std::min(left, chunk);
+        const int rc = launch_chunk(b, b->variant, b->bps, n, 0);
+        if (rc != SEIDART_OK) return rc;
+        left -= n;
+    }
+    b->steps_done += nsteps;
+    for (auto* s : b->solvers) seidart_solver_internal_advance(s, nsteps);
+    return SEIDART_OK;
+}
+
+// Wait; SEIDART_ERR_TIMEOUT if a grid barrier gave up, SEIDART_ERR_UNSTABLE
+// (first model / step) if a norm exceeded 1e25.
+int seidart_batch_sync(SeidartBatch* b) {
+    if (!b) return berr(SEIDART_ERR_ARG, "NULL batch");
+    int st = 0;
+    int rc = read_status(b, &st);
+    if (rc != SEIDART_OK) return rc;
+    if (st != 0) return berr(SEIDART_ERR_TIMEOUT, "a grid barrier did not complete within its spin budget");
+    for (int m = 0; m < b->nmodels; ++m) {
+        rc = seidart_solver_sync(b->solvers[m]);
+        if (rc != SEIDART_OK) return berr(rc, std::string("model ") + std::to_string(m) + ": " + seidart_last_error());
+    }
+    return SEIDART_OK;
+}
+
+// Test hook for the bounded barrier: one chunk whose barrier expects one CTA
+// more than the grid has; every CTA gives up after `spin_limit` spins.
+int seidart_batch_force_timeout(SeidartBatch* b, long long spin_limit) {
+    if (!b) return berr(SEIDART_ERR_ARG, "NULL batch");
+    const long long keep = b->spin_limit;
+    b->spin_limit = spin_limit;
+    int rc = launch_chunk(b, b->variant, b->bps, 1, 1);
+    b->spin_limit = keep;
+    if (rc != SEIDART_OK) return rc;
+    int st = 0;
+    rc = read_status(b, &st);
+    if (rc != SEIDART_OK) return rc;
+    // clear the status and barrier words for later use
+    const int ctl_clear[3] = {0, 0, 0};
+    cudaMemcpy(b->ctl + 1, ctl_clear, sizeof ctl_clear, cudaMemcpyHostToDevice);
+    return st != 0 ? SEIDART_ERR_TIMEOUT : SEIDART_OK;
+}
+
+SeidartSolver* seidart_batch_model(SeidartBatch* b, int m) {
+    return (b && m >= 0 && m < b->nmodels) ? b->solvers[m] : nullptr;
+}
+int seidart_batch_steps_done(const SeidartBatch* b) { return b ? b->steps_done : -1; }
+long long seidart_batch_launches(const SeidartBatch* b) { return b ? b->launches : -1; }
+int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid) {
+    if (!b) return berr(SEIDART_ERR_ARG, "NULL batch");
+    if (tx) *tx = kVariants[b->variant].tx;
+    if (ty) *ty = kVariants[b->variant].ty;
+    if (bps) *bps = b->bps;
+    if (grid) *grid = b->bps * b->nsm;
+    return SEIDART_OK;
+}
+int seidart_batch_num_variants(void) { return kNumVariants; }
+int seidart_batch_set_stream_sync(SeidartBatch* b) {
+    return b ? (cudaStreamSynchronize(b->stream) == cudaSuccess ? SEIDART_OK : SEIDART_ERR_CUDA) : SEIDART_ERR_ARG;
+}
+
+}  // extern "C"

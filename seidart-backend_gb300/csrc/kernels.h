@@ -2,6 +2,7 @@
 // (solver.cu) and the per-family kernel files.  Each launcher exists twice,
 // suffixed _f64 (drop-in FP64 build) and _f32 (fast FP32 build).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -129,10 +130,21 @@ struct S3Args {
     double* norms;    // [2][nt]: velocity norm, stress norm
     int nt;
     double* norms_part;  // [2][64] per-step partial maxima (FP32 z-marching kernels)
+    int* err;            // device error word: 1 = a bounded wait gave up
 };
-// FP32 z-marching kernels of seismic3_fast.cu (the FP32 path of seismic3)
-void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+// TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
+// (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes
+struct S3Maps {
+    CUtensorMap coef[33];
+    CUtensorMap v[3];
+};
+// FP32 z-marching kernels of seismic3_fast.cu (the FP32 path of seismic3);
+// with `maps` the stress half-step runs the TMA-fed kernel of seismic3_tma.cu
+void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr,
+                          const S3Maps* maps = nullptr);
 int seismic3_fast_norm_slots();
+bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps);
+void launch_seismic3_tma_stress(const S3Args<float>& a, const S3Maps& maps, cudaStream_t st);
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 

@@ -205,6 +205,7 @@ __global__ void __launch_bounds__(TX* TY, 2) s3f_velocity(S3Args<float> A, StepI
     qzz[0] = col ? ldz(F[8], g, gx, gy, kb) : 0.f; qzz[1] = col ? ldz(F[8], g, gx, gy, kb + 1) : 0.f;
     qr[0] = col ? ldz(A.rho, g, gx, gy, kb - 1) : 0.f; qr[1] = col ? ldz(A.rho, g, gx, gy, kb) : 0.f;
     double vmax = 0.0, smax = 0.0;
+    float vsq = 0.f, ssq = 0.f;
     for (int k = kb; k < ke; ++k) {
         const size_t c = g.at(gx, gy, k);
         qzz[2] = col ? ldz(F[8], g, gx, gy, k + 2) : 0.f;
@@ -286,12 +287,22 @@ __global__ void __launch_bounds__(TX* TY, 2) s3f_velocity(S3Args<float> A, StepI
             F[0][c] = vx;
             F[1][c] = vy;
             F[2][c] = vz;
-            vmax = nanmax(vmax, sqrt((double)vx * vx + (double)vy * vy + (double)vz * vz));
+            // squared norms in FP32 (FP64 throughput on this part is a small
+            // fraction of FP32); squares that would overflow FP32, or NaN,
+            // take the FP64 route so the blow-up test stays exact
+            const float vs = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+            if (vs < 3.0e38f) vsq = fmaxf(vsq, vs);
+            else vmax = nanmax(vmax, sqrt((double)vx * vx + (double)vy * vy + (double)vz * vz));
             const bool src_cell = A.stress_src && ((gx == is && gy == js && k == ks) || (gx == is + 1 && gy == js + 1 && k == ks) ||
                                                    (gx == is + 1 && gy == js && k == ks + 1) || (gx == is && gy == js + 1 && k == ks + 1));
             if (!src_cell) {
-                const double s1 = sxx, s2 = syy, s3 = qzz[0], s4 = sxy, s5 = qyz[2], s6 = qxz[2];
-                smax = nanmax(smax, sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6)));
+                const float s1 = sxx, s2 = syy, s3 = qzz[0], s4 = sxy, s5 = qyz[2], s6 = qxz[2];
+                const float ss = fmaf(s1, s1, fmaf(s2, s2, s3 * s3)) + 2.0f * fmaf(s4, s4, fmaf(s5, s5, s6 * s6));
+                if (ss < 3.0e38f) ssq = fmaxf(ssq, ss);
+                else {
+                    const double d1 = s1, d2 = s2, d3 = s3, d4 = s4, d5 = s5, d6 = s6;
+                    smax = nanmax(smax, sqrt(d1 * d1 + d2 * d2 + d3 * d3 + 2.0 * (d4 * d4 + d5 * d5 + d6 * d6)));
+                }
             }
         }
         __syncthreads();
@@ -300,6 +311,8 @@ __global__ void __launch_bounds__(TX* TY, 2) s3f_velocity(S3Args<float> A, StepI
         qzz[0] = qzz[1]; qzz[1] = qzz[2];
         qr[0] = qr[1]; qr[1] = qr[2];
     }
+    vmax = nanmax(vmax, sqrt((double)vsq));
+    smax = nanmax(smax, sqrt((double)ssq));
     vmax = block_max<TX * TY / 32>(vmax, red[0]);
     smax = block_max<TX * TY / 32>(smax, red[1]);
     if (tid == 0) {
@@ -365,10 +378,16 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
 
 }  // namespace
 
-void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h) {
+void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
+                          const S3Maps* maps) {
     const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
-    s3f_stress<<<grd, blk, 0, st>>>(a);
-    if (h) h->fn(h->ctx, 0, "s3f_stress");
+    if (maps) {
+        launch_seismic3_tma_stress(a, *maps, st);
+        if (h) h->fn(h->ctx, 0, "s3t_stress");
+    } else {
+        s3f_stress<<<grd, blk, 0, st>>>(a);
+        if (h) h->fn(h->ctx, 0, "s3f_stress");
+    }
     s3f_velocity<<<grd, blk, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 1, "s3f_velocity");
     if (a.stress_src) {

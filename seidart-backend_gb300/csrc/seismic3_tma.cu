@@ -1,0 +1,293 @@
+// seismic3_tma.cu -- FP32 3D stress half-step fed by TMA bulk tensor copies.
+//
+// The stress half-step of seismic3 (src/fortran/cpmlfdtd.f08:1761-1992)
+// streams 33 read-once arrays per cell (21 C_ij, 6 attenuation factors, the
+// 6 old stresses) plus the velocity stencil.  Issuing those loads from
+// threads leaves too few bytes in flight per SM, so here one elected thread
+// issues `cp.async.bulk.tensor` copies of whole 32x8 plane tiles into shared
+// memory, several planes ahead of the compute, and an mbarrier per stage
+// signals their arrival:
+//   * coefficient stages: the 33 tiles of one z plane (33 KiB);
+//   * velocity ring: vx, vy, vz planes k-2 .. k+2 with a 4/2-cell x/y halo
+//     (40 x 12 boxes), so every stencil read is a shared-memory read;
+//   * CPML memories and coefficients (shell cells only) use plain loads.
+// Every mbarrier wait is bounded: on expiry the CTA raises the solver's
+// error word, waits (bounded) for its own copies in flight and returns; the
+// host then reports SEIDART_ERR_TIMEOUT.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+constexpr int TX = 32, TY = 8;
+constexpr int VXB = TX + 8, VYB = TY + 4;  // velocity box: x from x0-4 (16-byte aligned), y from y0-2
+constexpr int NCOEF = 33;                  // C 21 + gamma 6 + sigma 6
+constexpr int SC = 2;                      // coefficient stages in flight
+constexpr int RV = 7;                      // velocity ring planes (5 in use + 2 ahead)
+constexpr int ZCH = 32;                    // planes per CTA
+constexpr long long WAIT_LIMIT = 1 << 20;  // bounded mbarrier polling
+
+struct __align__(128) Smem {
+    float coef[SC][NCOEF][TY][TX];
+    float v[RV][3][VYB][VXB];
+    unsigned long long full_c[SC];
+    unsigned long long full_v[RV];
+};
+
+__device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(sa(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false if the copy did not land within the budget
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
+    for (long long it = 0; it < WAIT_LIMIT; ++it)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            sa(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(sa(bar))
+        : "memory");
+}
+
+struct CpmlC {
+    float b, a, k;
+};
+__device__ __forceinline__ CpmlC cpml_at(const S3Args<float>& A, size_t c, bool half) {
+    return half ? CpmlC{__ldcs(A.cpml[5] + c), __ldcs(A.cpml[3] + c), __ldcs(A.cpml[1] + c)}
+                : CpmlC{__ldcs(A.cpml[4] + c), __ldcs(A.cpml[2] + c), __ldcs(A.cpml[0] + c)};
+}
+__device__ __forceinline__ float cpml_apply(float* m, size_t c, const CpmlC& p, float d) {
+    const float mv = p.b * m[c] + p.a * d;
+    m[c] = mv;
+    return d * p.k + mv;
+}
+template <int L>
+__device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, float (&gx)[3], float (&gy)[3],
+                                          float (&gz)[3]) {
+    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
+    const CpmlC px = cpml_at(A, c, xh), py = cpml_at(A, c, yh), pz = cpml_at(A, c, zh);
+    float* const* M = A.mem + 9 * (L - 1);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        gx[f] = cpml_apply(M[3 * f], c, px, gx[f]);
+        gy[f] = cpml_apply(M[3 * f + 1], c, py, gy[f]);
+        if (L == 2 && f == 0) {
+            // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
+            // (reference quirk, cpmlfdtd.f08:1855-1866)
+            M[2][c] = pz.b * M[2][c] + pz.a * gz[0];
+        } else {
+            gz[f] = cpml_apply(M[3 * f + 2], c, pz, gz[f]);
+        }
+    }
+}
+
+// coefficient tile order in a stage: C 0..20, gamma 21..26, sigma 27..32
+// (sigma slots in S3 field order: xx, xy, xz, yy, yz, zz)
+__device__ __forceinline__ float stress_new(const float (*cf)[TY][TX], int ty, int tx, int sidx, int c1, int c2,
+                                            int c3, int c4, int c5, int c6, int gidx, float dt, const float (&gx)[3],
+                                            const float (&gy)[3], const float (&gz)[3]) {
+    const float acc = cf[c1][ty][tx] * gx[0] + cf[c2][ty][tx] * gy[1] + cf[c3][ty][tx] * gz[2] +
+                      cf[c4][ty][tx] * (gz[1] + gy[2]) + cf[c5][ty][tx] * (gz[0] + gx[2]) +
+                      cf[c6][ty][tx] * (gx[1] + gy[0]);
+    return (cf[27 + sidx][ty][tx] + acc * dt) * cf[21 + gidx][ty][tx];
+}
+
+__global__ void __launch_bounds__(TX* TY, 2) s3t_stress(S3Args<float> A, const __grid_constant__ S3Maps maps) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int gx = x0 + tx, gy = y0 + ty;
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    const int kb = blockIdx.z * ZCH, ke = min(kb + ZCH, nz);
+    const size_t sxy = (size_t)nx * ny;
+    const bool col = gx < nx && gy < ny;
+    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+    const float dt = A.dt;
+    const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
+    const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
+    const bool colbox = A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1;
+    const unsigned coef_bytes = NCOEF * TX * TY * sizeof(float);
+    const unsigned v_bytes = 3 * VXB * VYB * sizeof(float);
+
+    // producer state (thread 0): copies in flight and the phase parity each
+    // will complete, for the bounded drain on the error path
+    unsigned pend_c = 0, pend_v = 0, par_c = 0, par_v = 0;
+    auto issue_coef = [&](int p) {
+        const int s = (p - kb) % SC;
+        mbar_expect_tx(&S.full_c[s], coef_bytes);
+        for (int a = 0; a < NCOEF; ++a) tma3(&S.coef[s][a][0][0], &maps.coef[a], x0, y0, p, &S.full_c[s]);
+        pend_c |= 1u << s;
+        par_c = (par_c & ~(1u << s)) | ((((unsigned)(p - kb) / SC) & 1u) << s);
+    };
+    auto issue_v = [&](int p) {
+        const int s = (p - (kb - 2)) % RV;
+        mbar_expect_tx(&S.full_v[s], v_bytes);
+        for (int f = 0; f < 3; ++f) tma3(&S.v[s][f][0][0], &maps.v[f], x0 - 4, y0 - 2, p, &S.full_v[s]);
+        pend_v |= 1u << s;
+        par_v = (par_v & ~(1u << s)) | ((((unsigned)(p - (kb - 2)) / RV) & 1u) << s);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < SC; ++s) mbar_init(&S.full_c[s], 1);
+        for (int s = 0; s < RV; ++s) mbar_init(&S.full_v[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int p = kb - 2; p < kb - 2 + RV && p <= ke + 1; ++p) issue_v(p);
+        for (int p = kb; p < kb + SC && p < ke; ++p) issue_coef(p);
+    }
+    __syncthreads();
+    bool fail = false;
+    // the first four velocity planes (kb-2 .. kb+1)
+    for (int p = kb - 2; p <= kb + 1 && !fail; ++p) fail = !mbar_wait(&S.full_v[(p - (kb - 2)) % RV], 0);
+
+    for (int k = kb; k < ke; ++k) {
+        const int sc = (k - kb) % SC, sv2 = (k + 2 - (kb - 2)) % RV;
+        if (!fail) fail = !mbar_wait(&S.full_c[sc], ((k - kb) / SC) & 1);
+        if (!fail) fail = !mbar_wait(&S.full_v[sv2], ((k + 2 - (kb - 2)) / RV) & 1);
+        if (__syncthreads_or(fail)) { fail = true; break; }
+        if (tid == 0) pend_c &= ~(1u << sc);
+        if (tid == 0) pend_v &= ~(1u << sv2);
+        const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+        const bool L1 = col && x14 && y13 && z12, L2 = col && x23 && y24 && z12;
+        const bool L3 = col && x23 && y13 && z34, L4 = col && x14 && y24 && z34;
+        if (L1 || L2 || L3 || L4) {
+            const size_t c = (size_t)gx + (size_t)nx * gy + sxy * k;
+            float fx[3], bx[3], fy[3], by[3], fz[3], bz[3];
+            const int r0 = (k - (kb - 2)) % RV;  // slot of plane k
+            const int rm2 = (k - 2 - (kb - 2)) % RV, rm1 = (k - 1 - (kb - 2)) % RV;
+            const int rp1 = (k + 1 - (kb - 2)) % RV, rp2 = sv2;
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                const float* r = &S.v[r0][f][ty + 2][tx + 4];
+                fx[f] = (27.0f * (r[1] - r[0]) - (r[2] - r[-1])) * hx;
+                bx[f] = (27.0f * (r[0] - r[-1]) - (r[1] - r[-2])) * hx;
+                fy[f] = (27.0f * (r[VXB] - r[0]) - (r[2 * VXB] - r[-VXB])) * hy;
+                by[f] = (27.0f * (r[0] - r[-VXB]) - (r[VXB] - r[-2 * VXB])) * hy;
+                const float qm2 = S.v[rm2][f][ty + 2][tx + 4], qm1 = S.v[rm1][f][ty + 2][tx + 4];
+                const float qp1 = S.v[rp1][f][ty + 2][tx + 4], qp2 = S.v[rp2][f][ty + 2][tx + 4];
+                fz[f] = (27.0f * (qp1 - r[0]) - (qp2 - qm1)) * hz;
+                bz[f] = (27.0f * (r[0] - qm1) - (qp1 - qm2)) * hz;
+            }
+            const bool pml = !(colbox && A.box.k0 <= k && k < A.box.k1);
+            const float(*cf)[TY][TX] = S.coef[sc];
+            // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
+            //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
+            // sigma slot (27+): 0 xx 1 xy 2 xz 3 yy 4 yz 5 zz; gamma (21+): x y z xy yz xz
+            if (L1) {
+                float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+                if (pml) loop_cpml<1>(A, c, ex, ey, ez);
+                __stcs(A.f[3] + c, stress_new(cf, ty, tx, 0, 0, 1, 2, 3, 4, 5, 0, dt, ex, ey, ez));
+                __stcs(A.f[6] + c, stress_new(cf, ty, tx, 3, 1, 6, 7, 8, 9, 10, 1, dt, ex, ey, ez));
+                __stcs(A.f[8] + c, stress_new(cf, ty, tx, 5, 2, 7, 11, 12, 13, 14, 2, dt, ex, ey, ez));
+            }
+            if (L2) {
+                float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+                if (pml) loop_cpml<2>(A, c, ex, ey, ez);
+                __stcs(A.f[4] + c, stress_new(cf, ty, tx, 1, 5, 10, 14, 17, 19, 20, 3, dt, ex, ey, ez));
+            }
+            if (L3) {
+                float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+                if (pml) loop_cpml<3>(A, c, ex, ey, ez);
+                __stcs(A.f[5] + c, stress_new(cf, ty, tx, 2, 4, 9, 13, 16, 18, 19, 5, dt, ex, ey, ez));
+            }
+            if (L4) {
+                float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+                if (pml) loop_cpml<4>(A, c, ex, ey, ez);
+                __stcs(A.f[7] + c, stress_new(cf, ty, tx, 4, 3, 8, 12, 15, 16, 17, 4, dt, ex, ey, ez));
+            }
+        }
+        __syncthreads();  // stage sc and ring slot of plane k-2 are free again
+        if (tid == 0) {
+            // order the threads' shared-memory reads before the async-proxy refills
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if (k + SC < ke) issue_coef(k + SC);
+            const int pn = k - 2 + RV;
+            if (pn <= ke + 1) issue_v(pn);
+        }
+    }
+    if (fail && tid == 0) {
+        atomicExch(A.err, 1);
+        // wait (bounded) for this CTA's copies in flight before shared memory is released
+        for (int s = 0; s < SC; ++s)
+            if (pend_c >> s & 1) mbar_wait(&S.full_c[s], par_c >> s & 1);
+        for (int s = 0; s < RV; ++s)
+            if (pend_v >> s & 1) mbar_wait(&S.full_v[s], par_v >> s & 1);
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx, int by) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)base, dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Build the tensor maps for a solver's arrays; false when the grid does not
+// meet the TMA rules (row pitch a multiple of 16 bytes) or the driver entry
+// point is unavailable, in which case the caller keeps the thread-load kernel.
+bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps) {
+    if (a.nx % 4 != 0) return false;
+    for (int q = 0; q < 21; ++q)
+        if (!make_map(&maps->coef[q], a.C[q], a.nx, a.ny, a.nz, TX, TY)) return false;
+    for (int q = 0; q < 6; ++q)
+        if (!make_map(&maps->coef[21 + q], a.g[q], a.nx, a.ny, a.nz, TX, TY)) return false;
+    // old stresses in field order xx, xy, xz, yy, yz, zz (slots 3..8)
+    for (int q = 0; q < 6; ++q)
+        if (!make_map(&maps->coef[27 + q], a.f[3 + q], a.nx, a.ny, a.nz, TX, TY)) return false;
+    for (int f = 0; f < 3; ++f)
+        if (!make_map(&maps->v[f], a.f[f], a.nx, a.ny, a.nz, VXB, VYB)) return false;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(s3t_stress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)) !=
+            cudaSuccess)
+            return false;
+        attr = true;
+    }
+    return true;
+}
+
+void launch_seismic3_tma_stress(const S3Args<float>& a, const S3Maps& maps, cudaStream_t st) {
+    const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
+    s3t_stress<<<grd, blk, sizeof(Smem), st>>>(a, maps);
+}

@@ -16,6 +16,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <string>
@@ -127,6 +128,12 @@ struct SeidartSolver {
     void* traces = nullptr;
     double* norms = nullptr;
     double* norms_part = nullptr;  // per-step partial maxima of the FP32 3D kernels
+    // FP32 3D kernel family: 0 z-marching tiles (default), 1 one thread per
+    // cell (env SEIDART_S3_KERNEL=cell selects it, for comparisons)
+    int s3_kernel = 0;
+    bool s3_tma = false;  // TMA-fed stress kernel usable (grid meets the TMA rules)
+    S3Maps s3_maps;       // its tensor maps
+    int* err_dev = nullptr;  // error word raised by bounded device waits
     int nnorm = 1;
     int steps_done = 0;
     int stress_src = 0;
@@ -424,6 +431,7 @@ void finish_args(SeidartSolver& s) {
         a.isrc = is; a.jsrc = js; a.ksrc = ks; a.stress_src = s.stress_src;
         a.nt = s.src.time_steps;
         a.norms_part = s.norms_part;
+        a.err = s.err_dev;
         break;
     }
     }
@@ -439,7 +447,11 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : launch_electromag2_f64(s.e2d, si, st, h); break;
     case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : launch_seismic25_f64(s.s25d, si, st, h); break;
     case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
-    case SEIDART_SEISMIC3: f32 ? launch_seismic3_fast(s.s3f, si, st, h) : launch_seismic3_f64(s.s3d, si, st, h); break;
+    case SEIDART_SEISMIC3:
+        if (!f32) launch_seismic3_f64(s.s3d, si, st, h);
+        else if (s.s3_kernel == 1) launch_seismic3_f32(s.s3f, si, st, h);
+        else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr);
+        break;
     }
 }
 
@@ -540,6 +552,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     s->esize = precision == SEIDART_FP32 ? 4 : 8;
     s->nrec = nrec;
     s->nnorm = is3 ? 2 : 1;
+    if (const char* k = getenv("SEIDART_S3_KERNEL")) s->s3_kernel = strcmp(k, "cell") == 0 ? 1 : 0;
     s->box = interior_box(*s, model);
     for (int q = 0; q < L.nsrc; ++q) {
         // stress-source series are every slot after the force components
@@ -570,6 +583,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->traces = s->carve((size_t)src->time_steps * L.ncomp * (nrec > 0 ? nrec : 1) * cf * s->esize);
         s->norms = (double*)s->carve(sizeof(double) * src->time_steps * s->nnorm);
         s->norms_part = (double*)s->carve(sizeof(double) * 2 * 64);
+        s->err_dev = (int*)s->carve(sizeof(int));
         if (pass == 0) {
             // model arrays: measured by running the set-up against a null arena
             derived.clear();
@@ -613,6 +627,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         }
     }
     if (precision == SEIDART_FP32) finish_args<float>(*s); else finish_args<double>(*s);
+    if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_kernel == 0) {
+        const char* t = getenv("SEIDART_S3_TMA");
+        if (!(t && strcmp(t, "0") == 0)) s->s3_tma = seismic3_tma_prepare(s->s3f, &s->s3_maps);
+    }
     *out = s;
     return SEIDART_OK;
 }
@@ -709,6 +727,11 @@ int seidart_solver_sync(SeidartSolver* s) {
     if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     CUDA_TRY(cudaGetLastError());
+    if (s->err_dev) {
+        int err = 0;
+        CUDA_TRY(cudaMemcpy(&err, s->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return set_err(SEIDART_ERR_TIMEOUT, "a bounded device wait (TMA copy) did not complete");
+    }
     if (s->steps_done == 0) return SEIDART_OK;
     std::vector<double> nrm(s->steps_done);
     CUDA_TRY(cudaMemcpy(nrm.data(), s->norms, sizeof(double) * s->steps_done, cudaMemcpyDeviceToHost));
@@ -809,6 +832,38 @@ int seidart_solver_destroy(SeidartSolver* s) {
     if (s->arena) cudaFree(s->arena);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
+    return SEIDART_OK;
+}
+
+// ---- internal hooks for the batched runtime (batch.cu); not part of the ABI
+int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec) {
+    if (!s || s->family != SEIDART_SEISMIC2 || s->precision != SEIDART_FP32) return set_err(SEIDART_ERR_ARG, "not an FP32 seismic2 solver");
+    *out = s->s2f;
+    if (rec) *rec = s->rec_dev;
+    return SEIDART_OK;
+}
+
+// zero fields, memories, traces and norms; back to step 1
+int seidart_solver_internal_reset(SeidartSolver* s) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const size_t n = s->ncell * (s->L.cplx ? 2 : 1) * s->esize;
+    for (void* f : s->fields) CUDA_TRY(cudaMemsetAsync(f, 0, n, s->stream));
+    for (void* m : s->mem) CUDA_TRY(cudaMemsetAsync(m, 0, n, s->stream));
+    const size_t tr = (size_t)s->src.time_steps * s->L.ncomp * (s->nrec > 0 ? s->nrec : 1) * (s->L.cplx ? 2 : 1) * s->esize;
+    CUDA_TRY(cudaMemsetAsync(s->traces, 0, tr, s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->norms, 0, sizeof(double) * s->src.time_steps * s->nnorm, s->stream));
+    const int one = 1;
+    CUDA_TRY(cudaMemcpyAsync(s->step_dev, &one, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->steps_done = 0;
+    return SEIDART_OK;
+}
+
+// account for steps advanced by another runtime on this solver's state
+int seidart_solver_internal_advance(SeidartSolver* s, int nsteps) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    s->steps_done += nsteps;
     return SEIDART_OK;
 }
 

@@ -326,3 +326,52 @@ def electromag25_blocks(n: int = 128, cpml: int = 10, nt: int = 400, h: float = 
                    xind=n // 2, zind=n // 4, model=model, src={"x": w, "y": 0.5 * w, "z": 0.25 * w},
                    receivers=rec.astype(np.int32), ky=ky,
                    meta={"vmax": vmax, "f0": f0, "seed": seed, "config": "electromag25 blocks"})
+
+
+# ------------------------------------------------------------ ragged batch
+def batch_layered_vti(nmodels: int = 64, nt: int = 3000, cpml: int = 20, seed: int = 5, nmin: int = 256,
+                      nmax: int = 1024, step: int = 32, nrec: int = 64, h: float = 1.0) -> list:
+    """The ragged multi-model workload: ``nmodels`` 2D elastic models with nx,
+    nz drawn uniformly from [nmin, nmax] in multiples of ``step``, each a
+    stack of 2-5 VTI layers with stiffness and density drawn from the ranges
+    of the two-layer model, its own Ricker source (f0 ~ U[30, 90] Hz) at a
+    random position in the top 20%, and ``nrec`` receivers; every model keeps
+    its own Courant-0.5 time step."""
+    rng = np.random.default_rng(seed)
+    out = []
+    sizes = np.arange(nmin, nmax + 1, step)
+    lo = {k: min(TWO_LAYER_TOP[k], TWO_LAYER_BOTTOM[k]) for k in TWO_LAYER_TOP}
+    hi = {k: max(TWO_LAYER_TOP[k], TWO_LAYER_BOTTOM[k]) for k in TWO_LAYER_TOP}
+    for m in range(nmodels):
+        nx, nz = int(rng.choice(sizes)), int(rng.choice(sizes))
+        nl = int(rng.integers(2, 6))
+        bounds = np.sort(rng.choice(np.arange(1, nz), size=nl - 1, replace=False)) if nl > 1 else []
+        lid = np.searchsorted(bounds, np.arange(nz), side="right")
+        lay = []
+        for _ in range(nl):
+            d = {k: rng.uniform(lo[k], hi[k]) for k in ("c11", "c33", "c55", "rho")}
+            d["c13"] = rng.uniform(lo["c13"], hi["c13"])
+            d["c15"] = d["c35"] = 0.0
+            lay.append(d)
+        mod = {k: np.empty((nx, nz)) for k in ("c11", "c13", "c15", "c33", "c35", "c55", "rho")}
+        for k in mod:
+            mod[k][:, :] = np.array([lay[L][k] for L in lid])[None, :]
+        rho_min = min(L["rho"] for L in lay)
+        vmax = max(np.sqrt(np.linalg.eigvalsh(mandel2(L["c11"], L["c13"], 0.0, L["c33"], 0.0, L["c55"])).max() / rho_min)
+                   for L in lay)
+        dt = courant_dt(vmax, (h, h))
+        f0 = float(rng.uniform(30.0, 90.0))
+        model = {k: pad_edge(v, cpml) for k, v in mod.items()}
+        for k in ("gamma_x", "gamma_z", "gamma_xz"):
+            model[k] = np.zeros_like(model["rho"], order="F")
+        shape = (nx + 2 * cpml, nz + 2 * cpml)
+        model.update(_cpml_model(shape, cpml, (h, h), dt, vmax, f0))
+        sx = int(rng.integers(1, nx + 1))
+        sz = int(rng.integers(1, max(2, nz // 5) + 1))
+        rx = _linspace_idx(1, nx, nrec)
+        rec = (rx + cpml - 1) + shape[0] * (max(1, nz // 10) + cpml - 1)
+        out.append(Problem(family=SEISMIC2, nx=shape[0], nz=shape[1], dx=h, dz=h, dt=dt, time_steps=nt, cpml=cpml,
+                           xind=sx, zind=sz, model=model, src={"z": ricker(nt, dt, f0)},
+                           receivers=rec.astype(np.int32),
+                           meta={"vmax": vmax, "f0": f0, "seed": seed, "config": "ragged batch"}))
+    return out

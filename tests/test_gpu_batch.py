@@ -1,0 +1,51 @@
+"""Ragged batch of 2D elastic models in one persistent cooperative launch."""
+import numpy as np
+import pytest
+
+import seidart_gpu as sg
+from seidart_gpu import models
+from seidart_gpu.batch import Batch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel()) / max(np.linalg.norm(np.asarray(b).ravel()), 1e-300)
+
+
+def small_batch(nt=60):
+    return models.batch_layered_vti(nmodels=5, nt=nt, cpml=6, nmin=24, nmax=88, step=8, nrec=6, seed=11)
+
+
+def test_batch_matches_single_model_runs(oracle):
+    probs = small_batch()
+    # one model with a stress source as well
+    probs[2].src["xx"] = 0.3 * probs[2].src["z"]
+    probs[2].src["xz"] = -0.2 * probs[2].src["z"]
+    with Batch(probs, autotune=True, trial_steps=4) as b:
+        assert b.tuning and len(b.tuning) >= 5
+        b.step(25, chunk=10)
+        b.step(probs[0].time_steps - 25)
+        b.sync()
+        for m, p in enumerate(probs):
+            single = sg.run(p, sg.FP32)
+            tr, nrm = b.traces(m)
+            f = b.fields(m)
+            assert rel_l2(tr, single["traces"]) <= 1e-6
+            for q in range(5):
+                assert rel_l2(f[q], single["fields"][q]) <= 1e-6
+            o = oracle.run_oracle(p)
+            assert rel_l2(tr, o["traces"]) <= 1e-4
+            assert rel_l2(nrm, o["norms"]) <= 1e-4
+
+
+def test_bounded_barrier_timeout_reports_status():
+    """A barrier that can never complete gives up within its spin budget;
+    the host sees SEIDART_ERR_TIMEOUT and the context stays usable."""
+    probs = small_batch(nt=10)
+    with Batch(probs, autotune=False) as b:
+        assert b.force_barrier_timeout(spin_limit=1 << 14) == -6
+    # the device still runs work afterwards
+    with Batch(small_batch(nt=10), autotune=False) as b2:
+        b2.step(10)
+        b2.sync()
