@@ -152,7 +152,7 @@ __device__ __forceinline__ void cell_stress(const BModel& a, int i, int j) {
 }
 
 // velocity half-step, force source, Dirichlet ring; returns the cell's |v|
-__device__ __forceinline__ double cell_velocity(const BModel& a, int i, int j, int it) {
+__device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, int it, float (&vo)[2]) {
     const int nx = a.nx, nz = a.nz;
     const size_t c = IXM(i, j);
     const float *sxx = a.f[2], *szz = a.f[3], *sxz = a.f[4], *rho = a.m[6];
@@ -194,12 +194,15 @@ __device__ __forceinline__ double cell_velocity(const BModel& a, int i, int j, i
     if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0.f; vz = 0.f; }
     a.f[0][c] = vx;
     a.f[1][c] = vz;
-    return sqrt((double)vx * vx + (double)vz * vz);
+    vo[0] = vx;
+    vo[1] = vz;
+    return vx * vx + vz * vz;
 }
 
 template <int TX, int TY>
 __global__ void __launch_bounds__(TX* TY) s2b_persistent(BatchArgs B, int nsteps) {
     __shared__ double red[TX * TY / 32];
+    __shared__ float redf[TX * TY / 32];
     const int it0 = *B.step;
     for (int s = 0; s < nsteps; ++s) {
         const int it = it0 + s;
@@ -214,9 +217,10 @@ __global__ void __launch_bounds__(TX* TY) s2b_persistent(BatchArgs B, int nsteps
         for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
             const BModel* M;
             int i, j;
-            double n = 0.0;
-            if (tile_cell<TX, TY>(B, t, M, i, j)) n = cell_velocity(*M, i, j, it);
-            n = block_max<TX * TY / 32>(n, red);
+            float sq = 0.f, vo[2] = {0.f, 0.f};
+            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity(*M, i, j, it, vo);
+            const double n = block_norm_f32<TX * TY / 32>(
+                sq, [&] { return sqrt((double)vo[0] * vo[0] + (double)vo[1] * vo[1]); }, redf, red);
             if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&M->norms[it - 1], n);
             __syncthreads();
         }

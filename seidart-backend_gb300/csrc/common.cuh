@@ -72,6 +72,25 @@ __device__ __forceinline__ double nanmax(double a, double b) {
     return (a != a) ? a : ((b != b) ? b : fmax(a, b));
 }
 
+__device__ __forceinline__ float nanmaxf(float a, float b) {
+    return (a != a) ? a : ((b != b) ? b : fmaxf(a, b));
+}
+
+// Block-wide max in FP32 (result valid in warp 0).
+template <int NW>
+__device__ __forceinline__ float block_maxf(float v, float* sh) {
+    for (int o = 16; o > 0; o >>= 1) v = nanmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < NW) ? sh[lane] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) v = nanmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
 // Block-wide max of v over NW warps; every thread of the block must call it.
 // The result is valid in warp 0.
 template <int NW>
@@ -86,4 +105,23 @@ __device__ __forceinline__ double block_max(double v, double* sh) {
         for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     }
     return v;
+}
+
+// Block max of a Euclidean norm for the FP32 kernels: the squared norm `sq`
+// is reduced in FP32 and one FP64 square root is taken per block.  If any
+// square in the block is not representable in FP32 (or is NaN), the block is
+// reduced again from the exact FP64 norms `exact()` so the 1e25 blow-up test
+// keeps FP64 semantics.  Every thread of the block must call it (uniform
+// control flow); the result is valid in warp 0.
+// (only thread 0 takes the FP64 square root; the other threads return 0)
+template <int NW, typename F>
+__device__ __forceinline__ double block_norm_f32(float sq, F exact, float* shf, double* shd) {
+    const int big = __syncthreads_or(!(sq < 3.0e38f));
+    const bool t0 = (threadIdx.x | threadIdx.y | threadIdx.z) == 0;
+    if (!big) {
+        const float m = block_maxf<NW>(sq, shf);
+        return t0 ? sqrt((double)m) : 0.0;
+    }
+    const double m = block_max<NW>(exact(), shd);
+    return t0 ? m : 0.0;
 }

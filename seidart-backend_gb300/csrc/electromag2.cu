@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(BX* BY) e2_e(E2Args<real> a, StepInfo si) {
     const int j = blockIdx.y * BY + threadIdx.y + 1;
     const int nx = a.nx, nz = a.nz;
     double nrm = 0.0;
+    float sq = 0.f, n0 = 0.f, n1 = 0.f;  // FP32 build: squared norm and its components
     if (i <= nx && j <= nz) {
         const size_t c = IX(i, j);
         real ex = a.f[0][c], ez = a.f[1][c];
@@ -103,9 +104,18 @@ __global__ void __launch_bounds__(BX* BY) e2_e(E2Args<real> a, StepInfo si) {
         if (i == 1 || i == nx || j == 1 || j == nz) { ex = 0; ez = 0; }
         a.f[0][c] = ex;
         a.f[1][c] = ez;
+#if SD_EXACT
         nrm = sqrt((double)ex * (double)ex + (double)ez * (double)ez);
+#else
+        sq = ex * ex + ez * ez; n0 = ex; n1 = ez;
+#endif
     }
+#if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
+#else
+    __shared__ float redf[BX * BY / 32];
+    nrm = block_norm_f32<BX * BY / 32>(sq, [&] { return sqrt((double)n0 * n0 + (double)n1 * n1); }, redf, red);
+#endif
     if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&a.norms[it - 1], nrm);
 }
 

@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(BX* BY) e25_e(E25Args<real> a, StepInfo si) {
     const int k = blockIdx.y * BY + threadIdx.y + 1;
     const int nx = a.nx, nz = a.nz;
     double nrm = 0.0;
+    float sq = 0.f, w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // FP32 build: squared norm and components
     if (i <= nx && k <= nz) {
         const size_t c = IX(i, k);
         cx ex = ld(a.f[0], c), ey = ld(a.f[1], c), ez = ld(a.f[2], c);
@@ -148,12 +149,23 @@ __global__ void __launch_bounds__(BX* BY) e25_e(E25Args<real> a, StepInfo si) {
         stc(a.f[0], c, ex);
         stc(a.f[1], c, ey);
         stc(a.f[2], c, ez);
+#if SD_EXACT
         const double n1 = (double)ex.re * ex.re + (double)ex.im * ex.im;
         const double n2 = (double)ey.re * ey.re + (double)ey.im * ey.im;
         const double n3 = (double)ez.re * ez.re + (double)ez.im * ez.im;
         nrm = sqrt(n1 + n2 + n3);
+#else
+        sq = (ex.re * ex.re + ex.im * ex.im) + (ey.re * ey.re + ey.im * ey.im) + (ez.re * ez.re + ez.im * ez.im);
+        w[0] = ex.re; w[1] = ex.im; w[2] = ey.re; w[3] = ey.im; w[4] = ez.re; w[5] = ez.im;
+#endif
     }
+#if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
+#else
+    __shared__ float redf[BX * BY / 32];
+    nrm = block_norm_f32<BX * BY / 32>(sq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + ((double)w[2] * w[2] + (double)w[3] * w[3]) +
+                                                       ((double)w[4] * w[4] + (double)w[5] * w[5])); }, redf, red);
+#endif
     if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&a.norms[it - 1], nrm);
 }
 

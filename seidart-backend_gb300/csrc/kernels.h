@@ -137,13 +137,18 @@ struct S3Args {
 struct S3Maps {
     CUtensorMap coef[33];
     CUtensorMap v[3];
+    int variant;  // tile shape / pipeline depth variant the maps were built for
 };
-// FP32 z-marching kernels of seismic3_fast.cu (the FP32 path of seismic3);
-// with `maps` the stress half-step runs the TMA-fed kernel of seismic3_tma.cu
-void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr,
-                          const S3Maps* maps = nullptr);
+// FP32 path of seismic3: kernel families per half-step
+enum { S3K_CELL = 0, S3K_ZMARCH = 1, S3K_TMA = 2 };
+void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
+                          const S3Maps* maps, int stress_kind, int velocity_kind);
+void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st);
+void launch_seismic3_cell_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st);
 int seismic3_fast_norm_slots();
-bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps);
+bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps, int variant);
+int seismic3_tma_variants();
+void seismic3_tma_variant_info(int v, int* tx, int* ty, int* sc, int* rv, int* minb);
 void launch_seismic3_tma_stress(const S3Args<float>& a, const S3Maps& maps, cudaStream_t st);
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);

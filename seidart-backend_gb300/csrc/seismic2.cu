@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(BX* BY) s2_velocity(S2Args<real> a, StepInfo s
     const int j = blockIdx.y * BY + threadIdx.y + 1;
     const int nx = a.nx, nz = a.nz;
     double nrm = 0.0;
+    float sq = 0.f, n0 = 0.f, n1 = 0.f;  // FP32 build: squared norm and its components
     if (i <= nx && j <= nz) {
         const size_t c = IX(i, j);
         const real* __restrict__ sxx = a.f[2];
@@ -194,9 +195,18 @@ __global__ void __launch_bounds__(BX* BY) s2_velocity(S2Args<real> a, StepInfo s
         if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0; vz = 0; }
         a.f[0][c] = vx;
         a.f[1][c] = vz;
+#if SD_EXACT
         nrm = sqrt((double)vx * (double)vx + (double)vz * (double)vz);
+#else
+        sq = vx * vx + vz * vz; n0 = vx; n1 = vz;
+#endif
     }
+#if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
+#else
+    __shared__ float redf[BX * BY / 32];
+    nrm = block_norm_f32<BX * BY / 32>(sq, [&] { return sqrt((double)n0 * n0 + (double)n1 * n1); }, redf, red);
+#endif
     if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&a.norms[it - 1], nrm);
 }
 #undef KAP

@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(BX* BY) s25_velocity(S25Args<real> a, StepInfo
     const int k = blockIdx.y * BY + threadIdx.y + 1;
     const int nx = a.nx, nz = a.nz;
     double nrm = 0.0;
+    float sq = 0.f, w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // FP32 build: squared norm and components
     if (i <= nx && k <= nz) {
         const size_t c = IX(i, k);
         const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && k - 1 >= a.box.k0 && k - 1 < a.box.k1);
@@ -185,12 +186,23 @@ __global__ void __launch_bounds__(BX* BY) s25_velocity(S25Args<real> a, StepInfo
         stc(a.f[0], c, vx);
         stc(a.f[1], c, vy);
         stc(a.f[2], c, vz);
+#if SD_EXACT
         const double n1 = (double)vx.re * vx.re + (double)vx.im * vx.im;
         const double n2 = (double)vy.re * vy.re + (double)vy.im * vy.im;
         const double n3 = (double)vz.re * vz.re + (double)vz.im * vz.im;
         nrm = sqrt(n1 + n2 + n3);
+#else
+        sq = (vx.re * vx.re + vx.im * vx.im) + (vy.re * vy.re + vy.im * vy.im) + (vz.re * vz.re + vz.im * vz.im);
+        w[0] = vx.re; w[1] = vx.im; w[2] = vy.re; w[3] = vy.im; w[4] = vz.re; w[5] = vz.im;
+#endif
     }
+#if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
+#else
+    __shared__ float redf[BX * BY / 32];
+    nrm = block_norm_f32<BX * BY / 32>(sq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + ((double)w[2] * w[2] + (double)w[3] * w[3]) +
+                                                       ((double)w[4] * w[4] + (double)w[5] * w[5])); }, redf, red);
+#endif
     if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&a.norms[it - 1], nrm);
 }
 

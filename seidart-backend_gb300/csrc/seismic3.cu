@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) s3_velocity(S3Args<real> a, StepIn
     const int k = blockIdx.z * BZ + threadIdx.z + 1;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     double vn = 0.0, sn = 0.0;
+    float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // FP32 build
     if (i <= nx && j <= ny && k <= nz) {
         const size_t c = IX(i, j, k);
         const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.j0 && j - 1 < a.box.j1 &&
@@ -208,18 +209,41 @@ __global__ void __launch_bounds__(BX* BY* BZ) s3_velocity(S3Args<real> a, StepIn
         a.f[0][c] = vx;
         a.f[1][c] = vy;
         a.f[2][c] = vz;
-        vn = sqrt((double)vx * vx + (double)vy * vy + (double)vz * vz);
         // stress norm: cells that a stress source touches afterwards are
         // handled by s3_stress_source
         const bool src_cell = a.stress_src && ((i == is && j == js && k == ks) || (i == is + 1 && j == js + 1 && k == ks) ||
                                                (i == is + 1 && j == js && k == ks + 1) || (i == is && j == js + 1 && k == ks + 1));
+#if SD_EXACT
+        vn = sqrt((double)vx * vx + (double)vy * vy + (double)vz * vz);
         if (!src_cell) {
             const double s1 = sxx[c], s2 = syy[c], s3 = szz[c], s4 = sxy[c], s5 = syz[c], s6 = sxz[c];
             sn = sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
         }
+#else
+        w[0] = vx; w[1] = vy; w[2] = vz;
+        vsq = vx * vx + vy * vy + vz * vz;
+        if (!src_cell) {
+            w[3] = sxx[c]; w[4] = syy[c]; w[5] = szz[c]; w[6] = sxy[c]; w[7] = syz[c]; w[8] = sxz[c];
+            ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
+        }
+#endif
     }
+#if SD_EXACT
     vn = block_max<BX * BY * BZ / 32>(vn, red);
     sn = block_max<BX * BY * BZ / 32>(sn, red2);
+#else
+    __shared__ float redf[BX * BY * BZ / 32];
+    vn = block_norm_f32<BX * BY * BZ / 32>(
+        vsq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); }, redf, red);
+    __syncthreads();
+    sn = block_norm_f32<BX * BY * BZ / 32>(
+        ssq,
+        [&] {
+            const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
+            return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+        },
+        redf, red2);
+#endif
     if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
         atomic_max_nonneg(&a.norms[it - 1], vn);
         atomic_max_nonneg(&a.norms[a.nt + it - 1], sn);

@@ -1,0 +1,264 @@
+// seismic3_cell.cu -- FP32 3D elastic half-steps, one thread per cell with
+// every load issued up front.
+//
+// Same arithmetic as the FP32 path of seismic3.cu (src/fortran/cpmlfdtd.f08:
+// 1761-1992 stress loops, :2014-2127 velocity loops).  What changes is the
+// memory schedule, shaped by two measurements on this part:
+//   * the kernels are latency bound unless each thread has many loads in
+//     flight, so a thread first issues all of its loads -- the 39 velocity
+//     stencil points (or 32 stress/density points) with clamped, branch-free
+//     indices, and the 33 (10) per-cell arrays -- and only then computes;
+//   * HBM rewards concurrently running CTAs that walk contiguous memory, so
+//     the grid is ordered x tiles, y tiles, z planes (no z-marching), and the
+//     read-once arrays stream with ld.global.cs.
+// Stencil neighbours are read through the read-only path (ld.global.nc), so
+// a value shared by adjacent cells comes from L1/L2, not HBM, after the first
+// read.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+constexpr int NSLOT = 64;
+
+__device__ __forceinline__ int cl(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+struct CpmlC {
+    float b, a, k;
+};
+__device__ __forceinline__ CpmlC cpml_at(const S3Args<float>& A, size_t c, bool half) {
+    return half ? CpmlC{__ldcs(A.cpml[5] + c), __ldcs(A.cpml[3] + c), __ldcs(A.cpml[1] + c)}
+                : CpmlC{__ldcs(A.cpml[4] + c), __ldcs(A.cpml[2] + c), __ldcs(A.cpml[0] + c)};
+}
+__device__ __forceinline__ float cpml_apply(float* m, size_t c, const CpmlC& p, float d) {
+    const float mv = p.b * m[c] + p.a * d;
+    m[c] = mv;
+    return d * p.k + mv;
+}
+template <int L>
+__device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, float (&gx)[3], float (&gy)[3],
+                                          float (&gz)[3]) {
+    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
+    const CpmlC px = cpml_at(A, c, xh), py = cpml_at(A, c, yh), pz = cpml_at(A, c, zh);
+    float* const* M = A.mem + 9 * (L - 1);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        gx[f] = cpml_apply(M[3 * f], c, px, gx[f]);
+        gy[f] = cpml_apply(M[3 * f + 1], c, py, gy[f]);
+        if (L == 2 && f == 0) {
+            // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
+            // (reference quirk, cpmlfdtd.f08:1855-1866)
+            M[2][c] = pz.b * M[2][c] + pz.a * gz[0];
+        } else {
+            gz[f] = cpml_apply(M[3 * f + 2], c, pz, gz[f]);
+        }
+    }
+}
+
+__device__ __forceinline__ float stress_new(const float (&C)[21], float so, float gm, int c1, int c2, int c3, int c4,
+                                            int c5, int c6, float dt, const float (&gx)[3], const float (&gy)[3],
+                                            const float (&gz)[3]) {
+    const float acc = C[c1] * gx[0] + C[c2] * gy[1] + C[c3] * gz[2] + C[c4] * (gz[1] + gy[2]) +
+                      C[c5] * (gz[0] + gx[2]) + C[c6] * (gx[1] + gy[0]);
+    return (so + acc * dt) * gm;
+}
+
+__global__ void __launch_bounds__(BX* BY) s3c_stress(S3Args<float> A) {
+    const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    if (gx >= nx || gy >= ny) return;
+    const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
+    const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
+    const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+    const bool L1 = x14 && y13 && z12, L2 = x23 && y24 && z12, L3 = x23 && y13 && z34, L4 = x14 && y24 && z34;
+    if (!(L1 || L2 || L3 || L4)) return;
+    const size_t sx = 1, sy = (size_t)nx, sz = (size_t)nx * ny;
+    const size_t c = (size_t)gx + sy * gy + sz * k;
+    // clamped neighbour offsets (cells that use a neighbour always have it in range)
+    const long ox[4] = {(long)cl(gx - 2, 0, nx - 1) - gx, (long)cl(gx - 1, 0, nx - 1) - gx,
+                        (long)cl(gx + 1, 0, nx - 1) - gx, (long)cl(gx + 2, 0, nx - 1) - gx};
+    const long oy[4] = {((long)cl(gy - 2, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy - 1, 0, ny - 1) - gy) * (long)sy,
+                        ((long)cl(gy + 1, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy + 2, 0, ny - 1) - gy) * (long)sy};
+    const long oz[4] = {((long)cl(k - 2, 0, nz - 1) - k) * (long)sz, ((long)cl(k - 1, 0, nz - 1) - k) * (long)sz,
+                        ((long)cl(k + 1, 0, nz - 1) - k) * (long)sz, ((long)cl(k + 2, 0, nz - 1) - k) * (long)sz};
+    (void)sx;
+    // ---- loads: 39 stencil points, 21 C_ij, 6 gamma factors, 6 old stresses
+    float v[3][13];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const float* p = A.f[f] + c;
+        v[f][0] = __ldg(p);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            v[f][1 + q] = __ldg(p + ox[q]);
+            v[f][5 + q] = __ldg(p + oy[q]);
+            v[f][9 + q] = __ldg(p + oz[q]);
+        }
+    }
+    float C[21], gm[6], so[6];
+#pragma unroll
+    for (int q = 0; q < 21; ++q) C[q] = __ldcs(A.C[q] + c);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) gm[q] = __ldcs(A.g[q] + c);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) so[q] = __ldcs(A.f[3 + q] + c);
+    // ---- derivatives: index 0 centre, 1..4 = -2,-1,+1,+2 along the axis
+    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+    float fx[3], bx[3], fy[3], by[3], fz[3], bz[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const float* a = v[f];
+        fx[f] = (27.0f * (a[3] - a[0]) - (a[4] - a[2])) * hx;
+        bx[f] = (27.0f * (a[0] - a[2]) - (a[3] - a[1])) * hx;
+        fy[f] = (27.0f * (a[7] - a[0]) - (a[8] - a[6])) * hy;
+        by[f] = (27.0f * (a[0] - a[6]) - (a[7] - a[5])) * hy;
+        fz[f] = (27.0f * (a[11] - a[0]) - (a[12] - a[10])) * hz;
+        bz[f] = (27.0f * (a[0] - a[10]) - (a[11] - a[9])) * hz;
+    }
+    const bool pml = !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
+                       k < A.box.k1);
+    const float dt = A.dt;
+    // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
+    //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
+    // so / gm order: sigma xx xy xz yy yz zz ; gamma x y z xy yz xz
+    if (L1) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<1>(A, c, ex, ey, ez);
+        __stcs(A.f[3] + c, stress_new(C, so[0], gm[0], 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
+        __stcs(A.f[6] + c, stress_new(C, so[3], gm[1], 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
+        __stcs(A.f[8] + c, stress_new(C, so[5], gm[2], 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
+    }
+    if (L2) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<2>(A, c, ex, ey, ez);
+        __stcs(A.f[4] + c, stress_new(C, so[1], gm[3], 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+    }
+    if (L3) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<3>(A, c, ex, ey, ez);
+        __stcs(A.f[5] + c, stress_new(C, so[2], gm[5], 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+    }
+    if (L4) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<4>(A, c, ex, ey, ez);
+        __stcs(A.f[7] + c, stress_new(C, so[4], gm[4], 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+    }
+}
+
+__global__ void __launch_bounds__(BX* BY) s3c_velocity(S3Args<float> A, StepInfo si) {
+    __shared__ float redf[2][BX * BY / 32];
+    __shared__ double redd[2][BX * BY / 32];
+    const int it = *si.step;
+    const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    const bool col = gx < nx && gy < ny;
+    float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (col) {
+        const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+        const size_t c = (size_t)gx + sy * gy + sz * k;
+        const long xm2 = (long)cl(gx - 2, 0, nx - 1) - gx, xm1 = (long)cl(gx - 1, 0, nx - 1) - gx;
+        const long xp1 = (long)cl(gx + 1, 0, nx - 1) - gx, xp2 = (long)cl(gx + 2, 0, nx - 1) - gx;
+        const long ym2 = ((long)cl(gy - 2, 0, ny - 1) - gy) * (long)sy, ym1 = ((long)cl(gy - 1, 0, ny - 1) - gy) * (long)sy;
+        const long yp1 = ((long)cl(gy + 1, 0, ny - 1) - gy) * (long)sy, yp2 = ((long)cl(gy + 2, 0, ny - 1) - gy) * (long)sy;
+        const long zm2 = ((long)cl(k - 2, 0, nz - 1) - k) * (long)sz, zm1 = ((long)cl(k - 1, 0, nz - 1) - k) * (long)sz;
+        const long zp1 = ((long)cl(k + 1, 0, nz - 1) - k) * (long)sz, zp2 = ((long)cl(k + 2, 0, nz - 1) - k) * (long)sz;
+        const float *Sxx = A.f[3] + c, *Sxy = A.f[4] + c, *Sxz = A.f[5] + c, *Syy = A.f[6] + c, *Syz = A.f[7] + c,
+                    *Szz = A.f[8] + c, *R = A.rho + c;
+        // ---- loads
+        const float sxx0 = __ldg(Sxx), sxxm1 = __ldg(Sxx + xm1), sxxm2 = __ldg(Sxx + xm2);
+        const float sxy0 = __ldg(Sxy), sxyp1 = __ldg(Sxy + xp1), sxyp2 = __ldg(Sxy + xp2);
+        const float sxyym1 = __ldg(Sxy + ym1), sxyym2 = __ldg(Sxy + ym2);
+        const float syy0 = __ldg(Syy), syyp1 = __ldg(Syy + yp1), syyp2 = __ldg(Syy + yp2);
+        const float sxz0 = __ldg(Sxz), sxzp1 = __ldg(Sxz + xp1), sxzp2 = __ldg(Sxz + xp2);
+        const float sxzzm1 = __ldg(Sxz + zm1), sxzzm2 = __ldg(Sxz + zm2);
+        const float syz0 = __ldg(Syz), syzym1 = __ldg(Syz + ym1), syzym2 = __ldg(Syz + ym2);
+        const float syzzm1 = __ldg(Syz + zm1), syzzm2 = __ldg(Syz + zm2);
+        const float szz0 = __ldg(Szz), szzp1 = __ldg(Szz + zp1), szzp2 = __ldg(Szz + zp2);
+        const float r0 = __ldg(R), rxm = __ldg(R + xm1), rxp = __ldg(R + xp1), rzm = __ldg(R + zm1), rzp = __ldg(R + zp1);
+        float vx = A.f[0][c], vy = A.f[1][c], vz = A.f[2][c];
+        const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+        const float dt = A.dt;
+        const int code = A.density_code;
+        const bool pml = !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
+                           k < A.box.k1);
+        const float byy = inv_mean_f(r0, r0, code);
+        if (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2) {  // vx
+            float d1 = (27.0f * (sxx0 - sxxm1) + sxxm2) * hx;
+            float d2 = (27.0f * (sxy0 - sxyym1) + sxyym2) * hy;
+            float d3 = (27.0f * (sxz0 - sxzzm1) + sxzzm2) * hz;
+            if (pml) {
+                const CpmlC p = cpml_at(A, c, true);
+                d1 = cpml_apply(A.mem[36], c, p, d1);
+                d2 = cpml_apply(A.mem[40], c, p, d2);
+                d3 = cpml_apply(A.mem[42], c, p, d3);
+            }
+            vx = vx + (d1 * inv_mean_f(r0, rxm, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+        }
+        if (gx >= 1 && gx <= nx - 3 && gy >= 1 && gy <= ny - 3 && k >= 2 && k <= nz - 2) {  // vy
+            float d1 = (27.0f * (sxyp1 - sxy0) - sxyp2) * hx;
+            float d2 = (27.0f * (syyp1 - syy0) - syyp2) * hy;
+            float d3 = (27.0f * (syz0 - syzzm1) + syzzm2) * hz;
+            if (pml) {
+                const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
+                d1 = cpml_apply(A.mem[39], c, ph, d1);
+                d2 = cpml_apply(A.mem[37], c, ph, d2);
+                d3 = cpml_apply(A.mem[44], c, pf, d3);
+            }
+            vy = vy + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+        }
+        if (gx >= 1 && gx <= nx - 3 && gy >= 2 && gy <= ny - 2 && k >= 1 && k <= nz - 3) {  // vz
+            float d1 = (27.0f * (sxzp1 - sxz0) - sxzp2) * hx;
+            float d2 = (27.0f * (syz0 - syzym1) + syzym2) * hy;
+            float d3 = (27.0f * (szzp1 - szz0) - szzp2) * hz;
+            if (pml) {
+                const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
+                d1 = cpml_apply(A.mem[41], c, ph, d1);
+                d2 = cpml_apply(A.mem[43], c, pf, d2);
+                d3 = cpml_apply(A.mem[38], c, ph, d3);
+            }
+            vz = vz + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzp, code)) * dt;
+        }
+        // force source (cpmlfdtd.f08:2214-2219)
+        const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
+        if (gx == is + 1 && gy == js && k == ks && A.src[0]) vx = vx + (float)A.src[0][it - 1] * dt / r0;
+        if (gx == is && gy == js + 1 && k == ks && A.src[1])
+            vy = vy + (float)A.src[1][it - 1] * dt / A.rho[(size_t)is + sy * js + sz * ks];
+        if (gx == is && gy == js && k == ks + 1 && A.src[2]) vz = vz + (float)A.src[2][it - 1] * dt / r0;
+        if (gx == 0 || gx == nx - 1 || gy == 0 || gy == ny - 1 || k == 0 || k == nz - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }
+        __stcs(A.f[0] + c, vx);
+        __stcs(A.f[1] + c, vy);
+        __stcs(A.f[2] + c, vz);
+        w[0] = vx; w[1] = vy; w[2] = vz;
+        vsq = vx * vx + vy * vy + vz * vz;
+        const bool src_cell = A.stress_src && ((gx == is && gy == js && k == ks) || (gx == is + 1 && gy == js + 1 && k == ks) ||
+                                               (gx == is + 1 && gy == js && k == ks + 1) || (gx == is && gy == js + 1 && k == ks + 1));
+        if (!src_cell) {
+            w[3] = sxx0; w[4] = syy0; w[5] = szz0; w[6] = sxy0; w[7] = syz0; w[8] = sxz0;
+            ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
+        }
+    }
+    const double vn = block_norm_f32<BX * BY / 32>(
+        vsq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); }, redf[0], redd[0]);
+    const double sn = block_norm_f32<BX * BY / 32>(
+        ssq,
+        [&] {
+            const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
+            return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+        },
+        redf[1], redd[1]);
+    if ((threadIdx.x | threadIdx.y) == 0) {
+        const int slot = (blockIdx.x + 7 * blockIdx.y + 13 * blockIdx.z) % NSLOT;
+        atomic_max_nonneg(A.norms_part + slot, vn);
+        atomic_max_nonneg(A.norms_part + NSLOT + slot, sn);
+    }
+}
+
+}  // namespace
+
+void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st) {
+    s3c_stress<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), 0, st>>>(a);
+}
+void launch_seismic3_cell_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st) {
+    s3c_velocity<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), 0, st>>>(a, s);
+}

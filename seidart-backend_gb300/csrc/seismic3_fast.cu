@@ -311,11 +311,14 @@ __global__ void __launch_bounds__(TX* TY, 2) s3f_velocity(S3Args<float> A, StepI
         qzz[0] = qzz[1]; qzz[1] = qzz[2];
         qr[0] = qr[1]; qr[1] = qr[2];
     }
-    vmax = nanmax(vmax, sqrt((double)vsq));
-    smax = nanmax(smax, sqrt((double)ssq));
-    vmax = block_max<TX * TY / 32>(vmax, red[0]);
+    __shared__ float redf[2][TX * TY / 32];
+    const float vq = block_maxf<TX * TY / 32>(vsq, redf[0]);
+    const float sq2 = block_maxf<TX * TY / 32>(ssq, redf[1]);
+    vmax = block_max<TX * TY / 32>(vmax, red[0]);  // FP64 fall-back values (normally 0)
     smax = block_max<TX * TY / 32>(smax, red[1]);
     if (tid == 0) {
+        vmax = nanmax(vmax, sqrt((double)vq));
+        smax = nanmax(smax, sqrt((double)sq2));
         const int slot = (blockIdx.x + 7 * blockIdx.y + 13 * blockIdx.z) % NSLOT;
         atomic_max_nonneg(A.norms_part + slot, vmax);
         atomic_max_nonneg(A.norms_part + NSLOT + slot, smax);
@@ -379,17 +382,25 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
 }  // namespace
 
 void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
-                          const S3Maps* maps) {
+                          const S3Maps* maps, int stress_kind, int velocity_kind) {
     const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
-    if (maps) {
+    if (stress_kind == S3K_TMA && maps) {
         launch_seismic3_tma_stress(a, *maps, st);
         if (h) h->fn(h->ctx, 0, "s3t_stress");
-    } else {
+    } else if (stress_kind == S3K_ZMARCH) {
         s3f_stress<<<grd, blk, 0, st>>>(a);
         if (h) h->fn(h->ctx, 0, "s3f_stress");
+    } else {
+        launch_seismic3_cell_stress(a, st);
+        if (h) h->fn(h->ctx, 0, "s3c_stress");
     }
-    s3f_velocity<<<grd, blk, 0, st>>>(a, s);
-    if (h) h->fn(h->ctx, 1, "s3f_velocity");
+    if (velocity_kind == S3K_ZMARCH) {
+        s3f_velocity<<<grd, blk, 0, st>>>(a, s);
+        if (h) h->fn(h->ctx, 1, "s3f_velocity");
+    } else {
+        launch_seismic3_cell_velocity(a, s, st);
+        if (h) h->fn(h->ctx, 1, "s3c_velocity");
+    }
     if (a.stress_src) {
         s3f_stress_source<<<1, 1, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 2, "s3f_stress_source");

@@ -24,19 +24,25 @@
 
 namespace {
 
-constexpr int TX = 32, TY = 8;
-constexpr int VXB = TX + 8, VYB = TY + 4;  // velocity box: x from x0-4 (16-byte aligned), y from y0-2
 constexpr int NCOEF = 33;                  // C 21 + gamma 6 + sigma 6
-constexpr int SC = 2;                      // coefficient stages in flight
-constexpr int RV = 7;                      // velocity ring planes (5 in use + 2 ahead)
 constexpr int ZCH = 32;                    // planes per CTA
 constexpr long long WAIT_LIMIT = 1 << 20;  // bounded mbarrier polling
 
-struct __align__(128) Smem {
-    float coef[SC][NCOEF][TY][TX];
-    float v[RV][3][VYB][VXB];
-    unsigned long long full_c[SC];
-    unsigned long long full_v[RV];
+// Tile shape TX x TY, SC coefficient stages, RV velocity ring planes (5 in use
+// plus RV-5 ahead), MINB CTAs per SM.  The velocity box starts at x0-4 so
+// its x coordinate stays 16-byte aligned, and at y0-2.
+template <int TX_, int TY_, int SC_, int RV_, int MINB_>
+struct Cfg {
+    static constexpr int TX = TX_, TY = TY_, SC = SC_, RV = RV_, MINB = MINB_;
+    static constexpr int VXB = TX + 8, VYB = TY + 4;
+    // each velocity box padded to a multiple of 128 bytes (TMA destinations)
+    static constexpr int VBOX = (VXB * VYB + 31) / 32 * 32;
+    struct __align__(128) Smem {
+        float coef[SC][NCOEF][TY][TX];
+        float v[RV][3][VBOX];
+        unsigned long long full_c[SC];
+        unsigned long long full_v[RV];
+    };
 };
 
 __device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -106,6 +112,7 @@ __device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, floa
 
 // coefficient tile order in a stage: C 0..20, gamma 21..26, sigma 27..32
 // (sigma slots in S3 field order: xx, xy, xz, yy, yz, zz)
+template <int TY, int TX>
 __device__ __forceinline__ float stress_new(const float (*cf)[TY][TX], int ty, int tx, int sidx, int c1, int c2,
                                             int c3, int c4, int c5, int c6, int gidx, float dt, const float (&gx)[3],
                                             const float (&gy)[3], const float (&gz)[3]) {
@@ -115,7 +122,11 @@ __device__ __forceinline__ float stress_new(const float (*cf)[TY][TX], int ty, i
     return (cf[27 + sidx][ty][tx] + acc * dt) * cf[21 + gidx][ty][tx];
 }
 
-__global__ void __launch_bounds__(TX* TY, 2) s3t_stress(S3Args<float> A, const __grid_constant__ S3Maps maps) {
+template <class K>
+__global__ void __launch_bounds__(K::TX* K::TY, K::MINB) s3t_stress(S3Args<float> A, const __grid_constant__ S3Maps maps) {
+    constexpr int TX = K::TX, TY = K::TY, SC = K::SC, RV = K::RV, VXB = K::VXB, VYB = K::VYB;
+    // velocity value at row y, column x of box (slot, field)
+    using Smem = typename K::Smem;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
@@ -146,7 +157,7 @@ __global__ void __launch_bounds__(TX* TY, 2) s3t_stress(S3Args<float> A, const _
     auto issue_v = [&](int p) {
         const int s = (p - (kb - 2)) % RV;
         mbar_expect_tx(&S.full_v[s], v_bytes);
-        for (int f = 0; f < 3; ++f) tma3(&S.v[s][f][0][0], &maps.v[f], x0 - 4, y0 - 2, p, &S.full_v[s]);
+        for (int f = 0; f < 3; ++f) tma3(&S.v[s][f][0], &maps.v[f], x0 - 4, y0 - 2, p, &S.full_v[s]);
         pend_v |= 1u << s;
         par_v = (par_v & ~(1u << s)) | ((((unsigned)(p - (kb - 2)) / RV) & 1u) << s);
     };
@@ -180,18 +191,20 @@ __global__ void __launch_bounds__(TX* TY, 2) s3t_stress(S3Args<float> A, const _
             const int rp1 = (k + 1 - (kb - 2)) % RV, rp2 = sv2;
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
-                const float* r = &S.v[r0][f][ty + 2][tx + 4];
+                const int o = (ty + 2) * VXB + tx + 4;
+                const float* r = &S.v[r0][f][o];
                 fx[f] = (27.0f * (r[1] - r[0]) - (r[2] - r[-1])) * hx;
                 bx[f] = (27.0f * (r[0] - r[-1]) - (r[1] - r[-2])) * hx;
                 fy[f] = (27.0f * (r[VXB] - r[0]) - (r[2 * VXB] - r[-VXB])) * hy;
                 by[f] = (27.0f * (r[0] - r[-VXB]) - (r[VXB] - r[-2 * VXB])) * hy;
-                const float qm2 = S.v[rm2][f][ty + 2][tx + 4], qm1 = S.v[rm1][f][ty + 2][tx + 4];
-                const float qp1 = S.v[rp1][f][ty + 2][tx + 4], qp2 = S.v[rp2][f][ty + 2][tx + 4];
+                const float qm2 = S.v[rm2][f][o], qm1 = S.v[rm1][f][o];
+                const float qp1 = S.v[rp1][f][o], qp2 = S.v[rp2][f][o];
                 fz[f] = (27.0f * (qp1 - r[0]) - (qp2 - qm1)) * hz;
                 bz[f] = (27.0f * (r[0] - qm1) - (qp1 - qm2)) * hz;
             }
             const bool pml = !(colbox && A.box.k0 <= k && k < A.box.k1);
             const float(*cf)[TY][TX] = S.coef[sc];
+            (void)VYB;
             // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
             //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
             // sigma slot (27+): 0 xx 1 xy 2 xz 3 yy 4 yz 5 zz; gamma (21+): x y z xy yz xz
@@ -261,33 +274,62 @@ bool make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+using V0 = Cfg<32, 8, 2, 7, 2>;
+using V1 = Cfg<32, 8, 4, 6, 1>;
+using V2 = Cfg<64, 4, 3, 6, 1>;
+using V3 = Cfg<128, 2, 3, 6, 1>;
+using V4 = Cfg<64, 4, 2, 6, 2>;
+struct VariantInfo {
+    int tx, ty, sc, rv, minb;
+    size_t smem;
+    const void* fn;
+};
+const VariantInfo kTma[] = {
+    {32, 8, 2, 7, 2, sizeof(V0::Smem), (const void*)s3t_stress<V0>},
+    {32, 8, 4, 6, 1, sizeof(V1::Smem), (const void*)s3t_stress<V1>},
+    {64, 4, 3, 6, 1, sizeof(V2::Smem), (const void*)s3t_stress<V2>},
+    {128, 2, 3, 6, 1, sizeof(V3::Smem), (const void*)s3t_stress<V3>},
+    {64, 4, 2, 6, 2, sizeof(V4::Smem), (const void*)s3t_stress<V4>},
+};
+constexpr int kNumTma = sizeof(kTma) / sizeof(kTma[0]);
+
 }  // namespace
 
-// Build the tensor maps for a solver's arrays; false when the grid does not
-// meet the TMA rules (row pitch a multiple of 16 bytes) or the driver entry
-// point is unavailable, in which case the caller keeps the thread-load kernel.
-bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps) {
-    if (a.nx % 4 != 0) return false;
+int seismic3_tma_variants() { return kNumTma; }
+void seismic3_tma_variant_info(int v, int* tx, int* ty, int* sc, int* rv, int* minb) {
+    const VariantInfo& V = kTma[v < 0 || v >= kNumTma ? 0 : v];
+    *tx = V.tx; *ty = V.ty; *sc = V.sc; *rv = V.rv; *minb = V.minb;
+}
+
+// Build the tensor maps of variant `v` for a solver's arrays; false when the
+// grid does not meet the TMA rules (row pitch a multiple of 16 bytes) or the
+// driver entry point is unavailable, in which case the caller keeps the
+// thread-load kernel.
+bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps, int v) {
+    if (v < 0 || v >= kNumTma || a.nx % 4 != 0) return false;
+    const VariantInfo& V = kTma[v];
     for (int q = 0; q < 21; ++q)
-        if (!make_map(&maps->coef[q], a.C[q], a.nx, a.ny, a.nz, TX, TY)) return false;
+        if (!make_map(&maps->coef[q], a.C[q], a.nx, a.ny, a.nz, V.tx, V.ty)) return false;
     for (int q = 0; q < 6; ++q)
-        if (!make_map(&maps->coef[21 + q], a.g[q], a.nx, a.ny, a.nz, TX, TY)) return false;
+        if (!make_map(&maps->coef[21 + q], a.g[q], a.nx, a.ny, a.nz, V.tx, V.ty)) return false;
     // old stresses in field order xx, xy, xz, yy, yz, zz (slots 3..8)
     for (int q = 0; q < 6; ++q)
-        if (!make_map(&maps->coef[27 + q], a.f[3 + q], a.nx, a.ny, a.nz, TX, TY)) return false;
+        if (!make_map(&maps->coef[27 + q], a.f[3 + q], a.nx, a.ny, a.nz, V.tx, V.ty)) return false;
     for (int f = 0; f < 3; ++f)
-        if (!make_map(&maps->v[f], a.f[f], a.nx, a.ny, a.nz, VXB, VYB)) return false;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(s3t_stress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)) !=
-            cudaSuccess)
-            return false;
-        attr = true;
+        if (!make_map(&maps->v[f], a.f[f], a.nx, a.ny, a.nz, V.tx + 8, V.ty + 4)) return false;
+    if (cudaFuncSetAttribute(V.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)V.smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
     }
+    maps->variant = v;
     return true;
 }
 
 void launch_seismic3_tma_stress(const S3Args<float>& a, const S3Maps& maps, cudaStream_t st) {
-    const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
-    s3t_stress<<<grd, blk, sizeof(Smem), st>>>(a, maps);
+    const VariantInfo& V = kTma[maps.variant];
+    const dim3 blk(V.tx, V.ty), grd((a.nx + V.tx - 1) / V.tx, (a.ny + V.ty - 1) / V.ty, (a.nz + ZCH - 1) / ZCH);
+    S3Args<float> ac = a;
+    S3Maps mc = maps;
+    void* args[] = {&ac, &mc};
+    cudaLaunchKernel(V.fn, grd, blk, args, V.smem, st);
 }

@@ -128,10 +128,12 @@ struct SeidartSolver {
     void* traces = nullptr;
     double* norms = nullptr;
     double* norms_part = nullptr;  // per-step partial maxima of the FP32 3D kernels
-    // FP32 3D kernel family: 0 z-marching tiles (default), 1 one thread per
-    // cell (env SEIDART_S3_KERNEL=cell selects it, for comparisons)
-    int s3_kernel = 0;
-    bool s3_tma = false;  // TMA-fed stress kernel usable (grid meets the TMA rules)
+    // FP32 3D kernels per half-step (S3K_CELL, S3K_ZMARCH, S3K_TMA); the
+    // environment variables SEIDART_S3_STRESS / SEIDART_S3_VELOCITY
+    // (cell | zmarch | tma) and SEIDART_S3_TMA (variant number) override them
+    int s3_stress_kind = S3K_CELL, s3_velocity_kind = S3K_CELL;
+    bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
+    int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
     int* err_dev = nullptr;  // error word raised by bounded device waits
     int nnorm = 1;
@@ -449,8 +451,8 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
     case SEIDART_SEISMIC3:
         if (!f32) launch_seismic3_f64(s.s3d, si, st, h);
-        else if (s.s3_kernel == 1) launch_seismic3_f32(s.s3f, si, st, h);
-        else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr);
+        else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr, s.s3_stress_kind,
+                                  s.s3_velocity_kind);
         break;
     }
 }
@@ -552,7 +554,15 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     s->esize = precision == SEIDART_FP32 ? 4 : 8;
     s->nrec = nrec;
     s->nnorm = is3 ? 2 : 1;
-    if (const char* k = getenv("SEIDART_S3_KERNEL")) s->s3_kernel = strcmp(k, "cell") == 0 ? 1 : 0;
+    {
+        auto kind = [](const char* e, int dflt) {
+            const char* v = getenv(e);
+            if (!v) return dflt;
+            return strcmp(v, "zmarch") == 0 ? (int)S3K_ZMARCH : strcmp(v, "tma") == 0 ? (int)S3K_TMA : (int)S3K_CELL;
+        };
+        s->s3_stress_kind = kind("SEIDART_S3_STRESS", s->s3_stress_kind);
+        s->s3_velocity_kind = kind("SEIDART_S3_VELOCITY", s->s3_velocity_kind);
+    }
     s->box = interior_box(*s, model);
     for (int q = 0; q < L.nsrc; ++q) {
         // stress-source series are every slot after the force components
@@ -627,9 +637,11 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         }
     }
     if (precision == SEIDART_FP32) finish_args<float>(*s); else finish_args<double>(*s);
-    if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_kernel == 0) {
+    if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_TMA) {
         const char* t = getenv("SEIDART_S3_TMA");
-        if (!(t && strcmp(t, "0") == 0)) s->s3_tma = seismic3_tma_prepare(s->s3f, &s->s3_maps);
+        const int v = (t && *t >= '0' && *t <= '9') ? atoi(t) : s->s3_tma_variant;
+        s->s3_tma = seismic3_tma_prepare(s->s3f, &s->s3_maps, v);
+        if (!s->s3_tma) s->s3_stress_kind = S3K_CELL;  // grid does not meet the TMA rules
     }
     *out = s;
     return SEIDART_OK;
@@ -866,6 +878,40 @@ int seidart_solver_internal_advance(SeidartSolver* s, int nsteps) {
     s->steps_done += nsteps;
     return SEIDART_OK;
 }
+
+// position the step counter (next step to compute = steps_done + 1)
+int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done) {
+    if (!s || steps_done < 0 || steps_done > s->src.time_steps) return set_err(SEIDART_ERR_ARG, "bad step");
+    const int next = steps_done + 1;
+    CUDA_TRY(cudaMemcpyAsync(s->step_dev, &next, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->steps_done = steps_done;
+    return SEIDART_OK;
+}
+
+// move the point source of an FP32 seismic2 solver (0-based cell) and point
+// its vertical-force series at device memory; cached graphs are dropped
+// because they hold the launch arguments by value
+int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
+                                       const double* dev_srcz) {
+    if (!s || s->family != SEIDART_SEISMIC2 || s->precision != SEIDART_FP32) return set_err(SEIDART_ERR_ARG, "bad solver");
+    if (isrc < 0 || isrc + 1 >= s->dom.nx || jsrc < 0 || jsrc + 1 >= s->dom.nz) return set_err(SEIDART_ERR_ARG, "source outside grid");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->s2f.isrc = isrc;
+    s->s2f.jsrc = jsrc;
+    s->s2f.src[S2_SRCX] = dev_srcx;
+    s->s2f.src[S2_SRCZ] = dev_srcz;
+    for (int q = 0; q < 2; ++q)
+        if (s->graph_exec[q]) { cudaGraphExecDestroy(s->graph_exec[q]); s->graph_exec[q] = nullptr; s->graph_len[q] = 0; }
+    return SEIDART_OK;
+}
+
+cudaStream_t seidart_solver_internal_stream(SeidartSolver* s) { return s ? s->stream : nullptr; }
+void* seidart_solver_internal_mem(SeidartSolver* s, int slot) {
+    return (s && slot >= 0 && slot < (int)s->mem.size()) ? s->mem[slot] : nullptr;
+}
+const void* seidart_solver_internal_traces(SeidartSolver* s) { return s ? s->traces : nullptr; }
+BoxH seidart_solver_internal_box(SeidartSolver* s) { return s ? s->box : BoxH{}; }
 
 int seidart_run(int family, int precision, const SeidartDomain* dom, const SeidartSource* src, int density_code,
                 const double* const* model, const double* const* srcfn, double* const* fields, int nrec,
