@@ -131,6 +131,8 @@ struct S3Args {
     int nt;
     double* norms_part;  // [2][64] per-step partial maxima (FP32 z-marching kernels)
     int* err;            // device error word: 1 = a bounded wait gave up
+    const float* packed; // FP32: tile-packed 21 C_ij + 6 gamma factors (bulk stress kernel), or NULL
+    int bulk_variant;    // FP32: occupancy variant of the bulk stress kernel
 };
 // TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
 // (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes
@@ -140,7 +142,7 @@ struct S3Maps {
     int variant;  // tile shape / pipeline depth variant the maps were built for
 };
 // FP32 path of seismic3: kernel families per half-step
-enum { S3K_CELL = 0, S3K_ZMARCH = 1, S3K_TMA = 2 };
+enum { S3K_CELL = 0, S3K_ZMARCH = 1, S3K_TMA = 2, S3K_BULK = 3 };
 void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
                           const S3Maps* maps, int stress_kind, int velocity_kind);
 void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st);
@@ -150,6 +152,11 @@ bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps, int variant);
 int seismic3_tma_variants();
 void seismic3_tma_variant_info(int v, int* tx, int* ty, int* sc, int* rv, int* minb);
 void launch_seismic3_tma_stress(const S3Args<float>& a, const S3Maps& maps, cudaStream_t st);
+size_t seismic3_bulk_bytes(int nx, int ny, int nz);
+int seismic3_bulk_variants();
+int seismic3_bulk_variant_minblocks(int v);
+cudaError_t seismic3_bulk_pack(const S3Args<float>& a, float* packed, cudaStream_t st);
+void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st);
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 

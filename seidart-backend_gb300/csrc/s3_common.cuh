@@ -1,0 +1,95 @@
+// s3_common.cuh -- device helpers shared by the FP32 one-cell-per-thread 3D
+// elastic kernels (seismic3_cell.cu, seismic3_bulk.cu): clamped stencil
+// offsets, the C-PML memory update of the stress loops
+// (src/fortran/cpmlfdtd.f08:1761-1992) and the anisotropic stress update, plus
+// the mbarrier / bulk-copy primitives of the shared-memory staged kernels.
+#pragma once
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace s3 {
+
+__device__ __forceinline__ int cl(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+struct CpmlC {
+    float b, a, k;
+};
+__device__ __forceinline__ CpmlC cpml_at(const S3Args<float>& A, size_t c, bool half) {
+    return half ? CpmlC{__ldcs(A.cpml[5] + c), __ldcs(A.cpml[3] + c), __ldcs(A.cpml[1] + c)}
+                : CpmlC{__ldcs(A.cpml[4] + c), __ldcs(A.cpml[2] + c), __ldcs(A.cpml[0] + c)};
+}
+__device__ __forceinline__ float cpml_apply(float* m, size_t c, const CpmlC& p, float d) {
+    const float mv = p.b * m[c] + p.a * d;
+    m[c] = mv;
+    return d * p.k + mv;
+}
+// C-PML correction of the nine derivatives of stress loop L (1: normal
+// stresses, 2: sigma_xy, 3: sigma_xz, 4: sigma_yz); memory slots 9(L-1)..
+template <int L>
+__device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, float (&gx)[3], float (&gy)[3],
+                                          float (&gz)[3]) {
+    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
+    const CpmlC px = cpml_at(A, c, xh), py = cpml_at(A, c, yh), pz = cpml_at(A, c, zh);
+    float* const* M = A.mem + 9 * (L - 1);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        gx[f] = cpml_apply(M[3 * f], c, px, gx[f]);
+        gy[f] = cpml_apply(M[3 * f + 1], c, py, gy[f]);
+        if (L == 2 && f == 0) {
+            // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
+            // (reference quirk, cpmlfdtd.f08:1855-1866)
+            M[2][c] = pz.b * M[2][c] + pz.a * gz[0];
+        } else {
+            gz[f] = cpml_apply(M[3 * f + 2], c, pz, gz[f]);
+        }
+    }
+}
+
+// sigma_new = (sigma_old + dt * sum_j C_ij e_j) / (1 + gamma dt); C read
+// through the accessor so the coefficients may come from registers or smem
+template <typename CF>
+__device__ __forceinline__ float stress_new(CF C, float so, float gm, int c1, int c2, int c3, int c4, int c5, int c6,
+                                            float dt, const float (&gx)[3], const float (&gy)[3],
+                                            const float (&gz)[3]) {
+    const float acc = C(c1) * gx[0] + C(c2) * gy[1] + C(c3) * gz[2] + C(c4) * (gz[1] + gy[2]) +
+                      C(c5) * (gz[0] + gx[2]) + C(c6) * (gx[1] + gy[0]);
+    return (so + acc * dt) * gm;
+}
+
+// ------------------------------------------------ mbarrier + bulk copies
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(saddr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false when the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity, int limit) {
+    for (int it = 0; it < limit; ++it)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+// contiguous global -> shared copy (both 16-byte aligned, bytes % 16 == 0)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+
+}  // namespace s3

@@ -1,0 +1,155 @@
+// seismic3_bulk.cu -- FP32 3D elastic stress half-step with the per-cell
+// coefficients staged in shared memory by one bulk copy per CTA.
+//
+// Same arithmetic as the FP32 stress loops of seismic3.cu
+// (src/fortran/cpmlfdtd.f08:1761-1992).  What changes is where the 27
+// read-only per-cell coefficients (21 C_ij and 6 attenuation factors
+// 1/(1 + gamma dt)) live:
+//   * at set-up they are repacked tile-major: for every 32 x 8 tile of one
+//     z plane a contiguous block [27][8][32] floats (27,648 bytes);
+//   * a CTA owns one tile: its first thread starts a single cp.async.bulk of
+//     that block into shared memory, then every thread issues its velocity
+//     stencil loads and old stresses and forms its derivatives while the
+//     copy is in flight, waits on the mbarrier (bounded) and finishes the
+//     update reading C_ij from shared memory.
+// The bytes in flight for the coefficient stream cost no registers, which is
+// what the register-bound one-cell kernels lack: they stall on load latency
+// with HBM a third busy.  A wait that gives up sets the solver's error word
+// and skips the update; the CTA still lets its copy land before exiting.
+#include "s3_common.cuh"
+
+namespace {
+
+using namespace s3;
+
+constexpr int BX = 32, BY = 8, NT = BX * BY, NCOEF = 27;
+constexpr unsigned TILE_BYTES = NCOEF * NT * sizeof(float);
+constexpr int WAIT_LIMIT = 1 << 20;
+
+__global__ void __launch_bounds__(NT) s3b_pack(S3Args<float> A, float* P) {
+    const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
+    float* dst = P + t * (NCOEF * NT) + threadIdx.y * BX + threadIdx.x;
+    const bool in = i < A.nx && j < A.ny;
+    const size_t c = in ? (size_t)i + (size_t)A.nx * ((size_t)j + (size_t)A.ny * k) : 0;
+#pragma unroll
+    for (int q = 0; q < 21; ++q) dst[q * NT] = in ? A.C[q][c] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dst[(21 + q) * NT] = in ? A.g[q][c] : 0.0f;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
+    extern __shared__ __align__(128) float coef[];  // [27][NT]
+    __shared__ __align__(8) unsigned long long bar;
+    const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
+    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if (tid == 0) {
+        const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, TILE_BYTES);
+        bulk_g2s(coef, A.packed + t * (NCOEF * NT), TILE_BYTES, &bar);
+    }
+    __syncthreads();
+    const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y;
+    const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
+    const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
+    const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+    const bool L1 = x14 && y13 && z12, L2 = x23 && y24 && z12, L3 = x23 && y13 && z34, L4 = x14 && y24 && z34;
+    const bool active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
+    const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+    const size_t c = active ? (size_t)gx + sy * gy + sz * k : 0;
+    float so[6], fx[3], bx[3], fy[3], by[3], fz[3], bz[3];
+    if (active) {
+        const long ox[4] = {(long)cl(gx - 2, 0, nx - 1) - gx, (long)cl(gx - 1, 0, nx - 1) - gx,
+                            (long)cl(gx + 1, 0, nx - 1) - gx, (long)cl(gx + 2, 0, nx - 1) - gx};
+        const long oy[4] = {((long)cl(gy - 2, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy - 1, 0, ny - 1) - gy) * (long)sy,
+                            ((long)cl(gy + 1, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy + 2, 0, ny - 1) - gy) * (long)sy};
+        const long oz[4] = {((long)cl(k - 2, 0, nz - 1) - k) * (long)sz, ((long)cl(k - 1, 0, nz - 1) - k) * (long)sz,
+                            ((long)cl(k + 1, 0, nz - 1) - k) * (long)sz, ((long)cl(k + 2, 0, nz - 1) - k) * (long)sz};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) so[q] = __ldcs(A.f[3 + q] + c);
+        const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const float* p = A.f[f] + c;
+            const float a0 = __ldg(p);
+            const float xm2 = __ldg(p + ox[0]), xm1 = __ldg(p + ox[1]), xp1 = __ldg(p + ox[2]), xp2 = __ldg(p + ox[3]);
+            const float ym2 = __ldg(p + oy[0]), ym1 = __ldg(p + oy[1]), yp1 = __ldg(p + oy[2]), yp2 = __ldg(p + oy[3]);
+            const float zm2 = __ldg(p + oz[0]), zm1 = __ldg(p + oz[1]), zp1 = __ldg(p + oz[2]), zp2 = __ldg(p + oz[3]);
+            fx[f] = (27.0f * (xp1 - a0) - (xp2 - xm1)) * hx;
+            bx[f] = (27.0f * (a0 - xm1) - (xp1 - xm2)) * hx;
+            fy[f] = (27.0f * (yp1 - a0) - (yp2 - ym1)) * hy;
+            by[f] = (27.0f * (a0 - ym1) - (yp1 - ym2)) * hy;
+            fz[f] = (27.0f * (zp1 - a0) - (zp2 - zm1)) * hz;
+            bz[f] = (27.0f * (a0 - zm1) - (zp1 - zm2)) * hz;
+        }
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, WAIT_LIMIT);
+    if (!ok) {
+        if (A.err) atomicExch(A.err, 1);
+        // the copy may still be in flight: keep the CTA (and its shared
+        // memory) alive until it lands, again with a bounded wait
+        if (tid == 0) mbar_wait_bounded(&bar, 0, WAIT_LIMIT);
+        return;
+    }
+    if (!active) return;
+    const auto CR = [&](int q) { return coef[q * NT + tid]; };
+    const auto GM = [&](int q) { return coef[(21 + q) * NT + tid]; };
+    const bool pml = !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
+                       k < A.box.k1);
+    const float dt = A.dt;
+    // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
+    //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
+    // so order: sigma xx xy xz yy yz zz ; gamma order: x y z xy yz xz
+    if (L1) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<1>(A, c, ex, ey, ez);
+        __stcs(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
+        __stcs(A.f[6] + c, stress_new(CR, so[3], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
+        __stcs(A.f[8] + c, stress_new(CR, so[5], GM(2), 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
+    }
+    if (L2) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<2>(A, c, ex, ey, ez);
+        __stcs(A.f[4] + c, stress_new(CR, so[1], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+    }
+    if (L3) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<3>(A, c, ex, ey, ez);
+        __stcs(A.f[5] + c, stress_new(CR, so[2], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+    }
+    if (L4) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<4>(A, c, ex, ey, ez);
+        __stcs(A.f[7] + c, stress_new(CR, so[4], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+    }
+}
+
+using StressFn = void (*)(S3Args<float>);
+// variant 2 (4 CTAs/SM) measured fastest on 352^3: 2.99 ms against 3.42 ms
+const StressFn kVariants[] = {s3b_stress<2>, s3b_stress<3>, s3b_stress<4>};
+const int kMinBlocks[] = {2, 3, 4};
+constexpr int NVAR = sizeof(kVariants) / sizeof(kVariants[0]);
+
+dim3 tile_grid(const S3Args<float>& a) { return dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz); }
+
+}  // namespace
+
+size_t seismic3_bulk_bytes(int nx, int ny, int nz) {
+    return (size_t)((nx + BX - 1) / BX) * ((ny + BY - 1) / BY) * nz * TILE_BYTES;
+}
+
+int seismic3_bulk_variants() { return NVAR; }
+int seismic3_bulk_variant_minblocks(int v) { return (v >= 0 && v < NVAR) ? kMinBlocks[v] : 0; }
+
+cudaError_t seismic3_bulk_pack(const S3Args<float>& a, float* packed, cudaStream_t st) {
+    s3b_pack<<<tile_grid(a), dim3(BX, BY), 0, st>>>(a, packed);
+    return cudaGetLastError();
+}
+
+void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st) {
+    const StressFn fn = kVariants[(variant >= 0 && variant < NVAR) ? variant : 0];
+    fn<<<tile_grid(a), dim3(BX, BY), TILE_BYTES, st>>>(a);
+}

@@ -14,55 +14,14 @@
 // Stencil neighbours are read through the read-only path (ld.global.nc), so
 // a value shared by adjacent cells comes from L1/L2, not HBM, after the first
 // read.
-#include "common.cuh"
-#include "kernels.h"
+#include "s3_common.cuh"
 
 namespace {
 
 constexpr int BX = 32, BY = 8;
 constexpr int NSLOT = 64;
 
-__device__ __forceinline__ int cl(int v, int lo, int hi) { return min(max(v, lo), hi); }
-
-struct CpmlC {
-    float b, a, k;
-};
-__device__ __forceinline__ CpmlC cpml_at(const S3Args<float>& A, size_t c, bool half) {
-    return half ? CpmlC{__ldcs(A.cpml[5] + c), __ldcs(A.cpml[3] + c), __ldcs(A.cpml[1] + c)}
-                : CpmlC{__ldcs(A.cpml[4] + c), __ldcs(A.cpml[2] + c), __ldcs(A.cpml[0] + c)};
-}
-__device__ __forceinline__ float cpml_apply(float* m, size_t c, const CpmlC& p, float d) {
-    const float mv = p.b * m[c] + p.a * d;
-    m[c] = mv;
-    return d * p.k + mv;
-}
-template <int L>
-__device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, float (&gx)[3], float (&gy)[3],
-                                          float (&gz)[3]) {
-    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
-    const CpmlC px = cpml_at(A, c, xh), py = cpml_at(A, c, yh), pz = cpml_at(A, c, zh);
-    float* const* M = A.mem + 9 * (L - 1);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-        gx[f] = cpml_apply(M[3 * f], c, px, gx[f]);
-        gy[f] = cpml_apply(M[3 * f + 1], c, py, gy[f]);
-        if (L == 2 && f == 0) {
-            // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
-            // (reference quirk, cpmlfdtd.f08:1855-1866)
-            M[2][c] = pz.b * M[2][c] + pz.a * gz[0];
-        } else {
-            gz[f] = cpml_apply(M[3 * f + 2], c, pz, gz[f]);
-        }
-    }
-}
-
-__device__ __forceinline__ float stress_new(const float (&C)[21], float so, float gm, int c1, int c2, int c3, int c4,
-                                            int c5, int c6, float dt, const float (&gx)[3], const float (&gy)[3],
-                                            const float (&gz)[3]) {
-    const float acc = C[c1] * gx[0] + C[c2] * gy[1] + C[c3] * gz[2] + C[c4] * (gz[1] + gy[2]) +
-                      C[c5] * (gz[0] + gx[2]) + C[c6] * (gx[1] + gy[0]);
-    return (so + acc * dt) * gm;
-}
+using namespace s3;
 
 __global__ void __launch_bounds__(BX* BY) s3c_stress(S3Args<float> A) {
     const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
@@ -119,30 +78,31 @@ __global__ void __launch_bounds__(BX* BY) s3c_stress(S3Args<float> A) {
     const bool pml = !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
                        k < A.box.k1);
     const float dt = A.dt;
+    const auto CR = [&](int q) { return C[q]; };
     // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
     //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
     // so / gm order: sigma xx xy xz yy yz zz ; gamma x y z xy yz xz
     if (L1) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) loop_cpml<1>(A, c, ex, ey, ez);
-        __stcs(A.f[3] + c, stress_new(C, so[0], gm[0], 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
-        __stcs(A.f[6] + c, stress_new(C, so[3], gm[1], 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
-        __stcs(A.f[8] + c, stress_new(C, so[5], gm[2], 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
+        __stcs(A.f[3] + c, stress_new(CR, so[0], gm[0], 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
+        __stcs(A.f[6] + c, stress_new(CR, so[3], gm[1], 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
+        __stcs(A.f[8] + c, stress_new(CR, so[5], gm[2], 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
     }
     if (L2) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) loop_cpml<2>(A, c, ex, ey, ez);
-        __stcs(A.f[4] + c, stress_new(C, so[1], gm[3], 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+        __stcs(A.f[4] + c, stress_new(CR, so[1], gm[3], 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
     }
     if (L3) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
         if (pml) loop_cpml<3>(A, c, ex, ey, ez);
-        __stcs(A.f[5] + c, stress_new(C, so[2], gm[5], 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+        __stcs(A.f[5] + c, stress_new(CR, so[2], gm[5], 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
     }
     if (L4) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
         if (pml) loop_cpml<4>(A, c, ex, ey, ez);
-        __stcs(A.f[7] + c, stress_new(C, so[4], gm[4], 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+        __stcs(A.f[7] + c, stress_new(CR, so[4], gm[4], 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
     }
 }
 

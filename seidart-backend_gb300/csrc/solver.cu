@@ -128,10 +128,12 @@ struct SeidartSolver {
     void* traces = nullptr;
     double* norms = nullptr;
     double* norms_part = nullptr;  // per-step partial maxima of the FP32 3D kernels
-    // FP32 3D kernels per half-step (S3K_CELL, S3K_ZMARCH, S3K_TMA); the
-    // environment variables SEIDART_S3_STRESS / SEIDART_S3_VELOCITY
-    // (cell | zmarch | tma) and SEIDART_S3_TMA (variant number) override them
-    int s3_stress_kind = S3K_CELL, s3_velocity_kind = S3K_CELL;
+    // FP32 3D kernels per half-step (S3K_BULK, S3K_CELL, S3K_ZMARCH, S3K_TMA);
+    // the environment variables SEIDART_S3_STRESS / SEIDART_S3_VELOCITY
+    // (bulk | cell | zmarch | tma) and SEIDART_S3_TMA / SEIDART_S3_BULK
+    // (variant numbers) override them
+    int s3_stress_kind = S3K_BULK, s3_velocity_kind = S3K_CELL;
+    float* s3_packed = nullptr;  // tile-packed coefficients of the bulk stress kernel
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
@@ -558,7 +560,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         auto kind = [](const char* e, int dflt) {
             const char* v = getenv(e);
             if (!v) return dflt;
-            return strcmp(v, "zmarch") == 0 ? (int)S3K_ZMARCH : strcmp(v, "tma") == 0 ? (int)S3K_TMA : (int)S3K_CELL;
+            return strcmp(v, "zmarch") == 0 ? (int)S3K_ZMARCH
+                   : strcmp(v, "tma") == 0  ? (int)S3K_TMA
+                   : strcmp(v, "bulk") == 0 ? (int)S3K_BULK
+                                            : (int)S3K_CELL;
         };
         s->s3_stress_kind = kind("SEIDART_S3_STRESS", s->s3_stress_kind);
         s->s3_velocity_kind = kind("SEIDART_S3_VELOCITY", s->s3_velocity_kind);
@@ -642,6 +647,23 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         const int v = (t && *t >= '0' && *t <= '9') ? atoi(t) : s->s3_tma_variant;
         s->s3_tma = seismic3_tma_prepare(s->s3f, &s->s3_maps, v);
         if (!s->s3_tma) s->s3_stress_kind = S3K_CELL;  // grid does not meet the TMA rules
+    }
+    if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_BULK) {
+        const char* t = getenv("SEIDART_S3_BULK");
+        s->s3f.bulk_variant = (t && *t >= '0' && *t <= '9') ? atoi(t) : 2;
+        if (s->s3f.bulk_variant >= seismic3_bulk_variants()) s->s3f.bulk_variant = 0;
+        const size_t bytes = seismic3_bulk_bytes(s->dom.nx, s->dom.ny, s->dom.nz);
+        if (cudaMalloc((void**)&s->s3_packed, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            seidart_solver_destroy(s);
+            return set_err(SEIDART_ERR_NOMEM, "cannot allocate %zu bytes for the packed 3D coefficients", bytes);
+        }
+        if (seismic3_bulk_pack(s->s3f, s->s3_packed, s->stream) != cudaSuccess ||
+            cudaStreamSynchronize(s->stream) != cudaSuccess) {
+            seidart_solver_destroy(s);
+            return set_err(SEIDART_ERR_CUDA, "coefficient packing failed: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        s->s3f.packed = s->s3_packed;
     }
     *out = s;
     return SEIDART_OK;
@@ -842,6 +864,7 @@ int seidart_solver_destroy(SeidartSolver* s) {
     for (int q = 0; q < 2; ++q)
         if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
     if (s->arena) cudaFree(s->arena);
+    if (s->s3_packed) cudaFree(s->s3_packed);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SEIDART_OK;
