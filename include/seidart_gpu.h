@@ -230,6 +230,60 @@ void electromag25c_(int nx, int ny, int nz, double dx, double dy, double dz, int
  * (src/fortran/main.f08:31-119); returns the process exit status. */
 int seidart_cli_main(int argc, char** argv);
 
+/* ---- batched 2D elastic runs (FP32).  No counterpart in the reference,
+ * which runs one model per process call (seismic2, cpmlfdtd.f08:311-576).
+ * nmodels independent seismic2 problems of any grid sizes advance together
+ * in one persistent cooperative launch per chunk of steps (captured in a
+ * CUDA graph); each model's arrays follow seidart_solver_create.  Grid-wide
+ * waits are bounded: seidart_batch_sync returns SEIDART_ERR_TIMEOUT when a
+ * barrier gave up.  autotune times every (tile shape, CTAs per SM) variant
+ * for trial_steps steps and keeps the fastest. */
+typedef struct SeidartBatch SeidartBatch;
+int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* doms, const SeidartSource* srcs,
+                         const int* density_codes, const double* const* const* models,
+                         const double* const* const* srcfn, const int* nrec, const int* const* rec_cells);
+int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, int* best_bps);
+int seidart_batch_tuning(const SeidartBatch* b, int variant, int* tx, int* ty, int* bps, double* ms);
+int seidart_batch_set_config(SeidartBatch* b, int variant, int bps);
+int seidart_batch_step(SeidartBatch* b, int nsteps, int chunk);
+int seidart_batch_sync(SeidartBatch* b);
+int seidart_batch_force_timeout(SeidartBatch* b, long long spin_limit);
+SeidartSolver* seidart_batch_model(SeidartBatch* b, int m);
+int seidart_batch_steps_done(const SeidartBatch* b);
+long long seidart_batch_launches(const SeidartBatch* b);
+int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid);
+int seidart_batch_num_variants(void);
+int seidart_batch_destroy(SeidartBatch* b);
+const char* seidart_batch_last_error(void);
+
+/* ---- misfit gradient of the 2D elastic solver (full-waveform inversion).
+ * No counterpart in the reference, which runs forward models only.  For
+ * L = 1/2 sum_shots sum_steps sum_receivers |v - d|^2 (vx and vz traces of
+ * the FP32 solver against observed data), seidart_fwi_gradient returns L and
+ * dL/d{c11, c13, c33, c55, rho} on the padded grid ([5][nx*nz] FP64, x
+ * fastest) from a hand-written discrete adjoint of the FP32 time loop with
+ * FP64 gradient accumulation and sqrt(nt) checkpointing (checkpoint_every =
+ * 0 picks ceil(sqrt(time_steps))).  model: S2_* slots as for
+ * seidart_solver_create; shots: interior force positions (xind, zind as in
+ * SeidartSource) and vertical-force series; observed[s]: [time_steps][2][nrec]
+ * (NULL = zeros).  grad may be NULL (loss only). */
+typedef struct SeidartFwi SeidartFwi;
+int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const SeidartSource* src, int density_code,
+                       const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
+                       const double* const* shot_srcz, int nrec, const int* rec_cells,
+                       const double* const* observed, int checkpoint_every);
+int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad);
+/* synthetic traces of every shot for the model: [nshots][time_steps][2][nrec] */
+int seidart_fwi_model_traces(SeidartFwi* f, double* traces);
+/* test hooks on one step with the source off; states are [17][nx*nz] FP32
+ * (vx vz sigmaxx sigmazz sigmaxz, then the 12 memory arrays in S2_M_* order) */
+int seidart_fwi_forward_step_host(SeidartFwi* f, float* x);
+int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam);
+long long seidart_fwi_launches(const SeidartFwi* f);
+int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count);
+int seidart_fwi_destroy(SeidartFwi* f);
+const char* seidart_fwi_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,640 @@
+// adjoint.cu -- misfit gradient of the 2D elastic solver by a hand-written
+// discrete adjoint (full-waveform inversion of seismic2,
+// src/fortran/cpmlfdtd.f08:311-576, FP32 fields).
+//
+// One forward step x_{n-1} -> x_n (state x = vx, vz, sigma_xx, sigma_zz,
+// sigma_xz and the 12 CPML memories) is the composition
+//     stress half-step S, velocity half-step V, force source, Dirichlet ring D
+// exactly as seismic2.cu computes it in FP32.  For the loss
+//     L = 1/2 sum_n sum_receivers |v_n(r) - d_n(r)|^2
+// the adjoint sweep runs n = N .. 1:
+//     lambda += dL/dv_n at the receivers;  lambda <- S^T V^T D^T lambda
+// where the transposes are written out by hand for the implemented operator:
+// CPML recursions (m' = b m + a d, d' = d/kappa + m'), attenuation
+// 1/(1 + gamma dt), the three-term velocity stencils, loop bounds and the
+// Dirichlet ring.  Gradients accumulate in FP64 per cell:
+//     dL/dc11, dL/dc13, dL/dc33, dL/dc55 from S, and the four face
+//     buoyancies of V (chained to rho on the host, plus the source term).
+// Memory: forward states are kept every K ~ sqrt(nt) steps; the sweep
+// recomputes one K-step segment at a time from its checkpoint and walks it
+// backwards (storage ~2 sqrt(nt) states, cost ~1 extra forward).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/seidart_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
+extern "C" int seidart_solver_internal_reset(SeidartSolver* s);
+extern "C" int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done);
+extern "C" int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
+                                                  const double* dev_srcz);
+extern "C" cudaStream_t seidart_solver_internal_stream(SeidartSolver* s);
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+constexpr int NS = 17;  // state arrays: vx vz sxx szz sxz M0..M11
+
+struct AdjArgs {
+    int nx, nz, density_code;
+    float dt, hx, hz;  // hx = 1/(24 dx)
+    BoxH box;
+    const float* m[16];  // FP32 model: c11 c13 c15 c33 c35 c55 rho gx gz gxz 1/k 1/kh a ah b bh
+    const float* xp;     // x_{n-1}, NS arrays of N
+    const float* xc;     // x_n
+    float* lam;          // adjoint state, NS arrays
+    float* scr;          // 12 scratch arrays: lf1..lf4, ld1..ld4, le1..le4
+    double* grad;        // 8 accumulators: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
+    size_t N;
+    int isrc, jsrc;
+    float srcz;          // force sample of this step
+    double* gsrc;        // accumulated lambda_vz(src) * f_n
+};
+
+__device__ __forceinline__ bool inN(int i, int k, int nx, int nz) { return k >= 2 && k <= nz - 2 && i >= 1 && i <= nx - 3; }
+__device__ __forceinline__ bool inS(int i, int k, int nx, int nz) { return k >= 1 && k <= nz - 3 && i >= 2 && i <= nx - 2; }
+__device__ __forceinline__ bool inX(int i, int k, int nx, int nz) { return k >= 2 && k <= nz - 2 && i >= 2 && i <= nx - 2; }
+__device__ __forceinline__ bool inZ(int i, int k, int nx, int nz) { return k >= 1 && k <= nz - 3 && i >= 1 && i <= nx - 3; }
+
+// value of array a at (i, k), zero outside the grid
+__device__ __forceinline__ float at(const float* a, int i, int k, int nx, int nz) {
+    return (i >= 0 && i < nx && k >= 0 && k < nz) ? a[(size_t)i + (size_t)nx * k] : 0.0f;
+}
+
+// ---------------------------------------------------------------- V^T (and D^T)
+__global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
+    const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+    const int nx = A.nx, nz = A.nz;
+    if (i >= nx || k >= nz) return;
+    const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
+    float* lam = A.lam;
+    float lvx = lam[c], lvz = lam[N + c];
+    if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { lvx = 0.f; lvz = 0.f; }  // D^T
+    lam[c] = lvx;
+    lam[N + c] = lvz;
+    if (i == A.isrc && k == A.jsrc) *A.gsrc += (double)lvz * (double)A.srcz;
+    const float* xc = A.xc;
+    const float *sxx = xc + 2 * N, *szz = xc + 3 * N, *sxz = xc + 4 * N;
+    const float* rho = A.m[6];
+    const bool pml = !(i >= A.box.i0 && i < A.box.i1 && k >= A.box.k0 && k < A.box.k1);
+    const float dt = A.dt, hx = A.hx, hz = A.hz;
+    float lf1 = 0.f, lf2 = 0.f, lf3 = 0.f, lf4 = 0.f;
+    if (inX(i, k, nx, nz)) {
+        const float bxx = inv_mean_f(rho[c], rho[c - 1], A.density_code);
+        const float bzx = inv_mean_f(rho[c], rho[c - nx], A.density_code);
+        float F1 = (27.0f * (sxx[c] - sxx[c - 1]) + sxx[c - 2]) * hx;
+        float F2 = (27.0f * (sxz[c] - sxz[c - nx]) + sxz[c - 2 * nx]) * hz;
+        const float p1 = dt * bxx * lvx, p2 = dt * bzx * lvx;
+        if (pml) {
+            const float ik = A.m[10][c], a = A.m[12][c], b = A.m[14][c];
+            F1 = F1 * ik + xc[(5 + 8) * N + c];
+            F2 = F2 * ik + xc[(5 + 11) * N + c];
+            float* l8 = lam + (5 + 8) * N + c;
+            float* l11 = lam + (5 + 11) * N + c;
+            lf1 = (ik + a) * p1 + a * *l8;
+            *l8 = b * (p1 + *l8);
+            lf2 = (ik + a) * p2 + a * *l11;
+            *l11 = b * (p2 + *l11);
+        } else {
+            lf1 = p1;
+            lf2 = p2;
+        }
+        A.grad[4 * N + c] += (double)(lvx * dt * F1);
+        A.grad[5 * N + c] += (double)(lvx * dt * F2);
+    }
+    if (inZ(i, k, nx, nz)) {
+        const float bxz = inv_mean_f(rho[c], rho[c + 1], A.density_code);
+        const float bzz = inv_mean_f(rho[c], rho[c + nx], A.density_code);
+        float F3 = (27.0f * (sxz[c + 1] - sxz[c]) - sxz[c + 2]) * hx;
+        float F4 = (27.0f * (szz[c + nx] - szz[c]) - szz[c + 2 * nx]) * hz;
+        const float p3 = dt * bxz * lvz, p4 = dt * bzz * lvz;
+        if (pml) {
+            const float ikh = A.m[11][c], ah = A.m[13][c], bh = A.m[15][c];
+            F3 = F3 * ikh + xc[(5 + 10) * N + c];
+            F4 = F4 * ikh + xc[(5 + 9) * N + c];
+            float* l10 = lam + (5 + 10) * N + c;
+            float* l9 = lam + (5 + 9) * N + c;
+            lf3 = (ikh + ah) * p3 + ah * *l10;
+            *l10 = bh * (p3 + *l10);
+            lf4 = (ikh + ah) * p4 + ah * *l9;
+            *l9 = bh * (p4 + *l9);
+        } else {
+            lf3 = p3;
+            lf4 = p4;
+        }
+        A.grad[6 * N + c] += (double)(lvz * dt * F3);
+        A.grad[7 * N + c] += (double)(lvz * dt * F4);
+    }
+    A.scr[c] = lf1;
+    A.scr[N + c] = lf2;
+    A.scr[2 * N + c] = lf3;
+    A.scr[3 * N + c] = lf4;
+}
+
+// ------------------------------------------------- gather of V^T, then S^T
+__global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
+    const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+    const int nx = A.nx, nz = A.nz;
+    if (i >= nx || k >= nz) return;
+    const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
+    const float hx = A.hx, hz = A.hz, dt = A.dt;
+    const float *lf1 = A.scr, *lf2 = A.scr + N, *lf3 = A.scr + 2 * N, *lf4 = A.scr + 3 * N;
+    // transposes of the three-term velocity stencils
+    const float lsxx = A.lam[2 * N + c] +
+                       hx * (27.0f * at(lf1, i, k, nx, nz) - 27.0f * at(lf1, i + 1, k, nx, nz) + at(lf1, i + 2, k, nx, nz));
+    const float lsxz = A.lam[4 * N + c] +
+                       hz * (27.0f * at(lf2, i, k, nx, nz) - 27.0f * at(lf2, i, k + 1, nx, nz) + at(lf2, i, k + 2, nx, nz)) +
+                       hx * (-27.0f * at(lf3, i, k, nx, nz) + 27.0f * at(lf3, i - 1, k, nx, nz) - at(lf3, i - 2, k, nx, nz));
+    const float lszz = A.lam[3 * N + c] +
+                       hz * (-27.0f * at(lf4, i, k, nx, nz) + 27.0f * at(lf4, i, k - 1, nx, nz) - at(lf4, i, k - 2, nx, nz));
+    const bool pml = !(i >= A.box.i0 && i < A.box.i1 && k >= A.box.k0 && k < A.box.k1);
+    const float* const* m = A.m;
+    const float* vx = A.xp;
+    const float* vz = A.xp + N;
+    const float* xc = A.xc;
+    float* lam = A.lam;
+    float ld1 = 0.f, ld2 = 0.f, ld3 = 0.f, ld4 = 0.f, le1 = 0.f, le2 = 0.f, le3 = 0.f, le4 = 0.f;
+    float nsxx = lsxx, nszz = lszz, nsxz = lsxz;
+    if (inN(i, k, nx, nz)) {
+        const float gx = m[7][c], gz = m[8][c];
+        const float px = dt * gx * lsxx, pz = dt * gz * lszz;
+        nsxx = gx * lsxx;
+        nszz = gz * lszz;
+        // forward rescaled derivatives of this step (for the gradients)
+        float D1 = (27.0f * (vx[c + 1] - vx[c]) - (vx[c + 2] - vx[c - 1])) * hx;
+        float D2 = (27.0f * (vz[c] - vz[c - nx]) - (vz[c + nx] - vz[c - 2 * nx])) * hz;
+        const float c11 = m[0][c], c13 = m[1][c], c15 = m[2][c], c33 = m[3][c], c35 = m[4][c];
+        float lD1 = c11 * px + c13 * pz, lD2 = c13 * px + c33 * pz, lD3 = c15 * px + c35 * pz;
+        if (pml) {
+            const float ik = m[10][c], ikh = m[11][c], a = m[12][c], ah = m[13][c], b = m[14][c], bh = m[15][c];
+            D1 = D1 * ikh + xc[(5 + 0) * N + c];
+            D2 = D2 * ik + xc[(5 + 3) * N + c];
+            float* l0 = lam + (5 + 0) * N + c;  // dvx_dx1 (half)
+            float* l1 = lam + (5 + 1) * N + c;  // dvx_dz1 (half)
+            float* l3 = lam + (5 + 3) * N + c;  // dvz_dz1 (full)
+            float* l2 = lam + (5 + 2) * N + c;  // dvz_dx1 (full)
+            ld1 = (ikh + ah) * lD1 + ah * *l0;
+            *l0 = bh * (lD1 + *l0);
+            ld4 = (ikh + ah) * lD3 + ah * *l1;
+            *l1 = bh * (lD3 + *l1);
+            ld2 = (ik + a) * lD2 + a * *l3;
+            *l3 = b * (lD2 + *l3);
+            ld3 = (ik + a) * lD3 + a * *l2;
+            *l2 = b * (lD3 + *l2);
+        } else {
+            ld1 = lD1;
+            ld2 = lD2;
+            ld3 = lD3;
+            ld4 = lD3;
+        }
+        A.grad[c] += (double)(px * D1);
+        A.grad[N + c] += (double)(px * D2 + pz * D1);
+        A.grad[2 * N + c] += (double)(pz * D2);
+    }
+    if (inS(i, k, nx, nz)) {
+        const float gxz = m[9][c];
+        const float pxz = dt * gxz * lsxz;
+        nsxz = gxz * lsxz;
+        float E3 = (27.0f * (vz[c] - vz[c - 1]) - (vz[c + 1] - vz[c - 2])) * hx;
+        float E4 = (27.0f * (vx[c + nx] - vx[c]) - (vx[c + 2 * nx] - vx[c - nx])) * hz;
+        const float lE1 = m[2][c] * pxz, lE2 = m[4][c] * pxz, lE34 = m[5][c] * pxz;
+        if (pml) {
+            const float ikh = m[11][c], ah = m[13][c], bh = m[15][c];
+            E3 = E3 * ikh + xc[(5 + 6) * N + c];
+            E4 = E4 * ikh + xc[(5 + 5) * N + c];
+            float* l4 = lam + (5 + 4) * N + c;  // dvx_dx2
+            float* l5 = lam + (5 + 5) * N + c;  // dvx_dz2
+            float* l6 = lam + (5 + 6) * N + c;  // dvz_dx2
+            float* l7 = lam + (5 + 7) * N + c;  // dvz_dz2
+            le1 = (ikh + ah) * lE1 + ah * *l4;
+            *l4 = bh * (lE1 + *l4);
+            le4 = (ikh + ah) * lE34 + ah * *l5;
+            *l5 = bh * (lE34 + *l5);
+            le3 = (ikh + ah) * lE34 + ah * *l6;
+            *l6 = bh * (lE34 + *l6);
+            le2 = (ikh + ah) * lE2 + ah * *l7;
+            *l7 = bh * (lE2 + *l7);
+        } else {
+            le1 = lE1;
+            le2 = lE2;
+            le3 = lE34;
+            le4 = lE34;
+        }
+        A.grad[3 * N + c] += (double)(pxz * (E3 + E4));
+    }
+    lam[2 * N + c] = nsxx;
+    lam[3 * N + c] = nszz;
+    lam[4 * N + c] = nsxz;
+    float* s = A.scr + 4 * N;
+    s[c] = ld1; s[N + c] = ld2; s[2 * N + c] = ld3; s[3 * N + c] = ld4;
+    s[4 * N + c] = le1; s[5 * N + c] = le2; s[6 * N + c] = le3; s[7 * N + c] = le4;
+}
+
+// ------------------------------------------------------ gather of S^T into v
+__global__ void __launch_bounds__(BX* BY) adj_gather_v(AdjArgs A) {
+    const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+    const int nx = A.nx, nz = A.nz;
+    if (i >= nx || k >= nz) return;
+    const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
+    const float hx = A.hx, hz = A.hz;
+    const float* s = A.scr + 4 * N;
+    const float *ld1 = s, *ld2 = s + N, *ld3 = s + 2 * N, *ld4 = s + 3 * N;
+    const float *le1 = s + 4 * N, *le2 = s + 5 * N, *le3 = s + 6 * N, *le4 = s + 7 * N;
+    // transposes of forward (F) and backward (B) 4th-order differences
+    auto FxT = [&](const float* d) {
+        return hx * (27.0f * at(d, i - 1, k, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i - 2, k, nx, nz) +
+                     at(d, i + 1, k, nx, nz));
+    };
+    auto BxT = [&](const float* d) {
+        return hx * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i + 1, k, nx, nz) - at(d, i - 1, k, nx, nz) +
+                     at(d, i + 2, k, nx, nz));
+    };
+    auto FzT = [&](const float* d) {
+        return hz * (27.0f * at(d, i, k - 1, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i, k - 2, nx, nz) +
+                     at(d, i, k + 1, nx, nz));
+    };
+    auto BzT = [&](const float* d) {
+        return hz * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i, k + 1, nx, nz) - at(d, i, k - 1, nx, nz) +
+                     at(d, i, k + 2, nx, nz));
+    };
+    A.lam[c] += FxT(ld1) + BzT(ld4) + BxT(le1) + FzT(le4);
+    A.lam[N + c] += BzT(ld2) + FxT(ld3) + FzT(le2) + BxT(le3);
+}
+
+// dL/dv_n at the receivers: residual of step n added to the adjoint velocity
+__global__ void adj_inject(float* lam, size_t N, const int* rec, int nrec, const float* resid) {
+    for (int r = threadIdx.x + blockIdx.x * blockDim.x; r < nrec; r += blockDim.x * gridDim.x) {
+        atomicAdd(lam + rec[r], resid[r]);
+        atomicAdd(lam + N + rec[r], resid[nrec + r]);
+    }
+}
+
+// residual r = traces - observed over all steps; loss += 1/2 sum r^2 (FP64)
+__global__ void residual_loss(const float* tr, const float* obs, float* res, size_t n, double* loss) {
+    __shared__ double red[8];
+    double acc = 0.0;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const float r = tr[q] - obs[q];
+        res[q] = r;
+        acc += (double)r * (double)r;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        atomicAdd(loss, 0.5 * t);
+    }
+}
+
+// gather/scatter of the 17 state arrays between a solver and a contiguous block
+struct StatePtrs {
+    float* p[NS];
+};
+__global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            if (to_block) blk[a * N + q] = s.p[a][q];
+            else s.p[a][q] = blk[a * N + q];
+        }
+    }
+}
+
+}  // namespace
+
+struct SeidartFwi {
+    SeidartSolver* s = nullptr;
+    S2Args<float> a{};
+    const int* rec = nullptr;
+    int nrec = 0, nt = 0, nshots = 0, K = 1, G = 1, density = 3;
+    size_t N = 0;
+    cudaStream_t st = nullptr;
+    std::vector<int> sx, sz;
+    double* dsrc = nullptr;     // [nshots][nt] force series (device)
+    float* dobs = nullptr;      // [nshots][nt][2][nrec] observed traces
+    float* dres = nullptr;      // [nt][2][nrec] residual of the current shot
+    float* ckpt = nullptr;      // [G][NS][N]
+    float* seg = nullptr;       // [K+1][NS][N]
+    float* lam = nullptr;       // [NS][N]
+    float* scr = nullptr;       // [12][N]
+    double* grad = nullptr;     // [8][N]
+    double* dscal = nullptr;    // [0] loss, [1] source term
+    std::vector<double> srch;   // host copy of the source series
+    StatePtrs ptrs{};
+    long long launches = 0;
+};
+
+namespace {
+std::string g_ferr;
+int ferr(int code, const std::string& m) {
+    g_ferr = m;
+    return code;
+}
+#define FCUDA(x)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (x);                                                      \
+        if (e_ != cudaSuccess) return ferr(SEIDART_ERR_CUDA, cudaGetErrorString(e_)); \
+    } while (0)
+
+AdjArgs adj_args(SeidartFwi* f, const float* xp, const float* xc, float srcz) {
+    AdjArgs A{};
+    A.nx = f->a.nx; A.nz = f->a.nz; A.density_code = f->a.density_code;
+    A.dt = f->a.dt; A.hx = 1.0f / (24.0f * f->a.dx); A.hz = 1.0f / (24.0f * f->a.dz);
+    A.box = f->a.box;
+    for (int q = 0; q < 16; ++q) A.m[q] = f->a.m[q];
+    A.xp = xp; A.xc = xc; A.lam = f->lam; A.scr = f->scr; A.grad = f->grad; A.N = f->N;
+    A.isrc = f->a.isrc; A.jsrc = f->a.jsrc; A.srcz = srcz; A.gsrc = f->dscal + 1;
+    return A;
+}
+
+void adjoint_step(SeidartFwi* f, int n, const float* xp, const float* xc, float srcz) {
+    const dim3 blk(BX, BY), grd((f->a.nx + BX - 1) / BX, (f->a.nz + BY - 1) / BY);
+    if (f->nrec > 0)
+        adj_inject<<<1, 256, 0, f->st>>>(f->lam, f->N, f->rec, f->nrec, f->dres + (size_t)(n - 1) * 2 * f->nrec);
+    const AdjArgs A = adj_args(f, xp, xc, srcz);
+    adj_velocity<<<grd, blk, 0, f->st>>>(A);
+    adj_stress<<<grd, blk, 0, f->st>>>(A);
+    adj_gather_v<<<grd, blk, 0, f->st>>>(A);
+    f->launches += 4;
+}
+
+int save_state(SeidartFwi* f, float* blk) {
+    copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, blk, f->N, 1);
+    ++f->launches;
+    return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "state copy");
+}
+int load_state(SeidartFwi* f, const float* blk) {
+    copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, const_cast<float*>(blk), f->N, 0);
+    ++f->launches;
+    return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "state copy");
+}
+
+// forward run of shot `sh` with checkpoints; leaves traces in the solver
+int forward_shot(SeidartFwi* f, int sh, bool checkpoints) {
+    int rc = seidart_solver_internal_reset(f->s);
+    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    rc = seidart_solver_internal_set_source(f->s, f->sx[sh], f->sz[sh], nullptr, f->dsrc + (size_t)sh * f->nt);
+    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    S2Args<float> a;
+    seidart_solver_internal_s2f(f->s, &a, nullptr);
+    f->a = a;
+    for (int g = 0; g < f->G; ++g) {
+        const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
+        if (checkpoints && (rc = save_state(f, f->ckpt + (size_t)g * NS * f->N)) != SEIDART_OK) return rc;
+        rc = seidart_solver_step(f->s, len);
+        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    }
+    return SEIDART_OK;
+}
+
+int shot_residual(SeidartFwi* f, int sh) {
+    const size_t n = (size_t)f->nt * 2 * f->nrec;
+    const float* tr = (const float*)f->a.traces;
+    residual_loss<<<152, 256, 0, f->st>>>(tr, f->dobs + (size_t)sh * n, f->dres, n, f->dscal);
+    ++f->launches;
+    return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "residual kernel");
+}
+
+int backward_shot(SeidartFwi* f, int sh) {
+    FCUDA(cudaMemsetAsync(f->lam, 0, sizeof(float) * NS * f->N, f->st));
+    const double* src = f->srch.data() + (size_t)sh * f->nt;
+    for (int g = f->G - 1; g >= 0; --g) {
+        const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
+        // recompute the segment from its checkpoint, keeping every state
+        int rc = load_state(f, f->ckpt + (size_t)g * NS * f->N);
+        if (rc != SEIDART_OK) return rc;
+        rc = seidart_solver_internal_set_step(f->s, t0);
+        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+        if ((rc = save_state(f, f->seg)) != SEIDART_OK) return rc;
+        for (int j = 1; j <= len; ++j) {
+            rc = seidart_solver_step(f->s, 1);
+            if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+            if ((rc = save_state(f, f->seg + (size_t)j * NS * f->N)) != SEIDART_OK) return rc;
+        }
+        for (int j = len; j >= 1; --j) {
+            const int n = t0 + j;
+            adjoint_step(f, n, f->seg + (size_t)(j - 1) * NS * f->N, f->seg + (size_t)j * NS * f->N, (float)src[n - 1]);
+        }
+        FCUDA(cudaGetLastError());
+    }
+    return SEIDART_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* seidart_fwi_last_error(void) { return g_ferr.c_str(); }
+
+int seidart_fwi_destroy(SeidartFwi* f) {
+    if (!f) return SEIDART_OK;
+    if (f->st) cudaStreamSynchronize(f->st);
+    for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dres, (void*)f->ckpt, (void*)f->seg, (void*)f->lam,
+                    (void*)f->scr, (void*)f->grad, (void*)f->dscal})
+        if (p) cudaFree(p);
+    if (f->s) seidart_solver_destroy(f->s);
+    delete f;
+    return SEIDART_OK;
+}
+
+// Create an FWI problem: one 2D elastic model (S2_* slots, host FP64), shots
+// with their own force position (interior indices) and vertical-force
+// series, a common receiver set, and observed traces per shot
+// ([time_steps][2][nrec], vx then vz).  checkpoint_every = 0 picks ceil(sqrt(nt)).
+int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const SeidartSource* src, int density_code,
+                       const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
+                       const double* const* shot_srcz, int nrec, const int* rec_cells,
+                       const double* const* observed, int checkpoint_every) {
+    if (!out || !dom || !src || !model || nshots < 1 || !shot_xind || !shot_zind || !shot_srcz)
+        return ferr(SEIDART_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    SeidartFwi* f = new SeidartFwi();
+    f->nt = src->time_steps;
+    f->nshots = nshots;
+    f->nrec = nrec;
+    f->density = density_code;
+    const double* srcs[S2_NSRC] = {nullptr, shot_srcz[0], nullptr, nullptr, nullptr};
+    SeidartSource s0 = *src;
+    s0.xind = shot_xind[0];
+    s0.zind = shot_zind[0];
+    int rc = seidart_solver_create(&f->s, SEIDART_SEISMIC2, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
+                                   rec_cells);
+    if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
+    seidart_solver_internal_s2f(f->s, &f->a, &f->rec);
+    f->st = seidart_solver_internal_stream(f->s);
+    f->N = (size_t)dom->nx * dom->nz;
+    for (int q = 0; q < 5; ++q) f->ptrs.p[q] = f->a.f[q];
+    for (int q = 0; q < 12; ++q) f->ptrs.p[5 + q] = f->a.mem[q];
+    f->K = checkpoint_every > 0 ? checkpoint_every : (int)ceil(sqrt((double)f->nt));
+    f->G = (f->nt + f->K - 1) / f->K;
+    for (int sh = 0; sh < nshots; ++sh) {
+        f->sx.push_back(shot_xind[sh] + dom->cpml - 1);
+        f->sz.push_back(shot_zind[sh] + dom->cpml - 1);
+        if (f->sx.back() < 0 || f->sx.back() + 1 >= dom->nx || f->sz.back() < 0 || f->sz.back() + 1 >= dom->nz) {
+            seidart_fwi_destroy(f);
+            return ferr(SEIDART_ERR_ARG, "shot source outside the grid");
+        }
+        f->srch.insert(f->srch.end(), shot_srcz[sh], shot_srcz[sh] + f->nt);
+    }
+    const size_t nobs = (size_t)f->nt * 2 * nrec;
+    if (cudaMalloc((void**)&f->dsrc, sizeof(double) * nshots * f->nt) != cudaSuccess ||
+        cudaMalloc((void**)&f->dobs, sizeof(float) * nshots * (nobs ? nobs : 1)) != cudaSuccess ||
+        cudaMalloc((void**)&f->dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
+        cudaMalloc((void**)&f->ckpt, sizeof(float) * f->G * NS * f->N) != cudaSuccess ||
+        cudaMalloc((void**)&f->seg, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
+        cudaMalloc((void**)&f->lam, sizeof(float) * NS * f->N) != cudaSuccess ||
+        cudaMalloc((void**)&f->scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
+        cudaMalloc((void**)&f->grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
+        cudaMalloc((void**)&f->dscal, sizeof(double) * 2) != cudaSuccess) {
+        cudaGetLastError();
+        seidart_fwi_destroy(f);
+        return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
+    }
+    cudaMemcpy(f->dsrc, f->srch.data(), sizeof(double) * nshots * f->nt, cudaMemcpyHostToDevice);
+    std::vector<float> tmp(nobs);
+    for (int sh = 0; sh < nshots && nobs; ++sh) {
+        if (!observed || !observed[sh]) {
+            std::fill(tmp.begin(), tmp.end(), 0.f);
+        } else {
+            for (size_t q = 0; q < nobs; ++q) tmp[q] = (float)observed[sh][q];
+        }
+        cudaMemcpy(f->dobs + (size_t)sh * nobs, tmp.data(), sizeof(float) * nobs, cudaMemcpyHostToDevice);
+    }
+    *out = f;
+    return SEIDART_OK;
+}
+
+// Loss and gradient over all shots.  grad (host, may be NULL) receives
+// [5][ncell] FP64: dL/dc11, dL/dc13, dL/dc33, dL/dc55, dL/drho.
+int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
+    if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
+    f->launches = 0;
+    FCUDA(cudaMemsetAsync(f->grad, 0, sizeof(double) * 8 * f->N, f->st));
+    FCUDA(cudaMemsetAsync(f->dscal, 0, sizeof(double) * 2, f->st));
+    std::vector<double> gsrc(f->nshots, 0.0);
+    for (int sh = 0; sh < f->nshots; ++sh) {
+        int rc = forward_shot(f, sh, grad != nullptr);
+        if (rc == SEIDART_OK) rc = shot_residual(f, sh);
+        if (rc == SEIDART_OK && grad) {
+            FCUDA(cudaMemsetAsync(f->dscal + 1, 0, sizeof(double), f->st));
+            rc = backward_shot(f, sh);
+            FCUDA(cudaMemcpyAsync(&gsrc[sh], f->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, f->st));
+        }
+        if (rc != SEIDART_OK) return rc;
+    }
+    FCUDA(cudaStreamSynchronize(f->st));
+    int rc = seidart_solver_sync(f->s);
+    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    if (loss) FCUDA(cudaMemcpy(loss, f->dscal, sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad) {
+        const size_t N = f->N;
+        std::vector<double> g(8 * N);
+        FCUDA(cudaMemcpy(g.data(), f->grad, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+        memcpy(grad, g.data(), sizeof(double) * 4 * N);
+        // chain the face buoyancies B = 1/mean(rho_a, rho_b) to rho (FP32 forward values)
+        std::vector<float> rho(N);
+        FCUDA(cudaMemcpy(rho.data(), f->a.m[S2_RHO], sizeof(float) * N, cudaMemcpyDeviceToHost));
+        double* gr = grad + 4 * N;
+        for (size_t q = 0; q < N; ++q) gr[q] = 0.0;
+        const int nx = f->a.nx, code = f->density;
+        auto dB = [code](double a, double b, double* da, double* db) {
+            switch (code) {
+            case 1: *da = -1.0 / (2.0 * a * a); *db = -1.0 / (2.0 * b * b); break;       // (a+b)/(2ab)
+            case 2: { const double B = 1.0 / sqrt(a * b); *da = -B / (2.0 * a); *db = -B / (2.0 * b); break; }
+            case 3: { const double s = a + b; *da = *db = -2.0 / (s * s); break; }       // 2/(a+b)
+            default: *da = -1.0 / (a * a); *db = 0.0; break;                            // 1/a
+            }
+        };
+        const size_t sz = (size_t)nx;
+        for (size_t q = 0; q < N; ++q) {
+            double da, db;
+            if (g[4 * N + q] != 0.0) { dB(rho[q], rho[q - 1], &da, &db); gr[q] += g[4 * N + q] * da; gr[q - 1] += g[4 * N + q] * db; }
+            if (g[5 * N + q] != 0.0) { dB(rho[q], rho[q - sz], &da, &db); gr[q] += g[5 * N + q] * da; gr[q - sz] += g[5 * N + q] * db; }
+            if (g[6 * N + q] != 0.0) { dB(rho[q], rho[q + 1], &da, &db); gr[q] += g[6 * N + q] * da; gr[q + 1] += g[6 * N + q] * db; }
+            if (g[7 * N + q] != 0.0) { dB(rho[q], rho[q + sz], &da, &db); gr[q] += g[7 * N + q] * da; gr[q + sz] += g[7 * N + q] * db; }
+        }
+        // force source term vz(src) += f_n / rho(src)
+        for (int sh = 0; sh < f->nshots; ++sh) {
+            const size_t c = (size_t)f->sx[sh] + sz * f->sz[sh];
+            gr[c] += -gsrc[sh] / ((double)rho[c] * (double)rho[c]);
+        }
+    }
+    return SEIDART_OK;
+}
+
+// Synthetic traces of every shot for the current model ([nshots][nt][2][nrec]).
+int seidart_fwi_model_traces(SeidartFwi* f, double* traces) {
+    if (!f || !traces) return ferr(SEIDART_ERR_ARG, "NULL");
+    const size_t n = (size_t)f->nt * 2 * f->nrec;
+    for (int sh = 0; sh < f->nshots; ++sh) {
+        int rc = forward_shot(f, sh, false);
+        if (rc == SEIDART_OK) rc = seidart_solver_sync(f->s);
+        if (rc == SEIDART_OK) rc = seidart_solver_traces(f->s, traces + sh * n, nullptr);
+        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    }
+    return SEIDART_OK;
+}
+
+// Adjoint test hook: apply one adjoint step (no receiver residual) to the
+// adjoint state lam (host, [17][ncell] FP32 in state order) with forward
+// states xprev/xcur ([17][ncell]); lam is updated in place.
+int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam) {
+    if (!f || !xprev || !xcur || !lam) return ferr(SEIDART_ERR_ARG, "NULL");
+    const size_t bytes = sizeof(float) * NS * f->N;
+    float *dp = nullptr, *dc = nullptr;
+    FCUDA(cudaMalloc((void**)&dp, bytes));
+    FCUDA(cudaMalloc((void**)&dc, bytes));
+    FCUDA(cudaMemcpy(dp, xprev, bytes, cudaMemcpyHostToDevice));
+    FCUDA(cudaMemcpy(dc, xcur, bytes, cudaMemcpyHostToDevice));
+    FCUDA(cudaMemcpy(f->lam, lam, bytes, cudaMemcpyHostToDevice));
+    S2Args<float> a;
+    seidart_solver_internal_s2f(f->s, &a, nullptr);
+    f->a = a;
+    const int nrec = f->nrec;
+    f->nrec = 0;  // no receiver injection
+    adjoint_step(f, 1, dp, dc, 0.0f);
+    f->nrec = nrec;
+    FCUDA(cudaStreamSynchronize(f->st));
+    FCUDA(cudaMemcpy(lam, f->lam, bytes, cudaMemcpyDeviceToHost));
+    cudaFree(dp);
+    cudaFree(dc);
+    return SEIDART_OK;
+}
+
+// Forward test hook: one forward step (source off) on a host state [17][ncell].
+int seidart_fwi_forward_step_host(SeidartFwi* f, float* x) {
+    if (!f || !x) return ferr(SEIDART_ERR_ARG, "NULL");
+    const size_t bytes = sizeof(float) * NS * f->N;
+    float* d = nullptr;
+    FCUDA(cudaMalloc((void**)&d, bytes));
+    FCUDA(cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice));
+    int rc = seidart_solver_internal_reset(f->s);
+    if (rc == SEIDART_OK) rc = seidart_solver_internal_set_source(f->s, f->sx[0], f->sz[0], nullptr, nullptr);
+    if (rc == SEIDART_OK) rc = load_state(f, d);
+    if (rc == SEIDART_OK) rc = seidart_solver_step(f->s, 1);
+    if (rc == SEIDART_OK) rc = save_state(f, d);
+    FCUDA(cudaStreamSynchronize(f->st));
+    FCUDA(cudaMemcpy(x, d, bytes, cudaMemcpyDeviceToHost));
+    cudaFree(d);
+    // restore the shot-0 source for later gradient calls
+    seidart_solver_internal_set_source(f->s, f->sx[0], f->sz[0], nullptr, f->dsrc);
+    return rc == SEIDART_OK ? SEIDART_OK : ferr(rc, seidart_last_error());
+}
+
+long long seidart_fwi_launches(const SeidartFwi* f) { return f ? f->launches : -1; }
+int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count) {
+    if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
+    if (every) *every = f->K;
+    if (count) *count = f->G;
+    return SEIDART_OK;
+}
+
+}  // extern "C"

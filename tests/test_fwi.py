@@ -1,0 +1,194 @@
+"""Misfit gradient of the 2D elastic solver (hand-written adjoint, csrc/adjoint.cu).
+
+CPU: the FP64 torch restatement used as gradient oracle reproduces oracle.c's
+traces, and its autograd gradient matches central differences of oracle.c.
+GPU: the adjoint step is the transpose of the forward step (dot-product test);
+the gradient matches the FP64 oracle gradient on a 64 x 64 instance and
+central differences (relative perturbation 1e-4) of the FP64 misfit at 8
+seeded cells within 1e-3; checkpoint spacing does not change it; the torch
+autograd wrapper returns it.
+"""
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+GRAD_TOL = 1e-3   # relative, gradient against FP64 oracle gradient and finite differences
+
+
+def _case(n=64, cpml=10, nt=300, nshots=2, nrec=16, density="arithmetic"):
+    """Start model (two layers) and true model (a +20% c11, c33, c55 Gaussian
+    anomaly between sources and interface).  The anomaly is strong and close
+    enough that the misfit is far above the FP32 rounding of the traces
+    (about 1e-6 relative), so the FP32 gradient can be held to 1e-3."""
+    from seidart_gpu import models
+    from seidart_gpu.fwi import Shot, with_model
+    anomaly = dict(x=n // 2, z=n // 3 + 2, sigma=n / 8, frac=0.20)
+    ref = models.seismic2_two_layer(n=n, cpml=cpml, nt=nt, src=(n // 2, 8), nrec=nrec, rec_z=6,
+                                    anomaly=anomaly, density=density)
+    start = models.seismic2_two_layer(n=n, cpml=cpml, nt=nt, src=(n // 2, 8), nrec=nrec, rec_z=6,
+                                      density=density, dt=ref.dt)
+    true = with_model(start, **{k: ref.model[k] for k in ("c11", "c33", "c55")})
+    xs = np.linspace(n // 4, 3 * n // 4, nshots).astype(int)
+    shots = [Shot(int(x), 8, start.src["z"]) for x in xs]
+    return start, true, shots
+
+
+def _shot_problem(p, shot):
+    return replace(p, xind=shot.xind, zind=shot.zind, src={"z": shot.srcz})
+
+
+def _oracle_observed(oracle, p, shots):
+    return [oracle.run_oracle(_shot_problem(p, s))["traces"] for s in shots]
+
+
+def _oracle_loss(oracle, p, shots, observed):
+    return sum(0.5 * float(np.sum((oracle.run_oracle(_shot_problem(p, s))["traces"] - o) ** 2))
+               for s, o in zip(shots, observed))
+
+
+# ------------------------------------------------------------------- CPU
+def test_grad_oracle_forward_matches_c_oracle(oracle):
+    torch = pytest.importorskip("torch")
+    from oracle import grad_torch
+    for density, code in (("arithmetic", 3), ("harmonic", 1), ("geometric", 2)):
+        start, true, shots = _case(n=32, cpml=6, nt=120, nshots=1, nrec=8, density=density)
+        p = _shot_problem(true, shots[0])
+        ref = oracle.run_oracle(p)["traces"]
+        m = {k: torch.tensor(v) for k, v in p.model.items()}
+        tr = grad_torch.forward_traces(m, p.dx, p.dz, p.dt, p.time_steps,
+                                       (p.xind + p.cpml - 1, p.zind + p.cpml - 1), p.src["z"],
+                                       np.asarray(p.receivers, dtype=np.int64), code).numpy()
+        assert np.linalg.norm(tr - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_grad_oracle_matches_finite_differences(oracle):
+    pytest.importorskip("torch")
+    from oracle import grad_torch
+    from seidart_gpu.fwi import with_model
+    start, true, shots = _case(n=32, cpml=6, nt=140, nshots=1, nrec=8)
+    obs = _oracle_observed(oracle, true, shots)
+    loss, g = grad_torch.misfit_and_gradient(start, shots, obs, 3)
+    assert loss == pytest.approx(_oracle_loss(oracle, start, shots, obs), rel=1e-12)
+    for key in ("c11", "rho"):
+        a = np.abs(g[key])
+        cell = np.unravel_index(np.argmax(a), a.shape)
+        base = start.model[key]
+        h = 1e-4 * base[cell]
+        plus, minus = base.copy(order="F"), base.copy(order="F")
+        plus[cell] += h
+        minus[cell] -= h
+        fd = (_oracle_loss(oracle, with_model(start, **{key: plus}), shots, obs)
+              - _oracle_loss(oracle, with_model(start, **{key: minus}), shots, obs)) / (2 * h)
+        assert abs(fd - g[key][cell]) <= 1e-5 * abs(fd)  # O(h^2) truncation of the difference
+
+
+# ------------------------------------------------------------------- GPU
+@pytest.mark.gpu
+def test_adjoint_is_transpose_of_step():
+    from seidart_gpu.fwi import NSTATE, Fwi
+    start, _, shots = _case(n=48, cpml=8, nt=20, nshots=1, nrec=4)
+    rng = np.random.default_rng(3)
+    n = start.ncell
+    with Fwi(start, shots) as f:
+        for trial in range(3):
+            x = rng.standard_normal((NSTATE, n)).astype(np.float32)
+            lam = rng.standard_normal((NSTATE, n)).astype(np.float32)
+            y = f.forward_step(x)
+            z = f.adjoint_step(x, y, lam)
+            lhs = float(np.dot(y.ravel().astype(np.float64), lam.ravel().astype(np.float64)))
+            rhs = float(np.dot(x.ravel().astype(np.float64), z.ravel().astype(np.float64)))
+            assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (trial, lhs, rhs)
+
+
+@pytest.fixture(scope="module")
+def fwi64(oracle):
+    pytest.importorskip("torch")
+    from oracle import grad_torch
+    start, true, shots = _case()
+    obs = _oracle_observed(oracle, true, shots)
+    loss, g = grad_torch.misfit_and_gradient(start, shots, obs, 3)
+    return start, shots, obs, loss, g
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.gpu
+def test_gradient_matches_fp64_oracle_gradient(fwi64):
+    from seidart_gpu.fwi import Fwi
+    start, shots, obs, loss64, g64 = fwi64
+    with Fwi(start, shots, obs) as f:
+        loss, g = f.gradient()
+        every, count = f.checkpointing
+    assert every == int(np.ceil(np.sqrt(start.time_steps))) and count * every >= start.time_steps
+    assert abs(loss - loss64) <= 1e-3 * loss64
+    for k in ("c11", "c13", "c33", "c55", "rho"):
+        assert _rel(g[k], g64[k]) <= GRAD_TOL, (k, _rel(g[k], g64[k]))
+
+
+@pytest.mark.gpu
+def test_gradient_matches_finite_differences(fwi64, oracle):
+    from seidart_gpu.fwi import Fwi, with_model
+    start, shots, obs, _, _ = fwi64
+    with Fwi(start, shots, obs) as f:
+        _, g = f.gradient()
+    rng = np.random.default_rng(11)
+    checked = 0
+    for key, ncell in (("c11", 3), ("c33", 2), ("c55", 1), ("rho", 2)):
+        a = np.abs(g[key])
+        strong = np.argwhere(a >= 0.2 * a.max())
+        for cell in strong[rng.choice(len(strong), size=ncell, replace=False)]:
+            cell = tuple(cell)
+            base = start.model[key]
+            h = 1e-4 * base[cell]
+            plus, minus = base.copy(order="F"), base.copy(order="F")
+            plus[cell] += h
+            minus[cell] -= h
+            fd = (_oracle_loss(oracle, with_model(start, **{key: plus}), shots, obs)
+                  - _oracle_loss(oracle, with_model(start, **{key: minus}), shots, obs)) / (2 * h)
+            assert abs(g[key][cell] - fd) <= GRAD_TOL * abs(fd), (key, cell, g[key][cell], fd)
+            checked += 1
+    assert checked == 8
+
+
+@pytest.mark.gpu
+def test_checkpoint_spacing_does_not_change_gradient(fwi64):
+    from seidart_gpu.fwi import Fwi
+    start, shots, obs, _, _ = fwi64
+    out = []
+    for every in (0, 1, 7, start.time_steps):
+        with Fwi(start, shots, obs, checkpoint_every=every) as f:
+            out.append(f.gradient())
+    for loss, g in out[1:]:
+        assert loss == pytest.approx(out[0][0], rel=1e-13)  # misfit summed with atomics
+        for k in g:
+            assert np.array_equal(g[k], out[0][1][k]), k
+
+
+@pytest.mark.gpu
+def test_torch_autograd_wrapper(fwi64):
+    torch = pytest.importorskip("torch")
+    from seidart_gpu.fwi import Fwi, seismic2_misfit
+    start, shots, obs, _, _ = fwi64
+    ts = [torch.tensor(start.model[k], requires_grad=True) for k in ("c11", "c13", "c33", "c55", "rho")]
+    loss = seismic2_misfit(*ts, start, shots, obs)
+    (2.0 * loss).backward()
+    with Fwi(start, shots, obs) as f:
+        l2, g = f.gradient()
+    assert float(loss.detach()) == pytest.approx(l2, rel=1e-13)
+    for t, k in zip(ts, ("c11", "c13", "c33", "c55", "rho")):
+        assert np.array_equal(t.grad.numpy(), 2.0 * g[k])
+
+
+@pytest.mark.gpu
+def test_model_traces_match_solver():
+    import seidart_gpu as sg
+    from seidart_gpu.fwi import Fwi
+    start, _, shots = _case(n=48, cpml=8, nt=80, nshots=2, nrec=6)
+    with Fwi(start, shots) as f:
+        tr = f.model_traces()
+    for s, shot in enumerate(shots):
+        ref = sg.run(_shot_problem(start, shot), sg.FP32)["traces"]
+        assert np.array_equal(tr[s], ref)
