@@ -284,6 +284,32 @@ int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count);
 int seidart_fwi_destroy(SeidartFwi* f);
 const char* seidart_fwi_last_error(void);
 
+/* ---- trace misfit without device allocation.  No counterpart in the
+ * reference (SeidarT-Backend computes no misfit); it is the no-allocation
+ * variant of the misfit reduction inside seidart_fwi_gradient, for callers
+ * whose device memory is owned by another allocator (a PyTorch caching
+ * allocator, a serving process with a fixed memory budget) and who cannot
+ * let a library call cudaMalloc/cudaFree, which take memory outside their
+ * pool and, for cudaFree, synchronise the device.
+ *   misfit[t] = 1/2 sum_{s < nsteps} (syn[s][t] - obs[s][t])^2, t < ntraces
+ *   *total    = sum_t misfit[t]
+ * syn, obs: device FP32 [nsteps][ntraces] (e.g. the [nt][2][nrec] traces of
+ * one shot, ntraces = 2 nrec); residual: device FP32 [nsteps][ntraces]
+ * receiving syn - obs, or NULL; misfit: host [ntraces] or NULL; total: host.
+ * Work runs on `stream` (a cudaStream_t; NULL = legacy default stream) of
+ * the current device, and the call returns after synchronising it.
+ * Scratch: a fixed device array of SEIDART_NOALLOC_MAX_TRACES + 32 doubles
+ * (64.25 KiB); ntraces above SEIDART_NOALLOC_MAX_TRACES returns
+ * SEIDART_ERR_ARG with the reason in seidart_last_error().  Its ntraces
+ * per-trace accumulators must start at zero: each call clears them on
+ * `stream` before use.  The first call on each device looks the array up
+ * (cudaGetSymbolAddress with that device current, which may load the
+ * module); make that first call before any stream capture begins.  Calls
+ * that overlap on one device share the scratch and race: serialise them. */
+#define SEIDART_NOALLOC_MAX_TRACES 8192
+int seidart_trace_misfit_noalloc(const float* syn, const float* obs, float* residual, int nsteps, int ntraces,
+                                 double* misfit, double* total, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

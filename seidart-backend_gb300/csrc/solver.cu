@@ -503,6 +503,9 @@ int graph_for(SeidartSolver& s, int len, cudaGraphExec_t* out) {
 extern "C" {
 
 const char* seidart_last_error(void) { return g_err.c_str(); }
+// error text for entry points defined in other files (read back through
+// seidart_last_error); not part of the ABI
+int seidart_internal_set_error(int code, const char* msg) { return set_err(code, "%s", msg); }
 
 int seidart_layout(int family, int* nmodel, int* nsrc, int* nfield, int* nmem, int* is_complex, int* nrec_comp) {
     Layout L;
