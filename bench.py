@@ -14,6 +14,13 @@ grid (stress half-step + velocity half-step, source, Dirichlet faces, norms,
   roofline  dominant kernel: algorithmic bytes per launch / its CUDA-event time
   cpu_baseline  the CPU restatement (reference production flags, OpenMP) on a
             bounded sample of the same workload
+  batched   the ragged multi-model 2D workload: 64 seismic2 models with nx, nz
+            in [256, 1024], 3000 steps, one persistent launch per graph chunk
+            with autotuned tiles; beside it the same models run one by one
+  fwi       the 2D elastic misfit gradient: 512^2 + 20 CPML, 3000 steps, 16
+            shots, 128 receivers, Gaussian anomaly target; gradient time
+            against one forward and a central-difference check of the
+            gradient at 8 seeded cells (FP64 forward runs, one shot)
 
 ``--impl reference`` times the CPU restatement of the reference time loops
 (oracle/, OpenMP, all host cores) on the same workload instead.
@@ -108,6 +115,12 @@ def make_problem(nt=None):
     return models.seismic3_layers(n=w["n"], cpml=w["cpml"], nt=nt or w["nt"], seed=w["seed"])
 
 
+# DRAM traffic / algorithmic bytes of one launch, from one ncu capture of the
+# 224^3 case (profiles/s3b_stress_224cube.md, profiles/s3c_velocity_224cube.md);
+# the bench scales it to its own launch by the algorithmic bytes.
+TRAFFIC_RATIO = {"s3b_stress": 1.113, "s3c_velocity": 1.049}
+
+
 def kernel_bytes(p, box_cells: int) -> dict:
     """Algorithmic bytes per launch (FP32): every array the kernel must touch,
     read or written once; CPML memories and coefficients only on the CPML
@@ -187,6 +200,117 @@ def cpu_baseline_sample(p=None, budget_s: float = 20.0) -> dict:
             "sample": f"{n} full time steps of the {p.nx}^3 grid after 1 untimed step (FP64, OpenMP, reference flags)"}
 
 
+def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
+    """Ragged batch: all models advance together; rate over the timed steps."""
+    import torch
+    import seidart_gpu as sg
+    from seidart_gpu import models
+    from seidart_gpu.batch import Batch
+    ps = models.batch_layered_vti(nmodels=nmodels, nt=nt)
+    cells = sum(p.ncell for p in ps)
+    t0 = time.perf_counter()
+    b = Batch(ps, autotune=True)
+    setup = time.perf_counter() - t0
+    b.step(warm)
+    b.sync()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(nt - warm, chunk=500)
+    b.sync()
+    dt = time.perf_counter() - t0
+    cfg = b.config()
+    launches = b.launches
+    b.close()
+    # the same models one by one (single-model FP32 solver), a bounded sample
+    seq_cells, seq_t = 0, 0.0
+    for p in ps[:8]:
+        q = dataclasses.replace(p, time_steps=300, src={k: v[:300] for k, v in p.src.items()})
+        with sg.Solver(q, sg.FP32) as s1:
+            s1.step(20)
+            s1.sync()
+            t1 = time.perf_counter()
+            s1.step(280)
+            s1.sync()
+            seq_t += time.perf_counter() - t1
+            seq_cells += q.ncell * 280
+    return {"value": cells * (nt - warm) / dt / 1e9, "unit": UNIT, "models": nmodels, "cells": cells,
+            "steps_timed": nt - warm, "seconds": dt, "setup_s": setup, "tuned": cfg, "gpu_launches": launches,
+            "one_by_one": {"value": seq_cells / seq_t / 1e9, "unit": UNIT,
+                           "sample": "first 8 models, 280 timed steps each, single-model FP32 solver"},
+            "dtype": "f32"}
+
+
+def bench_fwi(n: int = 512, nt: int = 3000, nshots: int = 16, ncheck: int = 8) -> dict:
+    """Misfit gradient over all shots: time against one forward, and central
+    differences (relative perturbation 1e-4, FP64 forward runs of shot 0) at
+    seeded cells where the shot-0 gradient is large."""
+    import seidart_gpu as sg
+    from seidart_gpu import models
+    from seidart_gpu.fwi import Fwi, Shot, with_model
+    an = dict(x=n // 2, z=int(300 * n / 512), sigma=20.0 * n / 512, frac=0.05)
+    ref = models.seismic2_two_layer(n=n, cpml=20, nt=nt, nrec=128, rec_z=20, anomaly=an)
+    start = models.seismic2_two_layer(n=n, cpml=20, nt=nt, nrec=128, rec_z=20, dt=ref.dt)
+    true = with_model(start, **{k: ref.model[k] for k in ("c11", "c33", "c55")})
+    xs = np.linspace(1, n, nshots + 2)[1:-1].astype(int)
+    shots = [Shot(int(x), 20, start.src["z"]) for x in xs]
+    with Fwi(true, shots) as f:
+        obs = list(f.model_traces())
+    with Fwi(start, shots, obs) as f:
+        f.loss()
+        t0 = time.perf_counter()
+        f.loss()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        loss, _ = f.gradient()
+        t_grad = time.perf_counter() - t0
+        launches = f.launches
+        every, count = f.checkpointing
+    p0 = dataclasses.replace(start, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    t0_ = dataclasses.replace(true, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    s64, o64 = sg.run(p0, sg.FP64)["traces"], sg.run(t0_, sg.FP64)["traces"]
+    s32 = sg.run(p0, sg.FP32)["traces"]
+    levels = {"residual_rel": float(np.linalg.norm(s64 - o64) / np.linalg.norm(s64)),
+              "fp32_rounding_rel": float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64)),
+              "note": "shot 0 of this configuration: FP64 start-vs-true trace difference against the FP32 "
+                      "forward's own rounding; the anomaly's reflection arrives after the last step, so the "
+                      "misfit is below FP32 rounding and the FD check below uses a start model 2% off in "
+                      "c11, c33, c55 on the same grid, shots, receivers and steps"}
+    # gradient check on shot 0 against FP64 central differences, start model 2% off
+    start_fd = with_model(start, **{k: 0.98 * start.model[k] for k in ("c11", "c33", "c55")})
+    p0 = dataclasses.replace(start_fd, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    with Fwi(start_fd, shots[:1], obs[:1]) as f:
+        _, g = f.gradient()
+
+    def loss64(p):
+        tr = sg.run(p, sg.FP64)["traces"]
+        return 0.5 * float(np.sum((tr - obs[0]) ** 2))
+
+    rng = np.random.default_rng(7)
+    errs = []
+    keys = ["c11", "c33", "c55", "rho"]
+    for q in range(ncheck):
+        key = keys[q % len(keys)]
+        a = np.abs(g[key])
+        strong = np.argwhere(a >= 0.2 * a.max())
+        cell = tuple(strong[rng.integers(len(strong))])
+        base = start_fd.model[key]
+        h = 1e-4 * base[cell]
+        plus, minus = base.copy(order="F"), base.copy(order="F")
+        plus[cell] += h
+        minus[cell] -= h
+        fd = (loss64(with_model(p0, **{key: plus})) - loss64(with_model(p0, **{key: minus}))) / (2 * h)
+        errs.append({"param": key, "cell": [int(c) for c in cell], "adjoint": float(g[key][cell]), "fd": fd,
+                     "rel_err": abs(float(g[key][cell]) - fd) / abs(fd)})
+    return {"gradients_per_s": 1.0 / t_grad, "gradient_s": t_grad, "forward_s": t_fwd,
+            "cost_vs_forward": t_grad / t_fwd, "loss": loss, "shots": nshots, "grid": [start.nx, start.nz],
+            "steps": nt, "checkpoint_every": every, "checkpoints": count, "gpu_launches": launches,
+            "misfit_levels": levels,
+            "fd_check": {"max_rel_err": max(e["rel_err"] for e in errs), "cells": errs,
+                         "perturbation": "relative 1e-4, central, FP64 forward (shot 0)",
+                         "start_model": "no anomaly, c11 c33 c55 x 0.98"},
+            "dtype": "f32 fields, f64 gradient accumulation"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -196,6 +320,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-fwi", action="store_true")
     ap.add_argument("--grid", type=int, default=WORKLOAD["n"],
                     help="interior cells per axis (default 320: the 3D configuration)")
     args = ap.parse_args()
@@ -306,6 +432,10 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline_sample(p)
+    if not args.no_batch and rank == 0:
+        extra["batched"] = bench_batch()
+    if not args.no_fwi and rank == 0:
+        extra["fwi"] = bench_fwi()
 
     if rank == 0:
         line = {
@@ -318,7 +448,9 @@ def main():
                        "l2": "inputs larger than L2 (about 14 GB moved per step vs 129 MB L2)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": TRAFFIC_RATIO[dom] * kb[dom] if dom in TRAFFIC_RATIO else None,
+                         "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
                          "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms},
             "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb},
             "kernels": kernels,
