@@ -18,6 +18,10 @@
 // Memory: forward states are kept every K ~ sqrt(nt) steps; the sweep
 // recomputes one K-step segment at a time from its checkpoint and walks it
 // backwards (storage ~2 sqrt(nt) states, cost ~1 extra forward).
+// Launches: per shot, one CUDA graph recomputes a K-step segment (saving
+// every state) and one walks it backwards; the step numbers come from a
+// device-side segment base, so the same two graphs replay for every segment
+// and a segment costs four host operations.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -35,6 +39,7 @@ extern "C" int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done
 extern "C" int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
                                                   const double* dev_srcz);
 extern "C" cudaStream_t seidart_solver_internal_stream(SeidartSolver* s);
+extern "C" StepInfo seidart_solver_internal_stepinfo(SeidartSolver* s);
 
 namespace {
 
@@ -53,7 +58,9 @@ struct AdjArgs {
     double* grad;        // 8 accumulators: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
     size_t N;
     int isrc, jsrc;
-    float srcz;          // force sample of this step
+    const double* srcz;  // force series of the shot (device), NULL = none
+    const int* base;     // device: steps before the segment; this step is n = *base + j
+    int j;
     double* gsrc;        // accumulated lambda_vz(src) * f_n
 };
 
@@ -78,7 +85,7 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
     if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { lvx = 0.f; lvz = 0.f; }  // D^T
     lam[c] = lvx;
     lam[N + c] = lvz;
-    if (i == A.isrc && k == A.jsrc) *A.gsrc += (double)lvz * (double)A.srcz;
+    if (i == A.isrc && k == A.jsrc && A.srcz) *A.gsrc += (double)lvz * (double)(float)A.srcz[*A.base + A.j - 1];
     const float* xc = A.xc;
     const float *sxx = xc + 2 * N, *szz = xc + 3 * N, *sxz = xc + 4 * N;
     const float* rho = A.m[6];
@@ -267,8 +274,10 @@ __global__ void __launch_bounds__(BX* BY) adj_gather_v(AdjArgs A) {
     A.lam[N + c] += BzT(ld2) + FxT(ld3) + FzT(le2) + BxT(le3);
 }
 
-// dL/dv_n at the receivers: residual of step n added to the adjoint velocity
-__global__ void adj_inject(float* lam, size_t N, const int* rec, int nrec, const float* resid) {
+// dL/dv_n at the receivers: residual of step n = *base + j added to the
+// adjoint velocity
+__global__ void adj_inject(float* lam, size_t N, const int* rec, int nrec, const float* dres, const int* base, int j) {
+    const float* resid = dres + (size_t)(*base + j - 1) * 2 * nrec;
     for (int r = threadIdx.x + blockIdx.x * blockDim.x; r < nrec; r += blockDim.x * gridDim.x) {
         atomicAdd(lam + rec[r], resid[r]);
         atomicAdd(lam + N + rec[r], resid[nrec + r]);
@@ -298,6 +307,24 @@ __global__ void residual_loss(const float* tr, const float* obs, float* res, siz
 struct StatePtrs {
     float* p[NS];
 };
+// start of a recomputed segment: solver step counter and segment base
+__global__ void seg_begin(int* step, int* base, int t0) {
+    *step = t0 + 1;
+    *base = t0;
+}
+
+// checkpoint -> solver state and -> first state of the segment buffer
+__global__ void restore_state(StatePtrs s, const float* __restrict__ ck, float* __restrict__ seg0, size_t N) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            const float v = ck[a * N + q];
+            s.p[a][q] = v;
+            seg0[a * N + q] = v;
+        }
+    }
+}
+
 __global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
 #pragma unroll
@@ -327,8 +354,13 @@ struct SeidartFwi {
     float* scr = nullptr;       // [12][N]
     double* grad = nullptr;     // [8][N]
     double* dscal = nullptr;    // [0] loss, [1] source term
+    int* dbase = nullptr;       // device segment base (steps before the segment)
     std::vector<double> srch;   // host copy of the source series
     StatePtrs ptrs{};
+    StepInfo si{};
+    // per-shot graphs: [0] full segments of K steps, [1] the shorter last one
+    cudaGraphExec_t rec_exec[2] = {nullptr, nullptr}, adj_exec[2] = {nullptr, nullptr};
+    int graph_len[2] = {0, 0};
     long long launches = 0;
 };
 
@@ -344,7 +376,7 @@ int ferr(int code, const std::string& m) {
         if (e_ != cudaSuccess) return ferr(SEIDART_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
 
-AdjArgs adj_args(SeidartFwi* f, const float* xp, const float* xc, float srcz) {
+AdjArgs adj_args(SeidartFwi* f, const float* xp, const float* xc, const double* srcz, int j) {
     AdjArgs A{};
     A.nx = f->a.nx; A.nz = f->a.nz; A.density_code = f->a.density_code;
     A.dt = f->a.dt; A.hx = 1.0f / (24.0f * f->a.dx); A.hz = 1.0f / (24.0f * f->a.dz);
@@ -352,14 +384,15 @@ AdjArgs adj_args(SeidartFwi* f, const float* xp, const float* xc, float srcz) {
     for (int q = 0; q < 16; ++q) A.m[q] = f->a.m[q];
     A.xp = xp; A.xc = xc; A.lam = f->lam; A.scr = f->scr; A.grad = f->grad; A.N = f->N;
     A.isrc = f->a.isrc; A.jsrc = f->a.jsrc; A.srcz = srcz; A.gsrc = f->dscal + 1;
+    A.base = f->dbase; A.j = j;
     return A;
 }
 
-void adjoint_step(SeidartFwi* f, int n, const float* xp, const float* xc, float srcz) {
+// adjoint of step n = *dbase + j (launched on f->st, possibly under capture)
+void adjoint_step(SeidartFwi* f, int j, const float* xp, const float* xc, const double* srcz) {
     const dim3 blk(BX, BY), grd((f->a.nx + BX - 1) / BX, (f->a.nz + BY - 1) / BY);
-    if (f->nrec > 0)
-        adj_inject<<<1, 256, 0, f->st>>>(f->lam, f->N, f->rec, f->nrec, f->dres + (size_t)(n - 1) * 2 * f->nrec);
-    const AdjArgs A = adj_args(f, xp, xc, srcz);
+    if (f->nrec > 0) adj_inject<<<1, 256, 0, f->st>>>(f->lam, f->N, f->rec, f->nrec, f->dres, f->dbase, j);
+    const AdjArgs A = adj_args(f, xp, xc, srcz, j);
     adj_velocity<<<grd, blk, 0, f->st>>>(A);
     adj_stress<<<grd, blk, 0, f->st>>>(A);
     adj_gather_v<<<grd, blk, 0, f->st>>>(A);
@@ -391,6 +424,7 @@ int forward_shot(SeidartFwi* f, int sh, bool checkpoints) {
         if (checkpoints && (rc = save_state(f, f->ckpt + (size_t)g * NS * f->N)) != SEIDART_OK) return rc;
         rc = seidart_solver_step(f->s, len);
         if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+        f->launches += (long long)len * seidart_step_launches(SEIDART_SEISMIC2, f->a.stress_src);
     }
     return SEIDART_OK;
 }
@@ -403,27 +437,63 @@ int shot_residual(SeidartFwi* f, int sh) {
     return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "residual kernel");
 }
 
+// Capture the recompute graph (len forward steps, each state saved to the
+// segment buffer) or the adjoint graph (len adjoint steps, last to first)
+// and instantiate it into *exec, updating an existing executable in place
+// when the topology allows.
+int capture_segment(SeidartFwi* f, int len, bool adjoint, const double* srcz, cudaGraphExec_t* exec) {
+    const size_t state = (size_t)NS * f->N;
+    FCUDA(cudaStreamBeginCapture(f->st, cudaStreamCaptureModeThreadLocal));
+    if (!adjoint) {
+        for (int j = 1; j <= len; ++j) {
+            launch_seismic2_f32(f->a, f->si, f->st);
+            copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, f->seg + (size_t)j * state, f->N, 1);
+        }
+    } else {
+        for (int j = len; j >= 1; --j) adjoint_step(f, j, f->seg + (size_t)(j - 1) * state, f->seg + (size_t)j * state, srcz);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(f->st, &g);
+    if (e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        return ferr(SEIDART_ERR_CUDA, std::string("segment capture: ") + cudaGetErrorString(e));
+    }
+    if (*exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(*exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(*exec);
+            *exec = nullptr;
+        }
+    }
+    if (!*exec) e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return ferr(SEIDART_ERR_CUDA, std::string("segment graph: ") + cudaGetErrorString(e));
+    return SEIDART_OK;
+}
+
 int backward_shot(SeidartFwi* f, int sh) {
     FCUDA(cudaMemsetAsync(f->lam, 0, sizeof(float) * NS * f->N, f->st));
-    const double* src = f->srch.data() + (size_t)sh * f->nt;
+    const double* srcz = f->dsrc + (size_t)sh * f->nt;
+    const int last = f->nt - (f->G - 1) * f->K;  // length of the last segment
+    const int lens[2] = {f->K, last};
+    for (int slot = 0; slot < 2; ++slot) {
+        if (slot == 1 && last == f->K) break;
+        int rc = capture_segment(f, lens[slot], false, srcz, &f->rec_exec[slot]);
+        if (rc == SEIDART_OK) rc = capture_segment(f, lens[slot], true, srcz, &f->adj_exec[slot]);
+        if (rc != SEIDART_OK) return rc;
+        f->graph_len[slot] = lens[slot];
+    }
+    const long long per_step = seidart_step_launches(SEIDART_SEISMIC2, f->a.stress_src) + 1;
     for (int g = f->G - 1; g >= 0; --g) {
         const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
-        // recompute the segment from its checkpoint, keeping every state
-        int rc = load_state(f, f->ckpt + (size_t)g * NS * f->N);
-        if (rc != SEIDART_OK) return rc;
-        rc = seidart_solver_internal_set_step(f->s, t0);
-        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-        if ((rc = save_state(f, f->seg)) != SEIDART_OK) return rc;
-        for (int j = 1; j <= len; ++j) {
-            rc = seidart_solver_step(f->s, 1);
-            if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-            if ((rc = save_state(f, f->seg + (size_t)j * NS * f->N)) != SEIDART_OK) return rc;
-        }
-        for (int j = len; j >= 1; --j) {
-            const int n = t0 + j;
-            adjoint_step(f, n, f->seg + (size_t)(j - 1) * NS * f->N, f->seg + (size_t)j * NS * f->N, (float)src[n - 1]);
-        }
+        const int slot = len == f->K ? 0 : 1;
+        seg_begin<<<1, 1, 0, f->st>>>(f->si.step, f->dbase, t0);
+        restore_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, f->ckpt + (size_t)g * NS * f->N, f->seg, f->N);
         FCUDA(cudaGetLastError());
+        FCUDA(cudaGraphLaunch(f->rec_exec[slot], f->st));
+        FCUDA(cudaGraphLaunch(f->adj_exec[slot], f->st));
+        f->launches += 2 + len * per_step + len * (f->nrec > 0 ? 4 : 3);
     }
     return SEIDART_OK;
 }
@@ -437,8 +507,12 @@ const char* seidart_fwi_last_error(void) { return g_ferr.c_str(); }
 int seidart_fwi_destroy(SeidartFwi* f) {
     if (!f) return SEIDART_OK;
     if (f->st) cudaStreamSynchronize(f->st);
+    for (int q = 0; q < 2; ++q) {
+        if (f->rec_exec[q]) cudaGraphExecDestroy(f->rec_exec[q]);
+        if (f->adj_exec[q]) cudaGraphExecDestroy(f->adj_exec[q]);
+    }
     for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dres, (void*)f->ckpt, (void*)f->seg, (void*)f->lam,
-                    (void*)f->scr, (void*)f->grad, (void*)f->dscal})
+                    (void*)f->scr, (void*)f->grad, (void*)f->dscal, (void*)f->dbase})
         if (p) cudaFree(p);
     if (f->s) seidart_solver_destroy(f->s);
     delete f;
@@ -470,6 +544,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
     seidart_solver_internal_s2f(f->s, &f->a, &f->rec);
     f->st = seidart_solver_internal_stream(f->s);
+    f->si = seidart_solver_internal_stepinfo(f->s);
     f->N = (size_t)dom->nx * dom->nz;
     for (int q = 0; q < 5; ++q) f->ptrs.p[q] = f->a.f[q];
     for (int q = 0; q < 12; ++q) f->ptrs.p[5 + q] = f->a.mem[q];
@@ -493,7 +568,8 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
         cudaMalloc((void**)&f->lam, sizeof(float) * NS * f->N) != cudaSuccess ||
         cudaMalloc((void**)&f->scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
         cudaMalloc((void**)&f->grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->dscal, sizeof(double) * 2) != cudaSuccess) {
+        cudaMalloc((void**)&f->dscal, sizeof(double) * 2) != cudaSuccess ||
+        cudaMalloc((void**)&f->dbase, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         seidart_fwi_destroy(f);
         return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
@@ -600,7 +676,8 @@ int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float
     f->a = a;
     const int nrec = f->nrec;
     f->nrec = 0;  // no receiver injection
-    adjoint_step(f, 1, dp, dc, 0.0f);
+    FCUDA(cudaMemsetAsync(f->dbase, 0, sizeof(int), f->st));
+    adjoint_step(f, 1, dp, dc, nullptr);
     f->nrec = nrec;
     FCUDA(cudaStreamSynchronize(f->st));
     FCUDA(cudaMemcpy(lam, f->lam, bytes, cudaMemcpyDeviceToHost));

@@ -125,3 +125,40 @@ __device__ __forceinline__ double block_norm_f32(float sq, F exact, float* shf, 
     const double m = block_max<NW>(exact(), shd);
     return t0 ? m : 0.0;
 }
+
+// Two max-norms of a block at once.  Non-negative FP32 squares order like
+// their bit patterns, with inf and NaN above every finite value, so one
+// redux.sync max per warp and one barrier give both block maxima.  A block
+// whose larger square is not below 3e38 (overflow, inf or NaN) redoes both in
+// FP64 through exa()/exb() (uniform branch).  Results are valid on thread 0:
+// sqrt of each maximum.  shu: [2][NW] unsigned, shd: [2][NW] double.
+template <int NW, typename FA, typename FB>
+__device__ __forceinline__ void block_norm2_f32(float sa, float sb, FA exa, FB exb, unsigned* shu, double* shd,
+                                                double& na, double& nb) {
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const unsigned ua = __reduce_max_sync(0xffffffffu, __float_as_uint(sa));
+    const unsigned ub = __reduce_max_sync(0xffffffffu, __float_as_uint(sb));
+    if ((tid & 31) == 0) {
+        shu[tid >> 5] = ua;
+        shu[NW + (tid >> 5)] = ub;
+    }
+    __syncthreads();
+    unsigned ma = 0u, mb = 0u;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        ma = max(ma, shu[w]);
+        mb = max(mb, shu[NW + w]);
+    }
+    const unsigned big = __float_as_uint(3.0e38f);  // squares at or above it go to FP64
+    if (ma >= big || mb >= big) {
+        const double a = block_max<NW>(exa(), shd);
+        const double b = block_max<NW>(exb(), shd + NW);
+        na = a;
+        nb = b;
+    } else if (tid == 0) {  // FP64 square roots are slow here: thread 0 only
+        na = sqrt((double)__uint_as_float(ma));
+        nb = sqrt((double)__uint_as_float(mb));
+    } else {
+        na = nb = 0.0;
+    }
+}

@@ -133,6 +133,8 @@ struct S3Args {
     int* err;            // device error word: 1 = a bounded wait gave up
     const float* packed; // FP32: tile-packed 21 C_ij + 6 gamma factors (bulk stress kernel), or NULL
     int bulk_variant;    // FP32: occupancy variant of the bulk stress kernel
+    int prefetch;        // FP32: L2 prefetch distance in tiles of the stress kernel (0 = off)
+    int prefetch_v;      // FP32: the same for the velocity kernel
 };
 // TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
 // (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes

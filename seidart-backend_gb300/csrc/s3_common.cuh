@@ -92,4 +92,30 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  : "memory");
 }
 
+// ------------------------------------------------------ L2 prefetch
+__device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Prefetch into L2 the rows of one 32 x 8 tile (tile indices tx, ty, plane k)
+// of `narr` arrays; row segment q of array q / 8 is covered by its first and
+// last element (a 128-byte segment spans at most two lines).  Work is spread
+// over the CTA's threads (tid of nthreads).
+__device__ __forceinline__ void pf_tile_rows(const float* const* arr, int narr, int tx, int ty, int k, int nx, int ny,
+                                             int tid, int nthreads) {
+    const int x0 = tx * 32, x1 = min(x0 + 31, nx - 1);
+    for (int q = tid; q < narr * 8; q += nthreads) {
+        const int y = ty * 8 + (q & 7);
+        if (y >= ny) continue;
+        const float* row = arr[q >> 3] + ((size_t)k * ny + y) * nx;
+        pf_l2(row + x0);
+        pf_l2(row + x1);
+    }
+}
+
+// true when the 32 x 8 tile (tx, ty, k) lies inside the inert interior box,
+// where no CPML memory or coefficient is touched
+__device__ __forceinline__ bool tile_in_box(const BoxH& b, int tx, int ty, int k, int nx, int ny) {
+    const int x0 = tx * 32, x1 = min(x0 + 32, nx), y0 = ty * 8, y1 = min(y0 + 8, ny);
+    return x0 >= b.i0 && x1 <= b.i1 && y0 >= b.j0 && y1 <= b.j1 && k >= b.k0 && k < b.k1;
+}
+
 }  // namespace s3

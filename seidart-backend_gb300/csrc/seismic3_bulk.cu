@@ -38,13 +38,32 @@ __global__ void __launch_bounds__(NT) s3b_pack(S3Args<float> A, float* P) {
     for (int q = 0; q < 6; ++q) dst[(21 + q) * NT] = in ? A.g[q][c] : 0.0f;
 }
 
+// L2 prefetch of everything the CTA `dist` tiles later in launch order will
+// read: its coefficient block, old stresses and velocities, and on shell
+// tiles the CPML memories and coefficients.  A hint only: no registers or
+// shared memory stay allocated for it.
+__device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, int tid) {
+    const long gx = gridDim.x, gy = gridDim.y;
+    const long lin = blockIdx.x + gx * (blockIdx.y + gy * (long)blockIdx.z) + dist;
+    if (lin >= gx * gy * (long)gridDim.z) return;
+    const int tx = (int)(lin % gx), ty = (int)((lin / gx) % gy), k = (int)(lin / (gx * gy));
+    if (k < 1 || k > A.nz - 2) return;
+    if (tid < NCOEF * NT / 32) pf_l2(A.packed + lin * (NCOEF * NT) + tid * 32);
+    pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, NT);
+    if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {
+        pf_tile_rows(A.mem, 36, tx, ty, k, A.nx, A.ny, tid, NT);
+        pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, NT);
+    }
+}
+
 template <int MINB>
 __global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
     extern __shared__ __align__(128) float coef[];  // [27][NT]
     __shared__ __align__(8) unsigned long long bar;
     const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
-    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
     const int tid = threadIdx.y * BX + threadIdx.x;
+    if (A.prefetch > 0) s3b_prefetch(A, A.prefetch, tid);
+    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
     if (tid == 0) {
         const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
         mbar_init(&bar, 1);

@@ -106,9 +106,26 @@ __global__ void __launch_bounds__(BX* BY) s3c_stress(S3Args<float> A) {
     }
 }
 
+// L2 prefetch for the CTA `dist` tiles later in launch order: stresses,
+// velocities, density, and on shell tiles the velocity-loop memories and the
+// CPML coefficients (a hint; nothing stays allocated for it)
+__device__ __forceinline__ void s3c_velocity_prefetch(const S3Args<float>& A, int dist, int tid) {
+    const long gx = gridDim.x, gy = gridDim.y;
+    const long lin = blockIdx.x + gx * (blockIdx.y + gy * (long)blockIdx.z) + dist;
+    if (lin >= gx * gy * (long)gridDim.z) return;
+    const int tx = (int)(lin % gx), ty = (int)((lin / gx) % gy), k = (int)(lin / (gx * gy));
+    pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, BX * BY);
+    pf_tile_rows(&A.rho, 1, tx, ty, k, A.nx, A.ny, tid, BX * BY);
+    if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {
+        pf_tile_rows(A.mem + 36, 9, tx, ty, k, A.nx, A.ny, tid, BX * BY);
+        pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, BX * BY);
+    }
+}
+
 __global__ void __launch_bounds__(BX* BY) s3c_velocity(S3Args<float> A, StepInfo si) {
-    __shared__ float redf[2][BX * BY / 32];
+    __shared__ unsigned redu[2 * BX * BY / 32];
     __shared__ double redd[2][BX * BY / 32];
+    if (A.prefetch_v > 0) s3c_velocity_prefetch(A, A.prefetch_v, threadIdx.y * BX + threadIdx.x);
     const int it = *si.step;
     const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
     const int nx = A.nx, ny = A.ny, nz = A.nz;
@@ -198,15 +215,14 @@ __global__ void __launch_bounds__(BX* BY) s3c_velocity(S3Args<float> A, StepInfo
             ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
         }
     }
-    const double vn = block_norm_f32<BX * BY / 32>(
-        vsq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); }, redf[0], redd[0]);
-    const double sn = block_norm_f32<BX * BY / 32>(
-        ssq,
+    double vn, sn;
+    block_norm2_f32<BX * BY / 32>(
+        vsq, ssq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); },
         [&] {
             const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
             return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
         },
-        redf[1], redd[1]);
+        redu, &redd[0][0], vn, sn);
     if ((threadIdx.x | threadIdx.y) == 0) {
         const int slot = (blockIdx.x + 7 * blockIdx.y + 13 * blockIdx.z) % NSLOT;
         atomic_max_nonneg(A.norms_part + slot, vn);
