@@ -99,97 +99,134 @@ __device__ __forceinline__ bool tile_cell(const BatchArgs& B, int t, const BMode
 
 #define IXM(fi, fk) ((size_t)((fi) - 1) + (size_t)nx * (size_t)((fk) - 1))
 
-// stress half-step of one cell (seismic2.cu FP32 arithmetic)
+// stress half-step of one cell (seismic2.cu FP32 arithmetic).  Every load
+// is issued before any arithmetic: the velocity stencil with clamped
+// (always valid) indices, the coefficients and old stresses, and on shell
+// cells the CPML coefficients and memories, so one cell costs one memory
+// round trip instead of a chain of them.
 __device__ __forceinline__ void cell_stress(const BModel& a, int i, int j) {
     const int nx = a.nx, nz = a.nz;
     const bool normal = (j >= 3 && j <= nz - 1 && i >= 2 && i <= nx - 2);
     const bool shear = (j >= 2 && j <= nz - 2 && i >= 3 && i <= nx - 1);
     if (!normal && !shear) return;
     const size_t c = IXM(i, j);
-    const float* __restrict__ vx = a.f[0];
-    const float* __restrict__ vz = a.f[1];
     const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
+    // clamped neighbour offsets (a cell only uses neighbours that exist)
+    const long xm2 = (long)max(i - 2, 1) - i, xm1 = (long)max(i - 1, 1) - i;
+    const long xp1 = (long)min(i + 1, nx) - i, xp2 = (long)min(i + 2, nx) - i;
+    const long zm2 = ((long)max(j - 2, 1) - j) * nx, zm1 = ((long)max(j - 1, 1) - j) * nx;
+    const long zp1 = ((long)min(j + 1, nz) - j) * nx, zp2 = ((long)min(j + 2, nz) - j) * nx;
+    // fields are written by this kernel across grid barriers: plain loads,
+    // never the read-only path; coefficients are constant and use __ldg
+    const float* VX = a.f[0] + c;
+    const float* VZ = a.f[1] + c;
+    const float x0 = VX[0], xa = VX[xm2], xb = VX[xm1], xc = VX[xp1], xd = VX[xp2];
+    const float xe = VX[zm2], xf = VX[zm1], xg = VX[zp1], xh = VX[zp2];
+    const float z0 = VZ[0], za = VZ[xm2], zb = VZ[xm1], zc = VZ[xp1], zd = VZ[xp2];
+    const float ze = VZ[zm2], zf = VZ[zm1], zg = VZ[zp1], zh = VZ[zp2];
+    const float c11 = __ldg(a.m[0] + c), c13 = __ldg(a.m[1] + c), c15 = __ldg(a.m[2] + c);
+    const float c33 = __ldg(a.m[3] + c), c35 = __ldg(a.m[4] + c), c55 = __ldg(a.m[5] + c);
+    const float gx = __ldg(a.m[7] + c), gz = __ldg(a.m[8] + c), gxz = __ldg(a.m[9] + c);
+    const float sxx = a.f[2][c], szz = a.f[3][c], sxz = a.f[4][c];
+    float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (pml) {
+        kap = __ldg(a.m[10] + c); kaph = __ldg(a.m[11] + c); aa = __ldg(a.m[12] + c);
+        ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) m[q] = a.mem[q][c];
+    }
     const float dt = a.dt, hx = a.hx, hz = a.hz;
 #define D4(p1, p0, p2, m1, h) ((27.0f * ((p1) - (p0)) - ((p2) - (m1))) * (h))
     if (normal) {
-        float dvx_dx = D4(vx[IXM(i + 1, j)], vx[c], vx[IXM(i + 2, j)], vx[IXM(i - 1, j)], hx);
-        float dvz_dz = D4(vz[c], vz[IXM(i, j - 1)], vz[IXM(i, j + 1)], vz[IXM(i, j - 2)], hz);
-        float dvz_dx = D4(vz[IXM(i + 1, j)], vz[c], vz[IXM(i + 2, j)], vz[IXM(i - 1, j)], hx);
-        float dvx_dz = D4(vx[c], vx[IXM(i, j - 1)], vx[IXM(i, j + 1)], vx[IXM(i, j - 2)], hz);
+        float dvx_dx = D4(xc, x0, xd, xb, hx);
+        float dvz_dz = D4(z0, zf, zg, ze, hz);
+        float dvz_dx = D4(zc, z0, zd, zb, hx);
+        float dvx_dz = D4(x0, xf, xg, xe, hz);
         if (pml) {
-            const float bh = a.m[15][c], ah = a.m[13][c], b = a.m[14][c], aa = a.m[12][c];
-            const float M0 = bh * a.mem[0][c] + ah * dvx_dx, M1 = bh * a.mem[1][c] + ah * dvx_dz;
-            const float M3 = b * a.mem[3][c] + aa * dvz_dz, M2 = b * a.mem[2][c] + aa * dvz_dx;
+            const float M0 = bh * m[0] + ah * dvx_dx, M1 = bh * m[1] + ah * dvx_dz;
+            const float M3 = b * m[3] + aa * dvz_dz, M2 = b * m[2] + aa * dvz_dx;
             a.mem[0][c] = M0; a.mem[1][c] = M1; a.mem[2][c] = M2; a.mem[3][c] = M3;
-            dvx_dx = dvx_dx * a.m[11][c] + M0;
-            dvx_dz = dvx_dz * a.m[11][c] + M1;
-            dvz_dz = dvz_dz * a.m[10][c] + M3;
-            dvz_dx = dvz_dx * a.m[10][c] + M2;
+            dvx_dx = dvx_dx * kaph + M0;
+            dvx_dz = dvx_dz * kaph + M1;
+            dvz_dz = dvz_dz * kap + M3;
+            dvz_dx = dvz_dx * kap + M2;
         }
-        const float c11 = a.m[0][c], c13 = a.m[1][c], c15 = a.m[2][c], c33 = a.m[3][c], c35 = a.m[4][c];
-        a.f[2][c] = (a.f[2][c] + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * a.m[7][c];
-        a.f[3][c] = (a.f[3][c] + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * a.m[8][c];
+        a.f[2][c] = (sxx + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * gx;
+        a.f[3][c] = (szz + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * gz;
     }
     if (shear) {
-        float dvx_dx = D4(vx[c], vx[IXM(i - 1, j)], vx[IXM(i + 1, j)], vx[IXM(i - 2, j)], hx);
-        float dvz_dz = D4(vz[IXM(i, j + 1)], vz[c], vz[IXM(i, j + 2)], vz[IXM(i, j - 1)], hz);
-        float dvz_dx = D4(vz[c], vz[IXM(i - 1, j)], vz[IXM(i + 1, j)], vz[IXM(i - 2, j)], hx);
-        float dvx_dz = D4(vx[IXM(i, j + 1)], vx[c], vx[IXM(i, j + 2)], vx[IXM(i, j - 1)], hz);
+        float dvx_dx = D4(x0, xb, xc, xa, hx);
+        float dvz_dz = D4(zg, z0, zh, zf, hz);
+        float dvz_dx = D4(z0, zb, zc, za, hx);
+        float dvx_dz = D4(xg, x0, xh, xf, hz);
         if (pml) {
-            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
-            const float M4 = bh * a.mem[4][c] + ah * dvx_dx, M5 = bh * a.mem[5][c] + ah * dvx_dz;
-            const float M7 = bh * a.mem[7][c] + ah * dvz_dz, M6 = bh * a.mem[6][c] + ah * dvz_dx;
+            const float M4 = bh * m[4] + ah * dvx_dx, M5 = bh * m[5] + ah * dvx_dz;
+            const float M7 = bh * m[7] + ah * dvz_dz, M6 = bh * m[6] + ah * dvz_dx;
             a.mem[4][c] = M4; a.mem[5][c] = M5; a.mem[6][c] = M6; a.mem[7][c] = M7;
-            dvx_dx = dvx_dx * kh + M4;
-            dvx_dz = dvx_dz * kh + M5;
-            dvz_dz = dvz_dz * kh + M7;
-            dvz_dx = dvz_dx * kh + M6;
+            dvx_dx = dvx_dx * kaph + M4;
+            dvx_dz = dvx_dz * kaph + M5;
+            dvz_dz = dvz_dz * kaph + M7;
+            dvz_dx = dvz_dx * kaph + M6;
         }
-        const float c15 = a.m[2][c], c35 = a.m[4][c], c55 = a.m[5][c];
-        a.f[4][c] = (a.f[4][c] + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * a.m[9][c];
+        a.f[4][c] = (sxz + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * gxz;
     }
 #undef D4
 }
 
-// velocity half-step, force source, Dirichlet ring; returns the cell's |v|
+// velocity half-step, force source, Dirichlet ring; returns the cell's |v|^2.
+// Loads first, as in cell_stress.
 __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, int it, float (&vo)[2]) {
     const int nx = a.nx, nz = a.nz;
     const size_t c = IXM(i, j);
-    const float *sxx = a.f[2], *szz = a.f[3], *sxz = a.f[4], *rho = a.m[6];
     const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
-    const float dt = a.dt, hx = a.hx, hz = a.hz;
+    const bool ux = (j >= 3 && j <= nz - 1 && i >= 3 && i <= nx - 1);
+    const bool uz = (j >= 2 && j <= nz - 2 && i >= 2 && i <= nx - 2);
+    const long xm2 = (long)max(i - 2, 1) - i, xm1 = (long)max(i - 1, 1) - i;
+    const long xp1 = (long)min(i + 1, nx) - i, xp2 = (long)min(i + 2, nx) - i;
+    const long zm2 = ((long)max(j - 2, 1) - j) * nx, zm1 = ((long)max(j - 1, 1) - j) * nx;
+    const long zp1 = ((long)min(j + 1, nz) - j) * nx, zp2 = ((long)min(j + 2, nz) - j) * nx;
+    const float *SXX = a.f[2] + c, *SZZ = a.f[3] + c, *SXZ = a.f[4] + c, *R = a.m[6] + c;
+    const float s0 = SXX[0], sm1 = SXX[xm1], sm2 = SXX[xm2];
+    const float q0 = SXZ[0], qm1 = SXZ[zm1], qm2 = SXZ[zm2], qp1 = SXZ[xp1], qp2 = SXZ[xp2];
+    const float w0 = SZZ[0], wp1 = SZZ[zp1], wp2 = SZZ[zp2];
+    const float r0 = __ldg(R), rxm = __ldg(R + xm1), rzm = __ldg(R + zm1), rxp = __ldg(R + xp1), rzp = __ldg(R + zp1);
     float vx = a.f[0][c], vz = a.f[1][c];
-    if (j >= 3 && j <= nz - 1 && i >= 3 && i <= nx - 1) {
-        const float bxx = inv_mean_f(rho[c], rho[IXM(i - 1, j)], a.density_code);
-        const float bzx = inv_mean_f(rho[c], rho[IXM(i, j - 1)], a.density_code);
-        float d1 = (27.0f * (sxx[c] - sxx[IXM(i - 1, j)]) + sxx[IXM(i - 2, j)]) * hx;
-        float d2 = (27.0f * (sxz[c] - sxz[IXM(i, j - 1)]) + sxz[IXM(i, j - 2)]) * hz;
+    float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m8 = 0.f, m9 = 0.f, m10 = 0.f, m11 = 0.f;
+    if (pml) {
+        kap = __ldg(a.m[10] + c); kaph = __ldg(a.m[11] + c); aa = __ldg(a.m[12] + c);
+        ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
+        m8 = a.mem[8][c]; m9 = a.mem[9][c]; m10 = a.mem[10][c]; m11 = a.mem[11][c];
+    }
+    const float dt = a.dt, hx = a.hx, hz = a.hz;
+    if (ux) {
+        const float bxx = inv_mean_f(r0, rxm, a.density_code);
+        const float bzx = inv_mean_f(r0, rzm, a.density_code);
+        float d1 = (27.0f * (s0 - sm1) + sm2) * hx;
+        float d2 = (27.0f * (q0 - qm1) + qm2) * hz;
         if (pml) {
-            const float b = a.m[14][c], aa = a.m[12][c], k = a.m[10][c];
-            const float M8 = b * a.mem[8][c] + aa * d1, M11 = b * a.mem[11][c] + aa * d2;
+            const float M8 = b * m8 + aa * d1, M11 = b * m11 + aa * d2;
             a.mem[8][c] = M8; a.mem[11][c] = M11;
-            d1 = d1 * k + M8;
-            d2 = d2 * k + M11;
+            d1 = d1 * kap + M8;
+            d2 = d2 * kap + M11;
         }
         vx = vx + dt * (d1 * bxx + d2 * bzx);
     }
-    if (j >= 2 && j <= nz - 2 && i >= 2 && i <= nx - 2) {
-        const float bxz = inv_mean_f(rho[c], rho[IXM(i + 1, j)], a.density_code);
-        const float bzz = inv_mean_f(rho[c], rho[IXM(i, j + 1)], a.density_code);
-        float d1 = (27.0f * (sxz[IXM(i + 1, j)] - sxz[c]) - sxz[IXM(i + 2, j)]) * hx;
-        float d2 = (27.0f * (szz[IXM(i, j + 1)] - szz[c]) - szz[IXM(i, j + 2)]) * hz;
+    if (uz) {
+        const float bxz = inv_mean_f(r0, rxp, a.density_code);
+        const float bzz = inv_mean_f(r0, rzp, a.density_code);
+        float d1 = (27.0f * (qp1 - q0) - qp2) * hx;
+        float d2 = (27.0f * (wp1 - w0) - wp2) * hz;
         if (pml) {
-            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
-            const float M10 = bh * a.mem[10][c] + ah * d1, M9 = bh * a.mem[9][c] + ah * d2;
+            const float M10 = bh * m10 + ah * d1, M9 = bh * m9 + ah * d2;
             a.mem[10][c] = M10; a.mem[9][c] = M9;
-            d1 = d1 * kh + M10;
-            d2 = d2 * kh + M9;
+            d1 = d1 * kaph + M10;
+            d2 = d2 * kaph + M9;
         }
         vz = vz + dt * (d1 * bxz + d2 * bzz);
     }
     if (i - 1 == a.isrc && j - 1 == a.jsrc) {
-        if (a.src[0]) vx = vx + (float)a.src[0][it - 1] / rho[c];
-        if (a.src[1]) vz = vz + (float)a.src[1][it - 1] / rho[c];
+        if (a.src[0]) vx = vx + (float)a.src[0][it - 1] / r0;
+        if (a.src[1]) vz = vz + (float)a.src[1][it - 1] / r0;
     }
     if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0.f; vz = 0.f; }
     a.f[0][c] = vx;
@@ -248,16 +285,132 @@ __global__ void __launch_bounds__(TX* TY) s2b_persistent(BatchArgs B, int nsteps
     if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) *B.step = it0 + nsteps;
 }
 
+__device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// L2 prefetch of every row tile t will read: velocities and stresses, the ten
+// per-cell coefficients (C, rho, gamma) and, on tiles reaching outside the
+// inert box, the 12 memories and 6 CPML coefficients.  A hint: nothing stays
+// allocated for it.
+template <int TX, int TY>
+__device__ __forceinline__ void tile_prefetch(const BatchArgs& B, int t, int tid) {
+    const BModel& M = B.models[B.tile_model[t]];
+    const int lt = t - M.tile0, tx = lt % M.tiles_x, tz = lt / M.tiles_x;
+    const int x0 = tx * TX, x1 = min(x0 + TX, M.nx) - 1, z0 = tz * TY, z1 = min(z0 + TY, M.nz);
+    const bool shell = !(x0 >= M.box.i0 && x1 < M.box.i1 && z0 >= M.box.k0 && z1 <= M.box.k1);
+    const int narr = shell ? 33 : 15;
+    for (int q = tid; q < narr * TY; q += TX * TY) {
+        const int a = q / TY, y = z0 + q % TY;
+        if (y >= z1) continue;
+        const float* base = a < 5 ? M.f[a] : a < 15 ? M.m[a - 5] : a < 27 ? M.mem[a - 15] : M.m[10 + a - 27];
+        const float* row = base + (size_t)y * M.nx;
+        pf_l2(row + x0);
+        if (TX > 32 && x0 + 32 <= x1) pf_l2(row + x0 + 32);
+        pf_l2(row + x1);
+    }
+}
+
+// Per-warp running max-norm of the current model, flushed with one atomic
+// when the tile walk moves to another model.  Squares are reduced as bit
+// patterns (redux.sync); a warp whose square reaches 3e38 (overflow, inf,
+// NaN) takes the FP64 norm of its cells instead.
+struct WarpNorm {
+    int model = -1;
+    float fmax = 0.0f;
+    double dmax = 0.0;
+    __device__ __forceinline__ void flush(const BatchArgs& B, int it, int lane) {
+        if (model >= 0 && lane == 0) atomic_max_nonneg(&B.models[model].norms[it - 1], nanmax(sqrt((double)fmax), dmax));
+        fmax = 0.0f;
+        dmax = 0.0;
+    }
+    __device__ __forceinline__ void add(float sq, const float (&vo)[2]) {
+        const unsigned u = __reduce_max_sync(0xffffffffu, __float_as_uint(sq));
+        if (u >= __float_as_uint(3.0e38f)) {
+            double e = sqrt((double)vo[0] * vo[0] + (double)vo[1] * vo[1]);
+            for (int o = 16; o > 0; o >>= 1) e = nanmax(e, __shfl_xor_sync(0xffffffffu, e, o));
+            dmax = nanmax(dmax, e);
+        } else {
+            fmax = fmaxf(fmax, __uint_as_float(u));
+        }
+    }
+};
+
+// Contiguous-range variant: CTA b walks tiles [b*T/G, (b+1)*T/G) in order, so
+// its tiles mostly share one model (descriptor stays in L1) and neighbouring
+// tile rows stay in L2; the rows of tile t+PD are prefetched while tile t
+// computes.
+template <int TX, int TY, int PD>
+__global__ void __launch_bounds__(TX* TY) s2b_chunked(BatchArgs B, int nsteps) {
+    const int tid = threadIdx.x + TX * threadIdx.y, lane = tid & 31;
+    const int t0 = (int)((long long)B.ntiles * blockIdx.x / gridDim.x);
+    const int t1 = (int)((long long)B.ntiles * (blockIdx.x + 1) / gridDim.x);
+    const int it0 = *B.step;
+    for (int s = 0; s < nsteps; ++s) {
+        const int it = it0 + s;
+        // phase 1: stress
+        for (int t = t0; t < t1; ++t) {
+            if (t + PD < t1) tile_prefetch<TX, TY>(B, t + PD, tid);
+            const BModel* M;
+            int i, j;
+            if (tile_cell<TX, TY>(B, t, M, i, j)) cell_stress(*M, i, j);
+        }
+        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY>(B, t, tid);
+        if (!grid_barrier(B)) return;
+        // phase 2: velocity, force source, Dirichlet, norms
+        WarpNorm wn;
+        for (int t = t0; t < t1; ++t) {
+            if (t + PD < t1) tile_prefetch<TX, TY>(B, t + PD, tid);
+            const int m = B.tile_model[t];
+            if (m != wn.model) {
+                wn.flush(B, it, lane);
+                wn.model = m;
+            }
+            const BModel* M;
+            int i, j;
+            float sq = 0.f, vo[2] = {0.f, 0.f};
+            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity(*M, i, j, it, vo);
+            wn.add(sq, vo);
+        }
+        wn.flush(B, it, lane);
+        if (!grid_barrier(B)) return;
+        // phase 3: per-model stress source and receivers
+        for (int m = blockIdx.x; m < B.nmodels; m += gridDim.x) {
+            const BModel& a = B.models[m];
+            if (a.stress_src && tid == 0) {
+                const int nx = a.nx;
+                const size_t c = IXM(a.isrc + 1, a.jsrc + 1), c1 = IXM(a.isrc + 2, a.jsrc + 2);
+                const float* rho = a.m[6];
+                if (a.src[2]) a.f[2][c] = a.f[2][c] + (float)a.src[2][it - 1] / rho[c];
+                if (a.src[3]) a.f[4][c1] = a.f[4][c1] + (float)a.src[3][it - 1] / rho[c1];
+                if (a.src[4]) a.f[3][c] = a.f[3][c] + (float)a.src[4][it - 1] / rho[c];
+            }
+            for (int r = tid; r < a.nrec; r += TX * TY) {
+                const size_t base = (size_t)(it - 1) * 2 * a.nrec;
+                a.traces[base + r] = a.f[0][a.rec[r]];
+                a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
+            }
+        }
+        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY>(B, t, tid);
+        if (!grid_barrier(B)) return;
+    }
+    if (blockIdx.x == 0 && tid == 0) *B.step = it0 + nsteps;
+}
+
 struct Variant {
     int tx, ty;
     const void* fn;
+    const char* walk;  // "strided": tile b, b+G, ...; "chunked": a contiguous range per CTA
 };
 const Variant kVariants[] = {
-    {32, 4, (const void*)s2b_persistent<32, 4>},
-    {32, 8, (const void*)s2b_persistent<32, 8>},
-    {64, 4, (const void*)s2b_persistent<64, 4>},
-    {32, 16, (const void*)s2b_persistent<32, 16>},
-    {64, 8, (const void*)s2b_persistent<64, 8>},
+    {32, 4, (const void*)s2b_persistent<32, 4>, "strided"},
+    {32, 8, (const void*)s2b_persistent<32, 8>, "strided"},
+    {64, 4, (const void*)s2b_persistent<64, 4>, "strided"},
+    {32, 16, (const void*)s2b_persistent<32, 16>, "strided"},
+    {64, 8, (const void*)s2b_persistent<64, 8>, "strided"},
+    {32, 8, (const void*)s2b_chunked<32, 8, 1>, "chunked"},
+    {32, 8, (const void*)s2b_chunked<32, 8, 2>, "chunked"},
+    {64, 4, (const void*)s2b_chunked<64, 4, 2>, "chunked"},
+    {32, 4, (const void*)s2b_chunked<32, 4, 2>, "chunked"},
+    {32, 16, (const void*)s2b_chunked<32, 16, 1>, "chunked"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

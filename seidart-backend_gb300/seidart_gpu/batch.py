@@ -110,6 +110,16 @@ class Batch:
         _check(lib().seidart_batch_config(self.handle, C.byref(tx), C.byref(ty), C.byref(bps), C.byref(grid)))
         return {"tile": [tx.value, ty.value], "ctas_per_sm": bps.value, "grid": grid.value}
 
+    def set_config(self, variant: int, ctas_per_sm: int) -> None:
+        """Use kernel variant ``variant`` (0 .. num_variants-1) with the given
+        CTAs per SM instead of the autotuned choice."""
+        _check(lib().seidart_batch_set_config(self.handle, int(variant), int(ctas_per_sm)))
+
+    @staticmethod
+    def num_variants() -> int:
+        _declare()
+        return lib().seidart_batch_num_variants()
+
     def _solver(self, m: int):
         return lib().seidart_batch_model(self.handle, m)
 

@@ -39,6 +39,24 @@ def test_batch_matches_single_model_runs(oracle):
             assert rel_l2(nrm, o["norms"]) <= 1e-4
 
 
+@pytest.mark.parametrize("variant", range(10))
+def test_every_kernel_variant_matches_single_runs(variant):
+    if variant >= Batch.num_variants():
+        pytest.skip("variant not built")
+    probs = small_batch(nt=40)
+    probs[1].src["zz"] = 0.25 * probs[1].src["z"]
+    with Batch(probs, autotune=False) as b:
+        b.set_config(variant, 1)
+        b.step(15, chunk=7)
+        b.step(probs[0].time_steps - 15)
+        b.sync()
+        for m, p in enumerate(probs):
+            single = sg.run(p, sg.FP32)
+            tr, nrm = b.traces(m)
+            assert rel_l2(tr, single["traces"]) <= 1e-6, (variant, m)
+            assert rel_l2(nrm, single["norms"]) <= 1e-6, (variant, m)
+
+
 def test_bounded_barrier_timeout_reports_status():
     """A barrier that can never complete gives up within its spin budget;
     the host sees SEIDART_ERR_TIMEOUT and the context stays usable."""
