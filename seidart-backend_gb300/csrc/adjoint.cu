@@ -35,6 +35,7 @@
 
 extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
 extern "C" int seidart_solver_internal_reset(SeidartSolver* s);
+extern "C" int seidart_solver_internal_advance(SeidartSolver* s, int nsteps);
 extern "C" int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done);
 extern "C" int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
                                                   const double* dev_srcz);
@@ -337,30 +338,41 @@ __global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
 
 }  // namespace
 
-struct SeidartFwi {
+// One shot in flight: its own solver (model copy, fields, stream, graphs),
+// checkpoint and segment buffers, adjoint state and FP64 gradient sums.
+// Lanes run concurrently on their own streams; their gradients are summed
+// on the device at the end.
+struct FwiLane {
     SeidartSolver* s = nullptr;
     S2Args<float> a{};
     const int* rec = nullptr;
-    int nrec = 0, nt = 0, nshots = 0, K = 1, G = 1, density = 3;
-    size_t N = 0;
     cudaStream_t st = nullptr;
-    std::vector<int> sx, sz;
-    double* dsrc = nullptr;     // [nshots][nt] force series (device)
-    float* dobs = nullptr;      // [nshots][nt][2][nrec] observed traces
-    float* dres = nullptr;      // [nt][2][nrec] residual of the current shot
+    StepInfo si{};
+    StatePtrs ptrs{};
+    int shot = -1;              // shot the lane's solver and graphs are set up for
+    bool graphs = false;        // segment graphs captured for `shot`
     float* ckpt = nullptr;      // [G][NS][N]
     float* seg = nullptr;       // [K+1][NS][N]
     float* lam = nullptr;       // [NS][N]
     float* scr = nullptr;       // [12][N]
+    float* dres = nullptr;      // [nt][2][nrec] residual of the lane's shot
     double* grad = nullptr;     // [8][N]
-    double* dscal = nullptr;    // [0] loss, [1] source term
+    double* dscal = nullptr;    // [0] misfit of the lane's shots
     int* dbase = nullptr;       // device segment base (steps before the segment)
-    std::vector<double> srch;   // host copy of the source series
-    StatePtrs ptrs{};
-    StepInfo si{};
-    // per-shot graphs: [0] full segments of K steps, [1] the shorter last one
+    // [0] full segments of K steps, [1] the shorter last one
     cudaGraphExec_t rec_exec[2] = {nullptr, nullptr}, adj_exec[2] = {nullptr, nullptr};
-    int graph_len[2] = {0, 0};
+    long long launches = 0;
+};
+
+struct SeidartFwi {
+    std::vector<FwiLane> lanes;
+    int nrec = 0, nt = 0, nshots = 0, K = 1, G = 1, density = 3;
+    size_t N = 0;
+    std::vector<int> sx, sz;
+    double* dsrc = nullptr;     // [nshots][nt] force series (device)
+    float* dobs = nullptr;      // [nshots][nt][2][nrec] observed traces
+    double* dgsrc = nullptr;    // [nshots] sum_n lambda_vz(src) f_n per shot
+    std::vector<double> srch;   // host copy of the source series
     long long launches = 0;
 };
 
@@ -376,64 +388,84 @@ int ferr(int code, const std::string& m) {
         if (e_ != cudaSuccess) return ferr(SEIDART_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
 
-AdjArgs adj_args(SeidartFwi* f, const float* xp, const float* xc, const double* srcz, int j) {
+// sum of lane gradients: dst[q] += src[q]
+__global__ void add_grad(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] += src[q];
+}
+
+AdjArgs adj_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, const double* srcz, int j) {
     AdjArgs A{};
-    A.nx = f->a.nx; A.nz = f->a.nz; A.density_code = f->a.density_code;
-    A.dt = f->a.dt; A.hx = 1.0f / (24.0f * f->a.dx); A.hz = 1.0f / (24.0f * f->a.dz);
-    A.box = f->a.box;
-    for (int q = 0; q < 16; ++q) A.m[q] = f->a.m[q];
-    A.xp = xp; A.xc = xc; A.lam = f->lam; A.scr = f->scr; A.grad = f->grad; A.N = f->N;
-    A.isrc = f->a.isrc; A.jsrc = f->a.jsrc; A.srcz = srcz; A.gsrc = f->dscal + 1;
-    A.base = f->dbase; A.j = j;
+    A.nx = L.a.nx; A.nz = L.a.nz; A.density_code = L.a.density_code;
+    A.dt = L.a.dt; A.hx = 1.0f / (24.0f * L.a.dx); A.hz = 1.0f / (24.0f * L.a.dz);
+    A.box = L.a.box;
+    for (int q = 0; q < 16; ++q) A.m[q] = L.a.m[q];
+    A.xp = xp; A.xc = xc; A.lam = L.lam; A.scr = L.scr; A.grad = L.grad; A.N = f->N;
+    A.isrc = L.a.isrc; A.jsrc = L.a.jsrc; A.srcz = srcz;
+    A.gsrc = f->dgsrc + (L.shot >= 0 ? L.shot : 0);
+    A.base = L.dbase; A.j = j;
     return A;
 }
 
-// adjoint of step n = *dbase + j (launched on f->st, possibly under capture)
-void adjoint_step(SeidartFwi* f, int j, const float* xp, const float* xc, const double* srcz) {
-    const dim3 blk(BX, BY), grd((f->a.nx + BX - 1) / BX, (f->a.nz + BY - 1) / BY);
-    if (f->nrec > 0) adj_inject<<<1, 256, 0, f->st>>>(f->lam, f->N, f->rec, f->nrec, f->dres, f->dbase, j);
-    const AdjArgs A = adj_args(f, xp, xc, srcz, j);
-    adj_velocity<<<grd, blk, 0, f->st>>>(A);
-    adj_stress<<<grd, blk, 0, f->st>>>(A);
-    adj_gather_v<<<grd, blk, 0, f->st>>>(A);
-    f->launches += 4;
+// adjoint of step n = *dbase + j (launched on the lane's stream, possibly under capture)
+void adjoint_step(SeidartFwi* f, FwiLane& L, int j, const float* xp, const float* xc, const double* srcz, int nrec) {
+    const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
+    if (nrec > 0) adj_inject<<<1, 256, 0, L.st>>>(L.lam, f->N, L.rec, nrec, L.dres, L.dbase, j);
+    const AdjArgs A = adj_args(f, L, xp, xc, srcz, j);
+    adj_velocity<<<grd, blk, 0, L.st>>>(A);
+    adj_stress<<<grd, blk, 0, L.st>>>(A);
+    adj_gather_v<<<grd, blk, 0, L.st>>>(A);
 }
 
-int save_state(SeidartFwi* f, float* blk) {
-    copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, blk, f->N, 1);
-    ++f->launches;
-    return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "state copy");
+void save_state(FwiLane& L, float* blk, size_t N) {
+    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, blk, N, 1);
+    ++L.launches;
 }
-int load_state(SeidartFwi* f, const float* blk) {
-    copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, const_cast<float*>(blk), f->N, 0);
-    ++f->launches;
-    return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "state copy");
+void load_state(FwiLane& L, const float* blk, size_t N) {
+    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, const_cast<float*>(blk), N, 0);
+    ++L.launches;
 }
 
-// forward run of shot `sh` with checkpoints; leaves traces in the solver
-int forward_shot(SeidartFwi* f, int sh, bool checkpoints) {
-    int rc = seidart_solver_internal_reset(f->s);
+// Point lane L at shot sh (its source position and series).  Waits for the
+// lane's stream only when the shot changes.
+int lane_set_shot(SeidartFwi* f, FwiLane& L, int sh) {
+    if (L.shot == sh) return SEIDART_OK;
+    const int rc = seidart_solver_internal_set_source(L.s, f->sx[sh], f->sz[sh], nullptr, f->dsrc + (size_t)sh * f->nt);
     if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    rc = seidart_solver_internal_set_source(f->s, f->sx[sh], f->sz[sh], nullptr, f->dsrc + (size_t)sh * f->nt);
-    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    S2Args<float> a;
-    seidart_solver_internal_s2f(f->s, &a, nullptr);
-    f->a = a;
-    for (int g = 0; g < f->G; ++g) {
-        const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
-        if (checkpoints && (rc = save_state(f, f->ckpt + (size_t)g * NS * f->N)) != SEIDART_OK) return rc;
-        rc = seidart_solver_step(f->s, len);
-        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-        f->launches += (long long)len * seidart_step_launches(SEIDART_SEISMIC2, f->a.stress_src);
-    }
+    seidart_solver_internal_s2f(L.s, &L.a, nullptr);
+    L.shot = sh;
+    L.graphs = false;
     return SEIDART_OK;
 }
 
-int shot_residual(SeidartFwi* f, int sh) {
+// zero the lane's state, traces and norms and restart its step counter,
+// all queued on the lane's stream (no host wait)
+int lane_reset(SeidartFwi* f, FwiLane& L) {
+    const size_t N = f->N;
+    for (int q = 0; q < NS; ++q) FCUDA(cudaMemsetAsync(L.ptrs.p[q], 0, sizeof(float) * N, L.st));
+    FCUDA(cudaMemsetAsync(L.a.traces, 0, sizeof(float) * (size_t)f->nt * 2 * (f->nrec > 0 ? f->nrec : 1), L.st));
+    FCUDA(cudaMemsetAsync(L.a.norms, 0, sizeof(double) * f->nt, L.st));
+    seg_begin<<<1, 1, 0, L.st>>>(L.si.step, L.dbase, 0);
+    FCUDA(cudaGetLastError());
+    seidart_solver_internal_advance(L.s, -seidart_solver_steps_done(L.s));
+    return SEIDART_OK;
+}
+
+// forward segment g of lane L (checkpoint first when asked)
+int lane_forward_segment(SeidartFwi* f, FwiLane& L, int g, bool checkpoints) {
+    const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
+    if (checkpoints) save_state(L, L.ckpt + (size_t)g * NS * f->N, f->N);
+    const int rc = seidart_solver_step(L.s, len);
+    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    L.launches += (long long)len * seidart_step_launches(SEIDART_SEISMIC2, L.a.stress_src);
+    return SEIDART_OK;
+}
+
+int lane_residual(SeidartFwi* f, FwiLane& L) {
     const size_t n = (size_t)f->nt * 2 * f->nrec;
-    const float* tr = (const float*)f->a.traces;
-    residual_loss<<<152, 256, 0, f->st>>>(tr, f->dobs + (size_t)sh * n, f->dres, n, f->dscal);
-    ++f->launches;
+    if (n == 0) return SEIDART_OK;
+    residual_loss<<<152, 256, 0, L.st>>>((const float*)L.a.traces, f->dobs + (size_t)L.shot * n, L.dres, n, L.dscal);
+    ++L.launches;
     return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "residual kernel");
 }
 
@@ -441,19 +473,21 @@ int shot_residual(SeidartFwi* f, int sh) {
 // segment buffer) or the adjoint graph (len adjoint steps, last to first)
 // and instantiate it into *exec, updating an existing executable in place
 // when the topology allows.
-int capture_segment(SeidartFwi* f, int len, bool adjoint, const double* srcz, cudaGraphExec_t* exec) {
+int capture_segment(SeidartFwi* f, FwiLane& L, int len, bool adjoint, cudaGraphExec_t* exec) {
     const size_t state = (size_t)NS * f->N;
-    FCUDA(cudaStreamBeginCapture(f->st, cudaStreamCaptureModeThreadLocal));
+    const double* srcz = f->dsrc + (size_t)L.shot * f->nt;
+    FCUDA(cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
     if (!adjoint) {
         for (int j = 1; j <= len; ++j) {
-            launch_seismic2_f32(f->a, f->si, f->st);
-            copy_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, f->seg + (size_t)j * state, f->N, 1);
+            launch_seismic2_f32(L.a, L.si, L.st);
+            copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, L.seg + (size_t)j * state, f->N, 1);
         }
     } else {
-        for (int j = len; j >= 1; --j) adjoint_step(f, j, f->seg + (size_t)(j - 1) * state, f->seg + (size_t)j * state, srcz);
+        for (int j = len; j >= 1; --j)
+            adjoint_step(f, L, j, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, srcz, f->nrec);
     }
     cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(f->st, &g);
+    cudaError_t e = cudaStreamEndCapture(L.st, &g);
     if (e != cudaSuccess || !g) {
         if (g) cudaGraphDestroy(g);
         return ferr(SEIDART_ERR_CUDA, std::string("segment capture: ") + cudaGetErrorString(e));
@@ -472,30 +506,102 @@ int capture_segment(SeidartFwi* f, int len, bool adjoint, const double* srcz, cu
     return SEIDART_OK;
 }
 
-int backward_shot(SeidartFwi* f, int sh) {
-    FCUDA(cudaMemsetAsync(f->lam, 0, sizeof(float) * NS * f->N, f->st));
-    const double* srcz = f->dsrc + (size_t)sh * f->nt;
+int lane_graphs(SeidartFwi* f, FwiLane& L) {
+    if (L.graphs) return SEIDART_OK;
     const int last = f->nt - (f->G - 1) * f->K;  // length of the last segment
     const int lens[2] = {f->K, last};
     for (int slot = 0; slot < 2; ++slot) {
         if (slot == 1 && last == f->K) break;
-        int rc = capture_segment(f, lens[slot], false, srcz, &f->rec_exec[slot]);
-        if (rc == SEIDART_OK) rc = capture_segment(f, lens[slot], true, srcz, &f->adj_exec[slot]);
+        int rc = capture_segment(f, L, lens[slot], false, &L.rec_exec[slot]);
+        if (rc == SEIDART_OK) rc = capture_segment(f, L, lens[slot], true, &L.adj_exec[slot]);
         if (rc != SEIDART_OK) return rc;
-        f->graph_len[slot] = lens[slot];
     }
-    const long long per_step = seidart_step_launches(SEIDART_SEISMIC2, f->a.stress_src) + 1;
-    for (int g = f->G - 1; g >= 0; --g) {
-        const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
-        const int slot = len == f->K ? 0 : 1;
-        seg_begin<<<1, 1, 0, f->st>>>(f->si.step, f->dbase, t0);
-        restore_state<<<4 * 152, 256, 0, f->st>>>(f->ptrs, f->ckpt + (size_t)g * NS * f->N, f->seg, f->N);
-        FCUDA(cudaGetLastError());
-        FCUDA(cudaGraphLaunch(f->rec_exec[slot], f->st));
-        FCUDA(cudaGraphLaunch(f->adj_exec[slot], f->st));
-        f->launches += 2 + len * per_step + len * (f->nrec > 0 ? 4 : 3);
+    L.graphs = true;
+    return SEIDART_OK;
+}
+
+// adjoint segment g of lane L: restore the checkpoint, recompute, walk back
+int lane_backward_segment(SeidartFwi* f, FwiLane& L, int g) {
+    const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
+    const int slot = len == f->K ? 0 : 1;
+    seg_begin<<<1, 1, 0, L.st>>>(L.si.step, L.dbase, t0);
+    restore_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, L.ckpt + (size_t)g * NS * f->N, L.seg, f->N);
+    FCUDA(cudaGetLastError());
+    FCUDA(cudaGraphLaunch(L.rec_exec[slot], L.st));
+    FCUDA(cudaGraphLaunch(L.adj_exec[slot], L.st));
+    const long long per_step = seidart_step_launches(SEIDART_SEISMIC2, L.a.stress_src) + 1;
+    L.launches += 2 + len * per_step + len * (f->nrec > 0 ? 4 : 3);
+    return SEIDART_OK;
+}
+
+// Run every shot: forward (with checkpoints when grad), misfit, and when grad
+// the adjoint sweep.  Shots go to lanes in rounds of nlanes; within a round
+// the host queues segment by segment across lanes so their streams overlap.
+int run_shots(SeidartFwi* f, bool grad, bool keep_traces_of_round, double* traces_out) {
+    const int nl = (int)f->lanes.size();
+    const size_t ntr = (size_t)f->nt * 2 * f->nrec;
+    for (int r0 = 0; r0 < f->nshots; r0 += nl) {
+        const int nr = std::min(nl, f->nshots - r0);
+        for (int l = 0; l < nr; ++l) {
+            int rc = lane_set_shot(f, f->lanes[l], r0 + l);
+            if (rc == SEIDART_OK) rc = lane_reset(f, f->lanes[l]);
+            if (rc != SEIDART_OK) return rc;
+        }
+        for (int g = 0; g < f->G; ++g)
+            for (int l = 0; l < nr; ++l) {
+                const int rc = lane_forward_segment(f, f->lanes[l], g, grad);
+                if (rc != SEIDART_OK) return rc;
+            }
+        for (int l = 0; l < nr; ++l) {
+            FwiLane& L = f->lanes[l];
+            const int rc = lane_residual(f, L);
+            if (rc != SEIDART_OK) return rc;
+            if (keep_traces_of_round) {
+                int rc2 = seidart_solver_sync(L.s);
+                if (rc2 == SEIDART_OK) rc2 = seidart_solver_traces(L.s, traces_out + (size_t)L.shot * ntr, nullptr);
+                if (rc2 != SEIDART_OK) return ferr(rc2, seidart_last_error());
+            }
+        }
+        if (!grad) continue;
+        for (int l = 0; l < nr; ++l) {
+            FwiLane& L = f->lanes[l];
+            FCUDA(cudaMemsetAsync(L.lam, 0, sizeof(float) * NS * f->N, L.st));
+            const int rc = lane_graphs(f, L);
+            if (rc != SEIDART_OK) return rc;
+        }
+        for (int g = f->G - 1; g >= 0; --g)
+            for (int l = 0; l < nr; ++l) {
+                const int rc = lane_backward_segment(f, f->lanes[l], g);
+                if (rc != SEIDART_OK) return rc;
+            }
     }
     return SEIDART_OK;
+}
+
+int sync_lanes(SeidartFwi* f) {
+    for (auto& L : f->lanes) {
+        const int rc = seidart_solver_sync(L.s);
+        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    }
+    return SEIDART_OK;
+}
+
+size_t lane_bytes(size_t N, int K, int G, int nt, int nrec) {
+    return sizeof(float) * ((size_t)G + K + 1 + 1 + 0) * NS * N + sizeof(float) * 12 * N + sizeof(double) * 8 * N +
+           sizeof(float) * (size_t)nt * 2 * (nrec > 0 ? nrec : 1) + sizeof(float) * 40 * N;  // + solver arena
+}
+
+void free_lane(FwiLane& L) {
+    if (L.st) cudaStreamSynchronize(L.st);
+    for (int q = 0; q < 2; ++q) {
+        if (L.rec_exec[q]) cudaGraphExecDestroy(L.rec_exec[q]);
+        if (L.adj_exec[q]) cudaGraphExecDestroy(L.adj_exec[q]);
+    }
+    for (void* p : {(void*)L.ckpt, (void*)L.seg, (void*)L.lam, (void*)L.scr, (void*)L.dres, (void*)L.grad,
+                    (void*)L.dscal, (void*)L.dbase})
+        if (p) cudaFree(p);
+    if (L.s) seidart_solver_destroy(L.s);
+    L = FwiLane();
 }
 
 }  // namespace
@@ -506,15 +612,9 @@ const char* seidart_fwi_last_error(void) { return g_ferr.c_str(); }
 
 int seidart_fwi_destroy(SeidartFwi* f) {
     if (!f) return SEIDART_OK;
-    if (f->st) cudaStreamSynchronize(f->st);
-    for (int q = 0; q < 2; ++q) {
-        if (f->rec_exec[q]) cudaGraphExecDestroy(f->rec_exec[q]);
-        if (f->adj_exec[q]) cudaGraphExecDestroy(f->adj_exec[q]);
-    }
-    for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dres, (void*)f->ckpt, (void*)f->seg, (void*)f->lam,
-                    (void*)f->scr, (void*)f->grad, (void*)f->dscal, (void*)f->dbase})
+    for (auto& L : f->lanes) free_lane(L);
+    for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dgsrc})
         if (p) cudaFree(p);
-    if (f->s) seidart_solver_destroy(f->s);
     delete f;
     return SEIDART_OK;
 }
@@ -522,7 +622,8 @@ int seidart_fwi_destroy(SeidartFwi* f) {
 // Create an FWI problem: one 2D elastic model (S2_* slots, host FP64), shots
 // with their own force position (interior indices) and vertical-force
 // series, a common receiver set, and observed traces per shot
-// ([time_steps][2][nrec], vx then vz).  checkpoint_every = 0 picks ceil(sqrt(nt)).
+// ([time_steps][2][nrec], vx then vz).  checkpoint_every = 0 picks
+// ceil(sqrt(nt)).  Up to one lane per shot, as device memory allows.
 int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const SeidartSource* src, int density_code,
                        const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
                        const double* const* shot_srcz, int nrec, const int* rec_cells,
@@ -535,19 +636,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     f->nshots = nshots;
     f->nrec = nrec;
     f->density = density_code;
-    const double* srcs[S2_NSRC] = {nullptr, shot_srcz[0], nullptr, nullptr, nullptr};
-    SeidartSource s0 = *src;
-    s0.xind = shot_xind[0];
-    s0.zind = shot_zind[0];
-    int rc = seidart_solver_create(&f->s, SEIDART_SEISMIC2, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
-                                   rec_cells);
-    if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
-    seidart_solver_internal_s2f(f->s, &f->a, &f->rec);
-    f->st = seidart_solver_internal_stream(f->s);
-    f->si = seidart_solver_internal_stepinfo(f->s);
     f->N = (size_t)dom->nx * dom->nz;
-    for (int q = 0; q < 5; ++q) f->ptrs.p[q] = f->a.f[q];
-    for (int q = 0; q < 12; ++q) f->ptrs.p[5 + q] = f->a.mem[q];
     f->K = checkpoint_every > 0 ? checkpoint_every : (int)ceil(sqrt((double)f->nt));
     f->G = (f->nt + f->K - 1) / f->K;
     for (int sh = 0; sh < nshots; ++sh) {
@@ -562,14 +651,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     const size_t nobs = (size_t)f->nt * 2 * nrec;
     if (cudaMalloc((void**)&f->dsrc, sizeof(double) * nshots * f->nt) != cudaSuccess ||
         cudaMalloc((void**)&f->dobs, sizeof(float) * nshots * (nobs ? nobs : 1)) != cudaSuccess ||
-        cudaMalloc((void**)&f->dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
-        cudaMalloc((void**)&f->ckpt, sizeof(float) * f->G * NS * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->seg, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->lam, sizeof(float) * NS * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
-        cudaMalloc((void**)&f->dscal, sizeof(double) * 2) != cudaSuccess ||
-        cudaMalloc((void**)&f->dbase, sizeof(int)) != cudaSuccess) {
+        cudaMalloc((void**)&f->dgsrc, sizeof(double) * nshots) != cudaSuccess) {
         cudaGetLastError();
         seidart_fwi_destroy(f);
         return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
@@ -584,6 +666,47 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
         }
         cudaMemcpy(f->dobs + (size_t)sh * nobs, tmp.data(), sizeof(float) * nobs, cudaMemcpyHostToDevice);
     }
+    // lanes: enough concurrent shots for about 1.2 M cells in flight (on a
+    // 552^2 grid 4 lanes measured 2.57 s per 16-shot gradient, 16 lanes
+    // 2.75 s, 1 lane 3.81 s), within 3/4 of the free device memory
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t per = lane_bytes(f->N, f->K, f->G, f->nt, nrec);
+    const size_t want = std::max<size_t>(1, (size_t)(1.2e6 / (double)f->N + 0.5));
+    int nl = (int)std::min<size_t>(std::min<size_t>((size_t)nshots, want), std::max<size_t>(1, (free_b / 4 * 3) / per));
+    const char* env = getenv("SEIDART_FWI_LANES");
+    if (env && atoi(env) > 0) nl = std::min(nl, atoi(env));
+    f->lanes.resize(nl);
+    for (int l = 0; l < nl; ++l) {
+        FwiLane& L = f->lanes[l];
+        const double* srcs[S2_NSRC] = {nullptr, shot_srcz[l], nullptr, nullptr, nullptr};
+        SeidartSource s0 = *src;
+        s0.xind = shot_xind[l];
+        s0.zind = shot_zind[l];
+        int rc = seidart_solver_create(&L.s, SEIDART_SEISMIC2, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
+                                       rec_cells);
+        if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
+        seidart_solver_internal_s2f(L.s, &L.a, &L.rec);
+        L.st = seidart_solver_internal_stream(L.s);
+        L.si = seidart_solver_internal_stepinfo(L.s);
+        for (int q = 0; q < 5; ++q) L.ptrs.p[q] = L.a.f[q];
+        for (int q = 0; q < 12; ++q) L.ptrs.p[5 + q] = L.a.mem[q];
+        if (cudaMalloc((void**)&L.ckpt, sizeof(float) * f->G * NS * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.seg, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.lam, sizeof(float) * NS * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
+            cudaMalloc((void**)&L.grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.dscal, sizeof(double) * 2) != cudaSuccess ||
+            cudaMalloc((void**)&L.dbase, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            seidart_fwi_destroy(f);
+            return ferr(SEIDART_ERR_NOMEM, "FWI lane allocation failed");
+        }
+        // the solver was created with shot l's source: point the lane at the shared series
+        rc = lane_set_shot(f, L, l);
+        if (rc != SEIDART_OK) { seidart_fwi_destroy(f); return rc; }
+    }
     *out = f;
     return SEIDART_OK;
 }
@@ -593,34 +716,44 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
 int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
     if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
     f->launches = 0;
-    FCUDA(cudaMemsetAsync(f->grad, 0, sizeof(double) * 8 * f->N, f->st));
-    FCUDA(cudaMemsetAsync(f->dscal, 0, sizeof(double) * 2, f->st));
-    std::vector<double> gsrc(f->nshots, 0.0);
-    for (int sh = 0; sh < f->nshots; ++sh) {
-        int rc = forward_shot(f, sh, grad != nullptr);
-        if (rc == SEIDART_OK) rc = shot_residual(f, sh);
-        if (rc == SEIDART_OK && grad) {
-            FCUDA(cudaMemsetAsync(f->dscal + 1, 0, sizeof(double), f->st));
-            rc = backward_shot(f, sh);
-            FCUDA(cudaMemcpyAsync(&gsrc[sh], f->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, f->st));
-        }
-        if (rc != SEIDART_OK) return rc;
+    for (auto& L : f->lanes) {
+        L.launches = 0;
+        FCUDA(cudaMemsetAsync(L.grad, 0, sizeof(double) * 8 * f->N, L.st));
+        FCUDA(cudaMemsetAsync(L.dscal, 0, sizeof(double) * 2, L.st));
     }
-    FCUDA(cudaStreamSynchronize(f->st));
-    int rc = seidart_solver_sync(f->s);
-    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    if (loss) FCUDA(cudaMemcpy(loss, f->dscal, sizeof(double), cudaMemcpyDeviceToHost));
+    FCUDA(cudaMemsetAsync(f->dgsrc, 0, sizeof(double) * f->nshots, f->lanes[0].st));
+    FCUDA(cudaStreamSynchronize(f->lanes[0].st));
+    int rc = run_shots(f, grad != nullptr, false, nullptr);
+    if (rc != SEIDART_OK) return rc;
+    rc = sync_lanes(f);
+    if (rc != SEIDART_OK) return rc;
+    double total = 0.0;
+    for (auto& L : f->lanes) {
+        double l = 0.0;
+        FCUDA(cudaMemcpy(&l, L.dscal, sizeof(double), cudaMemcpyDeviceToHost));
+        total += l;
+        f->launches += L.launches;
+    }
+    if (loss) *loss = total;
     if (grad) {
         const size_t N = f->N;
-        std::vector<double> g(8 * N);
-        FCUDA(cudaMemcpy(g.data(), f->grad, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+        FwiLane& L0 = f->lanes[0];
+        for (size_t l = 1; l < f->lanes.size(); ++l) {
+            add_grad<<<4 * 152, 256, 0, L0.st>>>(L0.grad, f->lanes[l].grad, 8 * N);
+            ++f->launches;
+        }
+        FCUDA(cudaGetLastError());
+        FCUDA(cudaStreamSynchronize(L0.st));
+        std::vector<double> g(8 * N), gsrc(f->nshots);
+        FCUDA(cudaMemcpy(g.data(), L0.grad, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+        FCUDA(cudaMemcpy(gsrc.data(), f->dgsrc, sizeof(double) * f->nshots, cudaMemcpyDeviceToHost));
         memcpy(grad, g.data(), sizeof(double) * 4 * N);
         // chain the face buoyancies B = 1/mean(rho_a, rho_b) to rho (FP32 forward values)
         std::vector<float> rho(N);
-        FCUDA(cudaMemcpy(rho.data(), f->a.m[S2_RHO], sizeof(float) * N, cudaMemcpyDeviceToHost));
+        FCUDA(cudaMemcpy(rho.data(), L0.a.m[S2_RHO], sizeof(float) * N, cudaMemcpyDeviceToHost));
         double* gr = grad + 4 * N;
         for (size_t q = 0; q < N; ++q) gr[q] = 0.0;
-        const int nx = f->a.nx, code = f->density;
+        const int nx = L0.a.nx, code = f->density;
         auto dB = [code](double a, double b, double* da, double* db) {
             switch (code) {
             case 1: *da = -1.0 / (2.0 * a * a); *db = -1.0 / (2.0 * b * b); break;       // (a+b)/(2ab)
@@ -649,14 +782,10 @@ int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
 // Synthetic traces of every shot for the current model ([nshots][nt][2][nrec]).
 int seidart_fwi_model_traces(SeidartFwi* f, double* traces) {
     if (!f || !traces) return ferr(SEIDART_ERR_ARG, "NULL");
-    const size_t n = (size_t)f->nt * 2 * f->nrec;
-    for (int sh = 0; sh < f->nshots; ++sh) {
-        int rc = forward_shot(f, sh, false);
-        if (rc == SEIDART_OK) rc = seidart_solver_sync(f->s);
-        if (rc == SEIDART_OK) rc = seidart_solver_traces(f->s, traces + sh * n, nullptr);
-        if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    }
-    return SEIDART_OK;
+    for (auto& L : f->lanes) FCUDA(cudaMemsetAsync(L.dscal, 0, sizeof(double) * 2, L.st));
+    int rc = run_shots(f, false, true, traces);
+    if (rc == SEIDART_OK) rc = sync_lanes(f);
+    return rc;
 }
 
 // Adjoint test hook: apply one adjoint step (no receiver residual) to the
@@ -664,23 +793,18 @@ int seidart_fwi_model_traces(SeidartFwi* f, double* traces) {
 // states xprev/xcur ([17][ncell]); lam is updated in place.
 int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam) {
     if (!f || !xprev || !xcur || !lam) return ferr(SEIDART_ERR_ARG, "NULL");
+    FwiLane& L = f->lanes[0];
     const size_t bytes = sizeof(float) * NS * f->N;
     float *dp = nullptr, *dc = nullptr;
     FCUDA(cudaMalloc((void**)&dp, bytes));
     FCUDA(cudaMalloc((void**)&dc, bytes));
     FCUDA(cudaMemcpy(dp, xprev, bytes, cudaMemcpyHostToDevice));
     FCUDA(cudaMemcpy(dc, xcur, bytes, cudaMemcpyHostToDevice));
-    FCUDA(cudaMemcpy(f->lam, lam, bytes, cudaMemcpyHostToDevice));
-    S2Args<float> a;
-    seidart_solver_internal_s2f(f->s, &a, nullptr);
-    f->a = a;
-    const int nrec = f->nrec;
-    f->nrec = 0;  // no receiver injection
-    FCUDA(cudaMemsetAsync(f->dbase, 0, sizeof(int), f->st));
-    adjoint_step(f, 1, dp, dc, nullptr);
-    f->nrec = nrec;
-    FCUDA(cudaStreamSynchronize(f->st));
-    FCUDA(cudaMemcpy(lam, f->lam, bytes, cudaMemcpyDeviceToHost));
+    FCUDA(cudaMemcpy(L.lam, lam, bytes, cudaMemcpyHostToDevice));
+    FCUDA(cudaMemsetAsync(L.dbase, 0, sizeof(int), L.st));
+    adjoint_step(f, L, 1, dp, dc, nullptr, 0);
+    FCUDA(cudaStreamSynchronize(L.st));
+    FCUDA(cudaMemcpy(lam, L.lam, bytes, cudaMemcpyDeviceToHost));
     cudaFree(dp);
     cudaFree(dc);
     return SEIDART_OK;
@@ -689,21 +813,27 @@ int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float
 // Forward test hook: one forward step (source off) on a host state [17][ncell].
 int seidart_fwi_forward_step_host(SeidartFwi* f, float* x) {
     if (!f || !x) return ferr(SEIDART_ERR_ARG, "NULL");
+    FwiLane& L = f->lanes[0];
     const size_t bytes = sizeof(float) * NS * f->N;
     float* d = nullptr;
     FCUDA(cudaMalloc((void**)&d, bytes));
     FCUDA(cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice));
-    int rc = seidart_solver_internal_reset(f->s);
-    if (rc == SEIDART_OK) rc = seidart_solver_internal_set_source(f->s, f->sx[0], f->sz[0], nullptr, nullptr);
-    if (rc == SEIDART_OK) rc = load_state(f, d);
-    if (rc == SEIDART_OK) rc = seidart_solver_step(f->s, 1);
-    if (rc == SEIDART_OK) rc = save_state(f, d);
-    FCUDA(cudaStreamSynchronize(f->st));
+    int rc = seidart_solver_internal_reset(L.s);
+    if (rc == SEIDART_OK) rc = seidart_solver_internal_set_source(L.s, f->sx[0], f->sz[0], nullptr, nullptr);
+    if (rc == SEIDART_OK) {
+        seidart_solver_internal_s2f(L.s, &L.a, nullptr);
+        load_state(L, d, f->N);
+        rc = seidart_solver_step(L.s, 1);
+    }
+    if (rc == SEIDART_OK) save_state(L, d, f->N);
+    FCUDA(cudaStreamSynchronize(L.st));
     FCUDA(cudaMemcpy(x, d, bytes, cudaMemcpyDeviceToHost));
     cudaFree(d);
-    // restore the shot-0 source for later gradient calls
-    seidart_solver_internal_set_source(f->s, f->sx[0], f->sz[0], nullptr, f->dsrc);
-    return rc == SEIDART_OK ? SEIDART_OK : ferr(rc, seidart_last_error());
+    // the lane's source was switched off: set it up again before the next run
+    L.shot = -1;
+    const int rc2 = lane_set_shot(f, L, 0);
+    if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
+    return rc2;
 }
 
 long long seidart_fwi_launches(const SeidartFwi* f) { return f ? f->launches : -1; }
