@@ -56,7 +56,7 @@ struct AdjArgs {
     const float* xc;     // x_n
     float* lam;          // adjoint state, NS arrays
     float* scr;          // 12 scratch arrays: lf1..lf4, ld1..ld4, le1..le4
-    double* grad;        // 8 accumulators: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
+    float* grad;         // 8 FP32 accumulators of the current segment: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
     size_t N;
     int isrc, jsrc;
     const double* srcz;  // force series of the shot (device), NULL = none
@@ -83,9 +83,12 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
     const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
     float* lam = A.lam;
     float lvx = lam[c], lvz = lam[N + c];
-    if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { lvx = 0.f; lvz = 0.f; }  // D^T
-    lam[c] = lvx;
-    lam[N + c] = lvz;
+    if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) {  // D^T
+        lvx = 0.f;
+        lvz = 0.f;
+        lam[c] = 0.f;
+        lam[N + c] = 0.f;
+    }
     if (i == A.isrc && k == A.jsrc && A.srcz) *A.gsrc += (double)lvz * (double)(float)A.srcz[*A.base + A.j - 1];
     const float* xc = A.xc;
     const float *sxx = xc + 2 * N, *szz = xc + 3 * N, *sxz = xc + 4 * N;
@@ -113,8 +116,8 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
             lf1 = p1;
             lf2 = p2;
         }
-        A.grad[4 * N + c] += (double)(lvx * dt * F1);
-        A.grad[5 * N + c] += (double)(lvx * dt * F2);
+        A.grad[4 * N + c] += lvx * dt * F1;
+        A.grad[5 * N + c] += lvx * dt * F2;
     }
     if (inZ(i, k, nx, nz)) {
         const float bxz = inv_mean_f(rho[c], rho[c + 1], A.density_code);
@@ -136,8 +139,8 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
             lf3 = p3;
             lf4 = p4;
         }
-        A.grad[6 * N + c] += (double)(lvz * dt * F3);
-        A.grad[7 * N + c] += (double)(lvz * dt * F4);
+        A.grad[6 * N + c] += lvz * dt * F3;
+        A.grad[7 * N + c] += lvz * dt * F4;
     }
     A.scr[c] = lf1;
     A.scr[N + c] = lf2;
@@ -201,9 +204,9 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
             ld3 = lD3;
             ld4 = lD3;
         }
-        A.grad[c] += (double)(px * D1);
-        A.grad[N + c] += (double)(px * D2 + pz * D1);
-        A.grad[2 * N + c] += (double)(pz * D2);
+        A.grad[c] += px * D1;
+        A.grad[N + c] += px * D2 + pz * D1;
+        A.grad[2 * N + c] += pz * D2;
     }
     if (inS(i, k, nx, nz)) {
         const float gxz = m[9][c];
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
             le3 = lE34;
             le4 = lE34;
         }
-        A.grad[3 * N + c] += (double)(pxz * (E3 + E4));
+        A.grad[3 * N + c] += pxz * (E3 + E4);
     }
     lam[2 * N + c] = nsxx;
     lam[3 * N + c] = nszz;
@@ -314,18 +317,6 @@ __global__ void seg_begin(int* step, int* base, int t0) {
     *base = t0;
 }
 
-// checkpoint -> solver state and -> first state of the segment buffer
-__global__ void restore_state(StatePtrs s, const float* __restrict__ ck, float* __restrict__ seg0, size_t N) {
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int a = 0; a < NS; ++a) {
-            const float v = ck[a * N + q];
-            s.p[a][q] = v;
-            seg0[a * N + q] = v;
-        }
-    }
-}
-
 __global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
 #pragma unroll
@@ -333,6 +324,147 @@ __global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
             if (to_block) blk[a * N + q] = s.p[a][q];
             else s.p[a][q] = blk[a * N + q];
         }
+    }
+}
+
+// ------------------------------------------- out-of-place recompute step
+// One forward step of the FP32 solver (the arithmetic of seismic2.cu's FP32
+// build, stress then velocity) reading state x_{j-1} from `in` and writing
+// x_j to `out`, so a recomputed segment needs no state copies.  Only cells a
+// step updates are written: every other cell of a segment buffer holds zero
+// from its allocation, as it does in the in-place solver (fields outside the
+// loops, memories outside the CPML shell).  Fields outside the loops are
+// copied through, so a restored checkpoint carries over unchanged.
+struct OopArgs {
+    S2Args<float> a;     // model, sizes, source position
+    const float* in;     // x_{j-1}: [NS][N]
+    float* out;          // x_j
+    size_t N;
+    const double* srcz;  // force series of the shot (device), NULL = none
+    const int* base;     // device: steps before the segment; this step is *base + j
+    int j;
+};
+
+#define D4F(p1, p0, p2, m1, h) ((27.0f * ((p1) - (p0)) - ((p2) - (m1))) * (h))
+
+__global__ void __launch_bounds__(BX* BY) oop_stress(OopArgs O) {
+    const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+    const S2Args<float>& a = O.a;
+    const int nx = a.nx, nz = a.nz;
+    if (i >= nx || k >= nz) return;
+    const size_t c = (size_t)i + (size_t)nx * k, N = O.N;
+    const float *vx = O.in, *vz = O.in + N;
+    const float* mi = O.in + 5 * N;
+    float* mo = O.out + 5 * N;
+    const bool normal = inN(i, k, nx, nz), shear = inS(i, k, nx, nz);
+    if (!normal) {
+        O.out[2 * N + c] = O.in[2 * N + c];
+        O.out[3 * N + c] = O.in[3 * N + c];
+    }
+    if (!shear) O.out[4 * N + c] = O.in[4 * N + c];
+    if (!normal && !shear) return;
+    const bool pml = !(i >= a.box.i0 && i < a.box.i1 && k >= a.box.k0 && k < a.box.k1);
+    const float dt = a.dt;
+    const float hx = 1.0f / (24.0f * a.dx), hz = 1.0f / (24.0f * a.dz);
+    if (normal) {
+        float dvx_dx = D4F(vx[c + 1], vx[c], vx[c + 2], vx[c - 1], hx);
+        float dvz_dz = D4F(vz[c], vz[c - nx], vz[c + nx], vz[c - 2 * nx], hz);
+        float dvz_dx = D4F(vz[c + 1], vz[c], vz[c + 2], vz[c - 1], hx);
+        float dvx_dz = D4F(vx[c], vx[c - nx], vx[c + nx], vx[c - 2 * nx], hz);
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], b = a.m[14][c], aa = a.m[12][c];
+            const float M0 = bh * mi[c] + ah * dvx_dx;
+            const float M1 = bh * mi[N + c] + ah * dvx_dz;
+            const float M3 = b * mi[3 * N + c] + aa * dvz_dz;
+            const float M2 = b * mi[2 * N + c] + aa * dvz_dx;
+            mo[c] = M0; mo[N + c] = M1; mo[2 * N + c] = M2; mo[3 * N + c] = M3;
+            dvx_dx = dvx_dx * a.m[11][c] + M0;
+            dvx_dz = dvx_dz * a.m[11][c] + M1;
+            dvz_dz = dvz_dz * a.m[10][c] + M3;
+            dvz_dx = dvz_dx * a.m[10][c] + M2;
+        }
+        const float c11 = a.m[0][c], c13 = a.m[1][c], c15 = a.m[2][c], c33 = a.m[3][c], c35 = a.m[4][c];
+        O.out[2 * N + c] = (O.in[2 * N + c] + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * a.m[7][c];
+        O.out[3 * N + c] = (O.in[3 * N + c] + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * a.m[8][c];
+    }
+    if (shear) {
+        float dvx_dx = D4F(vx[c], vx[c - 1], vx[c + 1], vx[c - 2], hx);
+        float dvz_dz = D4F(vz[c + nx], vz[c], vz[c + 2 * nx], vz[c - nx], hz);
+        float dvz_dx = D4F(vz[c], vz[c - 1], vz[c + 1], vz[c - 2], hx);
+        float dvx_dz = D4F(vx[c + nx], vx[c], vx[c + 2 * nx], vx[c - nx], hz);
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
+            const float M4 = bh * mi[4 * N + c] + ah * dvx_dx;
+            const float M5 = bh * mi[5 * N + c] + ah * dvx_dz;
+            const float M7 = bh * mi[7 * N + c] + ah * dvz_dz;
+            const float M6 = bh * mi[6 * N + c] + ah * dvz_dx;
+            mo[4 * N + c] = M4; mo[5 * N + c] = M5; mo[6 * N + c] = M6; mo[7 * N + c] = M7;
+            dvx_dx = dvx_dx * kh + M4;
+            dvx_dz = dvx_dz * kh + M5;
+            dvz_dz = dvz_dz * kh + M7;
+            dvz_dx = dvz_dx * kh + M6;
+        }
+        const float c15 = a.m[2][c], c35 = a.m[4][c], c55 = a.m[5][c];
+        O.out[4 * N + c] = (O.in[4 * N + c] + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * a.m[9][c];
+    }
+}
+
+__global__ void __launch_bounds__(BX* BY) oop_velocity(OopArgs O) {
+    const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
+    const S2Args<float>& a = O.a;
+    const int nx = a.nx, nz = a.nz;
+    if (i >= nx || k >= nz) return;
+    const size_t c = (size_t)i + (size_t)nx * k, N = O.N;
+    const float *sxx = O.out + 2 * N, *szz = O.out + 3 * N, *sxz = O.out + 4 * N;  // sigma of step j
+    const float* mi = O.in + 5 * N;
+    float* mo = O.out + 5 * N;
+    const float* rho = a.m[6];
+    const bool pml = !(i >= a.box.i0 && i < a.box.i1 && k >= a.box.k0 && k < a.box.k1);
+    const float dt = a.dt;
+    const float hx = 1.0f / (24.0f * a.dx), hz = 1.0f / (24.0f * a.dz);
+    float vx = O.in[c], vz = O.in[N + c];
+    if (inX(i, k, nx, nz)) {
+        const float bxx = inv_mean_f(rho[c], rho[c - 1], a.density_code);
+        const float bzx = inv_mean_f(rho[c], rho[c - nx], a.density_code);
+        float dsxx_dx = (27.0f * (sxx[c] - sxx[c - 1]) + sxx[c - 2]) * hx;
+        float dsxz_dz = (27.0f * (sxz[c] - sxz[c - nx]) + sxz[c - 2 * nx]) * hz;
+        if (pml) {
+            const float b = a.m[14][c], aa = a.m[12][c], kk = a.m[10][c];
+            const float M8 = b * mi[8 * N + c] + aa * dsxx_dx;
+            const float M11 = b * mi[11 * N + c] + aa * dsxz_dz;
+            mo[8 * N + c] = M8; mo[11 * N + c] = M11;
+            dsxx_dx = dsxx_dx * kk + M8;
+            dsxz_dz = dsxz_dz * kk + M11;
+        }
+        vx = vx + dt * (dsxx_dx * bxx + dsxz_dz * bzx);
+    }
+    if (inZ(i, k, nx, nz)) {
+        const float bxz = inv_mean_f(rho[c], rho[c + 1], a.density_code);
+        const float bzz = inv_mean_f(rho[c], rho[c + nx], a.density_code);
+        float dsxz_dx = (27.0f * (sxz[c + 1] - sxz[c]) - sxz[c + 2]) * hx;
+        float dszz_dz = (27.0f * (szz[c + nx] - szz[c]) - szz[c + 2 * nx]) * hz;
+        if (pml) {
+            const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
+            const float M10 = bh * mi[10 * N + c] + ah * dsxz_dx;
+            const float M9 = bh * mi[9 * N + c] + ah * dszz_dz;
+            mo[10 * N + c] = M10; mo[9 * N + c] = M9;
+            dsxz_dx = dsxz_dx * kh + M10;
+            dszz_dz = dszz_dz * kh + M9;
+        }
+        vz = vz + dt * (dsxz_dx * bxz + dszz_dz * bzz);
+    }
+    if (i == a.isrc && k == a.jsrc && O.srcz) vz = vz + (float)O.srcz[*O.base + O.j - 1] / rho[c];
+    if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { vx = 0.f; vz = 0.f; }
+    O.out[c] = vx;
+    O.out[N + c] = vz;
+}
+#undef D4F
+
+// end of a segment: fold its FP32 sums into the FP64 gradient and clear them
+__global__ void fold_grad(double* __restrict__ g64, float* __restrict__ g32, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        g64[q] += (double)g32[q];
+        g32[q] = 0.0f;
     }
 }
 
@@ -356,7 +488,8 @@ struct FwiLane {
     float* lam = nullptr;       // [NS][N]
     float* scr = nullptr;       // [12][N]
     float* dres = nullptr;      // [nt][2][nrec] residual of the lane's shot
-    double* grad = nullptr;     // [8][N]
+    double* grad = nullptr;     // [8][N] FP64 gradient sums over segments and shots
+    float* grad32 = nullptr;    // [8][N] FP32 sums within the current segment
     double* dscal = nullptr;    // [0] misfit of the lane's shots
     int* dbase = nullptr;       // device segment base (steps before the segment)
     // [0] full segments of K steps, [1] the shorter last one
@@ -400,7 +533,7 @@ AdjArgs adj_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, co
     A.dt = L.a.dt; A.hx = 1.0f / (24.0f * L.a.dx); A.hz = 1.0f / (24.0f * L.a.dz);
     A.box = L.a.box;
     for (int q = 0; q < 16; ++q) A.m[q] = L.a.m[q];
-    A.xp = xp; A.xc = xc; A.lam = L.lam; A.scr = L.scr; A.grad = L.grad; A.N = f->N;
+    A.xp = xp; A.xc = xc; A.lam = L.lam; A.scr = L.scr; A.grad = L.grad32; A.N = f->N;
     A.isrc = L.a.isrc; A.jsrc = L.a.jsrc; A.srcz = srcz;
     A.gsrc = f->dgsrc + (L.shot >= 0 ? L.shot : 0);
     A.base = L.dbase; A.j = j;
@@ -477,14 +610,17 @@ int capture_segment(SeidartFwi* f, FwiLane& L, int len, bool adjoint, cudaGraphE
     const size_t state = (size_t)NS * f->N;
     const double* srcz = f->dsrc + (size_t)L.shot * f->nt;
     FCUDA(cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
+    const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
     if (!adjoint) {
         for (int j = 1; j <= len; ++j) {
-            launch_seismic2_f32(L.a, L.si, L.st);
-            copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, L.seg + (size_t)j * state, f->N, 1);
+            OopArgs O{L.a, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, f->N, srcz, L.dbase, j};
+            oop_stress<<<grd, blk, 0, L.st>>>(O);
+            oop_velocity<<<grd, blk, 0, L.st>>>(O);
         }
     } else {
         for (int j = len; j >= 1; --j)
             adjoint_step(f, L, j, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, srcz, f->nrec);
+        fold_grad<<<4 * 152, 256, 0, L.st>>>(L.grad, L.grad32, 8 * f->N);
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(L.st, &g);
@@ -525,12 +661,12 @@ int lane_backward_segment(SeidartFwi* f, FwiLane& L, int g) {
     const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
     const int slot = len == f->K ? 0 : 1;
     seg_begin<<<1, 1, 0, L.st>>>(L.si.step, L.dbase, t0);
-    restore_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, L.ckpt + (size_t)g * NS * f->N, L.seg, f->N);
+    FCUDA(cudaMemcpyAsync(L.seg, L.ckpt + (size_t)g * NS * f->N, sizeof(float) * NS * f->N, cudaMemcpyDeviceToDevice,
+                          L.st));
     FCUDA(cudaGetLastError());
     FCUDA(cudaGraphLaunch(L.rec_exec[slot], L.st));
     FCUDA(cudaGraphLaunch(L.adj_exec[slot], L.st));
-    const long long per_step = seidart_step_launches(SEIDART_SEISMIC2, L.a.stress_src) + 1;
-    L.launches += 2 + len * per_step + len * (f->nrec > 0 ? 4 : 3);
+    L.launches += 1 + 2 * len + len * (f->nrec > 0 ? 4 : 3) + 1;
     return SEIDART_OK;
 }
 
@@ -598,7 +734,7 @@ void free_lane(FwiLane& L) {
         if (L.adj_exec[q]) cudaGraphExecDestroy(L.adj_exec[q]);
     }
     for (void* p : {(void*)L.ckpt, (void*)L.seg, (void*)L.lam, (void*)L.scr, (void*)L.dres, (void*)L.grad,
-                    (void*)L.dscal, (void*)L.dbase})
+                    (void*)L.grad32, (void*)L.dscal, (void*)L.dbase})
         if (p) cudaFree(p);
     if (L.s) seidart_solver_destroy(L.s);
     L = FwiLane();
@@ -697,11 +833,19 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
             cudaMalloc((void**)&L.scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
             cudaMalloc((void**)&L.grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.grad32, sizeof(float) * 8 * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.dscal, sizeof(double) * 2) != cudaSuccess ||
             cudaMalloc((void**)&L.dbase, sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
             seidart_fwi_destroy(f);
             return ferr(SEIDART_ERR_NOMEM, "FWI lane allocation failed");
+        }
+        // segment states are written only where a step updates them: start from zeros
+        if (cudaMemset(L.seg, 0, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
+            cudaMemset(L.grad32, 0, sizeof(float) * 8 * f->N) != cudaSuccess) {
+            cudaGetLastError();
+            seidart_fwi_destroy(f);
+            return ferr(SEIDART_ERR_CUDA, "FWI lane initialisation failed");
         }
         // the solver was created with shot l's source: point the lane at the shared series
         rc = lane_set_shot(f, L, l);
@@ -719,6 +863,7 @@ int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
     for (auto& L : f->lanes) {
         L.launches = 0;
         FCUDA(cudaMemsetAsync(L.grad, 0, sizeof(double) * 8 * f->N, L.st));
+        FCUDA(cudaMemsetAsync(L.grad32, 0, sizeof(float) * 8 * f->N, L.st));
         FCUDA(cudaMemsetAsync(L.dscal, 0, sizeof(double) * 2, L.st));
     }
     FCUDA(cudaMemsetAsync(f->dgsrc, 0, sizeof(double) * f->nshots, f->lanes[0].st));

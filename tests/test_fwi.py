@@ -5,8 +5,9 @@ traces, and its autograd gradient matches central differences of oracle.c.
 GPU: the adjoint step is the transpose of the forward step (dot-product test);
 the gradient matches the FP64 oracle gradient on a 64 x 64 instance and
 central differences (relative perturbation 1e-4) of the FP64 misfit at 8
-seeded cells within 1e-3; checkpoint spacing does not change it; the torch
-autograd wrapper returns it.
+seeded cells within 1e-3; checkpoint spacing changes it only by the
+rounding of the per-segment FP32 sums; the torch autograd wrapper returns
+it.
 """
 from dataclasses import replace
 
@@ -164,7 +165,8 @@ def test_checkpoint_spacing_does_not_change_gradient(fwi64):
     for loss, g in out[1:]:
         assert loss == pytest.approx(out[0][0], rel=1e-13)  # misfit summed with atomics
         for k in g:
-            assert np.array_equal(g[k], out[0][1][k]), k
+            # per-segment FP32 partial sums group the steps differently
+            assert _rel(g[k], out[0][1][k]) <= 1e-5, k
 
 
 @pytest.mark.gpu
