@@ -322,6 +322,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-fwi", action="store_true")
+    ap.add_argument("--fwi-profile-case", action="store_true",
+                    help="run one small misfit gradient (552^2 grid, 4 shots, 240 steps) and exit: the case "
+                         "the FWI launch list in profiles/ is captured on")
     ap.add_argument("--grid", type=int, default=WORKLOAD["n"],
                     help="interior cells per axis (default 320: the 3D configuration)")
     args = ap.parse_args()
@@ -334,6 +337,15 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.fwi_profile_case:
+        from seidart_gpu import models
+        from seidart_gpu.fwi import Fwi, Shot
+        p = models.seismic2_two_layer(n=512, cpml=20, nt=240, nrec=128, rec_z=20)
+        shots = [Shot(int(x), 20, p.src["z"]) for x in np.linspace(1, 512, 6)[1:-1].astype(int)]
+        with Fwi(p, shots, [np.zeros((240, 2, 128))] * 4) as f:
+            loss, _ = f.gradient()
+        print(json.dumps({"fwi_profile_case": "ok", "loss": loss}))
         return
 
     import torch
