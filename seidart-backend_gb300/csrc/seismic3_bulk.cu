@@ -56,37 +56,37 @@ __device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, i
     }
 }
 
-template <int MINB>
-__global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
-    extern __shared__ __align__(128) float coef[];  // [27][NT]
-    __shared__ __align__(8) unsigned long long bar;
-    const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
-    const int tid = threadIdx.y * BX + threadIdx.x;
-    if (A.prefetch > 0) s3b_prefetch(A, A.prefetch, tid);
-    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
-    if (tid == 0) {
-        const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
-        mbar_init(&bar, 1);
-        mbar_expect_tx(&bar, TILE_BYTES);
-        bulk_g2s(coef, A.packed + t * (NCOEF * NT), TILE_BYTES, &bar);
-    }
-    __syncthreads();
+// Everything after the bulk copy is started: stencil loads and derivatives
+// (overlapping the copy), the bounded wait, then the update with C_ij from
+// shared memory.  LEAN drops the clamps, loop-bound tests and CPML branches.
+template <bool LEAN>
+__device__ __forceinline__ void stress_tile(const S3Args<float>& A, const float* coef, unsigned long long* bar, int tid,
+                                            int k) {
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
     const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y;
-    const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
-    const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
-    const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
-    const bool L1 = x14 && y13 && z12, L2 = x23 && y24 && z12, L3 = x23 && y13 && z34, L4 = x14 && y24 && z34;
-    const bool active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
+    bool L1 = true, L2 = true, L3 = true, L4 = true, active = true;
+    if (!LEAN) {
+        const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
+        const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
+        const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+        L1 = x14 && y13 && z12; L2 = x23 && y24 && z12; L3 = x23 && y13 && z34; L4 = x14 && y24 && z34;
+        active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
+    }
     const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
     const size_t c = active ? (size_t)gx + sy * gy + sz * k : 0;
     float so[6], fx[3], bx[3], fy[3], by[3], fz[3], bz[3];
     if (active) {
-        const long ox[4] = {(long)cl(gx - 2, 0, nx - 1) - gx, (long)cl(gx - 1, 0, nx - 1) - gx,
-                            (long)cl(gx + 1, 0, nx - 1) - gx, (long)cl(gx + 2, 0, nx - 1) - gx};
-        const long oy[4] = {((long)cl(gy - 2, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy - 1, 0, ny - 1) - gy) * (long)sy,
-                            ((long)cl(gy + 1, 0, ny - 1) - gy) * (long)sy, ((long)cl(gy + 2, 0, ny - 1) - gy) * (long)sy};
-        const long oz[4] = {((long)cl(k - 2, 0, nz - 1) - k) * (long)sz, ((long)cl(k - 1, 0, nz - 1) - k) * (long)sz,
-                            ((long)cl(k + 1, 0, nz - 1) - k) * (long)sz, ((long)cl(k + 2, 0, nz - 1) - k) * (long)sz};
+        long ox[4] = {-2, -1, 1, 2}, oy[4] = {-2 * (long)sy, -(long)sy, (long)sy, 2 * (long)sy},
+             oz[4] = {-2 * (long)sz, -(long)sz, (long)sz, 2 * (long)sz};
+        if (!LEAN) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int d = q < 2 ? q - 2 : q - 1;
+                ox[q] = (long)cl(gx + d, 0, nx - 1) - gx;
+                oy[q] = ((long)cl(gy + d, 0, ny - 1) - gy) * (long)sy;
+                oz[q] = ((long)cl(k + d, 0, nz - 1) - k) * (long)sz;
+            }
+        }
 #pragma unroll
         for (int q = 0; q < 6; ++q) so[q] = __ldcs(A.f[3 + q] + c);
         const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
@@ -105,19 +105,19 @@ __global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
             bz[f] = (27.0f * (a0 - zm1) - (zp1 - zm2)) * hz;
         }
     }
-    const bool ok = mbar_wait_bounded(&bar, 0, WAIT_LIMIT);
+    const bool ok = mbar_wait_bounded(bar, 0, WAIT_LIMIT);
     if (!ok) {
         if (A.err) atomicExch(A.err, 1);
         // the copy may still be in flight: keep the CTA (and its shared
         // memory) alive until it lands, again with a bounded wait
-        if (tid == 0) mbar_wait_bounded(&bar, 0, WAIT_LIMIT);
+        if (tid == 0) mbar_wait_bounded(bar, 0, WAIT_LIMIT);
         return;
     }
     if (!active) return;
     const auto CR = [&](int q) { return coef[q * NT + tid]; };
     const auto GM = [&](int q) { return coef[(21 + q) * NT + tid]; };
-    const bool pml = !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
-                       k < A.box.k1);
+    const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 &&
+                                A.box.k0 <= k && k < A.box.k1);
     const float dt = A.dt;
     // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
     //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
@@ -144,6 +144,32 @@ __global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
         if (pml) loop_cpml<4>(A, c, ex, ey, ez);
         __stcs(A.f[7] + c, stress_new(CR, so[4], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
     }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
+    extern __shared__ __align__(128) float coef[];  // [27][NT]
+    __shared__ __align__(8) unsigned long long bar;
+    const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if (A.prefetch > 0) s3b_prefetch(A, A.prefetch, tid);
+    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
+    if (tid == 0) {
+        const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, TILE_BYTES);
+        bulk_g2s(coef, A.packed + t * (NCOEF * NT), TILE_BYTES, &bar);
+    }
+    __syncthreads();
+    // lean tiles: wholly inside the inert interior box and two cells from
+    // every face, so all four loops apply, no index is clamped and no CPML
+    // branch is taken
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+    const bool lean = x0 >= 2 && x0 + BX - 1 <= nx - 3 && y0 >= 2 && y0 + BY - 1 <= ny - 3 && k >= 2 && k <= nz - 3 &&
+                      x0 >= A.box.i0 && x0 + BX <= A.box.i1 && y0 >= A.box.j0 && y0 + BY <= A.box.j1 &&
+                      k >= A.box.k0 && k < A.box.k1;
+    if (lean) stress_tile<true>(A, coef, &bar, tid, k);
+    else stress_tile<false>(A, coef, &bar, tid, k);
 }
 
 using StressFn = void (*)(S3Args<float>);
