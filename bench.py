@@ -131,7 +131,7 @@ def kernel_bytes(p, box_cells: int) -> dict:
     velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
     # z-marching kernels (default) and one-thread-per-cell kernels
     return {"s3c_stress": stress, "s3c_velocity": velocity, "s3f_stress": stress, "s3f_velocity": velocity,
-            "s3t_stress": stress, "s3b_stress": stress}
+            "s3t_stress": stress, "s3b_stress": stress, "s3x_stress": stress}
 
 
 def step_bytes(p, box_cells: int) -> int:

@@ -135,7 +135,19 @@ struct S3Args {
     int bulk_variant;    // FP32: occupancy variant of the bulk stress kernel
     int prefetch;        // FP32: L2 prefetch distance in tiles of the stress kernel (0 = off)
     int prefetch_v;      // FP32: the same for the velocity kernel
+    const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
 };
+// TMA tensor maps of the staged FP32 3D stress kernel: old stresses (32 x 8
+// boxes), velocities with a 4/2-cell x/y halo (40 x 12 boxes) and without
+// (32 x 8 boxes, for the z neighbours)
+struct S3XMaps {
+    CUtensorMap sig[6];
+    CUtensorMap vh[3];
+    CUtensorMap vp[3];
+};
+bool seismic3_make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx, int by);
+bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* maps);
+void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st);
 // TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
 // (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes
 struct S3Maps {

@@ -92,6 +92,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  : "memory");
 }
 
+// 3D tensor-tile global -> shared copy (TMA); x * 4 must be a multiple of 16
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                          unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            saddr(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
+        : "memory");
+}
+
 // ------------------------------------------------------ L2 prefetch
 __device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 

@@ -172,6 +172,133 @@ __global__ void __launch_bounds__(NT, MINB) s3b_stress(S3Args<float> A) {
     else stress_tile<false>(A, coef, &bar, tid, k);
 }
 
+// ------------------------------------------------ fully staged variant
+// Everything the update reads per cell arrives by asynchronous copies into
+// shared memory before any thread computes: the coefficient block (one bulk
+// copy), the six old stresses (32 x 8 tensor tiles), the three velocities of
+// plane k with a 4-cell x / 2-cell y halo (40 x 12 tiles, from x0-4 so every
+// box starts 16-byte aligned) and of planes k-2, k-1, k+1, k+2 (32 x 8
+// tiles).  22 copies, issued one per lane of warp 0, one mbarrier.  Boxes
+// reaching outside the grid read zeros there; those values only enter
+// derivatives that the cell's loops do not use (as the clamped loads of the
+// register kernels).  Only CPML memories and coefficients on shell tiles
+// still travel through registers.
+constexpr int VHW = BX + 8, VHH = BY + 4;       // halo box 40 x 12
+constexpr int XS_SIG = NCOEF * NT;              // [6][NT]
+constexpr int XS_VH = XS_SIG + 6 * NT;          // [3][VHH][VHW]
+constexpr int XS_VZ = XS_VH + 3 * VHW * VHH;    // [3][4][NT]: z = k-2, k-1, k+1, k+2
+constexpr int XS_TOTAL = XS_VZ + 12 * NT;
+constexpr unsigned XS_BYTES = XS_TOTAL * sizeof(float);  // 51,840
+
+template <bool LEAN>
+__device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float* sm, unsigned long long* bar, int tid,
+                                            int k) {
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y;
+    bool L1 = true, L2 = true, L3 = true, L4 = true, active = true;
+    if (!LEAN) {
+        const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
+        const bool y13 = gy >= 2 && gy <= ny - 2, y24 = gy >= 1 && gy <= ny - 3;
+        const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+        L1 = x14 && y13 && z12; L2 = x23 && y24 && z12; L3 = x23 && y13 && z34; L4 = x14 && y24 && z34;
+        active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
+    }
+    const bool ok = mbar_wait_bounded(bar, 0, WAIT_LIMIT);
+    if (!ok) {
+        if (A.err) atomicExch(A.err, 1);
+        // copies may still be in flight: keep the CTA (and its shared
+        // memory) alive until they land, again with a bounded wait
+        if (tid == 0) mbar_wait_bounded(bar, 0, WAIT_LIMIT);
+        return;
+    }
+    if (!active) return;
+    const size_t c = (size_t)gx + (size_t)nx * ((size_t)gy + (size_t)ny * k);
+    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+    float fx[3], bx[3], fy[3], by[3], fz[3], bz[3];
+    const int hc = (threadIdx.y + 2) * VHW + threadIdx.x + 4;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const float* H = sm + XS_VH + f * VHW * VHH + hc;
+        const float* Z = sm + XS_VZ + f * 4 * NT + tid;
+        const float a0 = H[0];
+        const float xm2 = H[-2], xm1 = H[-1], xp1 = H[1], xp2 = H[2];
+        const float ym2 = H[-2 * VHW], ym1 = H[-VHW], yp1 = H[VHW], yp2 = H[2 * VHW];
+        const float zm2 = Z[0], zm1 = Z[NT], zp1 = Z[2 * NT], zp2 = Z[3 * NT];
+        fx[f] = (27.0f * (xp1 - a0) - (xp2 - xm1)) * hx;
+        bx[f] = (27.0f * (a0 - xm1) - (xp1 - xm2)) * hx;
+        fy[f] = (27.0f * (yp1 - a0) - (yp2 - ym1)) * hy;
+        by[f] = (27.0f * (a0 - ym1) - (yp1 - ym2)) * hy;
+        fz[f] = (27.0f * (zp1 - a0) - (zp2 - zm1)) * hz;
+        bz[f] = (27.0f * (a0 - zm1) - (zp1 - zm2)) * hz;
+    }
+    const float* so = sm + XS_SIG + tid;  // old stress q at so[q * NT]
+    const auto CR = [&](int q) { return sm[q * NT + tid]; };
+    const auto GM = [&](int q) { return sm[(21 + q) * NT + tid]; };
+    const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 &&
+                                A.box.k0 <= k && k < A.box.k1);
+    const float dt = A.dt;
+    // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
+    //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
+    // old stress order: xx xy xz yy yz zz ; gamma order: x y z xy yz xz
+    if (L1) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<1>(A, c, ex, ey, ez);
+        __stcs(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
+        __stcs(A.f[6] + c, stress_new(CR, so[3 * NT], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
+        __stcs(A.f[8] + c, stress_new(CR, so[5 * NT], GM(2), 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
+    }
+    if (L2) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
+        if (pml) loop_cpml<2>(A, c, ex, ey, ez);
+        __stcs(A.f[4] + c, stress_new(CR, so[NT], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+    }
+    if (L3) {
+        float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<3>(A, c, ex, ey, ez);
+        __stcs(A.f[5] + c, stress_new(CR, so[2 * NT], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+    }
+    if (L4) {
+        float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+        if (pml) loop_cpml<4>(A, c, ex, ey, ez);
+        __stcs(A.f[7] + c, stress_new(CR, so[4 * NT], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+    }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __grid_constant__ S3XMaps M) {
+    extern __shared__ __align__(128) float sm[];
+    __shared__ __align__(8) unsigned long long bar;
+    const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if (A.prefetch > 0) s3b_prefetch(A, A.prefetch, tid);
+    if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, XS_BYTES);
+    }
+    __syncthreads();
+    if (tid < 22) {  // one copy per lane of warp 0
+        if (tid == 0) {
+            const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
+            bulk_g2s(sm, A.packed + t * (NCOEF * NT), TILE_BYTES, &bar);
+        } else if (tid <= 6) {
+            tma_load3(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, &bar);
+        } else if (tid <= 9) {
+            tma_load3(sm + XS_VH + (tid - 7) * VHW * VHH, &M.vh[tid - 7], x0 - 4, y0 - 2, k, &bar);
+        } else {
+            const int q = tid - 10, f = q >> 2, zi = q & 3;
+            const int dz = zi < 2 ? zi - 2 : zi - 1;
+            tma_load3(sm + XS_VZ + q * NT, &M.vp[f], x0, y0, k + dz, &bar);
+        }
+    }
+    const bool lean = x0 >= 2 && x0 + BX - 1 <= nx - 3 && y0 >= 2 && y0 + BY - 1 <= ny - 3 && k >= 2 && k <= nz - 3 &&
+                      x0 >= A.box.i0 && x0 + BX <= A.box.i1 && y0 >= A.box.j0 && y0 + BY <= A.box.j1 &&
+                      k >= A.box.k0 && k < A.box.k1;
+    if (lean) staged_tile<true>(A, sm, &bar, tid, k);
+    else staged_tile<false>(A, sm, &bar, tid, k);
+}
+
 using StressFn = void (*)(S3Args<float>);
 // variant 2 (4 CTAs/SM) measured fastest on 352^3: 2.99 ms against 3.42 ms
 const StressFn kVariants[] = {s3b_stress<2>, s3b_stress<3>, s3b_stress<4>};
@@ -192,6 +319,29 @@ int seismic3_bulk_variant_minblocks(int v) { return (v >= 0 && v < NVAR) ? kMinB
 cudaError_t seismic3_bulk_pack(const S3Args<float>& a, float* packed, cudaStream_t st) {
     s3b_pack<<<tile_grid(a), dim3(BX, BY), 0, st>>>(a, packed);
     return cudaGetLastError();
+}
+
+// Tensor maps of the staged kernel; false when the grid does not meet the
+// tensor-copy rules (row pitch a multiple of 16 bytes) or the driver entry
+// point is missing, in which case the caller keeps the bulk kernel.
+bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* m) {
+    if (a.nx % 4 != 0 || !a.packed) return false;
+    for (int q = 0; q < 6; ++q)
+        if (!seismic3_make_map(&m->sig[q], a.f[3 + q], a.nx, a.ny, a.nz, BX, BY)) return false;
+    for (int f = 0; f < 3; ++f) {
+        if (!seismic3_make_map(&m->vh[f], a.f[f], a.nx, a.ny, a.nz, VHW, VHH)) return false;
+        if (!seismic3_make_map(&m->vp[f], a.f[f], a.nx, a.ny, a.nz, BX, BY)) return false;
+    }
+    if (cudaFuncSetAttribute((const void*)s3x_stress<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_BYTES) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st) {
+    s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
 }
 
 void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st) {

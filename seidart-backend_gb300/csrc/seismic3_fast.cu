@@ -384,7 +384,10 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
 void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
                           const S3Maps* maps, int stress_kind, int velocity_kind) {
     const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
-    if (stress_kind == S3K_BULK && a.packed) {
+    if (stress_kind == S3K_BULK && a.packed && a.staged) {
+        launch_seismic3_staged_stress(a, *(const S3XMaps*)a.staged, st);
+        if (h) h->fn(h->ctx, 0, "s3x_stress");
+    } else if (stress_kind == S3K_BULK && a.packed) {
         launch_seismic3_bulk_stress(a, a.bulk_variant, st);
         if (h) h->fn(h->ctx, 0, "s3b_stress");
     } else if (stress_kind == S3K_TMA && maps) {

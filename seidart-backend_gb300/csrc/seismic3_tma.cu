@@ -295,6 +295,10 @@ constexpr int kNumTma = sizeof(kTma) / sizeof(kTma[0]);
 
 }  // namespace
 
+bool seismic3_make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx, int by) {
+    return make_map(m, base, nx, ny, nz, bx, by);
+}
+
 int seismic3_tma_variants() { return kNumTma; }
 void seismic3_tma_variant_info(int v, int* tx, int* ty, int* sc, int* rv, int* minb) {
     const VariantInfo& V = kTma[v < 0 || v >= kNumTma ? 0 : v];

@@ -134,6 +134,7 @@ struct SeidartSolver {
     // (variant numbers) override them
     int s3_stress_kind = S3K_BULK, s3_velocity_kind = S3K_CELL;
     float* s3_packed = nullptr;  // tile-packed coefficients of the bulk stress kernel
+    S3XMaps s3_staged{};         // tensor maps of the staged stress kernel (when s3f.staged is set)
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
@@ -681,6 +682,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             return set_err(SEIDART_ERR_CUDA, "coefficient packing failed: %s", cudaGetErrorString(cudaGetLastError()));
         }
         s->s3f.packed = s->s3_packed;
+        // fully staged variant (TMA tiles for stresses and velocities) when the
+        // grid allows it; SEIDART_S3_STAGED=0 keeps the bulk kernel
+        const char* st = getenv("SEIDART_S3_STAGED");
+        if (!(st && *st == '0') && seismic3_staged_prepare(s->s3f, &s->s3_staged)) s->s3f.staged = &s->s3_staged;
     }
     *out = s;
     return SEIDART_OK;
