@@ -136,6 +136,8 @@ struct S3Args {
     int prefetch;        // FP32: L2 prefetch distance in tiles of the stress kernel (0 = off)
     int prefetch_v;      // FP32: the same for the velocity kernel
     const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
+    const void* staged_v;  // the same for the staged velocity kernel
+    int velocity_minb;     // FP32: CTAs per SM the cell velocity kernel is compiled for (4 .. 8)
 };
 // TMA tensor maps of the staged FP32 3D stress kernel: old stresses (32 x 8
 // boxes), velocities with a 4/2-cell x/y halo (40 x 12 boxes) and without
@@ -144,7 +146,11 @@ struct S3XMaps {
     CUtensorMap sig[6];
     CUtensorMap vh[3];
     CUtensorMap vp[3];
+    CUtensorMap sigh[5];  // stresses xx xy xz yy yz with the 40 x 12 halo box (velocity kernel)
+    CUtensorMap rhoh, rhop;  // density with and without the halo box
 };
+bool seismic3_staged_velocity_prepare(const S3Args<float>& a, S3XMaps* maps);
+void launch_seismic3_staged_velocity(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st);
 bool seismic3_make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx, int by);
 bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* maps);
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st);

@@ -236,7 +236,8 @@ __device__ __forceinline__ bool lean_tile(const S3Args<float>& A, int x0, int y0
     return true;
 }
 
-__global__ void __launch_bounds__(BX* BY) s3c_velocity(S3Args<float> A, StepInfo si) {
+template <int MINB>
+__global__ void __launch_bounds__(BX* BY, MINB) s3c_velocity(S3Args<float> A, StepInfo si) {
     __shared__ unsigned redu[2 * BX * BY / 32];
     __shared__ double redd[2][BX * BY / 32];
     if (A.prefetch_v > 0) s3c_velocity_prefetch(A, A.prefetch_v, threadIdx.y * BX + threadIdx.x);
@@ -262,11 +263,205 @@ __global__ void __launch_bounds__(BX* BY) s3c_velocity(S3Args<float> A, StepInfo
     }
 }
 
+// ------------------------------------------------ fully staged variant
+// The velocity half-step with every per-cell input staged in shared memory
+// by tensor-tile copies before any thread computes: the five stresses with
+// x/y stencils (xx xy xz yy yz) and the density as 40 x 12 halo tiles (from
+// x0-4, y0-2), sigma_zz of plane k and the z neighbours (sigma_xz, sigma_yz at
+// k-1, k-2; sigma_zz at k+1, k+2; density at k-1, k+1) and the old
+// velocities as 32 x 8 tiles: 18 copies, one per lane of warp 0, one
+// mbarrier.  Out-of-grid parts of a box read zeros and only feed updates the
+// cell does not make.  Only CPML memories and coefficients on shell tiles
+// still travel through registers.
+constexpr int XV_HW = BX + 8, XV_HH = BY + 4, XV_HB = XV_HW * XV_HH;  // 40 x 12
+constexpr int XV_SH = 0;                       // [5][XV_HB]: xx xy xz yy yz
+constexpr int XV_RH = 5 * XV_HB;               // [XV_HB]: rho
+constexpr int XV_P = 6 * XV_HB;                // plain tiles [12][NTV]
+constexpr int NTV = BX * BY;
+// plain tile slots
+constexpr int P_SZZ = 0, P_XZ1 = 1, P_XZ2 = 2, P_YZ1 = 3, P_YZ2 = 4, P_ZZ1 = 5, P_ZZ2 = 6, P_RM = 7, P_RP = 8, P_V = 9;
+constexpr int XV_TOTAL = XV_P + 12 * NTV;
+constexpr unsigned XV_BYTES = XV_TOTAL * sizeof(float);  // 23,808
+constexpr int WAIT_LIMIT_V = 1 << 20;
+
+template <bool LEAN>
+__device__ __forceinline__ void staged_velocity_cell(const S3Args<float>& A, const float* sm, int it, int gx, int gy,
+                                                     int k, int tid, float& vsq, float& ssq, float (&w)[9]) {
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+    const size_t c = (size_t)gx + sy * gy + sz * k;
+    const int hc = (threadIdx.y + 2) * XV_HW + threadIdx.x + 4;
+    const float *Sxx = sm + XV_SH + hc, *Sxy = sm + XV_SH + XV_HB + hc, *Sxz = sm + XV_SH + 2 * XV_HB + hc,
+                *Syy = sm + XV_SH + 3 * XV_HB + hc, *Syz = sm + XV_SH + 4 * XV_HB + hc, *R = sm + XV_RH + hc;
+    const float* P = sm + XV_P + tid;
+    const float sxx0 = Sxx[0], sxxm1 = Sxx[-1], sxxm2 = Sxx[-2];
+    const float sxy0 = Sxy[0], sxyp1 = Sxy[1], sxyp2 = Sxy[2], sxyym1 = Sxy[-XV_HW], sxyym2 = Sxy[-2 * XV_HW];
+    const float syy0 = Syy[0], syyp1 = Syy[XV_HW], syyp2 = Syy[2 * XV_HW];
+    const float sxz0 = Sxz[0], sxzp1 = Sxz[1], sxzp2 = Sxz[2], sxzzm1 = P[P_XZ1 * NTV], sxzzm2 = P[P_XZ2 * NTV];
+    const float syz0 = Syz[0], syzym1 = Syz[-XV_HW], syzym2 = Syz[-2 * XV_HW], syzzm1 = P[P_YZ1 * NTV],
+                syzzm2 = P[P_YZ2 * NTV];
+    const float szz0 = P[P_SZZ * NTV], szzp1 = P[P_ZZ1 * NTV], szzp2 = P[P_ZZ2 * NTV];
+    const float r0 = R[0], rxm = R[-1], rxp = R[1], rzm = P[P_RM * NTV], rzp = P[P_RP * NTV];
+    float vx = P[P_V * NTV], vy = P[(P_V + 1) * NTV], vz = P[(P_V + 2) * NTV];
+    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+    const float dt = A.dt;
+    const int code = A.density_code;
+    const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
+                                k < A.box.k1);
+    const float byy = inv_mean_f(r0, r0, code);
+    if (LEAN || (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2)) {  // vx
+        float d1 = (27.0f * (sxx0 - sxxm1) + sxxm2) * hx;
+        float d2 = (27.0f * (sxy0 - sxyym1) + sxyym2) * hy;
+        float d3 = (27.0f * (sxz0 - sxzzm1) + sxzzm2) * hz;
+        if (pml) {
+            const CpmlC p = cpml_at(A, c, true);
+            d1 = cpml_apply(A.mem[36], c, p, d1);
+            d2 = cpml_apply(A.mem[40], c, p, d2);
+            d3 = cpml_apply(A.mem[42], c, p, d3);
+        }
+        vx = vx + (d1 * inv_mean_f(r0, rxm, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+    }
+    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 1 && gy <= ny - 3 && k >= 2 && k <= nz - 2)) {  // vy
+        float d1 = (27.0f * (sxyp1 - sxy0) - sxyp2) * hx;
+        float d2 = (27.0f * (syyp1 - syy0) - syyp2) * hy;
+        float d3 = (27.0f * (syz0 - syzzm1) + syzzm2) * hz;
+        if (pml) {
+            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
+            d1 = cpml_apply(A.mem[39], c, ph, d1);
+            d2 = cpml_apply(A.mem[37], c, ph, d2);
+            d3 = cpml_apply(A.mem[44], c, pf, d3);
+        }
+        vy = vy + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+    }
+    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 2 && gy <= ny - 2 && k >= 1 && k <= nz - 3)) {  // vz
+        float d1 = (27.0f * (sxzp1 - sxz0) - sxzp2) * hx;
+        float d2 = (27.0f * (syz0 - syzym1) + syzym2) * hy;
+        float d3 = (27.0f * (szzp1 - szz0) - szzp2) * hz;
+        if (pml) {
+            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
+            d1 = cpml_apply(A.mem[41], c, ph, d1);
+            d2 = cpml_apply(A.mem[43], c, pf, d2);
+            d3 = cpml_apply(A.mem[38], c, ph, d3);
+        }
+        vz = vz + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzp, code)) * dt;
+    }
+    bool src_cell = false;
+    if (!LEAN) {
+        // force source (cpmlfdtd.f08:2214-2219)
+        const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
+        if (gx == is + 1 && gy == js && k == ks && A.src[0]) vx = vx + (float)A.src[0][it - 1] * dt / r0;
+        if (gx == is && gy == js + 1 && k == ks && A.src[1])
+            vy = vy + (float)A.src[1][it - 1] * dt / A.rho[(size_t)is + sy * js + sz * ks];
+        if (gx == is && gy == js && k == ks + 1 && A.src[2]) vz = vz + (float)A.src[2][it - 1] * dt / r0;
+        if (gx == 0 || gx == nx - 1 || gy == 0 || gy == ny - 1 || k == 0 || k == nz - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }
+        src_cell = A.stress_src && ((gx == is && gy == js && k == ks) || (gx == is + 1 && gy == js + 1 && k == ks) ||
+                                    (gx == is + 1 && gy == js && k == ks + 1) || (gx == is && gy == js + 1 && k == ks + 1));
+    }
+    __stcs(A.f[0] + c, vx);
+    __stcs(A.f[1] + c, vy);
+    __stcs(A.f[2] + c, vz);
+    w[0] = vx; w[1] = vy; w[2] = vz;
+    vsq = vx * vx + vy * vy + vz * vz;
+    if (!src_cell) {
+        w[3] = sxx0; w[4] = syy0; w[5] = szz0; w[6] = sxy0; w[7] = syz0; w[8] = sxz0;
+        ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
+    }
+}
+
+__global__ void __launch_bounds__(BX* BY) s3x_velocity(S3Args<float> A, StepInfo si, const __grid_constant__ S3XMaps M) {
+    extern __shared__ __align__(128) float sm[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ unsigned redu[2 * BX * BY / 32];
+    __shared__ double redd[2][BX * BY / 32];
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if (A.prefetch_v > 0) s3c_velocity_prefetch(A, A.prefetch_v, tid);
+    const int it = *si.step;
+    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY, k = blockIdx.z;
+    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
+    const int nx = A.nx, ny = A.ny;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, XV_BYTES);
+    }
+    __syncthreads();
+    if (tid < 18) {  // one copy per lane of warp 0
+        if (tid < 5) {
+            tma_load3(sm + XV_SH + tid * XV_HB, &M.sigh[tid], x0 - 4, y0 - 2, k, &bar);
+        } else if (tid == 5) {
+            tma_load3(sm + XV_RH, &M.rhoh, x0 - 4, y0 - 2, k, &bar);
+        } else {
+            const int q = tid - 6;  // plain slot
+            const CUtensorMap* map;
+            int z = k;
+            switch (q) {
+            case P_SZZ: map = &M.sig[5]; break;
+            case P_XZ1: map = &M.sig[2]; z = k - 1; break;
+            case P_XZ2: map = &M.sig[2]; z = k - 2; break;
+            case P_YZ1: map = &M.sig[4]; z = k - 1; break;
+            case P_YZ2: map = &M.sig[4]; z = k - 2; break;
+            case P_ZZ1: map = &M.sig[5]; z = k + 1; break;
+            case P_ZZ2: map = &M.sig[5]; z = k + 2; break;
+            case P_RM: map = &M.rhop; z = k - 1; break;
+            case P_RP: map = &M.rhop; z = k + 1; break;
+            default: map = &M.vp[q - P_V]; break;
+            }
+            tma_load3(sm + XV_P + q * NTV, map, x0, y0, z, &bar);
+        }
+    }
+    float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool ok = mbar_wait_bounded(&bar, 0, WAIT_LIMIT_V);
+    if (!ok) {
+        if (A.err) atomicExch(A.err, 1);
+        if (tid == 0) mbar_wait_bounded(&bar, 0, WAIT_LIMIT_V);
+    } else if (lean_tile(A, x0, y0, k, true)) {
+        staged_velocity_cell<true>(A, sm, it, gx, gy, k, tid, vsq, ssq, w);
+    } else if (gx < nx && gy < ny) {
+        staged_velocity_cell<false>(A, sm, it, gx, gy, k, tid, vsq, ssq, w);
+    }
+    double vn, sn;
+    block_norm2_f32<BX * BY / 32>(
+        vsq, ssq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); },
+        [&] {
+            const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
+            return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+        },
+        redu, &redd[0][0], vn, sn);
+    if (tid == 0) {
+        const int slot = (blockIdx.x + 7 * blockIdx.y + 13 * blockIdx.z) % NSLOT;
+        atomic_max_nonneg(A.norms_part + slot, vn);
+        atomic_max_nonneg(A.norms_part + NSLOT + slot, sn);
+    }
+}
+
 }  // namespace
+
+bool seismic3_staged_velocity_prepare(const S3Args<float>& a, S3XMaps* m) {
+    if (a.nx % 4 != 0) return false;
+    for (int q = 0; q < 5; ++q)
+        if (!seismic3_make_map(&m->sigh[q], a.f[3 + q], a.nx, a.ny, a.nz, XV_HW, XV_HH)) return false;
+    if (!seismic3_make_map(&m->rhoh, a.rho, a.nx, a.ny, a.nz, XV_HW, XV_HH)) return false;
+    if (!seismic3_make_map(&m->rhop, a.rho, a.nx, a.ny, a.nz, BX, BY)) return false;
+    for (int q = 0; q < 6; ++q)
+        if (!seismic3_make_map(&m->sig[q], a.f[3 + q], a.nx, a.ny, a.nz, BX, BY)) return false;
+    for (int f = 0; f < 3; ++f)
+        if (!seismic3_make_map(&m->vp[f], a.f[f], a.nx, a.ny, a.nz, BX, BY)) return false;
+    return true;
+}
+
+void launch_seismic3_staged_velocity(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st) {
+    s3x_velocity<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), XV_BYTES, st>>>(a, s, maps);
+}
 
 void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st) {
     s3c_stress<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), 0, st>>>(a);
 }
 void launch_seismic3_cell_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st) {
-    s3c_velocity<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), 0, st>>>(a, s);
+    const dim3 grd((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), blk(BX, BY);
+    switch (a.velocity_minb) {
+    case 5: s3c_velocity<5><<<grd, blk, 0, st>>>(a, s); break;
+    case 6: s3c_velocity<6><<<grd, blk, 0, st>>>(a, s); break;
+    case 7: s3c_velocity<7><<<grd, blk, 0, st>>>(a, s); break;
+    case 8: s3c_velocity<8><<<grd, blk, 0, st>>>(a, s); break;
+    default: s3c_velocity<4><<<grd, blk, 0, st>>>(a, s); break;
+    }
 }

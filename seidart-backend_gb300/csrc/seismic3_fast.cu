@@ -400,7 +400,10 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
         launch_seismic3_cell_stress(a, st);
         if (h) h->fn(h->ctx, 0, "s3c_stress");
     }
-    if (velocity_kind == S3K_ZMARCH) {
+    if (velocity_kind == S3K_CELL && a.staged_v) {
+        launch_seismic3_staged_velocity(a, *(const S3XMaps*)a.staged_v, s, st);
+        if (h) h->fn(h->ctx, 1, "s3x_velocity");
+    } else if (velocity_kind == S3K_ZMARCH) {
         s3f_velocity<<<grd, blk, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 1, "s3f_velocity");
     } else {

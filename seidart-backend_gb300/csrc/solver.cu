@@ -665,6 +665,8 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->s3f.prefetch = (t && *t >= '0' && *t <= '9') ? atoi(t) : 8;
         t = getenv("SEIDART_S3_PFV");
         s->s3f.prefetch_v = (t && *t >= '0' && *t <= '9') ? atoi(t) : 1216;
+        t = getenv("SEIDART_S3_VEL_MINB");
+        s->s3f.velocity_minb = (t && *t >= '4' && *t <= '8') ? atoi(t) : 6;  // 6: 1.07 ms vs 1.19 ms at 4 (352^3)
     }
     if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_BULK) {
         const char* t = getenv("SEIDART_S3_BULK");
@@ -686,6 +688,12 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         // grid allows it; SEIDART_S3_STAGED=0 keeps the bulk kernel
         const char* st = getenv("SEIDART_S3_STAGED");
         if (!(st && *st == '0') && seismic3_staged_prepare(s->s3f, &s->s3_staged)) s->s3f.staged = &s->s3_staged;
+        // staged velocity kernel: bit-identical but measured slower at 352^3
+        // (1.55 ms against 1.19 ms), so only on request
+        const char* sv = getenv("SEIDART_S3_STAGED_V");
+        if (s->s3f.staged && (sv && *sv == '1') && s->s3_velocity_kind == S3K_CELL &&
+            seismic3_staged_velocity_prepare(s->s3f, &s->s3_staged))
+            s->s3f.staged_v = &s->s3_staged;
     }
     *out = s;
     return SEIDART_OK;
