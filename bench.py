@@ -426,20 +426,24 @@ def main():
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
-        out = sg.run(pe, sg.FP32)
+        with sg.Solver(pe, sg.FP32) as se:   # host FP64 model, sources and initial fields in
+            se.step(pe.time_steps)
+            se.sync()
+            tr_out, nrm_out = se.traces()       # receiver traces and norms out
+            f_out = se.get_fields()             # final fields out
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
         barrier()
         model_bytes = sum(a.nbytes for a in pe.model_list())
         src_bytes = sum(a.nbytes for a in pe.src_list() if a is not None)
-        f_bytes = sum(a.nbytes for a in pe.field_list())
-        tr_bytes = out["traces"].nbytes + out["norms"].nbytes
+        f_bytes = sum(a.nbytes for a in f_out)
+        tr_bytes = tr_out.nbytes + nrm_out.nbytes
         e2e = {"value": world * pe.ncell * pe.time_steps / te / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int((model_bytes + src_bytes + f_bytes) / pe.time_steps),
                "d2h_bytes_per_step": int((f_bytes + tr_bytes) / pe.time_steps),
                "steps": pe.time_steps, "seconds": te,
-               "note": "seidart_run on host FP64 buffers: upload+FP32 conversion of the model, 1500 steps, "
-                       "copy-back of final fields, traces and norms"}
+               "note": "Solver API on host FP64 buffers: upload and FP32 conversion of the model, sources and "
+                       "initial fields, 1500 steps, copy-back of final fields, traces and norms"}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:

@@ -19,6 +19,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -134,6 +135,8 @@ struct SeidartSolver {
     // (variant numbers) override them
     int s3_stress_kind = S3K_BULK, s3_velocity_kind = S3K_CELL;
     float* s3_packed = nullptr;  // tile-packed coefficients of the bulk stress kernel
+    double* stage = nullptr;     // FP64 staging buffer for on-device precision conversion (FP32 solvers)
+    size_t stage_n = 0;          // its capacity in doubles
     S3XMaps s3_staged{};         // tensor maps of the staged stress kernel (when s3f.staged is set)
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
@@ -164,30 +167,73 @@ struct SeidartSolver {
 namespace {
 
 // Upload n values of `h` (FP64) as T into device memory d.
+// FP64 host data -> FP32 device arrays through an FP64 staging buffer and a
+// conversion kernel (the FP64 arithmetic of the derived forms rounded per
+// operation, as the host would compute it), so set-up and read-back do not
+// convert element by element on one host core.
+// mode 0: x;  1: 1/(1 + x dt) (attenuation factor);  2: 1/x
+__global__ void convert_to_f32(float* __restrict__ d, const double* __restrict__ h, size_t n, int mode, double dt) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        double x = h[q];
+        if (mode == 1) x = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(x, dt)));
+        else if (mode == 2) x = __ddiv_rn(1.0, x);
+        d[q] = __double2float_rn(x);
+    }
+}
+__global__ void convert_to_f64(double* __restrict__ d, const float* __restrict__ s, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        d[q] = (double)s[q];
+}
+
+int ensure_stage(SeidartSolver& s, size_t n) {
+    if (s.stage && s.stage_n >= n) return SEIDART_OK;
+    if (s.stage) cudaFree(s.stage);
+    s.stage = nullptr;
+    s.stage_n = 0;
+    if (cudaMalloc((void**)&s.stage, n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return SEIDART_ERR_NOMEM;
+    }
+    s.stage_n = n;
+    return SEIDART_OK;
+}
+
 template <typename T>
-int upload(void* d, const double* h, size_t n, cudaStream_t st) {
+int upload(SeidartSolver& s, void* d, const double* h, size_t n, int mode = 0) {
+    cudaStream_t st = s.stream;
     if (sizeof(T) == sizeof(double)) {
         CUDA_TRY(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         return SEIDART_OK;
     }
-    std::vector<float> tmp(n);
-    for (size_t q = 0; q < n; ++q) tmp[q] = (float)h[q];
-    CUDA_TRY(cudaMemcpyAsync(d, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
+    const size_t chunk = std::max<size_t>(s.ncell, 1 << 20);
+    if (ensure_stage(s, std::min(n, chunk)) != SEIDART_OK) return set_err(SEIDART_ERR_NOMEM, "staging buffer");
+    for (size_t o = 0; o < n; o += s.stage_n) {
+        const size_t m = std::min(s.stage_n, n - o);
+        CUDA_TRY(cudaMemcpyAsync(s.stage, h + o, m * sizeof(double), cudaMemcpyHostToDevice, st));
+        convert_to_f32<<<4 * 152, 256, 0, st>>>((float*)d + o, s.stage, m, mode, s.src.dt);
+        CUDA_TRY(cudaGetLastError());
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
     return SEIDART_OK;
 }
 template <typename T>
-int download(double* h, const void* d, size_t n, cudaStream_t st) {
+int download(SeidartSolver& s, double* h, const void* d, size_t n) {
+    cudaStream_t st = s.stream;
     if (sizeof(T) == sizeof(double)) {
         CUDA_TRY(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         return SEIDART_OK;
     }
-    std::vector<float> tmp(n);
-    CUDA_TRY(cudaMemcpyAsync(tmp.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    const size_t chunk = std::max<size_t>(s.ncell, 1 << 20);
+    if (ensure_stage(s, std::min(n, chunk)) != SEIDART_OK) return set_err(SEIDART_ERR_NOMEM, "staging buffer");
+    for (size_t o = 0; o < n; o += s.stage_n) {
+        const size_t m = std::min(s.stage_n, n - o);
+        convert_to_f64<<<4 * 152, 256, 0, st>>>(s.stage, (const float*)d + o, m);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(h + o, s.stage, m * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
-    for (size_t q = 0; q < n; ++q) h[q] = tmp[q];
     return SEIDART_OK;
 }
 
@@ -251,7 +297,13 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
     const double dt = s.src.dt;
     auto arr = [&](const double* h) -> const T* {
         T* d = (T*)s.carve(N * sizeof(T));
-        if (d && upload<T>(d, h, N, s.stream) != SEIDART_OK) return nullptr;
+        if (d && upload<T>(s, d, h, N) != SEIDART_OK) return nullptr;
+        return d;
+    };
+    // FP32 arrays of a derived form, converted on the device (mode of convert_to_f32)
+    auto arr_mode = [&](const double* h, int mode) -> const T* {
+        T* d = (T*)s.carve(N * sizeof(T));
+        if (d && upload<T>(s, d, h, N, mode) != SEIDART_OK) return nullptr;
         return d;
     };
     // while measuring (no arena yet) only sizes matter: skip the arithmetic
@@ -264,8 +316,9 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
         return v.data();
     };
     // FP32: gamma -> 1/(1+gamma dt), kappa -> 1/kappa (same memory traffic)
-    auto gam = [&](const double* g) { return f32 ? arr(derive([&](size_t q) { return 1.0 / (1.0 + g[q] * dt); })) : arr(g); };
-    auto kap = [&](const double* k) { return f32 ? arr(derive([&](size_t q) { return 1.0 / k[q]; })) : arr(k); };
+    auto gam = [&](const double* g) { return f32 ? arr_mode(g, 1) : arr(g); };
+    auto kap = [&](const double* k) { return f32 ? arr_mode(k, 2) : arr(k); };
+    (void)dt;
     const int cs = cpml_slot(s.family);
     const T* cp[6];
     cp[0] = kap(model[cs]);
@@ -330,7 +383,7 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
             if (f32) for (double& v : derived.back()) v = 1.0 / v;
             a.rho9[q] = arr(derived.back().data());
         }
-        a.rho = f32 ? arr(derive([&](size_t q) { return 1.0 / rho[q]; })) : arr(rho);
+        a.rho = f32 ? arr_mode(rho, 2) : arr(rho);
         for (int q = 0; q < 9; ++q) a.src[q] = dev_src[q];
         if constexpr (sizeof(T) == 8) s.s25d = a; else s.s25f = a;
         break;
@@ -715,8 +768,8 @@ int seidart_solver_set_fields(SeidartSolver* s, const double* const* fields) {
     const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
     for (int q = 0; q < s->L.nfield; ++q) {
         if (!fields[q]) continue;  // NULL keeps the current values
-        const int rc = s->precision == SEIDART_FP32 ? upload<float>(s->fields[q], fields[q], n, s->stream)
-                                                    : upload<double>(s->fields[q], fields[q], n, s->stream);
+        const int rc = s->precision == SEIDART_FP32 ? upload<float>(*s, s->fields[q], fields[q], n)
+                                                    : upload<double>(*s, s->fields[q], fields[q], n);
         if (rc != SEIDART_OK) return rc;
     }
     return SEIDART_OK;
@@ -742,8 +795,8 @@ int seidart_solver_get_fields(SeidartSolver* s, double* const* fields) {
     const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
     for (int q = 0; q < s->L.nfield; ++q) {
         if (!fields[q]) continue;
-        rc = s->precision == SEIDART_FP32 ? download<float>(fields[q], s->fields[q], n, s->stream)
-                                          : download<double>(fields[q], s->fields[q], n, s->stream);
+        rc = s->precision == SEIDART_FP32 ? download<float>(*s, fields[q], s->fields[q], n)
+                                          : download<double>(*s, fields[q], s->fields[q], n);
         if (rc != SEIDART_OK) return rc;
     }
     return SEIDART_OK;
@@ -754,8 +807,8 @@ int seidart_solver_get_memory(SeidartSolver* s, double* const* mem) {
     const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
     for (int q = 0; q < s->L.nmem; ++q) {
         if (!mem[q]) continue;
-        const int rc = s->precision == SEIDART_FP32 ? download<float>(mem[q], s->mem[q], n, s->stream)
-                                                    : download<double>(mem[q], s->mem[q], n, s->stream);
+        const int rc = s->precision == SEIDART_FP32 ? download<float>(*s, mem[q], s->mem[q], n)
+                                                    : download<double>(*s, mem[q], s->mem[q], n);
         if (rc != SEIDART_OK) return rc;
     }
     return SEIDART_OK;
@@ -810,8 +863,8 @@ int seidart_solver_traces(SeidartSolver* s, double* traces, double* norms) {
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     const size_t per = (size_t)s->L.ncomp * s->nrec * (s->L.cplx ? 2 : 1);
     if (traces && s->nrec > 0) {
-        const int rc = s->precision == SEIDART_FP32 ? download<float>(traces, s->traces, per * s->steps_done, s->stream)
-                                                    : download<double>(traces, s->traces, per * s->steps_done, s->stream);
+        const int rc = s->precision == SEIDART_FP32 ? download<float>(*s, traces, s->traces, per * s->steps_done)
+                                                    : download<double>(*s, traces, s->traces, per * s->steps_done);
         if (rc != SEIDART_OK) return rc;
     }
     if (norms) {
@@ -895,6 +948,7 @@ int seidart_solver_destroy(SeidartSolver* s) {
         if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
     if (s->arena) cudaFree(s->arena);
     if (s->s3_packed) cudaFree(s->s3_packed);
+    if (s->stage) cudaFree(s->stage);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SEIDART_OK;
