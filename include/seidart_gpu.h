@@ -284,6 +284,45 @@ int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count);
 int seidart_fwi_destroy(SeidartFwi* f);
 const char* seidart_fwi_last_error(void);
 
+/* ---- material pre-pass: material-ID image -> padded coefficient grids.
+ * Replaces stiffness_write / attenuation_write / permittivity_write[_c]
+ * (legacy/cpmlfdtd_cbindings.f95:60-611), whose C prototypes
+ * (legacy/cpmlfdtd_wrapper.c:7-10) pass the Fortran assumed-shape table as a
+ * bare pointer and drop stiffness_write's gradient argument, so the table's
+ * row count is an explicit argument here.
+ *   im:    [nz][nx] int32, x fastest: 1-based row numbers of the table
+ *   table: row-major [nmat][ncol] (complex: [nmat][ncol][re, im])
+ *          stiffness columns 2..23 = c11 c12 c13 c14 c15 c16 c22 c23 c24 c25
+ *          c26 c33 c34 c35 c36 c44 c45 c46 c55 c56 c66 rho; permittivity
+ *          columns 2..7 = eps11 12 13 22 23 33, 8..13 = sig11 12 13 22 23 33;
+ *          attenuation columns 1..3 = gamma_x gamma_y gamma_z
+ * Outputs are padded (nx+2 npml) x (nz+2 npml) FP64 grids, x fastest, with
+ * the interior values carried into the CPML in the reference's statement
+ * order (its corner and sig12/sig23 edge values included); attenuation leaves
+ * cpmlvalue in the CPML.  *_arrays fill caller buffers (out[q] may be NULL to
+ * skip one: 22 stiffness grids c11..c66, rho; 12 permittivity grids eps11
+ * eps12 eps13 eps22 eps23 eps33 sig11 .. sig33, the eps ones complex
+ * interleaved in the _c variant; 3 attenuation grids); *_write write the
+ * reference's .dat records (c11.dat … rho.dat, eps11.dat … sig33.dat,
+ * gamma_x.dat …) into `dir`.  gradient: [nz][nx] factor applied to the
+ * interior density, or NULL for none. */
+int seidart_stiffness_arrays(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                             const double* gradient, double* const* out);
+int seidart_stiffness_write(const char* dir, const int* im, int nx, int nz, const double* mlist, int nmat, int ncol,
+                            int npml, const double* gradient);
+int seidart_permittivity_arrays(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                                double* const* out);
+int seidart_permittivity_write(const char* dir, const int* im, int nx, int nz, const double* mlist, int nmat,
+                               int ncol, int npml);
+int seidart_permittivity_arrays_c(const int* im, int nx, int nz, const double* mlist_c, int nmat, int ncol, int npml,
+                                  double* const* out);
+int seidart_permittivity_write_c(const char* dir, const int* im, int nx, int nz, const double* mlist_c, int nmat,
+                                 int ncol, int npml);
+int seidart_attenuation_arrays(const int* im, int nx, int nz, const double* alist, int nmat, int ncol, int npml,
+                               double cpmlvalue, double* const* out);
+int seidart_attenuation_write(const char* dir, const int* im, int nx, int nz, const double* alist, int nmat, int ncol,
+                              int npml, double cpmlvalue);
+
 /* ---- trace misfit without device allocation.  No counterpart in the
  * reference (SeidarT-Backend computes no misfit); it is the no-allocation
  * variant of the misfit reduction inside seidart_fwi_gradient, for callers

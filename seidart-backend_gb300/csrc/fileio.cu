@@ -42,6 +42,8 @@
 extern "C" int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex,
                                               int* is_fp32, size_t* ncell, void** stream);
 
+extern "C" int seidart_internal_set_error(int code, const char* msg);
+
 namespace {
 
 std::string g_io_err;
@@ -347,6 +349,16 @@ bool load_grid(const std::string& dir, const std::string& name, size_t n, std::v
 extern "C" {
 
 const char* seidart_io_last_error(void) { return g_io_err.c_str(); }
+
+// one Fortran record (used by the material pre-pass writers); not part of the ABI
+int seidart_internal_write_record(const char* path, const void* data, size_t bytes) {
+    std::string why;
+    if (!write_record(path, data, bytes, why)) {
+        seidart_internal_set_error(SEIDART_ERR_IO, why.c_str());
+        return io_err(SEIDART_ERR_IO, why);
+    }
+    return SEIDART_OK;
+}
 
 int seidart_run_files(const char* dir_c, int family, int precision, const SeidartDomain* dom,
                       const SeidartSource* src, int density_code, const char* source_type, int single_output,
