@@ -18,6 +18,7 @@
  *   seismic3      src/fortran/cpmlfdtd.f08:1341-2313 (subroutine seismic3)
  *   electromag2   src/fortran/cpmlfdtd.f08:2317-2760 (subroutine electromag2)
  *   electromag25  src/fortran/cpmlfdtd.f08:2764-3350 (subroutine electromag25)
+ *   electromag3   src/fortran/cpmlfdtd.f08:3353-4001 (subroutine electromag3)
  *   legacy names  legacy/cpmlfdtd_wrapper.c:7-16     (seismic2_ ... electromag25c_)
  */
 #ifndef SEIDART_GPU_H
@@ -44,6 +45,7 @@ extern "C" {
 #define SEIDART_SEISMIC3      3
 #define SEIDART_ELECTROMAG2   4
 #define SEIDART_ELECTROMAG25  5
+#define SEIDART_ELECTROMAG3   6
 
 /* precision of the field arrays and stencil arithmetic */
 #define SEIDART_FP64 0   /* drop-in path: same operation order as the reference */
@@ -129,6 +131,19 @@ enum { E25_SRCX, E25_SRCY, E25_SRCZ, E25_NSRC };
 enum { E25_EX, E25_EY, E25_EZ, E25_HX, E25_HY, E25_HZ, E25_NFIELD };
 enum { E25_M_DEY_DX, E25_M_DEY_DZ, E25_M_DEX_DZ, E25_M_DEZ_DX,
        E25_M_DHZ_DX, E25_M_DHX_DZ, E25_M_DHY_DZ, E25_M_DHY_DX, E25_NMEM };
+
+/* electromag3 (src/fortran/cpmlfdtd.f08:3353-4001): relative permittivity
+ * e11..e33 and conductivity s11..s33 tensors, CPML coefficients; sources x y
+ * z; fields Ex Ey Ez Hx Hy Hz; the 12 memories in the reference's declaration
+ * order (:3392-3397) */
+enum { E3_E11, E3_E12, E3_E13, E3_E22, E3_E23, E3_E33,
+       E3_S11, E3_S12, E3_S13, E3_S22, E3_S23, E3_S33,
+       E3_KAPPA, E3_KAPPAH, E3_ACOEF, E3_ACOEFH, E3_BCOEF, E3_BCOEFH,
+       E3_NMODEL };
+enum { E3_SRCX, E3_SRCY, E3_SRCZ, E3_NSRC };
+enum { E3_EX, E3_EY, E3_EZ, E3_HX, E3_HY, E3_HZ, E3_NFIELD };
+enum { E3_M_DEX_DY, E3_M_DEY_DX, E3_M_DEX_DZ, E3_M_DEZ_DX, E3_M_DEZ_DY, E3_M_DEY_DZ,
+       E3_M_DHZ_DX, E3_M_DHX_DZ, E3_M_DHZ_DY, E3_M_DHY_DZ, E3_M_DHX_DY, E3_M_DHY_DX, E3_NMEM };
 
 /* Number of slots of each kind for a solver family; *is_complex = 1 for 2.5D.
  * *nrec_comp = number of receiver components recorded per receiver and step. */

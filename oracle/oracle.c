@@ -882,3 +882,171 @@ int oracle_electromag25(const SeidartDomain* d, const SeidartSource* s,
     free(buf);
     return status;
 }
+
+/* =====================================================================
+ * electromag3: cpmlfdtd.f08:3353-4001 (point sources; the plane-wave
+ * branch is not restated)
+ * ===================================================================== */
+int oracle_electromag3(const SeidartDomain* d, const SeidartSource* s,
+                       const double* const* model, const double* const* srcfn,
+                       double* const* fields, double* const* mem, int it0, int nsteps,
+                       int nrec, const int* rec, double* traces, double* norms) {
+    const int nx = d->nx, ny = d->ny, nz = d->nz;
+    const double dx = d->dx, dy = d->dy, dz = d->dz, dt = s->dt;
+    const double *sig11 = model[E3_S11], *sig12 = model[E3_S12], *sig13 = model[E3_S13],
+                 *sig22 = model[E3_S22], *sig23 = model[E3_S23], *sig33 = model[E3_S33],
+                 *kappa = model[E3_KAPPA], *kappa_half = model[E3_KAPPAH],
+                 *acoef = model[E3_ACOEF], *acoef_half = model[E3_ACOEFH],
+                 *bcoef = model[E3_BCOEF], *bcoef_half = model[E3_BCOEFH];
+    double *Ex = fields[E3_EX], *Ey = fields[E3_EY], *Ez = fields[E3_EZ],
+           *Hx = fields[E3_HX], *Hy = fields[E3_HY], *Hz = fields[E3_HZ];
+    double *m_dEx_dy = mem[E3_M_DEX_DY], *m_dEy_dx = mem[E3_M_DEY_DX], *m_dEx_dz = mem[E3_M_DEX_DZ],
+           *m_dEz_dx = mem[E3_M_DEZ_DX], *m_dEz_dy = mem[E3_M_DEZ_DY], *m_dEy_dz = mem[E3_M_DEY_DZ],
+           *m_dHz_dx = mem[E3_M_DHZ_DX], *m_dHx_dz = mem[E3_M_DHX_DZ], *m_dHz_dy = mem[E3_M_DHZ_DY],
+           *m_dHy_dz = mem[E3_M_DHY_DZ], *m_dHx_dy = mem[E3_M_DHX_DY], *m_dHy_dx = mem[E3_M_DHY_DX];
+    const int isource = s->xind + d->cpml, jsource = s->yind + d->cpml, ksource = s->zind + d->cpml;
+    const size_t N = (size_t)nx * ny * nz;
+    /* cpmlfdtd.f08:3484-3494, :3644-3666 */
+    const double dbHx = dt / MU0, daHx = 1.0, dbHy = dt / MU0, daHy = 1.0, dbHz = dt / MU0, daHz = 1.0;
+    double* buf = (double*)malloc(sizeof(double) * N * 15);
+    if (!buf) return -1;
+    double *e11 = buf, *e22 = buf + N, *e33 = buf + 2 * N;
+    double *aEx = buf + 3 * N, *bEx = buf + 4 * N, *cEx = buf + 5 * N, *bEy = buf + 6 * N,
+           *cEy = buf + 7 * N, *cEz = buf + 8 * N;
+    double *Ex_old = buf + 9 * N, *Ey_old = buf + 10 * N, *Ez_old = buf + 11 * N;
+    for (size_t c = 0; c < N; ++c) {
+        const double a11 = model[E3_E11][c] * EPS0, a12 = model[E3_E12][c] * EPS0,
+                     a13 = model[E3_E13][c] * EPS0, a22 = model[E3_E22][c] * EPS0,
+                     a23 = model[E3_E23][c] * EPS0, a33 = model[E3_E33][c] * EPS0;
+        const double det = a11 * (a22 * a33 - a23 * a23) - a12 * (a12 * a33 - a23 * a13) +
+                           a13 * (a12 * a23 - a22 * a13);
+        e11[c] = a11; e22[c] = a22; e33[c] = a33;
+        aEx[c] = (a22 * a33 - a23 * a23) / det;
+        bEx[c] = -((a12 * a33 - a23 * a13) / det);
+        cEx[c] = (a12 * a23 - a22 * a13) / det;
+        bEy[c] = (a11 * a33 - a13 * a13) / det;
+        cEy[c] = -((a11 * a23 - a12 * a13) / det);
+        cEz[c] = (a11 * a22 - a12 * a12) / det;
+    }
+    const double *aEy = bEx, *aEz = cEx, *bEz = cEy;
+    /* Ex_old = Ex at the start of every step (cpmlfdtd.f08:3668-3670, :3980-3982) */
+    memcpy(Ex_old, Ex, sizeof(double) * N);
+    memcpy(Ey_old, Ey, sizeof(double) * N);
+    memcpy(Ez_old, Ez, sizeof(double) * N);
+
+    for (int step = 0; step < nsteps; ++step) {
+        const int it = it0 + step + 1;
+        /* Hx: cpmlfdtd.f08:3695-3711 */
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 1; k <= nz - 1; ++k)
+            for (int i = 1; i <= nx - 1; ++i)
+                for (int j = 1; j <= ny - 1; ++j) {
+                    const size_t c = IX3(i, j, k);
+                    double dEz_dy = (Ez[IX3(i, j + 1, k)] - Ez[c]) / dy;
+                    double dEy_dz = (Ey[IX3(i, j, k + 1)] - Ey[c]) / dz;
+                    m_dEy_dz[c] = bcoef_half[c] * m_dEy_dz[c] + acoef_half[c] * dEy_dz;
+                    m_dEz_dy[c] = bcoef_half[c] * m_dEz_dy[c] + acoef_half[c] * dEz_dy;
+                    dEz_dy = dEz_dy / kappa_half[c] + m_dEz_dy[c];
+                    dEy_dz = dEy_dz / kappa_half[c] + m_dEy_dz[c];
+                    Hx[c] = daHx * Hx[c] + dbHx * (dEy_dz - dEz_dy);
+                }
+        /* Hy: cpmlfdtd.f08:3722-3741 */
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 1; k <= nz - 1; ++k)
+            for (int i = 1; i <= nx - 1; ++i)
+                for (int j = 1; j <= ny - 1; ++j) {
+                    const size_t c = IX3(i, j, k);
+                    double dEx_dz = (Ex[IX3(i, j, k + 1)] - Ex[c]) / dz;
+                    double dEz_dx = (Ez[IX3(i + 1, j, k)] - Ez[c]) / dx;
+                    m_dEx_dz[c] = bcoef[c] * m_dEx_dz[c] + acoef[c] * dEx_dz;
+                    m_dEz_dx[c] = bcoef[c] * m_dEz_dx[c] + acoef[c] * dEz_dx;
+                    dEx_dz = dEx_dz / kappa[c] + m_dEx_dz[c];
+                    dEz_dx = dEz_dx / kappa[c] + m_dEz_dx[c];
+                    Hy[c] = daHy * Hy[c] + dbHy * (dEz_dx - dEx_dz);
+                }
+        /* Hz: cpmlfdtd.f08:3752-3769 (k starts at 2) */
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
+            for (int i = 1; i <= nx - 1; ++i)
+                for (int j = 1; j <= ny - 1; ++j) {
+                    const size_t c = IX3(i, j, k);
+                    double dEx_dy = (Ex[IX3(i, j + 1, k)] - Ex[c]) / dy;
+                    double dEy_dx = (Ey[IX3(i + 1, j, k)] - Ey[c]) / dx;
+                    m_dEx_dy[c] = bcoef[c] * m_dEx_dy[c] + acoef[c] * dEx_dy;
+                    m_dEy_dx[c] = bcoef[c] * m_dEy_dx[c] + acoef[c] * dEy_dx;
+                    dEx_dy = dEx_dy / kappa[c] + m_dEx_dy[c];
+                    dEy_dx = dEy_dx / kappa[c] + m_dEy_dx[c];
+                    Hz[c] = daHz * Hz[c] + dbHz * (dEx_dy - dEy_dx);
+                }
+        /* E: cpmlfdtd.f08:3787-3825 */
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
+            for (int i = 2; i <= nx - 1; ++i)
+                for (int j = 2; j <= ny - 1; ++j) {
+                    const size_t c = IX3(i, j, k);
+                    double dHz_dy = (Hz[c] - Hz[IX3(i, j - 1, k)]) / dy;
+                    double dHy_dz = (Hy[c] - Hy[IX3(i, j, k - 1)]) / dz;
+                    double dHz_dx = (Hz[c] - Hz[IX3(i - 1, j, k)]) / dx;
+                    double dHx_dz = (Hx[c] - Hx[IX3(i, j, k - 1)]) / dz;
+                    double dHy_dx = (Hy[c] - Hy[IX3(i - 1, j, k)]) / dx;
+                    double dHx_dy = (Hx[c] - Hx[IX3(i, j - 1, k)]) / dy;
+                    m_dHz_dy[c] = bcoef_half[c] * m_dHz_dy[c] + acoef_half[c] * dHz_dy;
+                    m_dHy_dz[c] = bcoef[c] * m_dHy_dz[c] + acoef[c] * dHy_dz;
+                    m_dHz_dx[c] = bcoef_half[c] * m_dHz_dx[c] + acoef_half[c] * dHz_dx;
+                    m_dHx_dz[c] = bcoef_half[c] * m_dHx_dz[c] + acoef_half[c] * dHx_dz;
+                    m_dHx_dy[c] = bcoef_half[c] * m_dHx_dy[c] + acoef_half[c] * dHx_dy;
+                    m_dHy_dx[c] = bcoef_half[c] * m_dHy_dx[c] + acoef_half[c] * dHy_dx;
+                    dHz_dy = dHz_dy / kappa_half[c] + m_dHz_dy[c];
+                    dHy_dz = dHy_dz / kappa[c] + m_dHy_dz[c];
+                    dHz_dx = dHz_dx / kappa_half[c] + m_dHz_dx[c];
+                    dHx_dz = dHx_dz / kappa_half[c] + m_dHx_dz[c];
+                    dHx_dy = dHx_dy / kappa_half[c] + m_dHx_dy[c];
+                    dHy_dx = dHy_dx / kappa_half[c] + m_dHy_dx[c];
+                    const double rhs_x = dHz_dy - dHy_dz - (sig11[c] * Ex_old[c] + sig12[c] * Ey_old[c] + sig13[c] * Ez_old[c]);
+                    const double rhs_y = dHx_dz - dHz_dx - (sig12[c] * Ex_old[c] + sig22[c] * Ey_old[c] + sig23[c] * Ez_old[c]);
+                    const double rhs_z = dHy_dx - dHx_dy - (sig13[c] * Ex_old[c] + sig23[c] * Ey_old[c] + sig33[c] * Ez_old[c]);
+                    Ex[c] = Ex_old[c] + (aEx[c] * rhs_x + bEx[c] * rhs_y + cEx[c] * rhs_z) * dt;
+                    Ey[c] = Ey_old[c] + (aEy[c] * rhs_x + bEy[c] * rhs_y + cEy[c] * rhs_z) * dt;
+                    Ez[c] = Ez_old[c] + (aEz[c] * rhs_x + bEz[c] * rhs_y + cEz[c] * rhs_z) * dt;
+                }
+        /* point source: cpmlfdtd.f08:3901-3906 */
+        {
+            const size_t c = IX3(isource, jsource, ksource);
+            Ex[c] = Ex[c] + src_at(srcfn[E3_SRCX], it) * dt / e11[c];
+            Ey[c] = Ey[c] + src_at(srcfn[E3_SRCY], it) * dt / e22[c];
+            Ez[c] = Ez[c] + src_at(srcfn[E3_SRCZ], it) * dt / e33[c];
+        }
+        /* Dirichlet faces on all six fields: cpmlfdtd.f08:3912-3978 */
+        double* F[6] = {Ex, Ey, Ez, Hx, Hy, Hz};
+        for (int q = 0; q < 6; ++q) {
+            double* f = F[q];
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j) { f[IX3(1, j, k)] = 0.0; f[IX3(nx, j, k)] = 0.0; }
+            for (int k = 1; k <= nz; ++k)
+                for (int i = 1; i <= nx; ++i) { f[IX3(i, 1, k)] = 0.0; f[IX3(i, ny, k)] = 0.0; }
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) { f[IX3(i, j, 1)] = 0.0; f[IX3(i, j, nz)] = 0.0; }
+        }
+        memcpy(Ex_old, Ex, sizeof(double) * N);
+        memcpy(Ey_old, Ey, sizeof(double) * N);
+        memcpy(Ez_old, Ez, sizeof(double) * N);
+        /* norm: cpmlfdtd.f08:3987-3988 */
+        double velocnorm = 0.0;
+#pragma omp parallel for reduction(max : velocnorm) schedule(static)
+        for (size_t c = 0; c < N; ++c) {
+            const double n = sqrt(Ex[c] * Ex[c] + Ey[c] * Ey[c] + Ez[c] * Ez[c]);
+            velocnorm = velocnorm > n ? velocnorm : n;
+        }
+        if (norms) norms[step] = velocnorm;
+        if (traces)
+            for (int r = 0; r < nrec; ++r) {
+                traces[((size_t)step * 3 + 0) * nrec + r] = Ex[rec[r]];
+                traces[((size_t)step * 3 + 1) * nrec + r] = Ey[rec[r]];
+                traces[((size_t)step * 3 + 2) * nrec + r] = Ez[rec[r]];
+            }
+        if (velocnorm > STABILITY_THRESHOLD) { free(buf); return it; }
+    }
+    free(buf);
+    return 0;
+}
+

@@ -47,6 +47,10 @@ int oracle_electromag25(const SeidartDomain* d, const SeidartSource* s,
                         const double* const* model, const double* const* srcfn,
                         double* const* fields, double* const* mem, int it0, int nsteps,
                         int nrec, const int* rec, double* traces, double* norms);
+int oracle_electromag3(const SeidartDomain* d, const SeidartSource* s,
+                       const double* const* model, const double* const* srcfn,
+                       double* const* fields, double* const* mem, int it0, int nsteps,
+                       int nrec, const int* rec, double* traces, double* norms);
 /* Number of OpenMP threads the build uses (1 without OpenMP). */
 int oracle_threads(void);
 

@@ -19,9 +19,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 NAMES = {1: "oracle_seismic2", 2: "oracle_seismic25", 3: "oracle_seismic3", 4: "oracle_electromag2",
-         5: "oracle_electromag25"}
-NMEM = {1: 12, 2: 30, 3: 45, 4: 4, 5: 8}
-NCOMP = {1: 2, 2: 3, 3: 3, 4: 2, 5: 3}
+         5: "oracle_electromag25", 6: "oracle_electromag3"}
+NMEM = {1: 12, 2: 30, 3: 45, 4: 4, 5: 8, 6: 12}
+NCOMP = {1: 2, 2: 3, 3: 3, 4: 2, 5: 3, 6: 3}
 _libs = {}
 
 

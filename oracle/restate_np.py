@@ -291,3 +291,95 @@ def seismic3(p, nsteps):
         snorms.append(np.max(np.sqrt(sxx ** 2 + syy ** 2 + szz ** 2 + 2.0 * (sxy ** 2 + syz ** 2 + sxz ** 2))))
         traces.append(np.stack([w.ravel(order="F")[rec] for w in v]))
     return {"fields": f, "memory": M, "traces": np.array(traces), "norms": np.array([vnorms, snorms])}
+
+
+def electromag3(p, nsteps):
+    """cpmlfdtd.f08:3353-4001 on a Problem (point sources only)."""
+    m = {k: np.asarray(v) for k, v in p.model.items()}
+    nx, ny, nz = p.nx, p.ny, p.nz
+    dx, dy, dz, dt = p.dx, p.dy, p.dz, p.dt
+    f = p.field_list()
+    Ex, Ey, Ez, Hx, Hy, Hz = f
+    M = [np.zeros((nx, ny, nz), order="F") for _ in range(12)]
+    (mdEx_dy, mdEy_dx, mdEx_dz, mdEz_dx, mdEz_dy, mdEy_dz,
+     mdHz_dx, mdHx_dz, mdHz_dy, mdHy_dz, mdHx_dy, mdHy_dx) = M
+    k, kh, a, ah, b, bh = (m[n] for n in ("kappa", "kappa_half", "acoef", "acoef_half", "bcoef", "bcoef_half"))
+    e11, e12, e13 = m["e11"] * EPS0, m["e12"] * EPS0, m["e13"] * EPS0
+    e22, e23, e33 = m["e22"] * EPS0, m["e23"] * EPS0, m["e33"] * EPS0
+    s11, s12, s13, s22, s23, s33 = (m[n] for n in ("s11", "s12", "s13", "s22", "s23", "s33"))
+    det = e11 * (e22 * e33 - e23 * e23) - e12 * (e12 * e33 - e23 * e13) + e13 * (e12 * e23 - e22 * e13)
+    aEx = (e22 * e33 - e23 * e23) / det
+    bEx = -((e12 * e33 - e23 * e13) / det)
+    cEx = (e12 * e23 - e22 * e13) / det
+    aEy, bEy, cEy = bEx, (e11 * e33 - e13 * e13) / det, -((e11 * e23 - e12 * e13) / det)
+    aEz, bEz, cEz = cEx, cEy, (e11 * e22 - e12 * e12) / det
+    dbH = dt / MU0
+    I3 = (p.xind + p.cpml - 1, p.yind + p.cpml - 1, p.zind + p.cpml - 1)
+    rec = p.receiver_array()
+    Exo, Eyo, Ezo = (x.copy(order="F") for x in (Ex, Ey, Ez))
+    traces, norms = [], []
+
+    def sh(c, ax, s):
+        return tuple(slice(q.start + s, q.stop + s) if d == ax else q for d, q in enumerate(c))
+
+    for step in range(nsteps):
+        it = step + 1
+        c = (R(1, nx - 1), R(1, ny - 1), R(1, nz - 1))
+        dEz_dy = (Ez[sh(c, 1, 1)] - Ez[c]) / dy
+        dEy_dz = (Ey[sh(c, 2, 1)] - Ey[c]) / dz
+        mdEy_dz[c] = bh[c] * mdEy_dz[c] + ah[c] * dEy_dz
+        mdEz_dy[c] = bh[c] * mdEz_dy[c] + ah[c] * dEz_dy
+        dEz_dy = dEz_dy / kh[c] + mdEz_dy[c]
+        dEy_dz = dEy_dz / kh[c] + mdEy_dz[c]
+        Hx[c] = 1.0 * Hx[c] + dbH * (dEy_dz - dEz_dy)
+        dEx_dz = (Ex[sh(c, 2, 1)] - Ex[c]) / dz
+        dEz_dx = (Ez[sh(c, 0, 1)] - Ez[c]) / dx
+        mdEx_dz[c] = b[c] * mdEx_dz[c] + a[c] * dEx_dz
+        mdEz_dx[c] = b[c] * mdEz_dx[c] + a[c] * dEz_dx
+        dEx_dz = dEx_dz / k[c] + mdEx_dz[c]
+        dEz_dx = dEz_dx / k[c] + mdEz_dx[c]
+        Hy[c] = 1.0 * Hy[c] + dbH * (dEz_dx - dEx_dz)
+        c = (R(1, nx - 1), R(1, ny - 1), R(2, nz - 1))
+        dEx_dy = (Ex[sh(c, 1, 1)] - Ex[c]) / dy
+        dEy_dx = (Ey[sh(c, 0, 1)] - Ey[c]) / dx
+        mdEx_dy[c] = b[c] * mdEx_dy[c] + a[c] * dEx_dy
+        mdEy_dx[c] = b[c] * mdEy_dx[c] + a[c] * dEy_dx
+        dEx_dy = dEx_dy / k[c] + mdEx_dy[c]
+        dEy_dx = dEy_dx / k[c] + mdEy_dx[c]
+        Hz[c] = 1.0 * Hz[c] + dbH * (dEx_dy - dEy_dx)
+        c = (R(2, nx - 1), R(2, ny - 1), R(2, nz - 1))
+        dHz_dy = (Hz[c] - Hz[sh(c, 1, -1)]) / dy
+        dHy_dz = (Hy[c] - Hy[sh(c, 2, -1)]) / dz
+        dHz_dx = (Hz[c] - Hz[sh(c, 0, -1)]) / dx
+        dHx_dz = (Hx[c] - Hx[sh(c, 2, -1)]) / dz
+        dHy_dx = (Hy[c] - Hy[sh(c, 0, -1)]) / dx
+        dHx_dy = (Hx[c] - Hx[sh(c, 1, -1)]) / dy
+        mdHz_dy[c] = bh[c] * mdHz_dy[c] + ah[c] * dHz_dy
+        mdHy_dz[c] = b[c] * mdHy_dz[c] + a[c] * dHy_dz
+        mdHz_dx[c] = bh[c] * mdHz_dx[c] + ah[c] * dHz_dx
+        mdHx_dz[c] = bh[c] * mdHx_dz[c] + ah[c] * dHx_dz
+        mdHx_dy[c] = bh[c] * mdHx_dy[c] + ah[c] * dHx_dy
+        mdHy_dx[c] = bh[c] * mdHy_dx[c] + ah[c] * dHy_dx
+        dHz_dy = dHz_dy / kh[c] + mdHz_dy[c]
+        dHy_dz = dHy_dz / k[c] + mdHy_dz[c]
+        dHz_dx = dHz_dx / kh[c] + mdHz_dx[c]
+        dHx_dz = dHx_dz / kh[c] + mdHx_dz[c]
+        dHx_dy = dHx_dy / kh[c] + mdHx_dy[c]
+        dHy_dx = dHy_dx / kh[c] + mdHy_dx[c]
+        rx = dHz_dy - dHy_dz - (s11[c] * Exo[c] + s12[c] * Eyo[c] + s13[c] * Ezo[c])
+        ry = dHx_dz - dHz_dx - (s12[c] * Exo[c] + s22[c] * Eyo[c] + s23[c] * Ezo[c])
+        rz = dHy_dx - dHx_dy - (s13[c] * Exo[c] + s23[c] * Eyo[c] + s33[c] * Ezo[c])
+        Ex[c] = Exo[c] + (aEx[c] * rx + bEx[c] * ry + cEx[c] * rz) * dt
+        Ey[c] = Eyo[c] + (aEy[c] * rx + bEy[c] * ry + cEy[c] * rz) * dt
+        Ez[c] = Ezo[c] + (aEz[c] * rx + bEz[c] * ry + cEz[c] * rz) * dt
+        for fld, nm, e in ((Ex, "x", e11), (Ey, "y", e22), (Ez, "z", e33)):
+            if p.src.get(nm) is not None:
+                fld[I3] = fld[I3] + p.src[nm][it - 1] * dt / e[I3]
+        for w in f:
+            w[0] = 0.0; w[-1] = 0.0; w[:, 0] = 0.0; w[:, -1] = 0.0; w[:, :, 0] = 0.0; w[:, :, -1] = 0.0
+        Exo[...] = Ex
+        Eyo[...] = Ey
+        Ezo[...] = Ez
+        norms.append(np.max(np.sqrt(Ex ** 2 + Ey ** 2 + Ez ** 2)))
+        traces.append(np.stack([w.ravel(order="F")[rec] for w in (Ex, Ey, Ez)]))
+    return {"fields": f, "memory": M, "traces": np.array(traces), "norms": np.array(norms)}

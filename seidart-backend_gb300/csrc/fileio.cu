@@ -371,7 +371,7 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
     int nmodel, nsrc, nfield, nmem, cplx, ncomp;
     if (seidart_layout(family, &nmodel, &nsrc, &nfield, &nmem, &cplx, &ncomp) != SEIDART_OK)
         return io_err(SEIDART_ERR_ARG, "unknown family");
-    const bool is3 = family == SEIDART_SEISMIC3;
+    const bool is3 = family == SEIDART_SEISMIC3 || family == SEIDART_ELECTROMAG3;
     const size_t N = (size_t)dom->nx * (is3 ? dom->ny : 1) * dom->nz;
     const int nt = src->time_steps;
     std::string why;
@@ -414,6 +414,7 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
         out_slots = {E2_EX, E2_EZ}; out_chans = {"Ex", "Ez"};
         break;
     case SEIDART_ELECTROMAG25:
+    case SEIDART_ELECTROMAG3:  // electromag3 reads the same files (cpmlfdtd.f08:3468-3480, :3608-3615)
         mfiles = {"e11.dat", "e12.dat", "e13.dat", "e22.dat", "e23.dat", "e33.dat",
                   "s11.dat", "s12.dat", "s13.dat", "s22.dat", "s23.dat", "s33.dat"};
         sfiles = {"electromagneticsourcex.dat", "electromagneticsourcey.dat", "electromagneticsourcez.dat"};
@@ -478,7 +479,7 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
         const int frc = write_snapshots ? pipe.finish() : SEIDART_OK;
         if (rc == SEIDART_OK) rc = frc;
     }
-    if (rc == SEIDART_OK && is3) {
+    if (rc == SEIDART_OK && family == SEIDART_SEISMIC3) {
         // velocity_norm.dat and stress_norm.dat (cpmlfdtd.f08:2282-2283)
         std::vector<double> nrm(2 * (size_t)nt);
         rc = seidart_solver_traces(s, nullptr, nrm.data());
@@ -650,9 +651,8 @@ int seidart_cli_main(int argc, char** argv) {
     int single = 1;
     int fam;
     if (d.dim == 3.0) {
-        if (!seismic) { fprintf(stderr, "electromag3 is not provided by the GPU solvers\n"); return 2; }
-        fam = SEIDART_SEISMIC3;
-        printf(" Running 3D seismic model with %d time steps\n", s.time_steps);
+        fam = seismic ? SEIDART_SEISMIC3 : SEIDART_ELECTROMAG3;  // main.f08:88-97
+        printf(" Running 3D %s model with %d time steps\n", seismic ? "seismic" : "electromagnetic", s.time_steps);
     } else if (d.dim == 2.5) {
         fam = seismic ? SEIDART_SEISMIC25 : SEIDART_ELECTROMAG25;
         const char* so = getenv("SINGLE_OUTPUT");

@@ -111,6 +111,30 @@ struct E25Args {
 void launch_electromag25_f64(const E25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag25_f32(const E25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
+// ----------------------------------------------------------- electromag3
+// Derived coefficients (aEx .. cEz with the symmetric ones shared, eps_ii *
+// eps0 for the sources) are built on the host in FP64 from the reference's
+// formulas, then cast.  FP32: dx, dy, dz hold 1/dx, 1/dy, 1/dz and the kappa
+// slots 1/kappa.
+template <typename T>
+struct E3Args {
+    int nx, ny, nz;
+    T dx, dy, dz, dt, dbH;
+    BoxH box;
+    const T* sig[6];   // s11 s12 s13 s22 s23 s33
+    const T* inv[9];   // aEx bEx cEx aEy bEy cEy aEz bEz cEz
+    const T* eabs[3];  // eps11, eps22, eps33 times eps0
+    const T* cpml[6];  // kappa kappa_half acoef acoef_half bcoef bcoef_half
+    T* f[6];           // Ex Ey Ez Hx Hy Hz
+    T* mem[12];        // E3_M_* order
+    const double* src[3];
+    int isrc, jsrc, ksrc;  // 0-based source cell
+    T* traces;         // [nt][3][nrec]
+    double* norms;
+};
+void launch_electromag3_f64(const E3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag3_f32(const E3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+
 // -------------------------------------------------------------- seismic3
 template <typename T>
 struct S3Args {

@@ -61,6 +61,7 @@ bool layout_of(int fam, Layout* L) {
     case SEIDART_SEISMIC3: *L = {SEIDART_NMODEL3, S3_NSRC, S3_NFIELD, S3_NMEM, 0, 3}; return true;
     case SEIDART_ELECTROMAG2: *L = {E2_NMODEL, E2_NSRC, E2_NFIELD, E2_NMEM, 0, 2}; return true;
     case SEIDART_ELECTROMAG25: *L = {E25_NMODEL, E25_NSRC, E25_NFIELD, E25_NMEM, 1, 3}; return true;
+    case SEIDART_ELECTROMAG3: *L = {E3_NMODEL, E3_NSRC, E3_NFIELD, E3_NMEM, 0, 3}; return true;
     default: return false;
     }
 }
@@ -72,6 +73,7 @@ int cpml_slot(int fam) {
     case SEIDART_SEISMIC2: return S2_KAPPA;
     case SEIDART_ELECTROMAG2: return E2_KAPPA;
     case SEIDART_ELECTROMAG25: return E25_KAPPA;
+    case SEIDART_ELECTROMAG3: return E3_KAPPA;
     default: return SEIDART_KAPPA3;
     }
 }
@@ -93,6 +95,16 @@ void averaging2d(double* a, int ni, int nj, int code, int dir) {
     case 1: for (int j = 1; j <= nj; ++j) for (int i = 1; i <= ni - 1; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i + 1, j)], code); break;
     case 2: for (int j = 2; j <= nj; ++j) for (int i = 1; i <= ni; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i, j - 1)], code); break;
     default: for (int j = 1; j <= nj - 1; ++j) for (int i = 1; i <= ni; ++i) a[ix(i, j)] = scalar_mean_h(a[ix(i, j)], a[ix(i, j + 1)], code); break;
+    }
+}
+
+// zero the six faces of a 3D grid (electromag3's H fields, zeroed lazily)
+template <typename T>
+__global__ void zero_faces3d(T* f, int nx, int ny, int nz) {
+    const size_t n = (size_t)nx * ny * nz;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((size_t)nx * ny));
+        if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || k == 0 || k == nz - 1) f[c] = 0;
     }
 }
 
@@ -155,6 +167,7 @@ struct SeidartSolver {
     E2Args<double> e2d; E2Args<float> e2f;
     S25Args<double> s25d; S25Args<float> s25f;
     E25Args<double> e25d; E25Args<float> e25f;
+    E3Args<double> e3d; E3Args<float> e3f;
     S3Args<double> s3d; S3Args<float> s3f;
 
     void* carve(size_t bytes) {
@@ -249,7 +262,7 @@ BoxH interior_box(const SeidartSolver& s, const double* const* model) {
     const double *kap = model[cs], *kaph = model[cs + 1], *ac = model[cs + 2], *ach = model[cs + 3],
                  *bc = model[cs + 4], *bch = model[cs + 5];
     const int nx = s.dom.nx, nz = s.dom.nz, c = s.dom.cpml;
-    const bool is3 = s.family == SEIDART_SEISMIC3;
+    const bool is3 = s.family == SEIDART_SEISMIC3 || s.family == SEIDART_ELECTROMAG3;
     const int ny = is3 ? s.dom.ny : 1;
     BoxH b{c, nx - c, is3 ? c : 0, is3 ? ny - c : 1, c, nz - c};
     const BoxH empty{0, 0, 0, 0, 0, 0};
@@ -417,6 +430,35 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
         if constexpr (sizeof(T) == 8) s.e25d = a; else s.e25f = a;
         break;
     }
+    case SEIDART_ELECTROMAG3: {
+        // cpmlfdtd.f08:3643-3666 (the same inverse as electromag25, no clamp)
+        std::vector<double> det(s.arena ? N : 0);
+        const double* E[6];
+        for (int q = 0; q < 6; ++q) E[q] = model[E3_E11 + q];
+        auto ee = [&](int w, size_t q) { return E[w][q] * kEps0; };  // 0 e11 1 e12 2 e13 3 e22 4 e23 5 e33
+        for (size_t q = 0; q < det.size(); ++q) {
+            const double a11 = ee(0, q), a12 = ee(1, q), a13 = ee(2, q), a22 = ee(3, q), a23 = ee(4, q), a33 = ee(5, q);
+            det[q] = a11 * (a22 * a33 - a23 * a23) - a12 * (a12 * a33 - a23 * a13) + a13 * (a12 * a23 - a22 * a13);
+        }
+        auto inv = [&](size_t q, int w) {
+            const double a11 = ee(0, q), a12 = ee(1, q), a13 = ee(2, q), a22 = ee(3, q), a23 = ee(4, q), a33 = ee(5, q);
+            const double d = det[q];
+            const double aEx = (a22 * a33 - a23 * a23) / d, bEx = -((a12 * a33 - a23 * a13) / d),
+                         cEx = (a12 * a23 - a22 * a13) / d, bEy = (a11 * a33 - a13 * a13) / d,
+                         cEy = -((a11 * a23 - a12 * a13) / d), cEz = (a11 * a22 - a12 * a12) / d;
+            const double v[9] = {aEx, bEx, cEx, bEx, bEy, cEy, cEx, cEy, cEz};
+            return v[w];
+        };
+        E3Args<T> a{};
+        for (int w = 0; w < 9; ++w) a.inv[w] = arr(derive([&](size_t q) { return inv(q, w); }));
+        for (int w = 0; w < 6; ++w) a.sig[w] = arr(model[E3_S11 + w]);
+        const int ed[3] = {0, 3, 5};
+        for (int w = 0; w < 3; ++w) a.eabs[w] = arr(derive([&](size_t q) { return ee(ed[w], q); }));
+        for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
+        for (int q = 0; q < 3; ++q) a.src[q] = dev_src[q];
+        if constexpr (sizeof(T) == 8) s.e3d = a; else s.e3f = a;
+        break;
+    }
     case SEIDART_SEISMIC3: {
         S3Args<T> a{};
         for (int q = 0; q < 21; ++q) a.C[q] = arr(model[q]);
@@ -481,6 +523,18 @@ void finish_args(SeidartSolver& s) {
         a.isrc = is; a.ksrc = ks;
         break;
     }
+    case SEIDART_ELECTROMAG3: {
+        E3Args<T>& a = *(E3Args<T>*)(f32 ? (void*)&s.e3f : (void*)&s.e3d);
+        fill_common2<T>(s, a);
+        a.ny = s.dom.ny;
+        // the FP32 build multiplies by 1/dx, 1/dy, 1/dz
+        a.dx = f32 ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
+        a.dy = f32 ? (T)(1.0 / s.dom.dy) : (T)s.dom.dy;
+        a.dz = f32 ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
+        a.dbH = (T)(s.src.dt / kMu0);
+        a.isrc = is; a.jsrc = js; a.ksrc = ks;
+        break;
+    }
     case SEIDART_SEISMIC3: {
         S3Args<T>& a = *(S3Args<T>*)(f32 ? (void*)&s.s3f : (void*)&s.s3d);
         fill_common2<T>(s, a);
@@ -505,6 +559,7 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : launch_electromag2_f64(s.e2d, si, st, h); break;
     case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : launch_seismic25_f64(s.s25d, si, st, h); break;
     case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
+    case SEIDART_ELECTROMAG3: f32 ? launch_electromag3_f32(s.e3f, si, st, h) : launch_electromag3_f64(s.e3d, si, st, h); break;
     case SEIDART_SEISMIC3:
         if (!f32) launch_seismic3_f64(s.s3d, si, st, h);
         else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr, s.s3_stress_kind,
@@ -591,7 +646,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     if (density_code < 1 || density_code > 4)
         return set_err(SEIDART_ERR_ARG, "density_code %d: must be 1 harmonic, 2 geometric, 3 arithmetic, 4 none",
                        density_code);
-    const bool is3 = family == SEIDART_SEISMIC3;
+    const bool is3 = family == SEIDART_SEISMIC3 || family == SEIDART_ELECTROMAG3;
     const int nx = dom->nx, nz = dom->nz, ny = is3 ? dom->ny : 1;
     if (nx < 6 || nz < 6 || (is3 && ny < 6)) return set_err(SEIDART_ERR_ARG, "grid too small (need >= 6 cells per axis)");
     if (src->time_steps < 1) return set_err(SEIDART_ERR_ARG, "time_steps must be >= 1");
@@ -618,7 +673,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     s->ncell = N;
     s->esize = precision == SEIDART_FP32 ? 4 : 8;
     s->nrec = nrec;
-    s->nnorm = is3 ? 2 : 1;
+    s->nnorm = family == SEIDART_SEISMIC3 ? 2 : 1;  // seismic3 also tracks the stress norm
     {
         auto kind = [](const char* e, int dflt) {
             const char* v = getenv(e);
@@ -785,6 +840,16 @@ static int zero_rings(SeidartSolver* s) {
             zero_ring2d<double><<<(per + 255) / 256, 256, 0, s->stream>>>((double*)s->fields[E2_HY], s->dom.nx, s->dom.nz, 1);
         CUDA_TRY(cudaGetLastError());
     }
+    // electromag3: the six H faces are zeroed lazily by the next H update
+    if (s->family == SEIDART_ELECTROMAG3) {
+        for (int q = E3_HX; q <= E3_HZ; ++q) {
+            if (s->precision == SEIDART_FP32)
+                zero_faces3d<float><<<4 * 152, 256, 0, s->stream>>>((float*)s->fields[q], s->dom.nx, s->dom.ny, s->dom.nz);
+            else
+                zero_faces3d<double><<<4 * 152, 256, 0, s->stream>>>((double*)s->fields[q], s->dom.nx, s->dom.ny, s->dom.nz);
+        }
+        CUDA_TRY(cudaGetLastError());
+    }
     return SEIDART_OK;
 }
 
@@ -819,7 +884,7 @@ int seidart_solver_step(SeidartSolver* s, int nsteps) {
     if (nsteps < 0 || s->steps_done + nsteps > s->src.time_steps)
         return set_err(SEIDART_ERR_ARG, "stepping %d steps from step %d exceeds time_steps = %d", nsteps,
                        s->steps_done, s->src.time_steps);
-    const int chunk = s->family == SEIDART_SEISMIC3 ? 16 : 64;
+    const int chunk = (s->family == SEIDART_SEISMIC3 || s->family == SEIDART_ELECTROMAG3) ? 16 : 64;
     int left = nsteps;
     while (left > 0) {
         const int len = left >= chunk ? chunk : left;

@@ -21,7 +21,7 @@ ERRORS = {
     -7: "SEIDART_ERR_UNSUPPORTED",
 }
 
-SEISMIC2, SEISMIC25, SEISMIC3, ELECTROMAG2, ELECTROMAG25 = 1, 2, 3, 4, 5
+SEISMIC2, SEISMIC25, SEISMIC3, ELECTROMAG2, ELECTROMAG25, ELECTROMAG3 = 1, 2, 3, 4, 5, 6
 FP64, FP32 = 0, 1
 
 

@@ -15,11 +15,11 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import (ELECTROMAG2, ELECTROMAG25, FP32, FP64, SEISMIC2, SEISMIC3, SEISMIC25, Domain, Source, check,
+from ._lib import (ELECTROMAG2, ELECTROMAG3, ELECTROMAG25, FP32, FP64, SEISMIC2, SEISMIC3, SEISMIC25, Domain, Source, check,
                    lib, ptr_array)
 
 FAMILY_NAMES = {SEISMIC2: "seismic2", SEISMIC25: "seismic25", SEISMIC3: "seismic3",
-                ELECTROMAG2: "electromag2", ELECTROMAG25: "electromag25"}
+                ELECTROMAG2: "electromag2", ELECTROMAG25: "electromag25", ELECTROMAG3: "electromag3"}
 DENSITY_CODES = {"harmonic": 1, "geometric": 2, "arithmetic": 3, "none": 4}
 
 # Slot names in C-ABI order (include/seidart_gpu.h)
@@ -32,6 +32,7 @@ MODEL_SLOTS = {
     SEISMIC3: [*C21, "rho", "gamma_x", "gamma_y", "gamma_z", "gamma_xy", "gamma_yz", "gamma_xz", *CPML6],
     ELECTROMAG2: ["e11", "e13", "e33", "s11", "s13", "s33", *CPML6],
     ELECTROMAG25: ["e11", "e12", "e13", "e22", "e23", "e33", "s11", "s12", "s13", "s22", "s23", "s33", *CPML6],
+    ELECTROMAG3: ["e11", "e12", "e13", "e22", "e23", "e33", "s11", "s12", "s13", "s22", "s23", "s33", *CPML6],
 }
 SRC_SLOTS = {
     SEISMIC2: ["x", "z", "xx", "xz", "zz"],
@@ -39,6 +40,7 @@ SRC_SLOTS = {
     SEISMIC3: ["x", "y", "z", "xx", "xy", "xz", "yy", "yz", "zz"],
     ELECTROMAG2: ["x", "z"],
     ELECTROMAG25: ["x", "y", "z"],
+    ELECTROMAG3: ["x", "y", "z"],
 }
 FIELD_SLOTS = {
     SEISMIC2: ["vx", "vz", "sigmaxx", "sigmazz", "sigmaxz"],
@@ -46,6 +48,7 @@ FIELD_SLOTS = {
     SEISMIC3: ["vx", "vy", "vz", "sigmaxx", "sigmaxy", "sigmaxz", "sigmayy", "sigmayz", "sigmazz"],
     ELECTROMAG2: ["Ex", "Ez", "Hy"],
     ELECTROMAG25: ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"],
+    ELECTROMAG3: ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"],
 }
 
 
@@ -82,7 +85,11 @@ class Problem:
 
     @property
     def shape(self) -> tuple:
-        return (self.nx, self.ny, self.nz) if self.family == SEISMIC3 else (self.nx, self.nz)
+        return (self.nx, self.ny, self.nz) if self.is3d else (self.nx, self.nz)
+
+    @property
+    def is3d(self) -> bool:
+        return self.family in (SEISMIC3, ELECTROMAG3)
 
     @property
     def ncell(self) -> int:
@@ -93,7 +100,7 @@ class Problem:
         return self.family in (SEISMIC25, ELECTROMAG25)
 
     def domain(self) -> Domain:
-        dim = 3.0 if self.family == SEISMIC3 else (2.5 if self.is_complex else 2.0)
+        dim = 3.0 if self.is3d else (2.5 if self.is_complex else 2.0)
         return Domain(dim, self.nx, self.ny, self.nz, self.dx, self.dy, self.dz, self.cpml)
 
     def source(self) -> Source:
@@ -139,7 +146,7 @@ class Problem:
     def source_cell(self) -> int:
         """0-based linear index of the source cell (ind + cpml, 1-based)."""
         i, j, k = self.xind + self.cpml - 1, self.yind + self.cpml - 1, self.zind + self.cpml - 1
-        if self.family == SEISMIC3:
+        if self.is3d:
             return i + self.nx * (j + self.ny * k)
         return i + self.nx * k
 

@@ -70,12 +70,12 @@ def write_problem(problem, directory, source_type: str = "ac", json_extra: dict 
     import json
 
     from .api import FIELD_SLOTS, MODEL_SLOTS, SRC_SLOTS
-    from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC3, SEISMIC25
+    from ._lib import ELECTROMAG2, ELECTROMAG3, ELECTROMAG25, SEISMIC25
 
     d = Path(directory)
     d.mkdir(parents=True, exist_ok=True)
     fam = problem.family
-    seismic = fam not in (ELECTROMAG2, ELECTROMAG25)
+    seismic = fam not in (ELECTROMAG2, ELECTROMAG25, ELECTROMAG3)
     for name in MODEL_SLOTS[fam]:
         fname = {"kappa": "kappa_cpml", "kappa_half": "kappa_half_cpml", "acoef": "acoef_cpml",
                  "acoef_half": "acoef_half_cpml", "bcoef": "bcoef_cpml", "bcoef_half": "bcoef_half_cpml"}.get(name, name)
@@ -92,13 +92,13 @@ def write_problem(problem, directory, source_type: str = "ac", json_extra: dict 
         f = problem.fields0.get(name)
         key = "initialcondition" + (name[0].upper() + name[1:])
         write_record(d / f"{key}.dat", np.zeros(problem.shape, dtype=dt) if f is None else np.asarray(f, dt))
-    dim = 3 if fam == SEISMIC3 else (2.5 if fam in (SEISMIC25, ELECTROMAG25) else 2)
+    dim = 3 if problem.is3d else (2.5 if fam in (SEISMIC25, ELECTROMAG25) else 2)
     src = {"x": 0.0, "y": 0.0, "z": 0.0, "xind": problem.xind, "yind": problem.yind, "zind": problem.zind,
            "source_frequency": problem.meta.get("f0", 0.0), "x-z_rotation": 0.0, "x-y_rotation": 0.0,
            "y-z_rotation": 0.0, "amplitude": 1.0, "source_type": source_type, "source_wavelet": "ricker",
            "dt": problem.dt, "time_steps": problem.time_steps}
     js = {"Domain": {"dim": dim, "nx": problem.nx - 2 * problem.cpml,
-                     "ny": (problem.ny - 2 * problem.cpml) if fam == SEISMIC3 else 1,
+                     "ny": (problem.ny - 2 * problem.cpml) if problem.is3d else 1,
                      "nz": problem.nz - 2 * problem.cpml, "dx": problem.dx, "dy": problem.dy, "dz": problem.dz,
                      "cpml": problem.cpml, "nmats": 1, "image_file": "model.png"},
           "Seismic": {"Source": src}, "Electromagnetic": {"Source": src}}

@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._lib import ELECTROMAG2, ELECTROMAG25, SEISMIC2, SEISMIC3, SEISMIC25
+from ._lib import ELECTROMAG2, ELECTROMAG3, ELECTROMAG25, SEISMIC2, SEISMIC3, SEISMIC25
 from .api import C21, Problem
 from .cpml import cpml_grids
 
@@ -326,6 +326,54 @@ def electromag25_blocks(n: int = 128, cpml: int = 10, nt: int = 400, h: float = 
                    xind=n // 2, zind=n // 4, model=model, src={"x": w, "y": 0.5 * w, "z": 0.25 * w},
                    receivers=rec.astype(np.int32), ky=ky,
                    meta={"vmax": vmax, "f0": f0, "seed": seed, "config": "electromag25 blocks"})
+
+
+def electromag3_blocks(n: int = 96, cpml: int = 10, nt: int = 300, h: float = 0.02, f0: float = 100e6,
+                       seed: int = 6, nblocks: int = 6, nrec_side: int = 16, ny: int | None = None,
+                       nz: int | None = None) -> Problem:
+    """3D GPR model: a background of eps = 4, sigma = 1e-4 with ``nblocks``
+    seeded boxes, each with its own full symmetric eps tensor (diagonal
+    U[3, 25], off-diagonal up to 30% of the smallest diagonal) and diagonal
+    sigma U[0, 0.01]; a Gaussian-derivative point source driving all three E
+    components at the centre, a square receiver grid near the top."""
+    rng = np.random.default_rng(seed)
+    nx = n
+    ny = n if ny is None else ny
+    nz = n if nz is None else nz
+    comps = ("11", "12", "13", "22", "23", "33")
+    eps = {c: np.full((nx, ny, nz), 4.0 if c[0] == c[1] else 0.0) for c in comps}
+    sig = {c: np.full((nx, ny, nz), 1.0e-4 if c[0] == c[1] else 0.0) for c in comps}
+    dims = np.array([nx, ny, nz])
+    for _ in range(nblocks):
+        lo = rng.integers(0, dims - dims // 8)
+        w = rng.integers(dims // 16 + 1, dims // 3)
+        d = rng.uniform(3.0, 25.0, 3)
+        off = rng.uniform(-0.3, 0.3, 3) * min(d)
+        e = {"11": d[0], "22": d[1], "33": d[2], "12": off[0], "13": off[1], "23": off[2]}
+        sd = rng.uniform(0, 0.01, 3)
+        s = {"11": sd[0], "22": sd[1], "33": sd[2], "12": 0.0, "13": 0.0, "23": 0.0}
+        box = tuple(slice(lo[q], lo[q] + w[q]) for q in range(3))
+        for c in comps:
+            eps[c][box] = e[c]
+            sig[c][box] = s[c]
+    emin = min(eps[c].min() for c in ("11", "22", "33")) * 0.7
+    vmax = CLIGHT / np.sqrt(emin)
+    dt = courant_dt(vmax, (h, h, h))
+    shape = (nx + 2 * cpml, ny + 2 * cpml, nz + 2 * cpml)
+    model = {}
+    for c in comps:
+        model["e" + c] = pad_edge(eps[c], cpml)
+        model["s" + c] = pad_edge(sig[c], cpml)
+    model.update(_cpml_model(shape, cpml, (h, h, h), dt, vmax, f0))
+    rx = _linspace_idx(1, nx, nrec_side)
+    ry = _linspace_idx(1, ny, nrec_side)
+    RX, RY = np.meshgrid(rx, ry, indexing="ij")
+    rec = (RX.ravel() + cpml - 1) + shape[0] * ((RY.ravel() + cpml - 1) + shape[1] * (nz // 8 + cpml - 1))
+    w = gaussian(nt, dt, f0, 1)
+    return Problem(family=ELECTROMAG3, nx=shape[0], ny=shape[1], nz=shape[2], dx=h, dy=h, dz=h, dt=dt,
+                   time_steps=nt, cpml=cpml, xind=nx // 2, yind=ny // 2, zind=nz // 2, model=model,
+                   src={"x": w, "y": 0.5 * w, "z": 0.25 * w}, receivers=rec.astype(np.int32),
+                   meta={"vmax": vmax, "f0": f0, "seed": seed, "config": "electromag3 blocks"})
 
 
 # ------------------------------------------------------------ ragged batch

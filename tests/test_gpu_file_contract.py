@@ -55,6 +55,22 @@ def test_cli_seismic3_norm_files(tmp_path, oracle):
     assert np.array_equal(vn, o["norms"][0]) and np.array_equal(sn, o["norms"][1])
 
 
+def test_cli_electromag3_snapshots(tmp_path, oracle):
+    """dim = 3 with seismic=false runs electromag3 (main.f08:88-97): 3D Ex/Ey/Ez snapshots."""
+    p = models.electromag3_blocks(n=12, cpml=4, nt=10, nblocks=2, nrec_side=2, f0=8e8)
+    fio.write_problem(p, tmp_path)
+    r = subprocess.run([str(PKG / "seidartfdtd"), "input.json", "seismic=false"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    assert "3D electromagnetic" in r.stdout
+    for it in (1, 10):
+        o = oracle.run_oracle(p, nsteps=it)
+        for q, ch in enumerate(("Ex", "Ey", "Ez")):
+            snap = _snap(tmp_path, ch, it, p, threeD=True)
+            assert np.array_equal(snap, o["fields"][q].astype(np.float32)), f"{ch} step {it}"
+    assert not (tmp_path / "velocity_norm.dat").exists()
+
+
 def test_legacy_entry_point(tmp_path, oracle, monkeypatch):
     """cpmlfdtd.seismic2(nx, nz, dx, dz, src, npml, nstep) with the legacy dt rule."""
     from seidart_gpu import cpmlfdtd

@@ -38,7 +38,11 @@ def small_problems():
     p3 = models.seismic25_two_layer(n=48, cpml=8, nt=120, nrec=12)
     p4 = models.electromag25_blocks(n=48, cpml=8, nt=150, nrec=12)
     p5 = models.seismic3_layers(n=24, cpml=6, nt=40, nlayers=3, nrec_side=4, rec_z=3, src_z=6)
-    return {"seismic2": p1, "electromag2": p2, "seismic25": p3, "electromag25": p4, "seismic3": p5}
+    p6 = models.electromag3_blocks(n=22, cpml=5, nt=60, nblocks=4, nrec_side=4, f0=8e8)
+    for c in ("s12", "s13", "s23"):  # full conductivity tensor: every coupling term
+        p6.model[c][:] = 1e-3
+    return {"seismic2": p1, "electromag2": p2, "seismic25": p3, "electromag25": p4, "seismic3": p5,
+            "electromag3": p6}
 
 
 PROBLEMS = small_problems()
@@ -100,7 +104,7 @@ def test_seismic3_fp32_stress_source_density(oracle, density):
             assert rel_l2(g["memory"][q], o["memory"][q]) <= 10 * FP32_TOL, f"memory {q}"
 
 
-@pytest.mark.parametrize("name", ["seismic2", "electromag2", "seismic3"])
+@pytest.mark.parametrize("name", ["seismic2", "electromag2", "seismic3", "electromag3"])
 def test_chunked_stepping_matches_one_shot(name):
     """Graph chunks of different lengths (and a tail) give the same state."""
     p = PROBLEMS[name]
@@ -145,3 +149,14 @@ def test_unstable_reports_error(oracle):
     with pytest.raises(sg.UnstableError) as e:
         sg.run(p, sg.FP64)
     assert f"step {o['blowup']}" in str(e.value)
+
+
+def test_electromag3_initial_fields_and_interior_box(oracle):
+    """electromag3 from nonzero initial E (initialconditionEx/Ey/Ez) on a grid
+    whose interior holds an inert box (cells that skip the C-PML memories),
+    FP64 bit-exact, including the H faces that are zeroed on read-back."""
+    p = models.electromag3_blocks(n=36, cpml=6, nt=25, nblocks=3, nrec_side=3, f0=8e8)
+    rng = np.random.default_rng(11)
+    for q, nm in enumerate(("Ex", "Ey", "Ez")):
+        p.fields0[nm] = np.asfortranarray(rng.normal(0, 1e-3, p.shape))
+    assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))

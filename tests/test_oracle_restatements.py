@@ -63,3 +63,20 @@ def test_seismic3_c_equals_numpy(oracle):
         _same(a, b)
     _same(c["traces"], n["traces"])
     _same(c["norms"], n["norms"])
+
+
+def test_electromag3_c_equals_numpy(oracle):
+    p = models.electromag3_blocks(n=14, cpml=4, nt=30, nblocks=3, nrec_side=3)
+    # a full conductivity tensor exercises every coupling term
+    for c in ("s12", "s13", "s23"):
+        p.model[c][:] = 2e-4
+    p.model["s11"][:] = 3e-3
+    c = oracle.run_oracle(p)
+    n = restate_np.electromag3(p, p.time_steps)
+    for a, b in zip(c["fields"], n["fields"]):
+        _same(a, b)
+    for a, b in zip(c["memory"], n["memory"]):
+        _same(a, b)
+    _same(c["traces"], n["traces"])
+    _same(c["norms"], n["norms"])
+    assert np.max(np.abs(c["traces"])) > 0
