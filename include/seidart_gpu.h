@@ -287,11 +287,22 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
                        const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
                        const double* const* shot_srcz, int nrec, const int* rec_cells,
                        const double* const* observed, int checkpoint_every);
+/* Same for family = SEIDART_SEISMIC2 (as above) or SEIDART_ELECTROMAG2: model
+ * E2_* slots (density_code ignored), shot series drive Ez at the shot's cell,
+ * traces are Ex and Ez, and seidart_fwi_gradient returns [6][nx*nz]
+ * dL/d{eps11, eps13, eps33, sig11, sig13, sig33} (relative permittivities as
+ * in e11.dat, conductivities as in s11.dat) through the same checkpointed
+ * adjoint of the FP32 electromag2 step (cpmlfdtd.f08:2519-2748). */
+int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain* dom, const SeidartSource* src,
+                              int density_code, const double* const* model, int nshots, const int* shot_xind,
+                              const int* shot_zind, const double* const* shot_srcz, int nrec, const int* rec_cells,
+                              const double* const* observed, int checkpoint_every);
 int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad);
 /* synthetic traces of every shot for the model: [nshots][time_steps][2][nrec] */
 int seidart_fwi_model_traces(SeidartFwi* f, double* traces);
-/* test hooks on one step with the source off; states are [17][nx*nz] FP32
- * (vx vz sigmaxx sigmazz sigmaxz, then the 12 memory arrays in S2_M_* order) */
+/* test hooks on one step with the source off; states are [ns][nx*nz] FP32:
+ * seismic2 ns = 17 (vx vz sigmaxx sigmazz sigmaxz, then the 12 memory arrays
+ * in S2_M_* order), electromag2 ns = 7 (Ex Ez Hy, then E2_M_* order) */
 int seidart_fwi_forward_step_host(SeidartFwi* f, float* x);
 int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam);
 long long seidart_fwi_launches(const SeidartFwi* f);

@@ -158,3 +158,95 @@ def misfit_and_gradient(problem, shots, observed, density_code: int):
         loss = loss + 0.5 * ((tr - obs) ** 2).sum()
     loss.backward()
     return float(loss.detach()), {k: m[k].grad.numpy().copy() for k in keys}
+
+
+# ---------------------------------------------------------------- electromag2
+EPS0 = 8.85418782e-12                       # constants.f08
+MU0 = 4.0 * 3.141592653589793238462643 * 1.0e-7
+EM_KEYS = ("e11", "e13", "e33", "s11", "s13", "s33")
+
+
+def em2_forward_traces(m: dict, dx: float, dz: float, dt: float, nt: int, src_cell: tuple, srcz,
+                       rec: np.ndarray) -> torch.Tensor:
+    """Receiver traces [nt][2][nrec] (Ex, Ez) of one electromag2 shot whose
+    source drives Ez; the statements of oracle_electromag2 in oracle.c
+    (cpmlfdtd.f08:2519-2748: eps scaled by eps0, det clamped at 1e-18 eps0^2,
+    H then E update, Ez += f dt / eps33, ring on Ex, Ez, Hy) as torch
+    expressions on (nx, nz) FP64 tensors."""
+    e11, e13, e33 = m["e11"] * EPS0, m["e13"] * EPS0, m["e33"] * EPS0
+    s11, s13, s33 = m["s11"], m["s13"], m["s33"]
+    kap, kaph, ac, ach, bc, bch = (m[k] for k in ("kappa", "kappa_half", "acoef", "acoef_half", "bcoef",
+                                                  "bcoef_half"))
+    det = e11 * e33 - e13 * e13
+    floor = 1.0e-18 * EPS0 * EPS0
+    det = torch.where(det <= floor, torch.full_like(det, floor), det)
+    aEx, bEx = e33 / det, -e13 / det
+    dEx, eEx = (e33 * s11 - e13 * s13) / det, (e33 * s13 - e13 * s33) / det
+    aEz, bEz = -e13 / det, e11 / det
+    dEz, eEz = (e11 * s13 - e13 * s11) / det, (e11 * s33 - e13 * s13) / det
+    dbHy = dt / MU0
+    nx, nz = e11.shape
+    z = torch.zeros_like(e11)
+    Ex, Ez, Hy = z, z, z
+    m0, m1, m2, m3 = z, z, z, z
+    ri = torch.as_tensor(rec % nx, dtype=torch.long)
+    rk = torch.as_tensor(rec // nx, dtype=torch.long)
+    isrc, ksrc = src_cell
+    srcz = torch.as_tensor(np.asarray(srcz, dtype=np.float64))
+    ring = torch.ones_like(e11)
+    ring[0, :] = 0.0
+    ring[-1, :] = 0.0
+    ring[:, 0] = 0.0
+    ring[:, -1] = 0.0
+    H = (slice(0, nx - 1), slice(0, nz - 1))    # 1-based i, j = 1..n-1
+    E = (slice(1, nx), slice(1, nz))            # 1-based i, j = 2..n
+
+    def put(a, c, val):
+        out = a.clone()
+        out[c] = val
+        return out
+
+    out = []
+    for it in range(nt):
+        c = H
+        dEx_dz = (Ex[0:nx - 1, 1:nz] - Ex[c]) / dz
+        dEz_dx = (Ez[1:nx, 0:nz - 1] - Ez[c]) / dx
+        n0 = bc[c] * m0[c] + ac[c] * dEx_dz
+        n1 = bch[c] * m1[c] + ach[c] * dEz_dx
+        m0, m1 = put(m0, c, n0), put(m1, c, n1)
+        dEz_dx = dEz_dx / kaph[c] + n1
+        dEx_dz = dEx_dz / kap[c] + n0
+        Hy = put(Hy, c, 1.0 * Hy[c] + dbHy * (dEz_dx - dEx_dz))
+        c = E
+        dHy_dz = (Hy[c] - Hy[1:nx, 0:nz - 1]) / dz
+        dHy_dx = (Hy[c] - Hy[0:nx - 1, 1:nz]) / dx
+        n2 = bch[c] * m2[c] + ach[c] * dHy_dx
+        n3 = bc[c] * m3[c] + ac[c] * dHy_dz
+        m2, m3 = put(m2, c, n2), put(m3, c, n3)
+        dHy_dz = dHy_dz / kap[c] + n3
+        dHy_dx = dHy_dx / kaph[c] + n2
+        Exo, Ezo = Ex, Ez
+        nEz = Ezo[c] + (-aEz[c] * dHy_dz + bEz[c] * dHy_dx - dEz[c] * Exo[c] - eEz[c] * Ezo[c]) * dt
+        nEx = Exo[c] + (-aEx[c] * dHy_dz + bEx[c] * dHy_dx - dEx[c] * Exo[c] - eEx[c] * Ezo[c]) * dt
+        Ez, Ex = put(Ezo, c, nEz), put(Exo, c, nEx)
+        Ez = Ez.clone()
+        Ez[isrc, ksrc] = Ez[isrc, ksrc] + srcz[it] * dt / e33[isrc, ksrc]
+        Ex, Ez, Hy = Ex * ring, Ez * ring, Hy * ring
+        out.append(torch.stack([Ex[ri, rk], Ez[ri, rk]]))
+    return torch.stack(out)
+
+
+def em2_misfit_and_gradient(problem, shots, observed):
+    """FP64 L and dL/d{e11, e13, e33, s11, s13, s33} ((nx, nz) numpy arrays)
+    for an electromag2 Problem and the shot list the GPU adjoint takes."""
+    m = {k: torch.tensor(np.asarray(v, dtype=np.float64), requires_grad=k in EM_KEYS)
+         for k, v in problem.model.items()}
+    rec = np.asarray(problem.receivers, dtype=np.int64)
+    loss = torch.zeros((), dtype=torch.float64)
+    for s, shot in enumerate(shots):
+        tr = em2_forward_traces(m, problem.dx, problem.dz, problem.dt, problem.time_steps,
+                                (shot.xind + problem.cpml - 1, shot.zind + problem.cpml - 1), shot.srcz, rec)
+        obs = torch.as_tensor(np.asarray(observed[s], dtype=np.float64).reshape(tr.shape))
+        loss = loss + 0.5 * ((tr - obs) ** 2).sum()
+    loss.backward()
+    return float(loss.detach()), {k: m[k].grad.numpy().copy() for k in EM_KEYS}

@@ -34,6 +34,7 @@
 #include "kernels.h"
 
 extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
+extern "C" int seidart_solver_internal_e2f(SeidartSolver* s, E2Args<float>* out, const int** rec);
 extern "C" int seidart_solver_internal_reset(SeidartSolver* s);
 extern "C" int seidart_solver_internal_advance(SeidartSolver* s, int nsteps);
 extern "C" int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done);
@@ -45,7 +46,8 @@ extern "C" StepInfo seidart_solver_internal_stepinfo(SeidartSolver* s);
 namespace {
 
 constexpr int BX = 32, BY = 8;
-constexpr int NS = 17;  // state arrays: vx vz sxx szz sxz M0..M11
+constexpr int NS = 17;  // seismic2 state arrays: vx vz sxx szz sxz M0..M11
+constexpr int NS_EM = 7;  // electromag2 state arrays: Ex Ez Hy M0..M3
 
 struct AdjArgs {
     int nx, nz, density_code;
@@ -317,10 +319,9 @@ __global__ void seg_begin(int* step, int* base, int t0) {
     *base = t0;
 }
 
-__global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block) {
+__global__ void copy_state(StatePtrs s, float* blk, size_t N, int to_block, int ns) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < N; q += (size_t)gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int a = 0; a < NS; ++a) {
+        for (int a = 0; a < ns; ++a) {
             if (to_block) blk[a * N + q] = s.p[a][q];
             else s.p[a][q] = blk[a * N + q];
         }
@@ -476,16 +477,17 @@ __global__ void fold_grad(double* __restrict__ g64, float* __restrict__ g32, siz
 // on the device at the end.
 struct FwiLane {
     SeidartSolver* s = nullptr;
-    S2Args<float> a{};
+    S2Args<float> a{};          // seismic2 lanes
+    E2Args<float> e{};          // electromag2 lanes
     const int* rec = nullptr;
     cudaStream_t st = nullptr;
     StepInfo si{};
     StatePtrs ptrs{};
     int shot = -1;              // shot the lane's solver and graphs are set up for
     bool graphs = false;        // segment graphs captured for `shot`
-    float* ckpt = nullptr;      // [G][NS][N]
-    float* seg = nullptr;       // [K+1][NS][N]
-    float* lam = nullptr;       // [NS][N]
+    float* ckpt = nullptr;      // [G][ns][N]
+    float* seg = nullptr;       // [K+1][ns][N]
+    float* lam = nullptr;       // [ns][N]
     float* scr = nullptr;       // [12][N]
     float* dres = nullptr;      // [nt][2][nrec] residual of the lane's shot
     double* grad = nullptr;     // [8][N] FP64 gradient sums over segments and shots
@@ -499,13 +501,16 @@ struct FwiLane {
 
 struct SeidartFwi {
     std::vector<FwiLane> lanes;
+    int family = SEIDART_SEISMIC2, ns = NS;  // solver family and state arrays per cell
     int nrec = 0, nt = 0, nshots = 0, K = 1, G = 1, density = 3;
     size_t N = 0;
     std::vector<int> sx, sz;
     double* dsrc = nullptr;     // [nshots][nt] force series (device)
     float* dobs = nullptr;      // [nshots][nt][2][nrec] observed traces
-    double* dgsrc = nullptr;    // [nshots] sum_n lambda_vz(src) f_n per shot
+    double* dgsrc = nullptr;    // [nshots] sum_n lambda(src) f_n per shot (vz or Ez)
     std::vector<double> srch;   // host copy of the source series
+    std::vector<double> em[6];  // electromag2: host eps11 eps13 eps33 sig11 sig13 sig33 (for the chain rule)
+    double dt = 0.0;
     long long launches = 0;
 };
 
@@ -540,23 +545,52 @@ AdjArgs adj_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, co
     return A;
 }
 
+EmAdjArgs em_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, const double* srcz, int j) {
+    EmAdjArgs A{};
+    A.a = L.e;
+    A.xp = xp; A.xc = xc; A.lam = L.lam; A.scr = L.scr; A.grad = L.grad32; A.N = f->N;
+    A.srcz = srcz; A.base = L.dbase; A.j = j;
+    A.gsrc = f->dgsrc + (L.shot >= 0 ? L.shot : 0);
+    return A;
+}
+
+// grid extent of the lane's solver
+int lane_nx(const SeidartFwi* f, const FwiLane& L) { return f->family == SEIDART_ELECTROMAG2 ? L.e.nx : L.a.nx; }
+int lane_nz(const SeidartFwi* f, const FwiLane& L) { return f->family == SEIDART_ELECTROMAG2 ? L.e.nz : L.a.nz; }
+float* lane_traces(const SeidartFwi* f, const FwiLane& L) {
+    return f->family == SEIDART_ELECTROMAG2 ? L.e.traces : L.a.traces;
+}
+double* lane_norms(const SeidartFwi* f, const FwiLane& L) {
+    return f->family == SEIDART_ELECTROMAG2 ? L.e.norms : L.a.norms;
+}
+
 // adjoint of step n = *dbase + j (launched on the lane's stream, possibly under capture)
 void adjoint_step(SeidartFwi* f, FwiLane& L, int j, const float* xp, const float* xc, const double* srcz, int nrec) {
-    const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
     if (nrec > 0) adj_inject<<<1, 256, 0, L.st>>>(L.lam, f->N, L.rec, nrec, L.dres, L.dbase, j);
+    if (f->family == SEIDART_ELECTROMAG2) {
+        em2_adjoint_step(em_args(f, L, xp, xc, srcz, j), L.st);
+        return;
+    }
+    const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
     const AdjArgs A = adj_args(f, L, xp, xc, srcz, j);
     adj_velocity<<<grd, blk, 0, L.st>>>(A);
     adj_stress<<<grd, blk, 0, L.st>>>(A);
     adj_gather_v<<<grd, blk, 0, L.st>>>(A);
 }
 
-void save_state(FwiLane& L, float* blk, size_t N) {
-    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, blk, N, 1);
+void save_state(const SeidartFwi* f, FwiLane& L, float* blk) {
+    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, blk, f->N, 1, f->ns);
     ++L.launches;
 }
-void load_state(FwiLane& L, const float* blk, size_t N) {
-    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, const_cast<float*>(blk), N, 0);
+void load_state(const SeidartFwi* f, FwiLane& L, const float* blk) {
+    copy_state<<<4 * 152, 256, 0, L.st>>>(L.ptrs, const_cast<float*>(blk), f->N, 0, f->ns);
     ++L.launches;
+}
+
+// refresh the lane's copy of its solver's FP32 arguments
+void lane_args(SeidartFwi* f, FwiLane& L, const int** rec) {
+    if (f->family == SEIDART_ELECTROMAG2) seidart_solver_internal_e2f(L.s, &L.e, rec);
+    else seidart_solver_internal_s2f(L.s, &L.a, rec);
 }
 
 // Point lane L at shot sh (its source position and series).  Waits for the
@@ -565,7 +599,7 @@ int lane_set_shot(SeidartFwi* f, FwiLane& L, int sh) {
     if (L.shot == sh) return SEIDART_OK;
     const int rc = seidart_solver_internal_set_source(L.s, f->sx[sh], f->sz[sh], nullptr, f->dsrc + (size_t)sh * f->nt);
     if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    seidart_solver_internal_s2f(L.s, &L.a, nullptr);
+    lane_args(f, L, nullptr);
     L.shot = sh;
     L.graphs = false;
     return SEIDART_OK;
@@ -575,9 +609,9 @@ int lane_set_shot(SeidartFwi* f, FwiLane& L, int sh) {
 // all queued on the lane's stream (no host wait)
 int lane_reset(SeidartFwi* f, FwiLane& L) {
     const size_t N = f->N;
-    for (int q = 0; q < NS; ++q) FCUDA(cudaMemsetAsync(L.ptrs.p[q], 0, sizeof(float) * N, L.st));
-    FCUDA(cudaMemsetAsync(L.a.traces, 0, sizeof(float) * (size_t)f->nt * 2 * (f->nrec > 0 ? f->nrec : 1), L.st));
-    FCUDA(cudaMemsetAsync(L.a.norms, 0, sizeof(double) * f->nt, L.st));
+    for (int q = 0; q < f->ns; ++q) FCUDA(cudaMemsetAsync(L.ptrs.p[q], 0, sizeof(float) * N, L.st));
+    FCUDA(cudaMemsetAsync(lane_traces(f, L), 0, sizeof(float) * (size_t)f->nt * 2 * (f->nrec > 0 ? f->nrec : 1), L.st));
+    FCUDA(cudaMemsetAsync(lane_norms(f, L), 0, sizeof(double) * f->nt, L.st));
     seg_begin<<<1, 1, 0, L.st>>>(L.si.step, L.dbase, 0);
     FCUDA(cudaGetLastError());
     seidart_solver_internal_advance(L.s, -seidart_solver_steps_done(L.s));
@@ -587,17 +621,17 @@ int lane_reset(SeidartFwi* f, FwiLane& L) {
 // forward segment g of lane L (checkpoint first when asked)
 int lane_forward_segment(SeidartFwi* f, FwiLane& L, int g, bool checkpoints) {
     const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
-    if (checkpoints) save_state(L, L.ckpt + (size_t)g * NS * f->N, f->N);
+    if (checkpoints) save_state(f, L, L.ckpt + (size_t)g * f->ns * f->N);
     const int rc = seidart_solver_step(L.s, len);
     if (rc != SEIDART_OK) return ferr(rc, seidart_last_error());
-    L.launches += (long long)len * seidart_step_launches(SEIDART_SEISMIC2, L.a.stress_src);
+    L.launches += (long long)len * seidart_step_launches(f->family, f->family == SEIDART_SEISMIC2 ? L.a.stress_src : 0);
     return SEIDART_OK;
 }
 
 int lane_residual(SeidartFwi* f, FwiLane& L) {
     const size_t n = (size_t)f->nt * 2 * f->nrec;
     if (n == 0) return SEIDART_OK;
-    residual_loss<<<152, 256, 0, L.st>>>((const float*)L.a.traces, f->dobs + (size_t)L.shot * n, L.dres, n, L.dscal);
+    residual_loss<<<152, 256, 0, L.st>>>(lane_traces(f, L), f->dobs + (size_t)L.shot * n, L.dres, n, L.dscal);
     ++L.launches;
     return cudaGetLastError() == cudaSuccess ? SEIDART_OK : ferr(SEIDART_ERR_CUDA, "residual kernel");
 }
@@ -607,11 +641,16 @@ int lane_residual(SeidartFwi* f, FwiLane& L) {
 // and instantiate it into *exec, updating an existing executable in place
 // when the topology allows.
 int capture_segment(SeidartFwi* f, FwiLane& L, int len, bool adjoint, cudaGraphExec_t* exec) {
-    const size_t state = (size_t)NS * f->N;
+    const size_t state = (size_t)f->ns * f->N;
     const double* srcz = f->dsrc + (size_t)L.shot * f->nt;
     FCUDA(cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
     const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
-    if (!adjoint) {
+    if (!adjoint && f->family == SEIDART_ELECTROMAG2) {
+        for (int j = 1; j <= len; ++j) {
+            const EmOopArgs O{L.e, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, f->N, srcz, L.dbase, j};
+            em2_recompute_step(O, L.st);
+        }
+    } else if (!adjoint) {
         for (int j = 1; j <= len; ++j) {
             OopArgs O{L.a, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, f->N, srcz, L.dbase, j};
             oop_stress<<<grd, blk, 0, L.st>>>(O);
@@ -661,12 +700,13 @@ int lane_backward_segment(SeidartFwi* f, FwiLane& L, int g) {
     const int t0 = g * f->K, len = std::min(f->K, f->nt - t0);
     const int slot = len == f->K ? 0 : 1;
     seg_begin<<<1, 1, 0, L.st>>>(L.si.step, L.dbase, t0);
-    FCUDA(cudaMemcpyAsync(L.seg, L.ckpt + (size_t)g * NS * f->N, sizeof(float) * NS * f->N, cudaMemcpyDeviceToDevice,
-                          L.st));
+    FCUDA(cudaMemcpyAsync(L.seg, L.ckpt + (size_t)g * f->ns * f->N, sizeof(float) * f->ns * f->N,
+                          cudaMemcpyDeviceToDevice, L.st));
     FCUDA(cudaGetLastError());
     FCUDA(cudaGraphLaunch(L.rec_exec[slot], L.st));
     FCUDA(cudaGraphLaunch(L.adj_exec[slot], L.st));
-    L.launches += 1 + 2 * len + len * (f->nrec > 0 ? 4 : 3) + 1;
+    const int adj_kernels = f->family == SEIDART_ELECTROMAG2 ? 2 : 3;
+    L.launches += 1 + 2 * len + len * (adj_kernels + (f->nrec > 0 ? 1 : 0)) + 1;
     return SEIDART_OK;
 }
 
@@ -701,7 +741,8 @@ int run_shots(SeidartFwi* f, bool grad, bool keep_traces_of_round, double* trace
         if (!grad) continue;
         for (int l = 0; l < nr; ++l) {
             FwiLane& L = f->lanes[l];
-            FCUDA(cudaMemsetAsync(L.lam, 0, sizeof(float) * NS * f->N, L.st));
+            FCUDA(cudaMemsetAsync(L.lam, 0, sizeof(float) * f->ns * f->N, L.st));
+            FCUDA(cudaMemsetAsync(L.scr, 0, sizeof(float) * 12 * f->N, L.st));
             const int rc = lane_graphs(f, L);
             if (rc != SEIDART_OK) return rc;
         }
@@ -722,8 +763,8 @@ int sync_lanes(SeidartFwi* f) {
     return SEIDART_OK;
 }
 
-size_t lane_bytes(size_t N, int K, int G, int nt, int nrec) {
-    return sizeof(float) * ((size_t)G + K + 1 + 1 + 0) * NS * N + sizeof(float) * 12 * N + sizeof(double) * 8 * N +
+size_t lane_bytes(size_t N, int ns, int K, int G, int nt, int nrec) {
+    return sizeof(float) * ((size_t)G + K + 1 + 1 + 0) * ns * N + sizeof(float) * 12 * N + sizeof(double) * 8 * N +
            sizeof(float) * (size_t)nt * 2 * (nrec > 0 ? nrec : 1) + sizeof(float) * 40 * N;  // + solver arena
 }
 
@@ -738,6 +779,48 @@ void free_lane(FwiLane& L) {
         if (p) cudaFree(p);
     if (L.s) seidart_solver_destroy(L.s);
     L = FwiLane();
+}
+
+// Chain dL/d(aEx bEx dEx eEx aEz bEz dEz eEz) per cell to the relative
+// permittivities and conductivities (cpmlfdtd.f08:2519-2540: eps scaled by
+// eps0, det = eps11 eps33 - eps13^2 clamped at 1e-18 eps0^2, where its
+// derivative is zero), plus the Ez source term f dt / eps33 at each shot's
+// cell.  out: [6][N] eps11 eps13 eps33 sig11 sig13 sig33.
+void em_chain(const SeidartFwi* f, const std::vector<double>& g, const std::vector<double>& gsrc, double* out) {
+    const size_t N = f->N;
+    const double eps0 = 8.85418782e-12;  // constants.f08
+    const double floor = 1.0e-18 * eps0 * eps0;
+    for (size_t q = 0; q < N; ++q) {
+        const double E11 = f->em[0][q] * eps0, E13 = f->em[1][q] * eps0, E33 = f->em[2][q] * eps0;
+        const double s11 = f->em[3][q], s13 = f->em[4][q], s33 = f->em[5][q];
+        double det = E11 * E33 - E13 * E13;
+        double dd[6] = {E33, -2.0 * E13, E11, 0.0, 0.0, 0.0};
+        if (det <= floor) {
+            det = floor;
+            for (double& v : dd) v = 0.0;
+        }
+        // numerators of the eight coefficients and their partials in (E11 E13 E33 s11 s13 s33)
+        const double num[8] = {E33, -E13, E33 * s11 - E13 * s13, E33 * s13 - E13 * s33,
+                               -E13, E11, E11 * s13 - E13 * s11, E11 * s33 - E13 * s13};
+        const double dn[8][6] = {{0, 0, 1, 0, 0, 0},         {0, -1, 0, 0, 0, 0},
+                                 {0, -s13, s11, E33, -E13, 0}, {0, -s33, s13, 0, E33, -E13},
+                                 {0, -1, 0, 0, 0, 0},         {1, 0, 0, 0, 0, 0},
+                                 {s13, -s11, 0, -E13, E11, 0}, {s33, -s13, 0, 0, -E13, E11}};
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int w = 0; w < 8; ++w) {
+            const double gw = g[(size_t)w * N + q];
+            if (gw == 0.0) continue;
+            const double coef = num[w] / det;
+            for (int p = 0; p < 6; ++p) acc[p] += gw * (dn[w][p] - coef * dd[p]) / det;
+        }
+        for (int p = 0; p < 3; ++p) out[(size_t)p * N + q] = acc[p] * eps0;
+        for (int p = 3; p < 6; ++p) out[(size_t)p * N + q] = acc[p];
+    }
+    for (int sh = 0; sh < f->nshots; ++sh) {
+        const size_t c = (size_t)f->sx[sh] + (size_t)lane_nx(f, f->lanes[0]) * f->sz[sh];
+        const double E33 = f->em[2][c] * eps0;
+        out[2 * N + c] += -gsrc[sh] * f->dt / (E33 * E33) * eps0;
+    }
 }
 
 }  // namespace
@@ -755,24 +838,32 @@ int seidart_fwi_destroy(SeidartFwi* f) {
     return SEIDART_OK;
 }
 
-// Create an FWI problem: one 2D elastic model (S2_* slots, host FP64), shots
-// with their own force position (interior indices) and vertical-force
-// series, a common receiver set, and observed traces per shot
-// ([time_steps][2][nrec], vx then vz).  checkpoint_every = 0 picks
-// ceil(sqrt(nt)).  Up to one lane per shot, as device memory allows.
-int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const SeidartSource* src, int density_code,
-                       const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
-                       const double* const* shot_srcz, int nrec, const int* rec_cells,
-                       const double* const* observed, int checkpoint_every) {
+// Create an FWI problem: one 2D model (host FP64, the family's slots), shots
+// with their own source position (interior indices) and source series (the
+// vertical force of seismic2, the Ez source of electromag2), a common
+// receiver set, and observed traces per shot ([time_steps][2][nrec]: vx, vz
+// or Ex, Ez).  checkpoint_every = 0 picks ceil(sqrt(nt)).  Up to one lane
+// per shot, as device memory allows.
+int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain* dom, const SeidartSource* src,
+                              int density_code, const double* const* model, int nshots, const int* shot_xind,
+                              const int* shot_zind, const double* const* shot_srcz, int nrec, const int* rec_cells,
+                              const double* const* observed, int checkpoint_every) {
     if (!out || !dom || !src || !model || nshots < 1 || !shot_xind || !shot_zind || !shot_srcz)
         return ferr(SEIDART_ERR_ARG, "bad arguments");
+    if (family != SEIDART_SEISMIC2 && family != SEIDART_ELECTROMAG2)
+        return ferr(SEIDART_ERR_UNSUPPORTED, "the adjoint covers seismic2 and electromag2");
     *out = nullptr;
     SeidartFwi* f = new SeidartFwi();
+    f->family = family;
+    f->ns = family == SEIDART_ELECTROMAG2 ? NS_EM : NS;
+    f->dt = src->dt;
     f->nt = src->time_steps;
     f->nshots = nshots;
     f->nrec = nrec;
     f->density = density_code;
     f->N = (size_t)dom->nx * dom->nz;
+    if (family == SEIDART_ELECTROMAG2)
+        for (int q = 0; q < 6; ++q) f->em[q].assign(model[E2_E11 + q], model[E2_E11 + q] + f->N);
     f->K = checkpoint_every > 0 ? checkpoint_every : (int)ceil(sqrt((double)f->nt));
     f->G = (f->nt + f->K - 1) / f->K;
     for (int sh = 0; sh < nshots; ++sh) {
@@ -807,7 +898,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     // 2.75 s, 1 lane 3.81 s), within 3/4 of the free device memory
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    const size_t per = lane_bytes(f->N, f->K, f->G, f->nt, nrec);
+    const size_t per = lane_bytes(f->N, f->ns, f->K, f->G, f->nt, nrec);
     const size_t want = std::max<size_t>(1, (size_t)(1.2e6 / (double)f->N + 0.5));
     int nl = (int)std::min<size_t>(std::min<size_t>((size_t)nshots, want), std::max<size_t>(1, (free_b / 4 * 3) / per));
     const char* env = getenv("SEIDART_FWI_LANES");
@@ -815,21 +906,27 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     f->lanes.resize(nl);
     for (int l = 0; l < nl; ++l) {
         FwiLane& L = f->lanes[l];
+        // the force (seismic2) or the Ez source (electromag2) is the second source slot
         const double* srcs[S2_NSRC] = {nullptr, shot_srcz[l], nullptr, nullptr, nullptr};
         SeidartSource s0 = *src;
         s0.xind = shot_xind[l];
         s0.zind = shot_zind[l];
-        int rc = seidart_solver_create(&L.s, SEIDART_SEISMIC2, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
+        int rc = seidart_solver_create(&L.s, family, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
                                        rec_cells);
         if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
-        seidart_solver_internal_s2f(L.s, &L.a, &L.rec);
+        lane_args(f, L, &L.rec);
         L.st = seidart_solver_internal_stream(L.s);
         L.si = seidart_solver_internal_stepinfo(L.s);
-        for (int q = 0; q < 5; ++q) L.ptrs.p[q] = L.a.f[q];
-        for (int q = 0; q < 12; ++q) L.ptrs.p[5 + q] = L.a.mem[q];
-        if (cudaMalloc((void**)&L.ckpt, sizeof(float) * f->G * NS * f->N) != cudaSuccess ||
-            cudaMalloc((void**)&L.seg, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
-            cudaMalloc((void**)&L.lam, sizeof(float) * NS * f->N) != cudaSuccess ||
+        if (family == SEIDART_ELECTROMAG2) {
+            for (int q = 0; q < 3; ++q) L.ptrs.p[q] = L.e.f[q];
+            for (int q = 0; q < 4; ++q) L.ptrs.p[3 + q] = L.e.mem[q];
+        } else {
+            for (int q = 0; q < 5; ++q) L.ptrs.p[q] = L.a.f[q];
+            for (int q = 0; q < 12; ++q) L.ptrs.p[5 + q] = L.a.mem[q];
+        }
+        if (cudaMalloc((void**)&L.ckpt, sizeof(float) * f->G * f->ns * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.seg, sizeof(float) * (f->K + 1) * f->ns * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.lam, sizeof(float) * f->ns * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
             cudaMalloc((void**)&L.grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
@@ -841,7 +938,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
             return ferr(SEIDART_ERR_NOMEM, "FWI lane allocation failed");
         }
         // segment states are written only where a step updates them: start from zeros
-        if (cudaMemset(L.seg, 0, sizeof(float) * (f->K + 1) * NS * f->N) != cudaSuccess ||
+        if (cudaMemset(L.seg, 0, sizeof(float) * (f->K + 1) * f->ns * f->N) != cudaSuccess ||
             cudaMemset(L.grad32, 0, sizeof(float) * 8 * f->N) != cudaSuccess) {
             cudaGetLastError();
             seidart_fwi_destroy(f);
@@ -855,8 +952,18 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
     return SEIDART_OK;
 }
 
-// Loss and gradient over all shots.  grad (host, may be NULL) receives
-// [5][ncell] FP64: dL/dc11, dL/dc13, dL/dc33, dL/dc55, dL/drho.
+int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const SeidartSource* src, int density_code,
+                       const double* const* model, int nshots, const int* shot_xind, const int* shot_zind,
+                       const double* const* shot_srcz, int nrec, const int* rec_cells,
+                       const double* const* observed, int checkpoint_every) {
+    return seidart_fwi_create_family(out, SEIDART_SEISMIC2, dom, src, density_code, model, nshots, shot_xind,
+                                     shot_zind, shot_srcz, nrec, rec_cells, observed, checkpoint_every);
+}
+
+// Loss and gradient over all shots.  grad (host, may be NULL) receives FP64
+// per cell: seismic2 [5][ncell] dL/dc11, dL/dc13, dL/dc33, dL/dc55, dL/drho;
+// electromag2 [6][ncell] dL/deps11, dL/deps13, dL/deps33 (relative
+// permittivities, as in e11.dat ...), dL/dsig11, dL/dsig13, dL/dsig33.
 int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
     if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
     f->launches = 0;
@@ -892,6 +999,10 @@ int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
         std::vector<double> g(8 * N), gsrc(f->nshots);
         FCUDA(cudaMemcpy(g.data(), L0.grad, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
         FCUDA(cudaMemcpy(gsrc.data(), f->dgsrc, sizeof(double) * f->nshots, cudaMemcpyDeviceToHost));
+        if (f->family == SEIDART_ELECTROMAG2) {
+            em_chain(f, g, gsrc, grad);
+            return SEIDART_OK;
+        }
         memcpy(grad, g.data(), sizeof(double) * 4 * N);
         // chain the face buoyancies B = 1/mean(rho_a, rho_b) to rho (FP32 forward values)
         std::vector<float> rho(N);
@@ -934,12 +1045,13 @@ int seidart_fwi_model_traces(SeidartFwi* f, double* traces) {
 }
 
 // Adjoint test hook: apply one adjoint step (no receiver residual) to the
-// adjoint state lam (host, [17][ncell] FP32 in state order) with forward
-// states xprev/xcur ([17][ncell]); lam is updated in place.
+// adjoint state lam (host, [ns][ncell] FP32 in state order: 17 arrays for
+// seismic2, 7 for electromag2) with forward states xprev/xcur
+// ([ns][ncell]); lam is updated in place.
 int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam) {
     if (!f || !xprev || !xcur || !lam) return ferr(SEIDART_ERR_ARG, "NULL");
     FwiLane& L = f->lanes[0];
-    const size_t bytes = sizeof(float) * NS * f->N;
+    const size_t bytes = sizeof(float) * f->ns * f->N;
     float *dp = nullptr, *dc = nullptr;
     FCUDA(cudaMalloc((void**)&dp, bytes));
     FCUDA(cudaMalloc((void**)&dc, bytes));
@@ -947,7 +1059,11 @@ int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float
     FCUDA(cudaMemcpy(dc, xcur, bytes, cudaMemcpyHostToDevice));
     FCUDA(cudaMemcpy(L.lam, lam, bytes, cudaMemcpyHostToDevice));
     FCUDA(cudaMemsetAsync(L.dbase, 0, sizeof(int), L.st));
+    FCUDA(cudaMemsetAsync(L.scr, 0, sizeof(float) * 12 * f->N, L.st));
     adjoint_step(f, L, 1, dp, dc, nullptr, 0);
+    // electromag2 leaves the last gather into Ex, Ez to the next step: do it here
+    if (f->family == SEIDART_ELECTROMAG2) em2_adjoint_flush(em_args(f, L, dp, dc, nullptr, 1), L.st);
+    FCUDA(cudaGetLastError());
     FCUDA(cudaStreamSynchronize(L.st));
     FCUDA(cudaMemcpy(lam, L.lam, bytes, cudaMemcpyDeviceToHost));
     cudaFree(dp);
@@ -955,22 +1071,22 @@ int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float
     return SEIDART_OK;
 }
 
-// Forward test hook: one forward step (source off) on a host state [17][ncell].
+// Forward test hook: one forward step (source off) on a host state [ns][ncell].
 int seidart_fwi_forward_step_host(SeidartFwi* f, float* x) {
     if (!f || !x) return ferr(SEIDART_ERR_ARG, "NULL");
     FwiLane& L = f->lanes[0];
-    const size_t bytes = sizeof(float) * NS * f->N;
+    const size_t bytes = sizeof(float) * f->ns * f->N;
     float* d = nullptr;
     FCUDA(cudaMalloc((void**)&d, bytes));
     FCUDA(cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice));
     int rc = seidart_solver_internal_reset(L.s);
     if (rc == SEIDART_OK) rc = seidart_solver_internal_set_source(L.s, f->sx[0], f->sz[0], nullptr, nullptr);
     if (rc == SEIDART_OK) {
-        seidart_solver_internal_s2f(L.s, &L.a, nullptr);
-        load_state(L, d, f->N);
+        lane_args(f, L, nullptr);
+        load_state(f, L, d);
         rc = seidart_solver_step(L.s, 1);
     }
-    if (rc == SEIDART_OK) save_state(L, d, f->N);
+    if (rc == SEIDART_OK) save_state(f, L, d);
     FCUDA(cudaStreamSynchronize(L.st));
     FCUDA(cudaMemcpy(x, d, bytes, cudaMemcpyDeviceToHost));
     cudaFree(d);

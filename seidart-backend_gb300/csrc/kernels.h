@@ -66,6 +66,34 @@ struct E2Args {
 void launch_electromag2_f64(const E2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag2_f32(const E2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
+// Adjoint of one FP32 electromag2 step (adjoint_em.cu).  State arrays, N
+// cells each: Ex Ez Hy m_dEx_dz m_dEz_dx m_dHy_dx m_dHy_dz.
+struct EmAdjArgs {
+    E2Args<float> a;     // FP32 solver arguments (coefficients, CPML, sizes, source cell)
+    const float* xp;     // x_{n-1}: [7][N]
+    const float* xc;     // x_n
+    float* lam;          // adjoint state [7][N]
+    float* scr;          // [4][N]: E^T -> Hy gather (z, x), H^T -> E gather (Ex, Ez)
+    float* grad;         // [8][N] FP32 sums: aEx bEx dEx eEx aEz bEz dEz eEz
+    size_t N;
+    const double* srcz;  // Ez source series of the shot (device), NULL = none
+    const int* base;     // device: steps before the segment; this step is *base + j
+    int j;
+    double* gsrc;        // accumulated lambda_Ez(src) * f_n
+};
+struct EmOopArgs {
+    E2Args<float> a;
+    const float* in;     // x_{j-1}: [7][N]
+    float* out;          // x_j
+    size_t N;
+    const double* srcz;
+    const int* base;
+    int j;
+};
+void em2_adjoint_step(const EmAdjArgs& A, cudaStream_t st);
+void em2_adjoint_flush(const EmAdjArgs& A, cudaStream_t st);
+void em2_recompute_step(const EmOopArgs& O, cudaStream_t st);
+
 // ------------------------------------------------------------- seismic25
 // Complex fields are interleaved (re, im) arrays of T.  The nine face
 // densities are pre-averaged on the host exactly as the reference does

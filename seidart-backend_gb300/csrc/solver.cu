@@ -1027,6 +1027,13 @@ int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int*
     return SEIDART_OK;
 }
 
+int seidart_solver_internal_e2f(SeidartSolver* s, E2Args<float>* out, const int** rec) {
+    if (!s || s->family != SEIDART_ELECTROMAG2 || s->precision != SEIDART_FP32) return set_err(SEIDART_ERR_ARG, "not an FP32 electromag2 solver");
+    *out = s->e2f;
+    if (rec) *rec = s->rec_dev;
+    return SEIDART_OK;
+}
+
 // zero fields, memories, traces and norms; back to step 1
 int seidart_solver_internal_reset(SeidartSolver* s) {
     if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
@@ -1066,13 +1073,21 @@ int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done) {
 // because they hold the launch arguments by value
 int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
                                        const double* dev_srcz) {
-    if (!s || s->family != SEIDART_SEISMIC2 || s->precision != SEIDART_FP32) return set_err(SEIDART_ERR_ARG, "bad solver");
+    if (!s || (s->family != SEIDART_SEISMIC2 && s->family != SEIDART_ELECTROMAG2) || s->precision != SEIDART_FP32)
+        return set_err(SEIDART_ERR_ARG, "bad solver");
     if (isrc < 0 || isrc + 1 >= s->dom.nx || jsrc < 0 || jsrc + 1 >= s->dom.nz) return set_err(SEIDART_ERR_ARG, "source outside grid");
     CUDA_TRY(cudaStreamSynchronize(s->stream));
-    s->s2f.isrc = isrc;
-    s->s2f.jsrc = jsrc;
-    s->s2f.src[S2_SRCX] = dev_srcx;
-    s->s2f.src[S2_SRCZ] = dev_srcz;
+    if (s->family == SEIDART_SEISMIC2) {
+        s->s2f.isrc = isrc;
+        s->s2f.jsrc = jsrc;
+        s->s2f.src[S2_SRCX] = dev_srcx;
+        s->s2f.src[S2_SRCZ] = dev_srcz;
+    } else {
+        s->e2f.isrc = isrc;
+        s->e2f.jsrc = jsrc;
+        s->e2f.src[E2_SRCX] = dev_srcx;
+        s->e2f.src[E2_SRCZ] = dev_srcz;
+    }
     for (int q = 0; q < 2; ++q)
         if (s->graph_exec[q]) { cudaGraphExecDestroy(s->graph_exec[q]); s->graph_exec[q] = nullptr; s->graph_len[q] = 0; }
     return SEIDART_OK;

@@ -1,18 +1,24 @@
-"""Misfit gradient of the 2D elastic solver (full-waveform inversion).
+"""Misfit gradients of the 2D solvers (full-waveform inversion).
 
 :class:`Fwi` binds ``seidart_fwi_*`` of the C ABI: shots with their own
-vertical-force positions and series, a common receiver set and observed
-traces per shot.  :meth:`Fwi.gradient` returns the L2 receiver misfit
+source positions and series, a common receiver set and observed traces per
+shot.  :meth:`Fwi.gradient` returns the L2 receiver misfit
 
-    L = 1/2 sum_shots sum_steps sum_receivers (vx - dx)^2 + (vz - dz)^2
+    L = 1/2 sum_shots sum_steps sum_receivers (u_x - d_x)^2 + (u_z - d_z)^2
 
-of the FP32 solver and dL/d{c11, c13, c33, c55, rho} on the padded grid from
-the hand-written discrete adjoint (csrc/adjoint.cu): FP32 fields, FP64
-gradient accumulation, sqrt(nt) checkpointing with recomputation.
-:class:`Seismic2Misfit` wraps it as a ``torch.autograd.Function``; torch is
-imported only there.  The reference (SeidarT-Backend) has forward models only;
-the forward operator differentiated here is its seismic2 time loop
-(src/fortran/cpmlfdtd.f08:311-576) as computed by the FP32 solver.
+of the FP32 solver (u = vx, vz for seismic2, Ex, Ez for electromag2) and its
+gradient on the padded grid from a hand-written discrete adjoint
+(csrc/adjoint.cu, csrc/adjoint_em.cu): FP32 fields, FP64 gradient
+accumulation, sqrt(nt) checkpointing with recomputation.  seismic2 shots are
+vertical forces and the gradient is dL/d{c11, c13, c33, c55, rho};
+electromag2 shots drive Ez and the gradient is dL/d{e11, e13, e33, s11, s13,
+s33} (relative permittivity and conductivity, as in e11.dat ... s33.dat).
+``seismic2_misfit`` and ``electromag2_misfit`` wrap them as
+``torch.autograd.Function``s; torch is imported only there.  The reference
+(SeidarT-Backend) has forward models only; the forward operators
+differentiated here are its seismic2 and electromag2 time loops
+(src/fortran/cpmlfdtd.f08:311-576, :2519-2748) as computed by the FP32
+solvers.
 """
 from __future__ import annotations
 
@@ -21,11 +27,17 @@ from dataclasses import dataclass, replace
 
 import numpy as np
 
-from ._lib import SEISMIC2, SeidartError, UnstableError, lib, ptr_array
+from ._lib import ELECTROMAG2, SEISMIC2, SeidartError, UnstableError, lib, ptr_array
 from .api import Problem
 
 GRAD_KEYS = ("c11", "c13", "c33", "c55", "rho")
-NSTATE = 17  # vx vz sigmaxx sigmazz sigmaxz + 12 memory arrays
+GRAD_KEYS_EM = ("e11", "e13", "e33", "s11", "s13", "s33")
+NSTATE = 17     # vx vz sigmaxx sigmazz sigmaxz + 12 memory arrays
+NSTATE_EM = 7   # Ex Ez Hy + 4 memory arrays
+
+
+def grad_keys(family: int) -> tuple:
+    return GRAD_KEYS_EM if family == ELECTROMAG2 else GRAD_KEYS
 
 _DECL = False
 
@@ -38,6 +50,7 @@ def _declare():
     vp, i = C.c_void_p, C.c_int
     sig = {
         "seidart_fwi_create": (i, [C.POINTER(vp), vp, vp, i, vp, i, vp, vp, vp, i, vp, vp, i]),
+        "seidart_fwi_create_family": (i, [C.POINTER(vp), i, vp, vp, i, vp, i, vp, vp, vp, i, vp, vp, i]),
         "seidart_fwi_gradient": (i, [vp, vp, vp]),
         "seidart_fwi_model_traces": (i, [vp, vp]),
         "seidart_fwi_forward_step_host": (i, [vp, vp]),
@@ -61,18 +74,20 @@ def _check(rc: int) -> None:
 
 @dataclass
 class Shot:
-    """Vertical-force source of one shot: interior indices as in Problem."""
+    """Source of one shot (seismic2: vertical force; electromag2: Ez
+    source): interior indices as in Problem, series of time_steps samples."""
     xind: int
     zind: int
     srcz: np.ndarray
 
 
 class Fwi:
-    """Misfit and gradient of one 2D elastic model over several shots."""
+    """Misfit and gradient of one 2D model (seismic2 or electromag2) over
+    several shots."""
 
     def __init__(self, problem: Problem, shots: list[Shot], observed=None, checkpoint_every: int = 0):
-        if problem.family != SEISMIC2:
-            raise ValueError("the adjoint covers the 2D elastic solver (seismic2)")
+        if problem.family not in (SEISMIC2, ELECTROMAG2):
+            raise ValueError("the adjoint covers the 2D solvers seismic2 and electromag2")
         _declare()
         self.problem = problem
         self.shots = shots
@@ -94,21 +109,24 @@ class Fwi:
         xs = np.array([s.xind for s in shots], dtype=np.int32)
         zs = np.array([s.zind for s in shots], dtype=np.int32)
         h = C.c_void_p()
-        _check(lib().seidart_fwi_create(
-            C.byref(h), C.byref(problem.domain()), C.byref(problem.source()), problem.density_code(),
+        self.keys = grad_keys(problem.family)
+        self.nstate = NSTATE_EM if problem.family == ELECTROMAG2 else NSTATE
+        _check(lib().seidart_fwi_create_family(
+            C.byref(h), problem.family, C.byref(problem.domain()), C.byref(problem.source()), problem.density_code(),
             ptr_array(self._model), self.nshots, xs.ctypes.data, zs.ctypes.data, ptr_array(self._src),
             self.nrec, rec.ctypes.data if self.nrec else None, ptr_array(self._obs), int(checkpoint_every)))
         self.handle = h
 
     # ---------------------------------------------------------------- compute
     def gradient(self) -> tuple[float, dict]:
-        """(L, {c11, c13, c33, c55, rho: dL/dm on the padded (nx, nz) grid})."""
+        """(L, {key: dL/dm on the padded (nx, nz) grid}) with the keys of
+        :func:`grad_keys` for the problem's family."""
         loss = C.c_double()
         n = self.problem.ncell
-        g = np.zeros(5 * n, dtype=np.float64)
+        g = np.zeros(len(self.keys) * n, dtype=np.float64)
         _check(lib().seidart_fwi_gradient(self.handle, C.byref(loss), g.ctypes.data))
         shape = self.problem.shape
-        return loss.value, {k: g[q * n:(q + 1) * n].reshape(shape, order="F") for q, k in enumerate(GRAD_KEYS)}
+        return loss.value, {k: g[q * n:(q + 1) * n].reshape(shape, order="F") for q, k in enumerate(self.keys)}
 
     def loss(self) -> float:
         loss = C.c_double()
@@ -122,7 +140,7 @@ class Fwi:
         return out
 
     def forward_step(self, x: np.ndarray) -> np.ndarray:
-        """One step (source off) of a [17][ncell] FP32 state; returns the new state."""
+        """One step (source off) of an [nstate][ncell] FP32 state; returns the new state."""
         y = np.ascontiguousarray(x, dtype=np.float32).copy()
         _check(lib().seidart_fwi_forward_step_host(self.handle, y.ctypes.data))
         return y
@@ -197,16 +215,45 @@ def _torch_function():
         def backward(ctx, gout):
             return tuple(gout.to(g.dtype) * g for g in ctx.saved_tensors) + (None, None, None, None)
 
-    return Seismic2Misfit
+    class Electromag2Misfit(torch.autograd.Function):
+        """L(e11, e13, e33, s11, s13, s33) of an electromag2 problem with the
+        adjoint gradient as backward (same contract as Seismic2Misfit)."""
+
+        @staticmethod
+        def forward(ctx, e11, e13, e33, s11, s13, s33, problem, shots, observed, checkpoint_every=0):
+            ts = (e11, e13, e33, s11, s13, s33)
+            arrays = {k: t.detach().to("cpu", torch.float64).numpy() for k, t in zip(GRAD_KEYS_EM, ts)}
+            with Fwi(with_model(problem, **arrays), shots, observed, checkpoint_every) as f:
+                loss, grads = f.gradient()
+            ctx.save_for_backward(*[torch.from_numpy(np.ascontiguousarray(grads[k])).to(t.device, t.dtype)
+                                    for k, t in zip(GRAD_KEYS_EM, ts)])
+            return torch.tensor(loss, dtype=torch.float64, device=e11.device)
+
+        @staticmethod
+        def backward(ctx, gout):
+            return tuple(gout.to(g.dtype) * g for g in ctx.saved_tensors) + (None, None, None, None)
+
+    return Seismic2Misfit, Electromag2Misfit
 
 
 _MISFIT = None
 
 
-def seismic2_misfit(c11, c13, c33, c55, rho, problem: Problem, shots: list[Shot], observed, checkpoint_every: int = 0):
-    """Differentiable misfit: ``seismic2_misfit(...).backward()`` fills the
-    ``.grad`` of the five model tensors."""
+def _functions():
     global _MISFIT
     if _MISFIT is None:
         _MISFIT = _torch_function()
-    return _MISFIT.apply(c11, c13, c33, c55, rho, problem, shots, observed, checkpoint_every)
+    return _MISFIT
+
+
+def seismic2_misfit(c11, c13, c33, c55, rho, problem: Problem, shots: list[Shot], observed, checkpoint_every: int = 0):
+    """Differentiable misfit: ``seismic2_misfit(...).backward()`` fills the
+    ``.grad`` of the five model tensors."""
+    return _functions()[0].apply(c11, c13, c33, c55, rho, problem, shots, observed, checkpoint_every)
+
+
+def electromag2_misfit(e11, e13, e33, s11, s13, s33, problem: Problem, shots: list[Shot], observed,
+                       checkpoint_every: int = 0):
+    """Differentiable electromag2 misfit: ``.backward()`` fills the ``.grad``
+    of the six permittivity and conductivity tensors."""
+    return _functions()[1].apply(e11, e13, e33, s11, s13, s33, problem, shots, observed, checkpoint_every)
