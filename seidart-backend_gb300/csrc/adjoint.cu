@@ -21,7 +21,11 @@
 // Launches: per shot, one CUDA graph recomputes a K-step segment (saving
 // every state) and one walks it backwards; the step numbers come from a
 // device-side segment base, so the same two graphs replay for every segment
-// and a segment costs four host operations.
+// and a segment costs four host operations.  An adjoint step is two grid
+// passes: adj_velocity (receiver residuals, the gather of S^T left by the
+// step after, D^T, V^T) and adj_stress (gather of V^T, S^T).
+// The same driver runs the electromag2 adjoint (adjoint_em.cu) with a
+// 7-array state; the family decides the kernels and the gradient chain.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -65,6 +69,12 @@ struct AdjArgs {
     const int* base;     // device: steps before the segment; this step is n = *base + j
     int j;
     double* gsrc;        // accumulated lambda_vz(src) * f_n
+    // receiver residuals dL/dv_n, added where a cell holds receivers:
+    // rfirst[c] = first receiver at cell c (-1: none), rnext[r] = next one
+    const int* rfirst;
+    const int* rnext;
+    const float* dres;   // [nt][2][nrec], NULL = no residual (test hook)
+    int nrec;
 };
 
 __device__ __forceinline__ bool inN(int i, int k, int nx, int nz) { return k >= 2 && k <= nz - 2 && i >= 1 && i <= nx - 3; }
@@ -78,19 +88,59 @@ __device__ __forceinline__ float at(const float* a, int i, int k, int nx, int nz
 }
 
 // ---------------------------------------------------------------- V^T (and D^T)
+// transposes of forward (F) and backward (B) 4th-order differences, the
+// gather of S^T of the step after this one into vx, vz
+__device__ __forceinline__ void gather_sT(const AdjArgs& A, int i, int k, float& gvx, float& gvz) {
+    const int nx = A.nx, nz = A.nz;
+    const size_t N = A.N;
+    const float hx = A.hx, hz = A.hz;
+    const float* s = A.scr + 4 * N;
+    const float *ld1 = s, *ld2 = s + N, *ld3 = s + 2 * N, *ld4 = s + 3 * N;
+    const float *le1 = s + 4 * N, *le2 = s + 5 * N, *le3 = s + 6 * N, *le4 = s + 7 * N;
+    auto FxT = [&](const float* d) {
+        return hx * (27.0f * at(d, i - 1, k, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i - 2, k, nx, nz) +
+                     at(d, i + 1, k, nx, nz));
+    };
+    auto BxT = [&](const float* d) {
+        return hx * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i + 1, k, nx, nz) - at(d, i - 1, k, nx, nz) +
+                     at(d, i + 2, k, nx, nz));
+    };
+    auto FzT = [&](const float* d) {
+        return hz * (27.0f * at(d, i, k - 1, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i, k - 2, nx, nz) +
+                     at(d, i, k + 1, nx, nz));
+    };
+    auto BzT = [&](const float* d) {
+        return hz * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i, k + 1, nx, nz) - at(d, i, k - 1, nx, nz) +
+                     at(d, i, k + 2, nx, nz));
+    };
+    gvx = FxT(ld1) + BzT(ld4) + BxT(le1) + FzT(le4);
+    gvz = BzT(ld2) + FxT(ld3) + FzT(le2) + BxT(le3);
+}
+
+// Starts the adjoint of step n: completes lambda_v(n) (gather of S^T from
+// step n+1, receiver residuals of step n), then D^T and V^T.
 __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
     const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
     const int nx = A.nx, nz = A.nz;
     if (i >= nx || k >= nz) return;
     const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
     float* lam = A.lam;
-    float lvx = lam[c], lvz = lam[N + c];
+    float gvx, gvz;
+    gather_sT(A, i, k, gvx, gvz);
+    float lvx = lam[c] + gvx, lvz = lam[N + c] + gvz;
+    if (A.dres) {
+        const float* res = A.dres + (size_t)(*A.base + A.j - 1) * 2 * A.nrec;
+        for (int r = A.rfirst[c]; r >= 0; r = A.rnext[r]) {
+            lvx += res[r];
+            lvz += res[A.nrec + r];
+        }
+    }
     if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) {  // D^T
         lvx = 0.f;
         lvz = 0.f;
-        lam[c] = 0.f;
-        lam[N + c] = 0.f;
     }
+    lam[c] = lvx;
+    lam[N + c] = lvz;
     if (i == A.isrc && k == A.jsrc && A.srcz) *A.gsrc += (double)lvz * (double)(float)A.srcz[*A.base + A.j - 1];
     const float* xc = A.xc;
     const float *sxx = xc + 2 * N, *szz = xc + 3 * N, *sxz = xc + 4 * N;
@@ -249,45 +299,16 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
     s[4 * N + c] = le1; s[5 * N + c] = le2; s[6 * N + c] = le3; s[7 * N + c] = le4;
 }
 
-// ------------------------------------------------------ gather of S^T into v
-__global__ void __launch_bounds__(BX* BY) adj_gather_v(AdjArgs A) {
+// pending gather of S^T into vx, vz (host test hook only; the sweep leaves
+// it to the next step's adj_velocity)
+__global__ void __launch_bounds__(BX* BY) adj_flush_v(AdjArgs A) {
     const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
-    const int nx = A.nx, nz = A.nz;
-    if (i >= nx || k >= nz) return;
-    const size_t c = (size_t)i + (size_t)nx * k, N = A.N;
-    const float hx = A.hx, hz = A.hz;
-    const float* s = A.scr + 4 * N;
-    const float *ld1 = s, *ld2 = s + N, *ld3 = s + 2 * N, *ld4 = s + 3 * N;
-    const float *le1 = s + 4 * N, *le2 = s + 5 * N, *le3 = s + 6 * N, *le4 = s + 7 * N;
-    // transposes of forward (F) and backward (B) 4th-order differences
-    auto FxT = [&](const float* d) {
-        return hx * (27.0f * at(d, i - 1, k, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i - 2, k, nx, nz) +
-                     at(d, i + 1, k, nx, nz));
-    };
-    auto BxT = [&](const float* d) {
-        return hx * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i + 1, k, nx, nz) - at(d, i - 1, k, nx, nz) +
-                     at(d, i + 2, k, nx, nz));
-    };
-    auto FzT = [&](const float* d) {
-        return hz * (27.0f * at(d, i, k - 1, nx, nz) - 27.0f * at(d, i, k, nx, nz) - at(d, i, k - 2, nx, nz) +
-                     at(d, i, k + 1, nx, nz));
-    };
-    auto BzT = [&](const float* d) {
-        return hz * (27.0f * at(d, i, k, nx, nz) - 27.0f * at(d, i, k + 1, nx, nz) - at(d, i, k - 1, nx, nz) +
-                     at(d, i, k + 2, nx, nz));
-    };
-    A.lam[c] += FxT(ld1) + BzT(ld4) + BxT(le1) + FzT(le4);
-    A.lam[N + c] += BzT(ld2) + FxT(ld3) + FzT(le2) + BxT(le3);
-}
-
-// dL/dv_n at the receivers: residual of step n = *base + j added to the
-// adjoint velocity
-__global__ void adj_inject(float* lam, size_t N, const int* rec, int nrec, const float* dres, const int* base, int j) {
-    const float* resid = dres + (size_t)(*base + j - 1) * 2 * nrec;
-    for (int r = threadIdx.x + blockIdx.x * blockDim.x; r < nrec; r += blockDim.x * gridDim.x) {
-        atomicAdd(lam + rec[r], resid[r]);
-        atomicAdd(lam + N + rec[r], resid[nrec + r]);
-    }
+    if (i >= A.nx || k >= A.nz) return;
+    const size_t c = (size_t)i + (size_t)A.nx * k;
+    float gvx, gvz;
+    gather_sT(A, i, k, gvx, gvz);
+    A.lam[c] += gvx;
+    A.lam[A.N + c] += gvz;
 }
 
 // residual r = traces - observed over all steps; loss += 1/2 sum r^2 (FP64)
@@ -510,6 +531,8 @@ struct SeidartFwi {
     double* dgsrc = nullptr;    // [nshots] sum_n lambda(src) f_n per shot (vz or Ez)
     std::vector<double> srch;   // host copy of the source series
     std::vector<double> em[6];  // electromag2: host eps11 eps13 eps33 sig11 sig13 sig33 (for the chain rule)
+    int* rfirst = nullptr;      // [N] first receiver at each cell, -1 none (device)
+    int* rnext = nullptr;       // [nrec] next receiver at the same cell, -1 none (device)
     double dt = 0.0;
     long long launches = 0;
 };
@@ -542,6 +565,8 @@ AdjArgs adj_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, co
     A.isrc = L.a.isrc; A.jsrc = L.a.jsrc; A.srcz = srcz;
     A.gsrc = f->dgsrc + (L.shot >= 0 ? L.shot : 0);
     A.base = L.dbase; A.j = j;
+    A.rfirst = f->rfirst; A.rnext = f->rnext; A.nrec = f->nrec;
+    A.dres = f->nrec > 0 ? L.dres : nullptr;
     return A;
 }
 
@@ -551,6 +576,8 @@ EmAdjArgs em_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, c
     A.xp = xp; A.xc = xc; A.lam = L.lam; A.scr = L.scr; A.grad = L.grad32; A.N = f->N;
     A.srcz = srcz; A.base = L.dbase; A.j = j;
     A.gsrc = f->dgsrc + (L.shot >= 0 ? L.shot : 0);
+    A.rfirst = f->rfirst; A.rnext = f->rnext; A.nrec = f->nrec;
+    A.dres = f->nrec > 0 ? L.dres : nullptr;
     return A;
 }
 
@@ -564,18 +591,33 @@ double* lane_norms(const SeidartFwi* f, const FwiLane& L) {
     return f->family == SEIDART_ELECTROMAG2 ? L.e.norms : L.a.norms;
 }
 
-// adjoint of step n = *dbase + j (launched on the lane's stream, possibly under capture)
-void adjoint_step(SeidartFwi* f, FwiLane& L, int j, const float* xp, const float* xc, const double* srcz, int nrec) {
-    if (nrec > 0) adj_inject<<<1, 256, 0, L.st>>>(L.lam, f->N, L.rec, nrec, L.dres, L.dbase, j);
+// Adjoint of step n = *dbase + j (launched on the lane's stream, possibly
+// under capture): two grid passes.  The receiver residuals of step n
+// (inject = false: none) are added by the first pass, which also finishes the
+// gather left by step n+1; the gather this step leaves is finished by step
+// n-1 (or by adjoint_flush).
+void adjoint_step(SeidartFwi* f, FwiLane& L, int j, const float* xp, const float* xc, const double* srcz,
+                  bool inject) {
     if (f->family == SEIDART_ELECTROMAG2) {
-        em2_adjoint_step(em_args(f, L, xp, xc, srcz, j), L.st);
+        EmAdjArgs A = em_args(f, L, xp, xc, srcz, j);
+        if (!inject) A.dres = nullptr;
+        em2_adjoint_step(A, L.st);
         return;
     }
     const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
-    const AdjArgs A = adj_args(f, L, xp, xc, srcz, j);
+    AdjArgs A = adj_args(f, L, xp, xc, srcz, j);
+    if (!inject) A.dres = nullptr;
     adj_velocity<<<grd, blk, 0, L.st>>>(A);
     adj_stress<<<grd, blk, 0, L.st>>>(A);
-    adj_gather_v<<<grd, blk, 0, L.st>>>(A);
+}
+
+void adjoint_flush(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc) {
+    if (f->family == SEIDART_ELECTROMAG2) {
+        em2_adjoint_flush(em_args(f, L, xp, xc, nullptr, 1), L.st);
+        return;
+    }
+    const dim3 blk(BX, BY), grd((L.a.nx + BX - 1) / BX, (L.a.nz + BY - 1) / BY);
+    adj_flush_v<<<grd, blk, 0, L.st>>>(adj_args(f, L, xp, xc, nullptr, 1));
 }
 
 void save_state(const SeidartFwi* f, FwiLane& L, float* blk) {
@@ -658,7 +700,7 @@ int capture_segment(SeidartFwi* f, FwiLane& L, int len, bool adjoint, cudaGraphE
         }
     } else {
         for (int j = len; j >= 1; --j)
-            adjoint_step(f, L, j, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, srcz, f->nrec);
+            adjoint_step(f, L, j, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, srcz, true);
         fold_grad<<<4 * 152, 256, 0, L.st>>>(L.grad, L.grad32, 8 * f->N);
     }
     cudaGraph_t g = nullptr;
@@ -705,8 +747,7 @@ int lane_backward_segment(SeidartFwi* f, FwiLane& L, int g) {
     FCUDA(cudaGetLastError());
     FCUDA(cudaGraphLaunch(L.rec_exec[slot], L.st));
     FCUDA(cudaGraphLaunch(L.adj_exec[slot], L.st));
-    const int adj_kernels = f->family == SEIDART_ELECTROMAG2 ? 2 : 3;
-    L.launches += 1 + 2 * len + len * (adj_kernels + (f->nrec > 0 ? 1 : 0)) + 1;
+    L.launches += 1 + 2 * len + 2 * len + 1;
     return SEIDART_OK;
 }
 
@@ -832,7 +873,7 @@ const char* seidart_fwi_last_error(void) { return g_ferr.c_str(); }
 int seidart_fwi_destroy(SeidartFwi* f) {
     if (!f) return SEIDART_OK;
     for (auto& L : f->lanes) free_lane(L);
-    for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dgsrc})
+    for (void* p : {(void*)f->dsrc, (void*)f->dobs, (void*)f->dgsrc, (void*)f->rfirst, (void*)f->rnext})
         if (p) cudaFree(p);
     delete f;
     return SEIDART_OK;
@@ -884,6 +925,26 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
         return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
     }
     cudaMemcpy(f->dsrc, f->srch.data(), sizeof(double) * nshots * f->nt, cudaMemcpyHostToDevice);
+    {   // receiver chains per cell (several receivers may share a cell)
+        std::vector<int> first(f->N, -1), next(nrec > 0 ? nrec : 1, -1);
+        for (int r = nrec - 1; r >= 0; --r) {
+            const int c = rec_cells[r];
+            if (c < 0 || (size_t)c >= f->N) {
+                seidart_fwi_destroy(f);
+                return ferr(SEIDART_ERR_ARG, "receiver cell outside the grid");
+            }
+            next[r] = first[c];
+            first[c] = r;
+        }
+        if (cudaMalloc((void**)&f->rfirst, sizeof(int) * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&f->rnext, sizeof(int) * next.size()) != cudaSuccess) {
+            cudaGetLastError();
+            seidart_fwi_destroy(f);
+            return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
+        }
+        cudaMemcpy(f->rfirst, first.data(), sizeof(int) * f->N, cudaMemcpyHostToDevice);
+        cudaMemcpy(f->rnext, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice);
+    }
     std::vector<float> tmp(nobs);
     for (int sh = 0; sh < nshots && nobs; ++sh) {
         if (!observed || !observed[sh]) {
@@ -1060,9 +1121,9 @@ int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float
     FCUDA(cudaMemcpy(L.lam, lam, bytes, cudaMemcpyHostToDevice));
     FCUDA(cudaMemsetAsync(L.dbase, 0, sizeof(int), L.st));
     FCUDA(cudaMemsetAsync(L.scr, 0, sizeof(float) * 12 * f->N, L.st));
-    adjoint_step(f, L, 1, dp, dc, nullptr, 0);
-    // electromag2 leaves the last gather into Ex, Ez to the next step: do it here
-    if (f->family == SEIDART_ELECTROMAG2) em2_adjoint_flush(em_args(f, L, dp, dc, nullptr, 1), L.st);
+    adjoint_step(f, L, 1, dp, dc, nullptr, false);
+    // the step leaves its last gather to the next step: finish it here
+    adjoint_flush(f, L, dp, dc);
     FCUDA(cudaGetLastError());
     FCUDA(cudaStreamSynchronize(L.st));
     FCUDA(cudaMemcpy(lam, L.lam, bytes, cudaMemcpyDeviceToHost));

@@ -14,7 +14,8 @@
 //   source Ez' += f_n dt / eps33, then the Dirichlet ring on Ex', Ez'
 // (0-based indices; Hy' on the ring rows i = 0, k = 0 is used by this step's
 // E update and read as zero by the next H update).  The adjoint applies the
-// transposes in reverse order.  The scatter of a stencil transpose becomes a
+// transposes in reverse order, starting with the receiver residuals of the
+// step.  The scatter of a stencil transpose becomes a
 // gather over a scratch array: E^T leaves (lambda of rHz, rHx) x 1/dz, 1/dx
 // per cell for H^T to gather, H^T leaves (lambda of rEx, rEz) x 1/dz, 1/dx
 // for the gather into Ex, Ez -- which the next adjoint step's E^T performs
@@ -54,6 +55,13 @@ __global__ void __launch_bounds__(BX* BY) em_adj_e(EmAdjArgs A) {
     const float *q0 = A.scr + 2 * N, *q1 = A.scr + 3 * N;
     float lex = lam[c] + gather_x(q0, c, k, nx);
     float lez = lam[N + c] + gather_z(q1, c, i);
+    if (A.dres) {  // receiver residuals of this step
+        const float* res = A.dres + (size_t)(*A.base + A.j - 1) * 2 * A.nrec;
+        for (int r = A.rfirst[c]; r >= 0; r = A.rnext[r]) {
+            lex += res[r];
+            lez += res[A.nrec + r];
+        }
+    }
     const bool ring = i == 0 || i == nx - 1 || k == 0 || k == nz - 1;
     if (ring) { lex = 0.f; lez = 0.f; }
     if (i == a.isrc && k == a.jsrc && A.srcz) *A.gsrc += (double)lez * (double)(float)A.srcz[*A.base + A.j - 1];

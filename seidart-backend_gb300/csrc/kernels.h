@@ -80,6 +80,10 @@ struct EmAdjArgs {
     const int* base;     // device: steps before the segment; this step is *base + j
     int j;
     double* gsrc;        // accumulated lambda_Ez(src) * f_n
+    const int* rfirst;   // [N] first receiver at a cell (-1: none)
+    const int* rnext;    // [nrec] next receiver at the same cell
+    const float* dres;   // [nt][2][nrec] receiver residuals, NULL = none
+    int nrec;
 };
 struct EmOopArgs {
     E2Args<float> a;
