@@ -312,6 +312,71 @@ def bench_fwi(n: int = 512, nt: int = 3000, nshots: int = 16, ncheck: int = 8) -
             "dtype": "f32 fields, f64 gradient accumulation"}
 
 
+def bench_fwi_em(n: int = 512, nt: int = 3000, nshots: int = 8, ncheck: int = 6) -> dict:
+    """electromag2 misfit gradient (eps, sigma) on the GPR grid of the 2D EM
+    configuration's spacing: 512^2 + 20 CPML, 3000 steps, shots along z = 20
+    driving Ez, 128 receivers at z = 25; observed data from the background
+    plus a Gaussian anomaly (sigma 20 cells, +10% eps11 and eps33, x3
+    conductivity) at (256, 150).  Time against one forward, and central
+    differences (relative perturbation 1e-4, FP64 forward runs of shot 0) at
+    seeded cells where the shot-0 gradient is large."""
+    import seidart_gpu as sg
+    from seidart_gpu import models
+    from seidart_gpu.fwi import Fwi, Shot, with_model
+    p = models.electromag2_blocks(n=n, cpml=20, nt=nt, src=(n // 2, 20), nrec=128, rec_z=25, nblocks=0)
+    shape = p.shape
+    start = with_model(p, e13=np.full(shape, 0.2), s11=np.full(shape, 1e-3), s13=np.full(shape, 1e-4),
+                       s33=np.full(shape, 1.5e-3))
+    x = np.arange(shape[0])[:, None]
+    z = np.arange(shape[1])[None, :]
+    g = np.exp(-((x - (n // 2 + 20)) ** 2 + (z - (150 * n // 512 + 20)) ** 2) / (2 * (20.0 * n / 512) ** 2))
+    true = with_model(start, e11=start.model["e11"] * (1 + 0.1 * g), e33=start.model["e33"] * (1 + 0.1 * g),
+                      s11=start.model["s11"] * (1 + 2 * g), s33=start.model["s33"] * (1 + 2 * g))
+    xs = np.linspace(1, n, nshots + 2)[1:-1].astype(int)
+    shots = [Shot(int(xx), 20, start.src["z"]) for xx in xs]
+    with Fwi(true, shots) as f:
+        obs = list(f.model_traces())
+    with Fwi(start, shots, obs) as f:
+        f.loss()
+        t0 = time.perf_counter()
+        f.loss()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        loss, _ = f.gradient()
+        t_grad = time.perf_counter() - t0
+        launches = f.launches
+    with Fwi(start, shots[:1], obs[:1]) as f:
+        _, gr = f.gradient()
+    p0 = dataclasses.replace(start, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+
+    def loss64(q):
+        tr = sg.run(q, sg.FP64)["traces"]
+        return 0.5 * float(np.sum((tr - obs[0]) ** 2))
+
+    rng = np.random.default_rng(8)
+    errs = []
+    keys = ["e11", "e33", "s11", "s33", "e13", "s13"]
+    for q in range(ncheck):
+        key = keys[q % len(keys)]
+        a = np.abs(gr[key])
+        strong = np.argwhere(a >= 0.2 * a.max())
+        cell = tuple(strong[rng.integers(len(strong))])
+        base = start.model[key]
+        h = 1e-4 * abs(base[cell])
+        plus, minus = base.copy(order="F"), base.copy(order="F")
+        plus[cell] += h
+        minus[cell] -= h
+        fd = (loss64(with_model(p0, **{key: plus})) - loss64(with_model(p0, **{key: minus}))) / (2 * h)
+        errs.append({"param": key, "cell": [int(c) for c in cell], "adjoint": float(gr[key][cell]), "fd": fd,
+                     "rel_err": abs(float(gr[key][cell]) - fd) / abs(fd)})
+    return {"gradients_per_s": 1.0 / t_grad, "gradient_s": t_grad, "forward_s": t_fwd,
+            "cost_vs_forward": t_grad / t_fwd, "loss": loss, "shots": nshots, "grid": [start.nx, start.nz],
+            "steps": nt, "gpu_launches": launches,
+            "fd_check": {"max_rel_err": max(e["rel_err"] for e in errs), "cells": errs,
+                         "perturbation": "relative 1e-4, central, FP64 forward (shot 0)"},
+            "dtype": "f32 fields, f64 gradient accumulation"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,6 +518,7 @@ def main():
         extra["batched"] = bench_batch()
     if not args.no_fwi and rank == 0:
         extra["fwi"] = bench_fwi()
+        extra["fwi_em"] = bench_fwi_em()
 
     if rank == 0:
         line = {

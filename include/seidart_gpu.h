@@ -217,14 +217,23 @@ const char* seidart_last_error(void);
  * src/fortran/seidartio.f08:161-292), run all time steps and write the
  * per-step snapshots Vx|Vy|Vz|Ex|Ey|Ez.<it:06d>.<xind>[.<yind>].<zind>.dat
  * (float32 records if single_output, else float64; seidartio.f08:366-426)
- * and, for 3D, velocity_norm.dat / stress_norm.dat.  source_type "ac" loads
- * the force components, any other the stress components (seismic); "pw"
- * (plane wave) returns SEIDART_ERR_UNSUPPORTED.
- * Replaces: seismic2/25/3, electromag2/25 in src/fortran/cpmlfdtd.f08. */
+ * and, for 3D, velocity_norm.dat / stress_norm.dat.  The 2.5D solvers write
+ * zstd blocks instead unless FDTD_LEGACY_OUTPUT=TRUE: S25.|EM25.<first:06d>-
+ * <last:06d>.<xind>.<yind>.<zind>.blk.zst, float32 (x, 1, z, component, step)
+ * of the real parts with the CPML stripped, FDTD_STEPS_PER_BLOCK steps per
+ * file (default about 2 GiB, at most 500; seidartio.f08:462-734).
+ * source_type "ac" loads the force components, any other the stress
+ * components (seismic); "pw" (plane wave) returns SEIDART_ERR_UNSUPPORTED.
+ * Replaces: seismic2/25/3, electromag2/25/3 in src/fortran/cpmlfdtd.f08. */
 int seidart_run_files(const char* dir, int family, int precision, const SeidartDomain* dom,
                       const SeidartSource* src, int density_code, const char* source_type,
                       int single_output, int write_snapshots);
 const char* seidart_io_last_error(void);
+/* Write one zstd frame holding `bytes` of data: compressed at level 3 by the
+ * system libzstd when it can be loaded (as write_zstd_block does,
+ * seidartio.f08:528-585), else as raw (stored) zstd blocks; SEIDART_ZSTD_RAW=1
+ * forces raw blocks.  The 2.5D block writer uses it. */
+int seidart_zstd_write(const char* path, const void* data, size_t bytes);
 
 /* Legacy entry points with the argument layout of legacy/cpmlfdtd_wrapper.c:7-16
  * (padded nx[,ny],nz; spacings; PML thickness; src = interior source indices;

@@ -14,18 +14,34 @@
 // the ring is drained to pinned host memory on a second stream and a writer
 // thread writes the files, so disk I/O overlaps the following steps.
 //
+// The 2.5D solvers write zstd blocks by default (src/fortran/seidartio.f08:
+// 462-734, cpmlfdtd.f08:1295-1318, :3313-3336): the real parts of the three
+// output components, CPML stripped, float32, laid out (x, 1, z, component,
+// step) for up to steps_per_block steps per file
+// `S25.<first:06d>-<last:06d>.<xind>.<yind>.<zind>.blk.zst` (EM25. for
+// electromag25); FDTD_LEGACY_OUTPUT=TRUE selects the per-step files instead
+// and FDTD_STEPS_PER_BLOCK overrides the block length (default: about 2 GiB
+// of float32 per block, at most 500 steps).  A device kernel gathers each
+// step into a device block buffer; a full block is copied to pinned host
+// memory in one transfer and compressed and written by the writer thread
+// while the next block fills (two buffers).  Frames are compressed at level
+// 3 by the system libzstd when it can be loaded, else written as a valid
+// zstd frame of raw (stored) blocks, which every zstd decoder reads.
+//
 // Entry points: seidart_run_files (directory + Domain/Source, the body of
 // the reference's seismic2/25/3 and electromag2/25 subroutines), the legacy
 // C names seismic2_ ... electromag25c_ (legacy/cpmlfdtd_wrapper.c:7-16), and
 // seidart_cli_main, the `seidartfdtd <input.json> [seismic=..]
 // [density_method=..]` driver of src/fortran/main.f08.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 #include <errno.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <condition_variable>
 #include <cstdint>
 #include <deque>
@@ -170,6 +186,82 @@ struct JsonReader {
 std::string trim(const std::string& s) {
     size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
     return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+// ------------------------------------------------------------ zstd frames
+// libzstd's one-shot API, loaded at run time when present
+struct ZstdLib {
+    bool tried = false;
+    void* h = nullptr;
+    size_t (*bound)(size_t) = nullptr;
+    size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
+    unsigned (*is_error)(size_t) = nullptr;
+    bool load() {
+        if (tried) return h != nullptr;
+        tried = true;
+        const char* raw = getenv("SEIDART_ZSTD_RAW");
+        if (raw && *raw == '1') return false;
+        for (const char* nm : {"libzstd.so.1", "libzstd.so"}) {
+            h = dlopen(nm, RTLD_NOW | RTLD_LOCAL);
+            if (h) break;
+        }
+        if (!h) return false;
+        bound = (size_t(*)(size_t))dlsym(h, "ZSTD_compressBound");
+        compress = (size_t(*)(void*, size_t, const void*, size_t, int))dlsym(h, "ZSTD_compress");
+        is_error = (unsigned (*)(size_t))dlsym(h, "ZSTD_isError");
+        if (!bound || !compress || !is_error) {
+            dlclose(h);
+            h = nullptr;
+        }
+        return h != nullptr;
+    }
+};
+ZstdLib g_zstd;
+std::mutex g_zstd_mu;
+
+// One zstd frame (RFC 8878) holding `bytes` of data in raw blocks: magic,
+// frame header (8-byte content size, 128 KiB window), then blocks of at most
+// 128 KiB, each with a 3-byte header (last-block bit, type 0 = raw, size).
+void raw_zstd_frame(const char* data, size_t bytes, std::vector<char>& out) {
+    const size_t B = 128 * 1024;
+    out.clear();
+    out.reserve(bytes + 14 + 3 * (bytes / B + 1));
+    const uint8_t head[6] = {0x28, 0xB5, 0x2F, 0xFD, 0xC0, 0x38};  // magic; FCS 8 bytes; window 2^17
+    out.insert(out.end(), head, head + 6);
+    for (int b = 0; b < 8; ++b) out.push_back((char)((uint64_t)bytes >> (8 * b) & 0xFF));
+    size_t off = 0;
+    do {
+        const size_t n = bytes - off < B ? bytes - off : B;
+        const uint32_t last = off + n == bytes ? 1u : 0u;
+        const uint32_t hdr = last | (0u << 1) | ((uint32_t)n << 3);
+        out.push_back((char)(hdr & 0xFF));
+        out.push_back((char)(hdr >> 8 & 0xFF));
+        out.push_back((char)(hdr >> 16 & 0xFF));
+        out.insert(out.end(), data + off, data + off + n);
+        off += n;
+    } while (off < bytes);
+}
+
+bool write_zst(const std::string& path, const void* data, size_t bytes, std::string& why) {
+    std::vector<char> buf;
+    bool lib;
+    {
+        std::lock_guard<std::mutex> lk(g_zstd_mu);
+        lib = g_zstd.load();
+    }
+    if (lib) {
+        buf.resize(g_zstd.bound(bytes));
+        const size_t n = g_zstd.compress(buf.data(), buf.size(), data, bytes, 3);
+        if (g_zstd.is_error(n)) { why = path + ": zstd compression failed"; return false; }
+        buf.resize(n);
+    } else {
+        raw_zstd_frame((const char*)data, bytes, buf);
+    }
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) { why = "cannot open " + path + ": " + strerror(errno); return false; }
+    const bool ok = fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    if (fclose(f) != 0 || !ok) { why = "write failed: " + path; return false; }
+    return true;
 }
 
 // -------------------------------------------------------------- snapshots
@@ -320,6 +412,135 @@ struct SnapshotPipe {
     }
 };
 
+// Real parts of three 2D fields, CPML stripped, as float32 slabs
+// out[c][z][x] (one step of the (x, 1, z, component, step) block).
+template <typename T>
+__global__ void block_gather(const T* __restrict__ f0, const T* __restrict__ f1, const T* __restrict__ f2,
+                             float* __restrict__ out, int nx, int cpml, int onx, int onz, int stride) {
+    const size_t slab = (size_t)onx * onz;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < 3 * slab; q += (size_t)gridDim.x * blockDim.x) {
+        const int c = (int)(q / slab);
+        const size_t r = q - (size_t)c * slab;
+        const int x = (int)(r % onx), z = (int)(r / onx);
+        const size_t src = ((size_t)(x + cpml) + (size_t)nx * (z + cpml)) * stride;
+        const T* f = c == 0 ? f0 : (c == 1 ? f1 : f2);
+        out[q] = (float)f[src];
+    }
+}
+
+// zstd block output of the 2.5D solvers (see the file comment)
+struct BlockPipe {
+    SeidartSolver* s = nullptr;
+    std::vector<int> slots;
+    std::string prefix;            // "S25." or "EM25." (with the directory)
+    int nx = 0, nz = 0, cpml = 0, onx = 0, onz = 0, spb = 1, nt = 0;
+    int xind = 0, yind = 0, zind = 0;
+    size_t slab = 0;               // onx * onz
+    cudaStream_t comp = nullptr, copy = nullptr;
+    float* dblk[2] = {nullptr, nullptr};
+    float* hblk[2] = {nullptr, nullptr};
+    cudaEvent_t full[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    bool busy[2] = {false, false};
+    int cur = 0, in_block = 0, block_count = 0;
+    WriterThread writer;
+    std::string why;
+
+    static int steps_per_block(int onx, int onz) {
+        const char* e = getenv("FDTD_STEPS_PER_BLOCK");
+        if (e && *e) return std::max(1, atoi(e));
+        const double per = (double)onx * onz * 3 * 4;
+        int n = std::max(1, (int)(2147483648.0 / per));
+        return n > 500 ? 500 : n;
+    }
+    int init(SeidartSolver* solver, const std::vector<int>& sl, const std::string& pfx, const SeidartDomain* dom,
+             const SeidartSource* src) {
+        s = solver; slots = sl; prefix = pfx;
+        nx = dom->nx; nz = dom->nz; cpml = dom->cpml; nt = src->time_steps;
+        xind = src->xind; yind = src->yind; zind = src->zind;
+        onx = nx - 2 * cpml; onz = nz - 2 * cpml;
+        if (cpml < 0 || onx < 1 || onz < 1) return io_err(SEIDART_ERR_ARG, "cpml removes the entire zstd block output domain");
+        slab = (size_t)onx * onz;
+        spb = std::min(steps_per_block(onx, onz), std::max(nt, 1));
+        void* dev; int cplx, f32; void* st; size_t n;
+        if (seidart_solver_snapshot_source(s, slots[0], &dev, &cplx, &f32, &n, &st) != SEIDART_OK)
+            return io_err(SEIDART_ERR_ARG, "block output set-up failed");
+        comp = (cudaStream_t)st;
+        if (cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking) != cudaSuccess) return io_err(SEIDART_ERR_CUDA, "stream");
+        const size_t bytes = 3 * slab * spb * sizeof(float);
+        for (int b = 0; b < 2; ++b)
+            if (cudaMalloc((void**)&dblk[b], bytes) != cudaSuccess || cudaMallocHost((void**)&hblk[b], bytes) != cudaSuccess ||
+                cudaEventCreateWithFlags(&full[b], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming) != cudaSuccess)
+                return io_err(SEIDART_ERR_NOMEM, "zstd block buffer allocation failed");
+        return SEIDART_OK;
+    }
+    std::string block_name() const {
+        const int ii = (block_count - 1) * spb + 1, jj = std::min(block_count * spb, nt);
+        char name[160];
+        snprintf(name, sizeof name, "%06d-%06d.%d.%d.%d.blk.zst", ii, jj, xind, yind, zind);
+        return prefix + name;
+    }
+    // hand the current block to the copy stream and the writer
+    void flush() {
+        if (in_block == 0) return;
+        const int b = cur;
+        const size_t bytes = 3 * slab * (size_t)in_block * sizeof(float);
+        cudaEventRecord(full[b], comp);
+        cudaStreamWaitEvent(copy, full[b], 0);
+        cudaMemcpyAsync(hblk[b], dblk[b], bytes, cudaMemcpyDeviceToHost, copy);
+        cudaEventRecord(copied[b], copy);
+        busy[b] = true;
+        const std::string path = block_name();
+        cudaEvent_t ev = copied[b];
+        const char* host = (const char*)hblk[b];
+        writer.push([this, ev, path, host, bytes]() {
+            if (cudaEventSynchronize(ev) != cudaSuccess) { why = "block copy failed"; return false; }
+            std::string w;
+            if (!write_zst(path, host, bytes, w)) { why = w; return false; }
+            return true;
+        });
+        cur ^= 1;
+        in_block = 0;
+    }
+    int capture(int it) {
+        (void)it;
+        if (in_block == 0) {
+            ++block_count;
+            if (busy[cur]) {  // the buffer's previous block must be written out first
+                writer.drain();
+                busy[cur] = false;
+            }
+        }
+        void* dev[3]; int cplx = 0, f32 = 0; void* st; size_t n;
+        for (int c = 0; c < 3; ++c) seidart_solver_snapshot_source(s, slots[c], &dev[c], &cplx, &f32, &n, &st);
+        float* out = dblk[cur] + 3 * slab * (size_t)in_block;
+        const int stride = cplx ? 2 : 1;
+        if (f32) block_gather<float><<<4 * 152, 256, 0, comp>>>((const float*)dev[0], (const float*)dev[1], (const float*)dev[2], out, nx, cpml, onx, onz, stride);
+        else block_gather<double><<<4 * 152, 256, 0, comp>>>((const double*)dev[0], (const double*)dev[1], (const double*)dev[2], out, nx, cpml, onx, onz, stride);
+        if (cudaGetLastError() != cudaSuccess) return io_err(SEIDART_ERR_CUDA, "block gather launch failed");
+        if (++in_block == spb) flush();
+        return SEIDART_OK;
+    }
+    int finish() {
+        flush();
+        if (copy) cudaStreamSynchronize(copy);
+        writer.drain();
+        if (writer.failed) return io_err(SEIDART_ERR_IO, why.empty() ? "zstd block write failed" : why);
+        return SEIDART_OK;
+    }
+    ~BlockPipe() {
+        if (copy) cudaStreamSynchronize(copy);
+        writer.drain();
+        for (int b = 0; b < 2; ++b) {
+            if (dblk[b]) cudaFree(dblk[b]);
+            if (hblk[b]) cudaFreeHost(hblk[b]);
+            if (full[b]) cudaEventDestroy(full[b]);
+            if (copied[b]) cudaEventDestroy(copied[b]);
+        }
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+
 // ------------------------------------------------------------ input files
 struct Inputs {
     std::vector<std::vector<double>> model, src, fields;
@@ -349,6 +570,14 @@ bool load_grid(const std::string& dir, const std::string& name, size_t n, std::v
 extern "C" {
 
 const char* seidart_io_last_error(void) { return g_io_err.c_str(); }
+
+// one zstd frame of `bytes` (libzstd level 3 when it loads, else raw blocks)
+int seidart_zstd_write(const char* path, const void* data, size_t bytes) {
+    if (!path || (!data && bytes)) return io_err(SEIDART_ERR_ARG, "NULL argument");
+    std::string why;
+    if (!write_zst(path, data, bytes, why)) return io_err(SEIDART_ERR_IO, why);
+    return SEIDART_OK;
+}
 
 // one Fortran record (used by the material pre-pass writers); not part of the ABI
 int seidart_internal_write_record(const char* path, const void* data, size_t bytes) {
@@ -461,22 +690,34 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
     if (is3) snprintf(suffix, sizeof suffix, ".%d.%d.%d.dat", src->xind, src->yind, src->zind);
     else snprintf(suffix, sizeof suffix, ".%d.%d.dat", src->xind, src->zind);
     {
+        // 2.5D: zstd blocks unless FDTD_LEGACY_OUTPUT=TRUE (seidartio.f08:685-735)
+        const char* legacy_env = getenv("FDTD_LEGACY_OUTPUT");
+        const bool blocks = write_snapshots && (family == SEIDART_SEISMIC25 || family == SEIDART_ELECTROMAG25) &&
+                            !(legacy_env && strcmp(legacy_env, "TRUE") == 0);
+        const bool per_step = write_snapshots && !blocks;
+        const std::string dirpfx = dir == "." ? std::string() : dir + "/";
         SnapshotPipe pipe;
-        if (write_snapshots) {
+        BlockPipe bpipe;
+        if (per_step) {
             // output paths are relative to the working directory like the reference
             std::string sfx = suffix;
-            std::string dirpfx = dir == "." ? std::string() : dir + "/";
             for (auto& c : out_chans) c = dirpfx + c;
             rc = pipe.init(s, out_slots, out_chans, single_output != 0, sfx);
             if (rc != SEIDART_OK) { seidart_solver_destroy(s); return rc; }
         }
+        if (blocks) {
+            rc = bpipe.init(s, out_slots, dirpfx + (family == SEIDART_SEISMIC25 ? "S25." : "EM25."), dom, src);
+            if (rc != SEIDART_OK) { seidart_solver_destroy(s); return rc; }
+        }
         for (int it = 1; it <= nt && rc == SEIDART_OK; ++it) {
             rc = seidart_solver_step(s, 1);
-            if (rc == SEIDART_OK && write_snapshots) rc = pipe.capture(it);
+            if (rc == SEIDART_OK && per_step) rc = pipe.capture(it);
+            if (rc == SEIDART_OK && blocks) rc = bpipe.capture(it);
             // check the blow-up norm every 64 steps (the reference checks every step and stops)
             if (rc == SEIDART_OK && (it % 64 == 0 || it == nt)) rc = seidart_solver_sync(s);
         }
-        const int frc = write_snapshots ? pipe.finish() : SEIDART_OK;
+        int frc = per_step ? pipe.finish() : SEIDART_OK;
+        if (blocks && frc == SEIDART_OK) frc = bpipe.finish();
         if (rc == SEIDART_OK) rc = frc;
     }
     if (rc == SEIDART_OK && family == SEIDART_SEISMIC3) {
@@ -500,8 +741,9 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
 // number of steps, single-precision output flag.  Inputs come from the
 // working directory.  The legacy layout has no time step: it is derived from
 // the model with the legacy rules, dt = min(h)/sqrt(3 max(c11/rho, c33/rho))
-// for the elastic solvers (legacy/cpmlfdtd_cbindings.f95:867-868) and
-// dt = min(h)/(2 c/sqrt(min eps)) for the EM solvers.
+// for the 2D elastic solver (legacy/cpmlfdtd_cbindings.f95:867-868),
+// 0.7 min(h)/sqrt(3 max(c11/rho, c22/rho, c33/rho)) for the 3D one (:1227-1228)
+// and dt = min(h)/(2 c/sqrt(min eps)) for the EM solvers (:2302).
 static int legacy_dt(const std::string& dir, int family, size_t N, double hmin, double* dt) {
     std::string why;
     std::vector<double> a, b, r;
@@ -512,6 +754,14 @@ static int legacy_dt(const std::string& dir, int family, size_t N, double hmin, 
         double m = 0.0;
         for (size_t q = 0; q < N; ++q) m = fmax(m, fmax(a[q] / r[q], b[q] / r[q]));
         *dt = hmin / sqrt(3.0 * m);
+    } else if (family == SEIDART_SEISMIC3) {
+        std::vector<double> c22;
+        if (!load_grid(dir, "c11.dat", N, a, why) || !load_grid(dir, "c22.dat", N, c22, why) ||
+            !load_grid(dir, "c33.dat", N, b, why) || !load_grid(dir, "rho.dat", N, r, why))
+            return io_err(SEIDART_ERR_IO, why);
+        double m = 0.0;
+        for (size_t q = 0; q < N; ++q) m = fmax(m, fmax(a[q] / r[q], fmax(c22[q] / r[q], b[q] / r[q])));
+        *dt = 0.7 * hmin / sqrt(3.0 * m);
     } else {
         const char* names[3] = {"e11.dat", "e22.dat", "e33.dat"};
         double emin = 1e300;
@@ -529,12 +779,12 @@ static int legacy_run(int family, int nx, int ny, int nz, double dx, double dy, 
                       int nstep, int single_output) {
     if (!src) return io_err(SEIDART_ERR_ARG, "src is NULL");
     SeidartDomain d{};
-    d.dim = family == SEIDART_SEISMIC3 ? 3.0 : (family == SEIDART_SEISMIC25 || family == SEIDART_ELECTROMAG25 ? 2.5 : 2.0);
-    d.nx = nx; d.ny = family == SEIDART_SEISMIC3 ? ny : 1; d.nz = nz;
+    const bool three = family == SEIDART_SEISMIC3 || family == SEIDART_ELECTROMAG3;
+    d.dim = three ? 3.0 : (family == SEIDART_SEISMIC25 || family == SEIDART_ELECTROMAG25 ? 2.5 : 2.0);
+    d.nx = nx; d.ny = three ? ny : 1; d.nz = nz;
     d.dx = dx; d.dy = dy; d.dz = dz; d.cpml = npml;
     SeidartSource s{};
     s.time_steps = nstep;
-    const bool three = family == SEIDART_SEISMIC3;
     s.xind = src[0];
     s.yind = three ? src[1] : 0;
     s.zind = three ? src[2] : src[1];
@@ -551,23 +801,21 @@ static int legacy_run(int family, int nx, int ny, int nz, double dx, double dy, 
 void seismic2_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output) {
     legacy_run(SEIDART_SEISMIC2, nx, 1, nz, dx, 1.0, dz, npoints_pml, src, nstep, single_output);
 }
+// The binding's seismic25 / electromag25 are 3D solvers on (nx, ny, nz) with
+// 3D snapshots (legacy/cpmlfdtd_cbindings.f95:1088-1641, :2184-2640): they
+// run the 3D loops, src = interior (xind, yind, zind).
 void seismic25_(int nx, int ny, int nz, double dx, double dy, double dz, int npoints_pml, int* src, int nstep,
                 int single_output) {
-    (void)ny; (void)dy;
-    int s2[2] = {src ? src[0] : 0, src ? src[2] : 0};
-    legacy_run(SEIDART_SEISMIC25, nx, 1, nz, dx, 1.0, dz, npoints_pml, src ? s2 : nullptr, nstep, single_output);
+    legacy_run(SEIDART_SEISMIC3, nx, ny, nz, dx, dy, dz, npoints_pml, src, nstep, single_output);
 }
 void electromag2_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output) {
     legacy_run(SEIDART_ELECTROMAG2, nx, 1, nz, dx, 1.0, dz, npoints_pml, src, nstep, single_output);
 }
 void electromag25_(int nx, int ny, int nz, double dx, double dy, double dz, int npoints_pml, int* src, int nstep,
                    int single_output) {
-    (void)ny; (void)dy;
-    int s2[2] = {src ? src[0] : 0, src ? src[2] : 0};
-    legacy_run(SEIDART_ELECTROMAG25, nx, 1, nz, dx, 1.0, dz, npoints_pml, src ? s2 : nullptr, nstep, single_output);
+    legacy_run(SEIDART_ELECTROMAG3, nx, ny, nz, dx, dy, dz, npoints_pml, src, nstep, single_output);
 }
-// The complex-valued legacy variants map onto the same solvers: the current
-// reference's 2.5D EM solver already carries complex fields.
+// The complex-valued legacy variants map onto the same (real) solvers.
 void electromag2c_(int nx, int nz, double dx, double dz, int npoints_pml, int* src, int nstep, int single_output) {
     electromag2_(nx, nz, dx, dz, npoints_pml, src, nstep, single_output);
 }

@@ -86,7 +86,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             list(ex.map(run, todo))
     objs = [str(obj) for _, obj in jobs]
     if force or todo or not LIB.exists() or _stale(LIB, [Path(o) for o in objs]):
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", str(LIB), *objs]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", str(LIB), *objs, "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

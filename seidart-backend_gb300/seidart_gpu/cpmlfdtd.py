@@ -3,11 +3,14 @@
 Mirrors ``seidart.fortran.cpmlfdtd`` (legacy/__init__.py:2-12,
 legacy/cpmlfdtd_wrapper.py:13-43, legacy/cpmlfdtd_wrapper.c:139-375): the
 solver functions take the argument layout of the CPython wrapper
-``(nx, nz, dx, dz, src, npoints_pml, nstep[, single_output])`` (2.5D:
-``(nx, ny, nz, dx, dy, dz, src, npoints_pml, nstep[, single_output])``),
-read the .dat inputs from the working directory and write the per-step
-snapshot files there, like the reference.  Each call goes through ctypes to
-the C entry points seismic2_ ... electromag25c_ of libseidart_gpu.so.
+``(nx, nz, dx, dz, src, npoints_pml, nstep[, single_output])`` (seismic25,
+electromag25[c]: ``(nx, ny, nz, dx, dy, dz, src, npoints_pml, nstep[,
+single_output])``), read the .dat inputs from the working directory and
+write the per-step snapshot files there, like the reference.  The binding's
+seismic25 and electromag25 are 3D solvers with 3D snapshots
+(legacy/cpmlfdtd_cbindings.f95:1088, :2184); they run the 3D loops
+(seismic3, electromag3).  Each call goes through ctypes to the C entry
+points seismic2_ ... electromag25c_ of libseidart_gpu.so.
 
 nx, nz (ny) are the padded grid sizes; ``src`` holds the interior source
 indices (x, z) or (x, y, z).  Errors raise SeidartError (the reference's

@@ -57,6 +57,80 @@ def read_record(path, dtype=np.float64, shape=None) -> np.ndarray:
     return a
 
 
+def _zstd_lib():
+    import ctypes
+    import ctypes.util
+    for name in ("libzstd.so.1", ctypes.util.find_library("zstd")):
+        if not name:
+            continue
+        try:
+            L = ctypes.CDLL(name)
+        except OSError:
+            continue
+        L.ZSTD_getFrameContentSize.restype = ctypes.c_ulonglong
+        L.ZSTD_getFrameContentSize.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+        L.ZSTD_decompress.restype = ctypes.c_size_t
+        L.ZSTD_decompress.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]
+        L.ZSTD_isError.restype = ctypes.c_uint
+        L.ZSTD_isError.argtypes = [ctypes.c_size_t]
+        return L
+    return None
+
+
+def _raw_frame(buf: bytes) -> bytes:
+    """Content of a zstd frame made of raw blocks only (RFC 8878: magic,
+    frame header, 3-byte block headers); other block types need libzstd."""
+    if buf[:4] != b"\x28\xb5\x2f\xfd":
+        raise ValueError("not a zstd frame")
+    fhd = buf[4]
+    single = (fhd >> 5) & 1
+    fcs_size = {0: 1 if single else 0, 1: 2, 2: 4, 3: 8}[fhd >> 6]
+    did_size = {0: 0, 1: 1, 2: 2, 3: 4}[fhd & 3]
+    pos = 5 + (0 if single else 1) + did_size + fcs_size
+    out = bytearray()
+    while True:
+        hdr = buf[pos] | (buf[pos + 1] << 8) | (buf[pos + 2] << 16)
+        pos += 3
+        last, btype, size = hdr & 1, (hdr >> 1) & 3, hdr >> 3
+        if btype != 0:
+            raise ValueError("compressed zstd block: libzstd is needed to read it")
+        out += buf[pos:pos + size]
+        pos += size
+        if last:
+            return bytes(out)
+
+
+def read_zstd(path) -> bytes:
+    """Decompressed content of a one-frame .zst file (libzstd when it loads,
+    else frames of raw blocks)."""
+    import ctypes
+    buf = Path(path).read_bytes()
+    L = _zstd_lib()
+    if L is None:
+        return _raw_frame(buf)
+    n = L.ZSTD_getFrameContentSize(buf, len(buf))
+    if n >= (1 << 64) - 2:
+        raise ValueError(f"{path}: zstd frame without a content size")
+    out = ctypes.create_string_buffer(max(int(n), 1))
+    got = L.ZSTD_decompress(out, int(n), buf, len(buf))
+    if L.ZSTD_isError(got):
+        raise ValueError(f"{path}: zstd decompression failed")
+    return out.raw[:got]
+
+
+def block_name(prefix: str, first: int, last: int, xind: int, yind: int, zind: int) -> str:
+    """2.5D zstd block file name (src/fortran/cpmlfdtd.f08:1300-1302, :3318-3320)."""
+    return f"{prefix}.{first:06d}-{last:06d}.{xind}.{yind}.{zind}.blk.zst"
+
+
+def read_block(path, onx: int, onz: int) -> np.ndarray:
+    """One 2.5D output block as float32 (onx, 1, onz, 3, steps), Fortran order
+    (seidartio.f08:604-677)."""
+    a = np.frombuffer(read_zstd(path), dtype=np.float32)
+    steps = a.size // (onx * onz * 3)
+    return a.reshape((onx, 1, onz, 3, steps), order="F")
+
+
 def snapshot_name(channel: str, it: int, xind: int, zind: int, yind: int | None = None) -> str:
     """write_image2 / write_image3 file names (src/fortran/seidartio.f08:380, :414)."""
     if yind is None:
