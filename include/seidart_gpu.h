@@ -73,6 +73,23 @@ typedef struct SeidartSource {
     double ky;             /* 2.5D wavenumber (reference reads env KY) */
 } SeidartSource;
 
+/* Plane-wave source parameters (the plane-wave fields of the reference's
+ * Source record, src/fortran/seidart_types.f08; plane_wave_source.f08).
+ * kind: SEIDART_PW_S for source_type "pw" (elastic also "pws", "pw_s",
+ * "pw-s": transverse polarisation), SEIDART_PW_P for "pwp", "pw_p", "pw-p"
+ * (elastic only: polarisation along the propagation direction).  wavelet:
+ * 0 gaus0 (also any other name), 1 gaus1, 2 gaus2.  Angles in degrees
+ * (JSON "x-z_rotation", "x-y_rotation", "y-z_rotation"); frequency is
+ * "source_frequency" (Hz), amplitude "amplitude". */
+#define SEIDART_PW_S 1
+#define SEIDART_PW_P 2
+typedef struct SeidartPlaneWave {
+    int kind;
+    int wavelet;
+    double x_z_rotation, x_y_rotation, y_z_rotation;
+    double amplitude, frequency;
+} SeidartPlaneWave;
+
 /* ---------------------------------------------------------- array slots
  * Host arrays are passed as `const double* const* arrays` in these orders.
  * Model arrays are read-only grids; source series have time_steps entries
@@ -181,6 +198,27 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision,
 /* Use a caller-owned cudaStream_t (passed as void*; NULL = the handle's own). */
 int seidart_solver_set_stream(SeidartSolver* s, void* stream);
 int seidart_solver_set_fields(SeidartSolver* s, const double* const* fields);
+/* Switch the solver to a plane-wave source (pw != NULL; pw->kind 0 switches
+ * back to point sources): the injection faces, polarisation and background
+ * speed are set up from the parameters and the host model (the family's
+ * slots, as given to seidart_solver_create: the speed comes from the
+ * stiffness / permittivity eigenvalues over the grid).  The point-source
+ * series are not applied while the plane wave is on (the reference loads
+ * none); electromag25 sets the plane wave up but, like the reference
+ * (cpmlfdtd.f08:3261-3266), never injects it.
+ * Replaces: the plane-wave branches of cpmlfdtd.f08 (seismic2 :186-227,
+ * :452-512; seismic25 :802-834, :1207-1260; seismic3 :1548-1606,
+ * :2133-2203; electromag2 :2436-2476, :2626-2673; electromag3 :3523-3578,
+ * :3833-3900) and plane_wave_source.f08. */
+int seidart_solver_set_plane_wave(SeidartSolver* s, const SeidartPlaneWave* pw, const double* const* model);
+/* The set-up figures of a plane wave without a solver (host only): out[0]
+ * background speed, out[1] impedance (EM; 0 elastic), out[2..4] direction
+ * p, out[5..7] polarisation ehat, out[8] number of injection faces,
+ * out[9..11] their axes (0 x, 1 y, 2 z; -1 unused), out[12..14] their
+ * 0-based fixed indices.  No reference counterpart (the reference keeps these
+ * in locals of each solver). */
+int seidart_plane_wave_setup(int family, const SeidartDomain* dom, const SeidartSource* src,
+                             const SeidartPlaneWave* pw, const double* const* model, double* out);
 int seidart_solver_get_fields(SeidartSolver* s, double* const* fields);
 /* CPML memory variables expanded to full grids (zeros where not stored). */
 int seidart_solver_get_memory(SeidartSolver* s, double* const* mem);
@@ -228,6 +266,13 @@ const char* seidart_last_error(void);
 int seidart_run_files(const char* dir, int family, int precision, const SeidartDomain* dom,
                       const SeidartSource* src, int density_code, const char* source_type,
                       int single_output, int write_snapshots);
+/* The same with the plane-wave parameters of the run (used when
+ * source_type names a plane wave: "pw" for every family, and for the
+ * elastic ones "pws", "pw_s", "pw-s", "pwp", "pw_p", "pw-p"; the source
+ * series files are then not read).  pw may be NULL for point sources. */
+int seidart_run_files_pw(const char* dir, int family, int precision, const SeidartDomain* dom,
+                         const SeidartSource* src, int density_code, const char* source_type,
+                         int single_output, int write_snapshots, const SeidartPlaneWave* pw);
 const char* seidart_io_last_error(void);
 /* Write one zstd frame holding `bytes` of data: compressed at level 3 by the
  * system libzstd when it can be loaded (as write_zstd_block does,

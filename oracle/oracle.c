@@ -57,6 +57,200 @@ static inline double scalar_mean(double a, double b, int code) {
 static inline double src_at(const double* a, int it) { return a ? a[it - 1] : 0.0; }
 
 /* =====================================================================
+ * Plane-wave sources: plane_wave_source.f08 statement by statement.
+ * Fortran matrices are kept column-major: A(i,j) = A[(i-1) + 3*(j-1)].
+ * ===================================================================== */
+static OraclePw g_pw;
+static int g_pw_on = 0;
+void oracle_set_plane_wave(const OraclePw* pw) {
+    g_pw_on = pw && pw->on;
+    if (g_pw_on) g_pw = *pw;
+}
+
+#define F3(A, i, j) (A)[((i) - 1) + 3 * ((j) - 1)]
+static void matmul33(const double* A, const double* B, double* C) {
+    for (int i = 1; i <= 3; ++i)
+        for (int j = 1; j <= 3; ++j) {
+            double acc = 0.0;
+            for (int k = 1; k <= 3; ++k) acc += F3(A, i, k) * F3(B, k, j);
+            F3(C, i, j) = acc;
+        }
+}
+static void matvec3(const double* A, const double* x, double* y) {
+    for (int i = 1; i <= 3; ++i) {
+        double acc = 0.0;
+        for (int k = 1; k <= 3; ++k) acc += F3(A, i, k) * x[k - 1];
+        y[i - 1] = acc;
+    }
+}
+static double pw_norm2(const double* v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+static double pw_dot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* rotmat: plane_wave_source.f08:76-108 (reshape fills columns) */
+static void pw_rotmat(double axz, double axy, double ayz, double* R) {
+    const double deg2rad = 3.1415926535897932384626433832795 / 180;
+    const double cx = cos(deg2rad * ayz), cy = cos(deg2rad * axz), cz = cos(deg2rad * axy);
+    const double sx = sin(deg2rad * ayz), sy = sin(deg2rad * axz), sz = sin(deg2rad * axy);
+    const double Rx[9] = {1.0, 0.0, 0.0, 0.0, cx, -sx, 0.0, sx, cx};
+    const double Ry[9] = {cy, 0.0, sy, 0.0, 1.0, 0.0, -sy, 0.0, cy};
+    const double Rz[9] = {cz, -sz, 0.0, sz, cz, 0.0, 0.0, 0.0, 1.0};
+    double T[9];
+    matmul33(Rz, Rx, T);
+    matmul33(Ry, T, R);
+}
+
+/* direction_polarization_vector: plane_wave_source.f08:110-139 */
+static void pw_direction(double axz, double axy, double ayz, double* p, double* ehat) {
+    const double k0[3] = {0.0, 0.0, 1.0}, e0[3] = {1.0, 0.0, 0.0};
+    double R[9], tmp[3];
+    pw_rotmat(axz, axy, ayz, R);
+    matvec3(R, k0, p);
+    double nrm = pw_norm2(p);
+    if (nrm > 0.0) for (int q = 0; q < 3; ++q) p[q] = p[q] / nrm;
+    matvec3(R, e0, tmp);
+    double d = pw_dot(tmp, p);
+    for (int q = 0; q < 3; ++q) tmp[q] = tmp[q] - d * p[q];
+    nrm = pw_norm2(tmp);
+    if (nrm > 0.0) {
+        for (int q = 0; q < 3; ++q) ehat[q] = tmp[q] / nrm;
+    } else {
+        if (fabs(p[0]) < 0.9) { tmp[0] = 1.0; tmp[1] = 0.0; tmp[2] = 0.0; }
+        else { tmp[0] = 0.0; tmp[1] = 1.0; tmp[2] = 0.0; }
+        d = pw_dot(tmp, p);
+        for (int q = 0; q < 3; ++q) tmp[q] = tmp[q] - d * p[q];
+        nrm = pw_norm2(tmp);
+        for (int q = 0; q < 3; ++q) ehat[q] = nrm > 0.0 ? tmp[q] / nrm : 0.0;
+    }
+}
+
+/* wavelet: plane_wave_source.f08:141-161 */
+static double pw_wavelet(double t, double f0, int type) {
+    const double t0 = 1.5 / f0;
+    const double a = 3.1415926535897932384626433832795 * f0 * (t - t0);
+    const double g = exp(-a * a);
+    if (type == 1) return -2.0 * a * g;
+    if (type == 2) return (1.0 - 2.0 * a * a) * g;
+    return g;
+}
+
+/* boundary_seismic_field: plane_wave_source.f08:196-230 */
+static void pw_seismic_field(const double* r, const double* r0, double t, double* V, double* strain) {
+    double p[3], ehat[3], dr[3];
+    pw_direction(g_pw.x_z_rotation, g_pw.x_y_rotation, g_pw.y_z_rotation, p, ehat);
+    if (g_pw.p_wave) for (int q = 0; q < 3; ++q) ehat[q] = p[q];
+    for (int q = 0; q < 3; ++q) dr[q] = r[q] - r0[q];
+    const double tau = t - pw_dot(p, dr) / g_pw.v;
+    const double s = g_pw.amplitude * pw_wavelet(tau, g_pw.frequency, g_pw.wavelet);
+    for (int q = 0; q < 3; ++q) V[q] = s * ehat[q];
+    const double scale = -s / g_pw.v;
+    strain[0] = scale * ehat[0] * p[0];
+    strain[1] = scale * ehat[1] * p[1];
+    strain[2] = scale * ehat[2] * p[2];
+    strain[3] = scale * (ehat[1] * p[2] + ehat[2] * p[1]);
+    strain[4] = scale * (ehat[0] * p[2] + ehat[2] * p[0]);
+    strain[5] = scale * (ehat[0] * p[1] + ehat[1] * p[0]);
+}
+
+/* boundary_em_field: plane_wave_source.f08:163-194 */
+static void pw_em_field(const double* r, const double* r0, double t, double* E, double* H) {
+    double p[3], ehat[3], dr[3], hhat[3];
+    pw_direction(g_pw.x_z_rotation, g_pw.x_y_rotation, g_pw.y_z_rotation, p, ehat);
+    for (int q = 0; q < 3; ++q) dr[q] = r[q] - r0[q];
+    const double tau = t - pw_dot(p, dr) / g_pw.v;
+    const double s = g_pw.amplitude * pw_wavelet(tau, g_pw.frequency, g_pw.wavelet);
+    for (int q = 0; q < 3; ++q) E[q] = s * ehat[q];
+    hhat[0] = p[1] * ehat[2] - p[2] * ehat[1];
+    hhat[1] = p[2] * ehat[0] - p[0] * ehat[2];
+    hhat[2] = p[0] * ehat[1] - p[1] * ehat[0];
+    const double hn = pw_norm2(hhat);
+    if (hn > 0.0) for (int q = 0; q < 3; ++q) hhat[q] = hhat[q] / hn;
+    for (int q = 0; q < 3; ++q) H[q] = (s / g_pw.eta) * hhat[q];
+}
+
+/* set-up of one solver (e.g. cpmlfdtd.f08:186-227): active faces, r0, the
+ * face locations and the 1-based loop ranges (inset 2, electromag3: 3) */
+typedef struct PwGeom {
+    int active[6];
+    double r0[3], loc[3];
+    int imin, imax, jmin, jmax, kmin, kmax;
+} PwGeom;
+static void pw_geom(const SeidartDomain* d, int three, int inset, PwGeom* G) {
+    double p[3], ehat[3];
+    pw_direction(g_pw.x_z_rotation, g_pw.x_y_rotation, g_pw.y_z_rotation, p, ehat);
+    const double eps = 1.0 * 1.0e-6;
+    for (int q = 0; q < 6; ++q) G->active[q] = 0;
+    if (p[0] > eps) G->active[0] = 1;
+    if (p[0] < -eps) G->active[1] = 1;
+    if (p[1] > eps) G->active[2] = 1;
+    if (p[1] < -eps) G->active[3] = 1;
+    if (p[2] > eps) G->active[4] = 1;
+    if (p[2] < -eps) G->active[5] = 1;
+    const double XMIN = d->dx * (1 + d->cpml), XMAX = d->dx * (d->nx - d->cpml);
+    const double YMIN = d->dy * (1 + d->cpml), YMAX = d->dy * (d->ny - d->cpml);
+    const double ZMIN = d->dz * (1 + d->cpml), ZMAX = d->dz * (d->nz - d->cpml);
+    const double XMID = 0.50 * (XMIN + XMAX), YMID = 0.50 * (YMIN + YMAX), ZMID = 0.50 * (ZMIN + ZMAX);
+    G->r0[0] = XMID; G->r0[1] = three ? YMID : 0.0; G->r0[2] = ZMID;
+    G->loc[0] = XMID; G->loc[1] = YMID; G->loc[2] = ZMID;
+    if (G->active[0]) { G->r0[0] = XMIN; G->loc[0] = XMIN; }
+    if (G->active[1]) { G->r0[0] = XMAX; G->loc[0] = XMAX; }
+    if (three && G->active[2]) { G->r0[1] = YMIN; G->loc[1] = YMIN; }
+    if (three && G->active[3]) { G->r0[1] = YMAX; G->loc[1] = YMAX; }
+    if (G->active[4]) { G->r0[2] = ZMIN; G->loc[2] = ZMIN; }
+    if (G->active[5]) { G->r0[2] = ZMAX; G->loc[2] = ZMAX; }
+    G->imin = d->cpml + inset; G->imax = d->nx - d->cpml - (inset - 1);
+    G->jmin = d->cpml + inset; G->jmax = d->ny - d->cpml - (inset - 1);
+    G->kmin = d->cpml + inset; G->kmax = d->nz - d->cpml - (inset - 1);
+}
+static int nint_(double x) { return (int)lround(x); }
+
+/* C_ij (1-based Voigt row a, column b) of the upper-triangle C21 order */
+static double cij(const double* const* C, int a, int b, size_t c) {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    return C[(lo - 1) * 6 - (lo - 1) * (lo - 2) / 2 + (hi - lo)][c];
+}
+/* add_plane_wave_stress: cpmlfdtd.f08:16-50 (s[0..5] = sxx syy szz syz sxz sxy) */
+static void pw_add_stress(const double* const* C, size_t c, const double* st, double* s) {
+    for (int a = 1; a <= 6; ++a) {
+        double acc = s[a - 1];
+        for (int b = 1; b <= 6; ++b) acc = acc + cij(C, a, b, c) * st[b - 1];
+        s[a - 1] = acc;
+    }
+}
+/* 3D face loops of seismic3 / electromag3 (x face, y face, z face), calling
+ * body(cell, r) for every cell of each active face in the reference's order */
+#define PW_FACES3(G, dx, dy, dz, ...)                                                             \
+    do {                                                                                          \
+        double r[3];                                                                              \
+        if ((G).active[0] || (G).active[1]) {                                                     \
+            const int ii = nint_((G).loc[0] / (dx));                                              \
+            for (int jj = (G).jmin; jj <= (G).jmax; ++jj)                                         \
+                for (int kk = (G).kmin; kk <= (G).kmax; ++kk) {                                   \
+                    r[0] = (G).loc[0]; r[1] = jj * (dy); r[2] = kk * (dz);                        \
+                    const size_t c = IX3(ii, jj, kk);                                             \
+                    __VA_ARGS__                                                                   \
+                }                                                                                 \
+        }                                                                                         \
+        if ((G).active[2] || (G).active[3]) {                                                     \
+            const int jj = nint_((G).loc[1] / (dy));                                              \
+            for (int ii = (G).imin; ii <= (G).imax; ++ii)                                         \
+                for (int kk = (G).kmin; kk <= (G).kmax; ++kk) {                                   \
+                    r[0] = ii * (dx); r[1] = (G).loc[1]; r[2] = kk * (dz);                        \
+                    const size_t c = IX3(ii, jj, kk);                                             \
+                    __VA_ARGS__                                                                   \
+                }                                                                                 \
+        }                                                                                         \
+        if ((G).active[4] || (G).active[5]) {                                                     \
+            const int kk = nint_((G).loc[2] / (dz));                                              \
+            for (int ii = (G).imin; ii <= (G).imax; ++ii)                                         \
+                for (int jj = (G).jmin; jj <= (G).jmax; ++jj) {                                   \
+                    r[0] = ii * (dx); r[1] = jj * (dy); r[2] = (G).loc[2];                        \
+                    const size_t c = IX3(ii, jj, kk);                                             \
+                    __VA_ARGS__                                                                   \
+                }                                                                                 \
+        }                                                                                         \
+    } while (0)
+
+/* =====================================================================
  * seismic2: cpmlfdtd.f08:311-576
  * ===================================================================== */
 int oracle_seismic2(const SeidartDomain* d, const SeidartSource* s, int density_code,
@@ -156,6 +350,29 @@ int oracle_seismic2(const SeidartDomain* d, const SeidartSource* s, int density_
                 dszz_dz = dszz_dz / kappa_half[c] + m_dszz_dz[c];
                 vz[c] = vz[c] + dt * (dsxz_dx / rhoxz + dszz_dz / rhozz);
             }
+        if (g_pw_on) {  /* plane wave: cpmlfdtd.f08:454-512 */
+            PwGeom G;
+            pw_geom(d, 0, 2, &G);
+            const double t = it * s->dt;
+            double r[3], V[3], st[6];
+            for (int face = 0; face < 2; ++face) {
+                const int xface = face == 0;
+                if (xface ? !(G.active[0] || G.active[1]) : !(G.active[4] || G.active[5])) continue;
+                const int fixed = xface ? nint_(G.loc[0] / dx) : nint_(G.loc[2] / dz);
+                const int lo = xface ? G.kmin : G.imin, hi = xface ? G.kmax : G.imax;
+                for (int ip = lo; ip <= hi; ++ip) {
+                    if (xface) { r[0] = G.loc[0]; r[1] = 0.0; r[2] = ip * dz; }
+                    else { r[0] = ip * dx; r[1] = 0.0; r[2] = G.loc[2]; }
+                    pw_seismic_field(r, G.r0, t, V, st);
+                    const size_t c = xface ? IX2(fixed, ip) : IX2(ip, fixed);
+                    vx[c] = vx[c] + V[0];
+                    vz[c] = vz[c] + V[2];
+                    sigmaxx[c] = sigmaxx[c] + c11[c] * st[0] + c13[c] * st[2] + c15[c] * st[4];
+                    sigmazz[c] = sigmazz[c] + c13[c] * st[0] + c33[c] * st[2] + c35[c] * st[4];
+                    sigmaxz[c] = sigmaxz[c] + c15[c] * st[0] + c35[c] * st[2] + c55[c] * st[4];
+                }
+            }
+        } else
         /* point source: cpmlfdtd.f08:519-523 (no dt on the force terms) */
         {
             const size_t c = IX2(isource, jsource), c1 = IX2(isource + 1, jsource + 1);
@@ -366,6 +583,35 @@ int oracle_seismic25(const SeidartDomain* d, const SeidartSource* s, int density
                 e = ccpml(mem[S25_M_DSZZ_DZ], c, bcoef_half[c], acoef_half[c], kappa_half[c], e);
                 cst(vz, c, cadd(cld(vz, c), cmulr(cadd(cadd(cdivr(a, rhoxz[c]), cdivr(b, rhoyz[c])), cdivr(e, rhozz[c])), dt)));
             }
+        if (g_pw_on) {  /* plane wave: cpmlfdtd.f08:1208-1260 (real parts) */
+            PwGeom G;
+            pw_geom(d, 0, 2, &G);
+            const double t = it * dt;
+            double r[3], V[3], st[6];
+            for (int face = 0; face < 2; ++face) {
+                const int xface = face == 0;
+                if (xface ? !(G.active[0] || G.active[1]) : !(G.active[4] || G.active[5])) continue;
+                const int fixed = xface ? nint_(G.loc[0] / dx) : nint_(G.loc[2] / dz);
+                const int lo = xface ? G.kmin : G.imin, hi = xface ? G.kmax : G.imax;
+                for (int ip = lo; ip <= hi; ++ip) {
+                    if (xface) { r[0] = G.loc[0]; r[1] = 0.0; r[2] = ip * dz; }
+                    else { r[0] = ip * dx; r[1] = 0.0; r[2] = G.loc[2]; }
+                    pw_seismic_field(r, G.r0, t, V, st);
+                    const size_t c = xface ? IX2(fixed, ip) : IX2(ip, fixed);
+                    vx[2 * c] = vx[2 * c] + V[0];
+                    vy[2 * c] = vy[2 * c] + V[1];
+                    vz[2 * c] = vz[2 * c] + V[2];
+                    double tmp[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                    pw_add_stress(C, c, st, tmp);
+                    sxx[2 * c] = sxx[2 * c] + tmp[0];
+                    syy[2 * c] = syy[2 * c] + tmp[1];
+                    szz[2 * c] = szz[2 * c] + tmp[2];
+                    syz[2 * c] = syz[2 * c] + tmp[3];
+                    sxz[2 * c] = sxz[2 * c] + tmp[4];
+                    sxy[2 * c] = sxy[2 * c] + tmp[5];
+                }
+            }
+        } else
         /* point source: cpmlfdtd.f08:1268-1276 (real part only) */
         {
 #define ADDRE(arr, i, k, val) arr[2 * IX2(i, k)] = arr[2 * IX2(i, k)] + (val)
@@ -568,6 +814,21 @@ int oracle_seismic3(const SeidartDomain* d, const SeidartSource* s, int density_
                     e = rcpml(mem[S3_M_DSZZ_DZ], c, bcoef_half[c], acoef_half[c], kappa_half[c], e);
                     vz[c] = vz[c] + (a / rhoxz + b / rhoyz + e / rhozz) * dt;
                 }
+        if (g_pw_on) {  /* plane wave: cpmlfdtd.f08:2133-2203 */
+            PwGeom G;
+            pw_geom(d, 1, 2, &G);
+            const double t = it * dt;
+            double V[3], st[6];
+            PW_FACES3(G, dx, dy, dz, {
+                pw_seismic_field(r, G.r0, t, V, st);
+                vx[c] = vx[c] + V[0];
+                vy[c] = vy[c] + V[1];
+                vz[c] = vz[c] + V[2];
+                double sg[6] = {sxx[c], syy[c], szz[c], syz[c], sxz[c], sxy[c]};
+                pw_add_stress(C, c, st, sg);
+                sxx[c] = sg[0]; syy[c] = sg[1]; szz[c] = sg[2]; syz[c] = sg[3]; sxz[c] = sg[4]; sxy[c] = sg[5];
+            });
+        } else
         /* point source: cpmlfdtd.f08:2210-2219 */
         {
             const int is = isource, js = jsource, ks = ksource;
@@ -690,6 +951,27 @@ int oracle_electromag2(const SeidartDomain* d, const SeidartSource* s,
                 Ez[c] = Ezo[c] + (-aEz[c] * dHy_dz + bEz[c] * dHy_dx - dEz[c] * Exo[c] - eEz[c] * Ezo[c]) * dt;
                 Ex[c] = Exo[c] + (-aEx[c] * dHy_dz + bEx[c] * dHy_dx - dEx[c] * Exo[c] - eEx[c] * Ezo[c]) * dt;
             }
+        if (g_pw_on) {  /* plane wave: cpmlfdtd.f08:2626-2673 */
+            PwGeom G;
+            pw_geom(d, 0, 2, &G);
+            const double t = it * s->dt;
+            double r[3], E[3], H[3];
+            for (int face = 0; face < 2; ++face) {
+                const int xface = face == 0;
+                if (xface ? !(G.active[0] || G.active[1]) : !(G.active[4] || G.active[5])) continue;
+                const int fixed = xface ? nint_(G.loc[0] / dx) : nint_(G.loc[2] / dz);
+                const int lo = xface ? G.kmin : G.imin, hi = xface ? G.kmax : G.imax;
+                for (int ip = lo; ip <= hi; ++ip) {
+                    if (xface) { r[0] = G.loc[0]; r[1] = 0.0; r[2] = ip * dz; }
+                    else { r[0] = ip * dx; r[1] = 0.0; r[2] = G.loc[2]; }
+                    pw_em_field(r, G.r0, t, E, H);
+                    const size_t c = xface ? IX2(fixed, ip) : IX2(ip, fixed);
+                    Ex[c] = Ex[c] + E[0];
+                    Ez[c] = Ez[c] + E[2];
+                    Hy[c] = Hy[c] + H[1];
+                }
+            }
+        } else
         /* point source: cpmlfdtd.f08:2678-2681 */
         {
             const size_t c = IX2(isource, jsource);
@@ -1009,6 +1291,17 @@ int oracle_electromag3(const SeidartDomain* d, const SeidartSource* s,
                     Ey[c] = Ey_old[c] + (aEy[c] * rhs_x + bEy[c] * rhs_y + cEy[c] * rhs_z) * dt;
                     Ez[c] = Ez_old[c] + (aEz[c] * rhs_x + bEz[c] * rhs_y + cEz[c] * rhs_z) * dt;
                 }
+        if (g_pw_on) {  /* plane wave: cpmlfdtd.f08:3833-3900 */
+            PwGeom G;
+            pw_geom(d, 1, 3, &G);
+            const double t = it * s->dt;
+            double E[3], H[3];
+            PW_FACES3(G, dx, dy, dz, {
+                pw_em_field(r, G.r0, t, E, H);
+                Ex[c] = Ex[c] + E[0]; Ey[c] = Ey[c] + E[1]; Ez[c] = Ez[c] + E[2];
+                Hx[c] = Hx[c] + H[0]; Hy[c] = Hy[c] + H[1]; Hz[c] = Hz[c] + H[2];
+            });
+        } else
         /* point source: cpmlfdtd.f08:3901-3906 */
         {
             const size_t c = IX3(isource, jsource, ksource);

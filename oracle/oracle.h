@@ -54,6 +54,17 @@ int oracle_electromag3(const SeidartDomain* d, const SeidartSource* s,
 /* Number of OpenMP threads the build uses (1 without OpenMP). */
 int oracle_threads(void);
 
+/* Plane-wave source for the following oracle_* calls (NULL or on = 0: point
+ * sources).  v is the background speed (cbackground / vbackground) and eta
+ * the impedance (EM), which the reference takes from LAPACK eigenvalues
+ * (tensor_operations.f08); the caller computes them the same way.
+ * p_wave: source_type "pwp" (elastic); wavelet 0 gaus0, 1 gaus1, 2 gaus2. */
+typedef struct OraclePw {
+    int on, p_wave, wavelet;
+    double x_z_rotation, x_y_rotation, y_z_rotation, amplitude, frequency, v, eta;
+} OraclePw;
+void oracle_set_plane_wave(const OraclePw* pw);
+
 #ifdef __cplusplus
 }
 #endif

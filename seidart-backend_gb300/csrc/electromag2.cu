@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(BX* BY) e2_e(E2Args<real> a, StepInfo si) {
 #else
         sq = ex * ex + ez * ez; n0 = ex; n1 = ez;
 #endif
+        // plane-wave face cells: their norm is taken after the injection
+        if (a.pw.on && pw_cell(a.pw, i - 1, 0, j - 1)) { nrm = 0.0; sq = 0.f; n0 = 0.f; n1 = 0.f; }
     }
 #if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
@@ -140,6 +142,7 @@ void SD_NAME(launch_electromag2)(const E2Args<real>& a, const StepInfo& s, cudaS
     if (h) h->fn(h->ctx, 0, "e2_h");
     e2_e<<<grd, blk, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 1, "e2_e");
+    if (a.pw.on) pw_electromag2<real>(a, s, st);
     e2_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 2, "e2_epilogue");
 }

@@ -156,6 +156,8 @@ __global__ void __launch_bounds__(BX* BY) e3_e(E3Args<real> a, StepInfo si) {
 #else
         sq = ex * ex + ey * ey + ez * ez; n0 = ex; n1 = ey; n2 = ez;
 #endif
+        // plane-wave face cells: their norm is taken after the injection
+        if (a.pw.on && pw_cell(a.pw, i - 1, j - 1, k - 1)) { nrm = 0.0; sq = 0.f; n0 = n1 = n2 = 0.f; }
     }
 #if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
@@ -190,6 +192,7 @@ void SD_NAME(launch_electromag3)(const E3Args<real>& a, const StepInfo& s, cudaS
     if (h) h->fn(h->ctx, 0, "e3_h");
     e3_e<<<grd, blk, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 1, "e3_e");
+    if (a.pw.on) pw_electromag3<real>(a, s, st);
     e3_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 2, "e3_epilogue");
 }

@@ -592,11 +592,23 @@ int seidart_internal_write_record(const char* path, const void* data, size_t byt
 int seidart_run_files(const char* dir_c, int family, int precision, const SeidartDomain* dom,
                       const SeidartSource* src, int density_code, const char* source_type, int single_output,
                       int write_snapshots) {
+    return seidart_run_files_pw(dir_c, family, precision, dom, src, density_code, source_type, single_output,
+                                write_snapshots, nullptr);
+}
+
+int seidart_run_files_pw(const char* dir_c, int family, int precision, const SeidartDomain* dom,
+                         const SeidartSource* src, int density_code, const char* source_type, int single_output,
+                         int write_snapshots, const SeidartPlaneWave* pw_in) {
     if (!dom || !src) return io_err(SEIDART_ERR_ARG, "NULL domain/source");
     const std::string dir = dir_c && *dir_c ? dir_c : ".";
     const std::string stype = source_type ? trim(source_type) : std::string("ac");
-    if (stype == "pw" || stype == "plane" || stype == "planewave")
-        return io_err(SEIDART_ERR_UNSUPPORTED, "plane-wave sources are not supported by the GPU solvers");
+    // is_plane_wave_source / is_p_wave_source (plane_wave_source.f08:20-36)
+    // for the elastic solvers; the EM solvers test source_type == 'pw'
+    const bool seis_family = family == SEIDART_SEISMIC2 || family == SEIDART_SEISMIC25 || family == SEIDART_SEISMIC3;
+    const bool p_wave = seis_family && (stype == "pwp" || stype == "pw_p" || stype == "pw-p");
+    const bool plane = stype == "pw" || (seis_family && (p_wave || stype == "pws" || stype == "pw_s" || stype == "pw-s"));
+    if (plane && !pw_in)
+        return io_err(SEIDART_ERR_ARG, "source_type \"" + stype + "\" needs the plane-wave parameters");
     int nmodel, nsrc, nfield, nmem, cplx, ncomp;
     if (seidart_layout(family, &nmodel, &nsrc, &nfield, &nmem, &cplx, &ncomp) != SEIDART_OK)
         return io_err(SEIDART_ERR_ARG, "unknown family");
@@ -657,7 +669,7 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
     // sources: 'ac' loads the force components, any other type the stress
     // components (cpmlfdtd.f08:230-237); EM loads the point-source components
     std::vector<const double*> srcp(nsrc, nullptr);
-    for (int q = 0; q < nsrc; ++q) {
+    for (int q = 0; q < nsrc && !plane; ++q) {  // a plane wave loads no source series
         const bool is_force = !seis || q < (family == SEIDART_SEISMIC2 ? 2 : 3);
         if (seis && is_force != force) continue;
         std::vector<char> rec;
@@ -685,6 +697,11 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
     int rc = seidart_solver_create(&s, family, precision, dom, src, density_code, mp.data(), srcp.data(), 0, nullptr);
     if (rc != SEIDART_OK) return io_err(rc, seidart_last_error());
     rc = seidart_solver_set_fields(s, fp.data());
+    if (rc == SEIDART_OK && plane) {
+        SeidartPlaneWave pwp = *pw_in;
+        pwp.kind = p_wave ? SEIDART_PW_P : SEIDART_PW_S;
+        rc = seidart_solver_set_plane_wave(s, &pwp, mp.data());
+    }
     if (rc != SEIDART_OK) { seidart_solver_destroy(s); return io_err(rc, seidart_last_error()); }
     char suffix[96];
     if (is3) snprintf(suffix, sizeof suffix, ".%d.%d.%d.dat", src->xind, src->yind, src->zind);
@@ -892,6 +909,19 @@ int seidart_cli_main(int argc, char** argv) {
     if (!js.num(pre + "yind", yi)) yi = 0;
     s.time_steps = (int)ts; s.xind = (int)xi; s.yind = (int)yi; s.zind = (int)zi;
     const std::string stype = trim(js.text(pre + "source_type"));
+    // plane-wave fields of the Source record (seidartio.f08:80-85, :101-106)
+    SeidartPlaneWave pw{};
+    {
+        double v0;
+        if (js.num(pre + "source_frequency", v0)) pw.frequency = v0;
+        if (js.num(pre + "x-z_rotation", v0)) pw.x_z_rotation = v0;
+        if (js.num(pre + "x-y_rotation", v0)) pw.x_y_rotation = v0;
+        if (js.num(pre + "y-z_rotation", v0)) pw.y_z_rotation = v0;
+        if (js.num(pre + "amplitude", v0)) pw.amplitude = v0;
+        const std::string wl = trim(js.text(pre + "source_wavelet"));
+        pw.wavelet = wl == "gaus1" ? 1 : wl == "gaus2" ? 2 : 0;  // wavelet(), plane_wave_source.f08:141-161
+        pw.kind = SEIDART_PW_S;
+    }
     const char* ky = getenv("KY");
     s.ky = ky ? atof(ky) : 0.0;
     // 2.5D solvers read SINGLE_OUTPUT and DENSITY_METHOD (default harmonic) from the environment
@@ -917,8 +947,8 @@ int seidart_cli_main(int argc, char** argv) {
     }
     if (fam == SEIDART_ELECTROMAG2 || fam == SEIDART_ELECTROMAG25 || fam == SEIDART_SEISMIC2) d.ny = 1;
     (void)v;
-    const int rc = seidart_run_files(".", fam, precision, &d, &s, code, stype.empty() ? "ac" : stype.c_str(), single,
-                                     snaps ? 1 : 0);
+    const int rc = seidart_run_files_pw(".", fam, precision, &d, &s, code, stype.empty() ? "ac" : stype.c_str(), single,
+                                        snaps ? 1 : 0, &pw);
     if (rc == SEIDART_ERR_UNSTABLE) { fprintf(stderr, "code became unstable and blew up\n"); return 3; }
     if (rc != SEIDART_OK) { fprintf(stderr, "seidartfdtd: error %d: %s\n", rc, g_io_err.c_str()); return 4; }
     return 0;

@@ -20,6 +20,33 @@ struct LaunchHook {
 // Per-step scalars common to all families.  The 1-based step number lives in
 // device memory (*step) and the last kernel of every step increments it, so
 // one captured CUDA graph of G steps replays from any starting step.
+// Plane-wave injection (planewave.cu): up to three faces of the interior
+// box, applied in x, y, z order after the velocity / E update.  0-based
+// cells; a face fixes one axis and spans inclusive ranges on the others.
+struct PwFace {
+    int axis;          // 0: x, 1: y, 2: z
+    int fixed;         // index along `axis`
+    int lo[3], hi[3];  // inclusive ranges per axis (the fixed axis: fixed..fixed)
+};
+struct PwDev {
+    int on;            // 0: point sources
+    int em;            // 1: E/H fields, 0: elastic
+    int nface;
+    int wavelet;       // 0 gaus0, 1 gaus1, 2 gaus2
+    PwFace face[3];
+    double p[3], ehat[3], hhat[3], r0[3], loc[3], h[3];
+    double v, eta, amp, f0, dt;
+};
+// true when cell (i, j, k) lies on an injection face: the velocity / E
+// kernels leave it out of their max-norms, the injection takes it
+__host__ __device__ inline bool pw_cell(const PwDev& pw, int i, int j, int k) {
+    for (int f = 0; f < pw.nface; ++f) {
+        const PwFace& F = pw.face[f];
+        if (i >= F.lo[0] && i <= F.hi[0] && j >= F.lo[1] && j <= F.hi[1] && k >= F.lo[2] && k <= F.hi[2]) return true;
+    }
+    return false;
+}
+
 struct StepInfo {
     int* step;       // device: 1-based number of the step being computed
     int nrec;        // receivers
@@ -42,6 +69,7 @@ struct S2Args {
     int stress_src;        // 1 if any stress-source series is non-zero
     T* traces;             // [nt][2][nrec]
     double* norms;         // [nt]
+    PwDev pw;              // plane-wave source (pw.on = 0: point sources)
 };
 void launch_seismic2_f64(const S2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic2_f32(const S2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
@@ -62,6 +90,7 @@ struct E2Args {
     int isrc, jsrc;
     T* traces;        // [nt][2][nrec]
     double* norms;
+    PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag2_f64(const E2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag2_f32(const E2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
@@ -119,6 +148,7 @@ struct S25Args {
     int stress_src;
     T* traces;         // [nt][3][nrec] complex
     double* norms;
+    PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_seismic25_f64(const S25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic25_f32(const S25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
@@ -139,6 +169,7 @@ struct E25Args {
     int isrc, ksrc;
     T* traces;         // [nt][3][nrec] complex
     double* norms;
+    PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag25_f64(const E25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag25_f32(const E25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
@@ -163,6 +194,7 @@ struct E3Args {
     int isrc, jsrc, ksrc;  // 0-based source cell
     T* traces;         // [nt][3][nrec]
     double* norms;
+    PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag3_f64(const E3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag3_f32(const E3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
@@ -184,6 +216,7 @@ struct S3Args {
     int stress_src;
     T* traces;        // [nt][3][nrec]
     double* norms;    // [2][nt]: velocity norm, stress norm
+    PwDev pw;         // plane-wave source (pw.on = 0: point sources)
     int nt;
     double* norms_part;  // [2][64] per-step partial maxima (FP32 z-marching kernels)
     int* err;            // device error word: 1 = a bounded wait gave up
@@ -233,6 +266,13 @@ int seismic3_bulk_variants();
 int seismic3_bulk_variant_minblocks(int v);
 cudaError_t seismic3_bulk_pack(const S3Args<float>& a, float* packed, cudaStream_t st);
 void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st);
+// plane-wave injection and the max-norms of the face cells (planewave.cu),
+// launched by each family before its epilogue when a.pw.on
+template <typename T> void pw_seismic2(const S2Args<T>& a, const StepInfo& s, cudaStream_t st);
+template <typename T> void pw_seismic25(const S25Args<T>& a, const StepInfo& s, cudaStream_t st);
+template <typename T> void pw_seismic3(const S3Args<T>& a, const StepInfo& s, cudaStream_t st);
+template <typename T> void pw_electromag2(const E2Args<T>& a, const StepInfo& s, cudaStream_t st);
+template <typename T> void pw_electromag3(const E3Args<T>& a, const StepInfo& s, cudaStream_t st);
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 

@@ -200,6 +200,8 @@ __global__ void __launch_bounds__(BX* BY) s2_velocity(S2Args<real> a, StepInfo s
 #else
         sq = vx * vx + vz * vz; n0 = vx; n1 = vz;
 #endif
+        // plane-wave face cells: their norm is taken after the injection
+        if (a.pw.on && pw_cell(a.pw, i - 1, 0, j - 1)) { nrm = 0.0; sq = 0.f; n0 = 0.f; n1 = 0.f; }
     }
 #if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
@@ -250,6 +252,7 @@ void SD_NAME(launch_seismic2)(const S2Args<real>& a, const StepInfo& s, cudaStre
         s2_stress_source<<<1, 1, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 2, "s2_stress_source");
     }
+    if (a.pw.on) pw_seismic2<real>(a, s, st);
     s2_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 3, "s2_epilogue");
 }

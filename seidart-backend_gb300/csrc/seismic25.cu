@@ -195,6 +195,11 @@ __global__ void __launch_bounds__(BX* BY) s25_velocity(S25Args<real> a, StepInfo
         sq = (vx.re * vx.re + vx.im * vx.im) + (vy.re * vy.re + vy.im * vy.im) + (vz.re * vz.re + vz.im * vz.im);
         w[0] = vx.re; w[1] = vx.im; w[2] = vy.re; w[3] = vy.im; w[4] = vz.re; w[5] = vz.im;
 #endif
+        // plane-wave face cells: their norm is taken after the injection
+        if (a.pw.on && pw_cell(a.pw, i - 1, 0, k - 1)) {
+            nrm = 0.0; sq = 0.f;
+            for (float& x : w) x = 0.f;
+        }
     }
 #if SD_EXACT
     nrm = block_max<BX * BY / 32>(nrm, red);
@@ -253,6 +258,7 @@ void SD_NAME(launch_seismic25)(const S25Args<real>& a, const StepInfo& s, cudaSt
         s25_stress_source<<<1, 1, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 2, "s25_stress_source");
     }
+    if (a.pw.on) pw_seismic25<real>(a, s, st);
     s25_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 3, "s25_epilogue");
 }

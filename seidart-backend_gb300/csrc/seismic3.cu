@@ -227,6 +227,11 @@ __global__ void __launch_bounds__(BX* BY* BZ) s3_velocity(S3Args<real> a, StepIn
             ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
         }
 #endif
+        // plane-wave face cells: their norms are taken after the injection
+        if (a.pw.on && pw_cell(a.pw, i - 1, j - 1, k - 1)) {
+            vn = 0.0; sn = 0.0; vsq = 0.f; ssq = 0.f;
+            for (float& x : w) x = 0.f;
+        }
     }
 #if SD_EXACT
     vn = block_max<BX * BY * BZ / 32>(vn, red);
@@ -301,6 +306,7 @@ void SD_NAME(launch_seismic3)(const S3Args<real>& a, const StepInfo& s, cudaStre
         s3_stress_source<<<1, 1, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 2, "s3_stress_source");
     }
+    if (a.pw.on) pw_seismic3<real>(a, s, st);
     s3_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 3, "s3_epilogue");
 }

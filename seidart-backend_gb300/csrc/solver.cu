@@ -26,6 +26,10 @@
 #include "../../include/seidart_gpu.h"
 #include "kernels.h"
 
+// plane-wave set-up (planewave.cu)
+int pw_setup(int family, const SeidartDomain* dom, const SeidartSource* src, const SeidartPlaneWave* in,
+             const double* const* model, PwDev* out, std::string& why);
+
 namespace {
 
 thread_local std::string g_err;
@@ -549,7 +553,24 @@ void finish_args(SeidartSolver& s) {
     }
 }
 
-int launches_per_step(const SeidartSolver& s) { return 3 + (s.stress_src ? 1 : 0); }
+const PwDev& solver_pw(const SeidartSolver& s) {
+    const bool f = s.precision == SEIDART_FP32;
+    switch (s.family) {
+    case SEIDART_SEISMIC2: return f ? s.s2f.pw : s.s2d.pw;
+    case SEIDART_SEISMIC25: return f ? s.s25f.pw : s.s25d.pw;
+    case SEIDART_SEISMIC3: return f ? s.s3f.pw : s.s3d.pw;
+    case SEIDART_ELECTROMAG2: return f ? s.e2f.pw : s.e2d.pw;
+    case SEIDART_ELECTROMAG3: return f ? s.e3f.pw : s.e3d.pw;
+    default: return f ? s.e25f.pw : s.e25d.pw;
+    }
+}
+
+// kernels per step: update pair + epilogue, the stress-source kernel, and a
+// plane wave's face launches plus its norm launch
+int launches_per_step(const SeidartSolver& s) {
+    const PwDev& pw = solver_pw(s);
+    return 3 + (s.stress_src ? 1 : 0) + (pw.on && pw.nface > 0 ? pw.nface + 1 : 0);
+}
 
 void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nullptr) {
     StepInfo si{s.step_dev, s.nrec, s.rec_dev};
@@ -562,6 +583,7 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG3: f32 ? launch_electromag3_f32(s.e3f, si, st, h) : launch_electromag3_f64(s.e3d, si, st, h); break;
     case SEIDART_SEISMIC3:
         if (!f32) launch_seismic3_f64(s.s3d, si, st, h);
+        else if (s.s3f.pw.on) launch_seismic3_f32(s.s3f, si, st, h);  // plane waves: the one-cell kernels
         else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr, s.s3_stress_kind,
                                   s.s3_velocity_kind);
         break;
@@ -1071,6 +1093,46 @@ int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done) {
 // move the point source of an FP32 seismic2 solver (0-based cell) and point
 // its vertical-force series at device memory; cached graphs are dropped
 // because they hold the launch arguments by value
+int seidart_solver_set_plane_wave(SeidartSolver* s, const SeidartPlaneWave* in, const double* const* model) {
+    if (!s || !in) return set_err(SEIDART_ERR_ARG, "NULL argument");
+    PwDev pw{};
+    if (in->kind != 0) {
+        if (in->kind != SEIDART_PW_S && in->kind != SEIDART_PW_P) return set_err(SEIDART_ERR_ARG, "unknown plane-wave kind %d", in->kind);
+        if (!model) return set_err(SEIDART_ERR_ARG, "the plane-wave set-up needs the host model");
+        for (int q = 0; q < s->L.nmodel; ++q)
+            if (!model[q]) return set_err(SEIDART_ERR_ARG, "model array %d is NULL", q);
+        std::string why;
+        const int rc = pw_setup(s->family, &s->dom, &s->src, in, model, &pw, why);
+        if (rc != SEIDART_OK) return set_err(rc, "%s", why.c_str());
+    }
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    // point-source series are not applied while a plane wave is on
+    // (electromag25 keeps its point source, cpmlfdtd.f08:3261-3266)
+    const bool drop = pw.on != 0;
+    auto apply = [&](auto& a, int nsrc) {
+        a.pw = pw;
+        if (drop)
+            for (int q = 0; q < nsrc; ++q) a.src[q] = nullptr;
+    };
+    switch (s->family) {
+    case SEIDART_SEISMIC2: apply(s->s2d, S2_NSRC); apply(s->s2f, S2_NSRC); break;
+    case SEIDART_SEISMIC25: apply(s->s25d, 9); apply(s->s25f, 9); break;
+    case SEIDART_SEISMIC3: apply(s->s3d, 9); apply(s->s3f, 9); break;
+    case SEIDART_ELECTROMAG2: apply(s->e2d, E2_NSRC); apply(s->e2f, E2_NSRC); break;
+    case SEIDART_ELECTROMAG3: apply(s->e3d, E3_NSRC); apply(s->e3f, E3_NSRC); break;
+    default: break;  // electromag25: set up, never injected
+    }
+    if (drop && (s->family == SEIDART_SEISMIC2 || s->family == SEIDART_SEISMIC25 || s->family == SEIDART_SEISMIC3)) {
+        s->stress_src = 0;
+        s->s2d.stress_src = s->s2f.stress_src = 0;
+        s->s25d.stress_src = s->s25f.stress_src = 0;
+        s->s3d.stress_src = s->s3f.stress_src = 0;
+    }
+    for (int q = 0; q < 2; ++q)
+        if (s->graph_exec[q]) { cudaGraphExecDestroy(s->graph_exec[q]); s->graph_exec[q] = nullptr; s->graph_len[q] = 0; }
+    return SEIDART_OK;
+}
+
 int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
                                        const double* dev_srcz) {
     if (!s || (s->family != SEIDART_SEISMIC2 && s->family != SEIDART_ELECTROMAG2) || s->precision != SEIDART_FP32)

@@ -47,6 +47,17 @@ class Source(C.Structure):
                 ("zind", C.c_int), ("ky", C.c_double)]
 
 
+class PlaneWave(C.Structure):
+    """SeidartPlaneWave: kind 1 = transverse ("pw"), 2 = P wave ("pwp");
+    wavelet 0 gaus0, 1 gaus1, 2 gaus2; rotations in degrees."""
+    _fields_ = [("kind", C.c_int), ("wavelet", C.c_int), ("x_z_rotation", C.c_double),
+                ("x_y_rotation", C.c_double), ("y_z_rotation", C.c_double), ("amplitude", C.c_double),
+                ("frequency", C.c_double)]
+
+
+PW_S, PW_P = 1, 2
+WAVELETS = {"gaus0": 0, "gaus1": 1, "gaus2": 2}
+
 DPP = C.POINTER(C.c_void_p)
 
 _SIGS = {
@@ -57,6 +68,7 @@ _SIGS = {
                                         C.POINTER(Source), C.c_int, DPP, DPP, C.c_int, C.c_void_p]),
     "seidart_solver_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "seidart_solver_set_fields": (C.c_int, [C.c_void_p, DPP]),
+    "seidart_solver_set_plane_wave": (C.c_int, [C.c_void_p, C.POINTER(PlaneWave), DPP]),
     "seidart_solver_get_fields": (C.c_int, [C.c_void_p, DPP]),
     "seidart_solver_get_memory": (C.c_int, [C.c_void_p, DPP]),
     "seidart_solver_step": (C.c_int, [C.c_void_p, C.c_int]),

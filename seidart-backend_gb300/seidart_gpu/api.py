@@ -82,6 +82,22 @@ class Problem:
     ky: float = 0.0
     density: str = "arithmetic"
     meta: dict = field(default_factory=dict)
+    # plane-wave source: {"kind": "pw" | "pwp", "wavelet": "gaus0|1|2",
+    # "x_z_rotation", "x_y_rotation", "y_z_rotation" (degrees), "amplitude",
+    # "frequency"}; None = point sources from `src`
+    plane_wave: dict | None = None
+
+    def plane_wave_struct(self):
+        """The plane_wave dict as a SeidartPlaneWave (None without one)."""
+        pw = self.plane_wave
+        if not pw:
+            return None
+        kind = pw.get("kind", "pw")
+        return _lib.PlaneWave(_lib.PW_P if kind in ("pwp", "pw_p", "pw-p") else _lib.PW_S,
+                              _lib.WAVELETS.get(pw.get("wavelet", "gaus0"), 0),
+                              float(pw.get("x_z_rotation", 0.0)), float(pw.get("x_y_rotation", 0.0)),
+                              float(pw.get("y_z_rotation", 0.0)), float(pw.get("amplitude", 1.0)),
+                              float(pw["frequency"]))
 
     @property
     def shape(self) -> tuple:
@@ -169,6 +185,9 @@ class Solver:
                                           rec.ctypes.data if len(rec) else None))
         self.handle = h
         self.set_fields(problem.field_list())
+        pw = problem.plane_wave_struct()
+        if pw is not None:
+            check(lib().seidart_solver_set_plane_wave(self.handle, C.byref(pw), ptr_array(self._model)))
 
     # ------------------------------------------------------------------ state
     def set_fields(self, fields: list) -> None:

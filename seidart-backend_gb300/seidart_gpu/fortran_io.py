@@ -171,6 +171,12 @@ def write_problem(problem, directory, source_type: str = "ac", json_extra: dict 
            "source_frequency": problem.meta.get("f0", 0.0), "x-z_rotation": 0.0, "x-y_rotation": 0.0,
            "y-z_rotation": 0.0, "amplitude": 1.0, "source_type": source_type, "source_wavelet": "ricker",
            "dt": problem.dt, "time_steps": problem.time_steps}
+    pw = problem.plane_wave
+    if pw:
+        src.update({"source_type": pw.get("kind", "pw"), "source_wavelet": pw.get("wavelet", "gaus0"),
+                    "source_frequency": pw["frequency"], "amplitude": pw.get("amplitude", 1.0),
+                    "x-z_rotation": pw.get("x_z_rotation", 0.0), "x-y_rotation": pw.get("x_y_rotation", 0.0),
+                    "y-z_rotation": pw.get("y_z_rotation", 0.0)})
     js = {"Domain": {"dim": dim, "nx": problem.nx - 2 * problem.cpml,
                      "ny": (problem.ny - 2 * problem.cpml) if problem.is3d else 1,
                      "nz": problem.nz - 2 * problem.cpml, "dx": problem.dx, "dy": problem.dy, "dz": problem.dz,
