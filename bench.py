@@ -345,9 +345,21 @@ def bench_fwi_em(n: int = 512, nt: int = 3000, nshots: int = 8, ncheck: int = 6)
         loss, _ = f.gradient()
         t_grad = time.perf_counter() - t0
         launches = f.launches
-    with Fwi(start, shots[:1], obs[:1]) as f:
-        _, gr = f.gradient()
+    # misfit against FP32 rounding on shot 0 (as for the elastic leg), then
+    # the central-difference check on a start model whose residual is far
+    # above that rounding: eps11, eps33 5% low, sigma11, sigma33 x 1.5
     p0 = dataclasses.replace(start, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    t0_ = dataclasses.replace(true, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    s64, o64 = sg.run(p0, sg.FP64)["traces"], sg.run(t0_, sg.FP64)["traces"]
+    s32 = sg.run(p0, sg.FP32)["traces"]
+    levels = {"residual_rel": float(np.linalg.norm(s64 - o64) / np.linalg.norm(s64)),
+              "fp32_rounding_rel": float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64))}
+    start_fd = with_model(start, e11=0.95 * start.model["e11"], e33=0.95 * start.model["e33"],
+                          s11=1.5 * start.model["s11"], s33=1.5 * start.model["s33"])
+    with Fwi(start_fd, shots[:1], obs[:1]) as f:
+        _, gr = f.gradient()
+    p0 = dataclasses.replace(start_fd, xind=shots[0].xind, zind=shots[0].zind, src={"z": shots[0].srcz})
+    start = start_fd
 
     def loss64(q):
         tr = sg.run(q, sg.FP64)["traces"]
@@ -371,9 +383,10 @@ def bench_fwi_em(n: int = 512, nt: int = 3000, nshots: int = 8, ncheck: int = 6)
                      "rel_err": abs(float(gr[key][cell]) - fd) / abs(fd)})
     return {"gradients_per_s": 1.0 / t_grad, "gradient_s": t_grad, "forward_s": t_fwd,
             "cost_vs_forward": t_grad / t_fwd, "loss": loss, "shots": nshots, "grid": [start.nx, start.nz],
-            "steps": nt, "gpu_launches": launches,
+            "steps": nt, "gpu_launches": launches, "misfit_levels": levels,
             "fd_check": {"max_rel_err": max(e["rel_err"] for e in errs), "cells": errs,
-                         "perturbation": "relative 1e-4, central, FP64 forward (shot 0)"},
+                         "perturbation": "relative 1e-4, central, FP64 forward (shot 0)",
+                         "start_model": "no anomaly, eps11 eps33 x 0.95, sigma11 sigma33 x 1.5"},
             "dtype": "f32 fields, f64 gradient accumulation"}
 
 
