@@ -224,6 +224,8 @@ struct S3Args {
     int bulk_variant;    // FP32: occupancy variant of the bulk stress kernel
     int prefetch;        // FP32: L2 prefetch distance in tiles of the stress kernel (0 = off)
     int prefetch_v;      // FP32: the same for the velocity kernel
+    int pf_d[3];         // `prefetch` as tile offsets (x, y, z) on the 32 x 8 x 1 tile grid
+    int pfv_d[3];        // the same for `prefetch_v`
     const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
     const void* staged_v;  // the same for the staged velocity kernel
     int velocity_minb;     // FP32: CTAs per SM the cell velocity kernel is compiled for (4 .. 8)

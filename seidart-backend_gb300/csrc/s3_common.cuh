@@ -121,6 +121,18 @@ __device__ __forceinline__ void pf_tile_rows(const float* const* arr, int narr, 
     }
 }
 
+// The tile `d` (x, y, z offsets of a distance in launch order) after this
+// CTA's on the launch grid, with carries; false past the last tile.  The host
+// splits the distance once, so no thread divides.
+__device__ __forceinline__ bool tile_ahead(const int (&d)[3], int& tx, int& ty, int& k) {
+    int x = (int)blockIdx.x + d[0], y = (int)blockIdx.y + d[1], z = (int)blockIdx.z + d[2];
+    if (x >= (int)gridDim.x) { x -= gridDim.x; ++y; }
+    if (y >= (int)gridDim.y) { y -= gridDim.y; ++z; }
+    if (z >= (int)gridDim.z) return false;
+    tx = x; ty = y; k = z;
+    return true;
+}
+
 // true when the 32 x 8 tile (tx, ty, k) lies inside the inert interior box,
 // where no CPML memory or coefficient is touched
 __device__ __forceinline__ bool tile_in_box(const BoxH& b, int tx, int ty, int k, int nx, int ny) {

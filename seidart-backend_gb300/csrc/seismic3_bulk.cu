@@ -43,11 +43,11 @@ __global__ void __launch_bounds__(NT) s3b_pack(S3Args<float> A, float* P) {
 // tiles the CPML memories and coefficients.  A hint only: no registers or
 // shared memory stay allocated for it.
 __device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, int tid) {
-    const long gx = gridDim.x, gy = gridDim.y;
-    const long lin = blockIdx.x + gx * (blockIdx.y + gy * (long)blockIdx.z) + dist;
-    if (lin >= gx * gy * (long)gridDim.z) return;
-    const int tx = (int)(lin % gx), ty = (int)((lin / gx) % gy), k = (int)(lin / (gx * gy));
+    (void)dist;  // A.pf_d holds it split into tile offsets
+    int tx, ty, k;
+    if (!tile_ahead(A.pf_d, tx, ty, k)) return;
     if (k < 1 || k > A.nz - 2) return;
+    const size_t lin = (size_t)tx + (size_t)gridDim.x * ((size_t)ty + (size_t)gridDim.y * k);
     if (tid < NCOEF * NT / 32) pf_l2(A.packed + lin * (NCOEF * NT) + tid * 32);
     pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, NT);
     if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {

@@ -110,10 +110,9 @@ __global__ void __launch_bounds__(BX* BY) s3c_stress(S3Args<float> A) {
 // velocities, density, and on shell tiles the velocity-loop memories and the
 // CPML coefficients (a hint; nothing stays allocated for it)
 __device__ __forceinline__ void s3c_velocity_prefetch(const S3Args<float>& A, int dist, int tid) {
-    const long gx = gridDim.x, gy = gridDim.y;
-    const long lin = blockIdx.x + gx * (blockIdx.y + gy * (long)blockIdx.z) + dist;
-    if (lin >= gx * gy * (long)gridDim.z) return;
-    const int tx = (int)(lin % gx), ty = (int)((lin / gx) % gy), k = (int)(lin / (gx * gy));
+    (void)dist;  // A.pfv_d holds it split into tile offsets
+    int tx, ty, k;
+    if (!tile_ahead(A.pfv_d, tx, ty, k)) return;
     pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, BX * BY);
     pf_tile_rows(&A.rho, 1, tx, ty, k, A.nx, A.ny, tid, BX * BY);
     if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {

@@ -797,6 +797,11 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->s3f.prefetch_v = (t && *t >= '0' && *t <= '9') ? atoi(t) : 1216;
         t = getenv("SEIDART_S3_VEL_MINB");
         s->s3f.velocity_minb = (t && *t >= '4' && *t <= '8') ? atoi(t) : 6;  // 6: 1.07 ms vs 1.19 ms at 4 (352^3)
+        // the distances as offsets on the 32 x 8 x 1 tile grid of both kernels
+        const int gx = (s->dom.nx + 31) / 32, gy = (s->dom.ny + 7) / 8;
+        auto split = [&](int d, int* o) { o[0] = d % gx; o[1] = (d / gx) % gy; o[2] = d / (gx * gy); };
+        split(s->s3f.prefetch, s->s3f.pf_d);
+        split(s->s3f.prefetch_v, s->s3f.pfv_d);
     }
     if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_BULK) {
         const char* t = getenv("SEIDART_S3_BULK");
