@@ -506,12 +506,17 @@ def main():
         barrier()
         t0 = time.perf_counter()
         with sg.Solver(pe, sg.FP32) as se:   # host FP64 model, sources and initial fields in
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
             se.step(pe.time_steps)
             se.sync()
+            t2 = time.perf_counter()
             tr_out, nrm_out = se.traces()       # receiver traces and norms out
             f_out = se.get_fields()             # final fields out
+            t3 = time.perf_counter()
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
+        phases = {"setup_s": t1 - t0, "steps_s": t2 - t1, "readback_s": t3 - t2, "teardown_s": t0 + te - t3}
         barrier()
         model_bytes = sum(a.nbytes for a in pe.model_list())
         src_bytes = sum(a.nbytes for a in pe.src_list() if a is not None)
@@ -520,7 +525,7 @@ def main():
         e2e = {"value": world * pe.ncell * pe.time_steps / te / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int((model_bytes + src_bytes + f_bytes) / pe.time_steps),
                "d2h_bytes_per_step": int((f_bytes + tr_bytes) / pe.time_steps),
-               "steps": pe.time_steps, "seconds": te,
+               "steps": pe.time_steps, "seconds": te, "phases": phases,
                "note": "Solver API on host FP64 buffers: upload and FP32 conversion of the model, sources and "
                        "initial fields, 1500 steps, copy-back of final fields, traces and norms"}
 
