@@ -131,7 +131,8 @@ def kernel_bytes(p, box_cells: int) -> dict:
     stress = WORD * (42 * n + 78 * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12; shell: 36 memories R+W + 6 coefficients
     velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
     # z-marching kernels (default) and one-thread-per-cell kernels
-    return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3f_stress": stress, "s3f_velocity": velocity,
+    return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3p_velocity": velocity,
+            "s3f_stress": stress, "s3f_velocity": velocity,
             "s3t_stress": stress, "s3b_stress": stress, "s3x_stress": stress}
 
 

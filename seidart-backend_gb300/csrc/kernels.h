@@ -226,6 +226,8 @@ struct S3Args {
     int prefetch_v;      // FP32: the same for the velocity kernel
     int pf_d[3];         // `prefetch` as tile offsets (x, y, z) on the 32 x 8 x 1 tile grid
     int pfv_d[3];        // the same for `prefetch_v`
+    int pfp_d[3];        // the pair velocity kernel's prefetch distance on its 32 x 16 x 1 tile grid
+    int velocity_pair;   // FP32: 1 = the cell-pair velocity kernel (nx even)
     const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
     const void* staged_v;  // the same for the staged velocity kernel
     int velocity_minb;     // FP32: CTAs per SM the cell velocity kernel is compiled for (4 .. 8)
@@ -258,6 +260,7 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
                           const S3Maps* maps, int stress_kind, int velocity_kind);
 void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st);
 void launch_seismic3_cell_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st);
+void launch_seismic3_pair_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st);
 int seismic3_fast_norm_slots();
 bool seismic3_tma_prepare(const S3Args<float>& a, S3Maps* maps, int variant);
 int seismic3_tma_variants();

@@ -262,6 +262,173 @@ __global__ void __launch_bounds__(BX* BY, MINB) s3c_velocity(S3Args<float> A, St
     }
 }
 
+// ------------------------------------------------ cell-pair variant
+// Each thread updates the two x-adjacent cells (x, x+1), x even, of a
+// 32 x 16 tile (16 x 16 threads).  On lean tiles every input comes from an
+// aligned float2 load that serves both cells -- 29 loads and their address
+// arithmetic per pair instead of 64 -- and the arithmetic per cell is the
+// one-cell kernel's; other tiles run the one-cell path for each cell.
+// Needs nx even (every pair then starts 8 bytes aligned).
+constexpr int PX = 16, PY = 16;     // threads per CTA
+constexpr int TPX = 32, TPY = 16;   // cells per tile
+
+__device__ __forceinline__ float fmax_bits(float a, float b) {
+    // non-negative floats order like their bit patterns; NaN wins
+    return __uint_as_float(max(__float_as_uint(a), __float_as_uint(b)));
+}
+
+// the lean update of one cell from its stencil values (velocity_cell<true>'s
+// expressions); returns the new velocity and the squared norms
+__device__ __forceinline__ void vel_lean_cell(float sxx0, float sxxm1, float sxxm2, float sxy0, float sxyym1,
+                                              float sxyym2, float sxyp1, float sxyp2, float syy0, float syyp1,
+                                              float syyp2, float sxz0, float sxzzm1, float sxzzm2, float sxzp1,
+                                              float sxzp2, float syz0, float syzym1, float syzym2, float syzzm1,
+                                              float syzzm2, float szz0, float szzp1, float szzp2, float r0, float rxm,
+                                              float rxp, float rzm, float rzp, float hx, float hy, float hz,
+                                              float dt, int code, float& vx, float& vy, float& vz, float& vsq,
+                                              float& ssq) {
+    const float byy = inv_mean_f(r0, r0, code);
+    {
+        const float d1 = (27.0f * (sxx0 - sxxm1) + sxxm2) * hx;
+        const float d2 = (27.0f * (sxy0 - sxyym1) + sxyym2) * hy;
+        const float d3 = (27.0f * (sxz0 - sxzzm1) + sxzzm2) * hz;
+        vx = vx + (d1 * inv_mean_f(r0, rxm, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+    }
+    {
+        const float d1 = (27.0f * (sxyp1 - sxy0) - sxyp2) * hx;
+        const float d2 = (27.0f * (syyp1 - syy0) - syyp2) * hy;
+        const float d3 = (27.0f * (syz0 - syzzm1) + syzzm2) * hz;
+        vy = vy + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
+    }
+    {
+        const float d1 = (27.0f * (sxzp1 - sxz0) - sxzp2) * hx;
+        const float d2 = (27.0f * (syz0 - syzym1) + syzym2) * hy;
+        const float d3 = (27.0f * (szzp1 - szz0) - szzp2) * hz;
+        vz = vz + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzp, code)) * dt;
+    }
+    vsq = vx * vx + vy * vy + vz * vz;
+    ssq = sxx0 * sxx0 + syy0 * syy0 + szz0 * szz0 + 2.0f * (sxy0 * sxy0 + syz0 * syz0 + sxz0 * sxz0);
+}
+
+__device__ __forceinline__ void velocity_pair_lean(const S3Args<float>& A, int gx, int gy, int k, float& vsq,
+                                                   float& ssq) {
+    const long sy = A.nx, sz = (long)A.nx * A.ny;
+    const size_t c = (size_t)gx + (size_t)sy * gy + (size_t)sz * k;
+    auto L = [&](const float* base, long off) { return __ldg(reinterpret_cast<const float2*>(base + c + off)); };
+    const float *Sxx = A.f[3], *Sxy = A.f[4], *Sxz = A.f[5], *Syy = A.f[6], *Syz = A.f[7], *Szz = A.f[8], *R = A.rho;
+    const float2 sxx_m = L(Sxx, -2), sxx_0 = L(Sxx, 0);
+    const float2 sxy_0 = L(Sxy, 0), sxy_p = L(Sxy, 2), sxy_y1 = L(Sxy, -sy), sxy_y2 = L(Sxy, -2 * sy);
+    const float2 sxz_0 = L(Sxz, 0), sxz_p = L(Sxz, 2), sxz_z1 = L(Sxz, -sz), sxz_z2 = L(Sxz, -2 * sz);
+    const float2 syy_0 = L(Syy, 0), syy_y1 = L(Syy, sy), syy_y2 = L(Syy, 2 * sy);
+    const float2 syz_0 = L(Syz, 0), syz_y1 = L(Syz, -sy), syz_y2 = L(Syz, -2 * sy), syz_z1 = L(Syz, -sz),
+                 syz_z2 = L(Syz, -2 * sz);
+    const float2 szz_0 = L(Szz, 0), szz_z1 = L(Szz, sz), szz_z2 = L(Szz, 2 * sz);
+    const float2 r_m = L(R, -2), r_0 = L(R, 0), r_p = L(R, 2), r_zm = L(R, -sz), r_zp = L(R, sz);
+    float2* V0 = reinterpret_cast<float2*>(A.f[0] + c);
+    float2* V1 = reinterpret_cast<float2*>(A.f[1] + c);
+    float2* V2 = reinterpret_cast<float2*>(A.f[2] + c);
+    float2 vx = *V0, vy = *V1, vz = *V2;
+    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
+    const float dt = A.dt;
+    const int code = A.density_code;
+    float vs0, ss0, vs1, ss1;
+    // cell x: x-2, x-1 from the pair below, x+1, x+2 from this pair and the next
+    vel_lean_cell(sxx_0.x, sxx_m.y, sxx_m.x, sxy_0.x, sxy_y1.x, sxy_y2.x, sxy_0.y, sxy_p.x, syy_0.x, syy_y1.x,
+                  syy_y2.x, sxz_0.x, sxz_z1.x, sxz_z2.x, sxz_0.y, sxz_p.x, syz_0.x, syz_y1.x, syz_y2.x, syz_z1.x,
+                  syz_z2.x, szz_0.x, szz_z1.x, szz_z2.x, r_0.x, r_m.y, r_0.y, r_zm.x, r_zp.x, hx, hy, hz, dt, code,
+                  vx.x, vy.x, vz.x, vs0, ss0);
+    // cell x+1
+    vel_lean_cell(sxx_0.y, sxx_0.x, sxx_m.y, sxy_0.y, sxy_y1.y, sxy_y2.y, sxy_p.x, sxy_p.y, syy_0.y, syy_y1.y,
+                  syy_y2.y, sxz_0.y, sxz_z1.y, sxz_z2.y, sxz_p.x, sxz_p.y, syz_0.y, syz_y1.y, syz_y2.y, syz_z1.y,
+                  syz_z2.y, szz_0.y, szz_z1.y, szz_z2.y, r_0.y, r_0.x, r_p.x, r_zm.y, r_zp.y, hx, hy, hz, dt, code,
+                  vx.y, vy.y, vz.y, vs1, ss1);
+    __stcs(V0, vx);
+    __stcs(V1, vy);
+    __stcs(V2, vz);
+    vsq = fmax_bits(vs0, vs1);
+    ssq = fmax_bits(ss0, ss1);
+}
+
+// lean test of a 32 x 16 pair tile (the same rules as lean_tile)
+__device__ __forceinline__ bool lean_tile_p(const S3Args<float>& A, int x0, int y0, int k) {
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    if (!(x0 >= 2 && x0 + TPX - 1 <= nx - 3 && y0 >= 2 && y0 + TPY - 1 <= ny - 3 && k >= 2 && k <= nz - 3)) return false;
+    if (!(x0 >= A.box.i0 && x0 + TPX <= A.box.i1 && y0 >= A.box.j0 && y0 + TPY <= A.box.j1 && k >= A.box.k0 &&
+          k < A.box.k1))
+        return false;
+    const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
+    if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + TPX && js + 1 >= y0 && js < y0 + TPY) return false;
+    return true;
+}
+
+// L2 prefetch for the pair tile `A.pfp_d` tiles later (16 rows per tile)
+__device__ __forceinline__ void s3p_velocity_prefetch(const S3Args<float>& A, int tid) {
+    int tx, ty, k;
+    if (!tile_ahead(A.pfp_d, tx, ty, k)) return;
+    for (int half = 0; half < 2; ++half) {
+        const int ty8 = 2 * ty + half;  // the two 32 x 8 row blocks of the tile
+        pf_tile_rows(A.f, 9, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
+        pf_tile_rows(&A.rho, 1, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
+        if (!tile_in_box(A.box, tx, ty8, k, A.nx, A.ny)) {
+            pf_tile_rows(A.mem + 36, 9, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
+            pf_tile_rows(A.cpml, 6, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
+        }
+    }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, StepInfo si) {
+    __shared__ unsigned redu[2 * PX * PY / 32];
+    __shared__ double redd[2][PX * PY / 32];
+    const int tid = threadIdx.y * PX + threadIdx.x;
+    if (A.prefetch_v > 0) s3p_velocity_prefetch(A, tid);
+    const int it = *si.step;
+    const int x0 = blockIdx.x * TPX + 2 * threadIdx.x, gy = blockIdx.y * TPY + threadIdx.y, k = blockIdx.z;
+    const int nx = A.nx, ny = A.ny;
+    float vsq = 0.f, ssq = 0.f;
+    if (lean_tile_p(A, blockIdx.x * TPX, blockIdx.y * TPY, k)) {
+        velocity_pair_lean(A, x0, gy, k, vsq, ssq);
+    } else if (gy < ny) {
+        float w[9];
+        for (int q = 0; q < 2; ++q) {
+            if (x0 + q >= nx) break;
+            float vs = 0.f, ss = 0.f;
+            velocity_cell<false>(A, it, x0 + q, gy, k, vs, ss, w);
+            vsq = fmax_bits(vsq, vs);
+            ssq = fmax_bits(ssq, ss);
+        }
+    }
+    // FP64 fallback (a square at or above 3e38): exact norms of this thread's
+    // cells, read back (its own writes) -- a blow-up path
+    auto exact = [&](bool stress) {
+        double m = 0.0;
+        if (gy >= ny) return m;
+        for (int q = 0; q < 2; ++q) {
+            if (x0 + q >= nx) break;
+            const size_t c = (size_t)(x0 + q) + (size_t)nx * ((size_t)gy + (size_t)ny * k);
+            double n;
+            if (!stress) {
+                const double a = A.f[0][c], b = A.f[1][c], d = A.f[2][c];
+                n = sqrt(a * a + b * b + d * d);
+            } else {
+                const double s1 = A.f[3][c], s2 = A.f[6][c], s3 = A.f[8][c], s4 = A.f[4][c], s5 = A.f[7][c],
+                             s6 = A.f[5][c];
+                n = sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+            }
+            m = nanmax(m, n);
+        }
+        return m;
+    };
+    double vn, sn;
+    block_norm2_f32<PX * PY / 32>(vsq, ssq, [&] { return exact(false); }, [&] { return exact(true); }, redu,
+                                  &redd[0][0], vn, sn);
+    if (tid == 0) {
+        const int slot = (blockIdx.x + 7 * blockIdx.y + 13 * blockIdx.z) % NSLOT;
+        atomic_max_nonneg(A.norms_part + slot, vn);
+        atomic_max_nonneg(A.norms_part + NSLOT + slot, sn);
+    }
+}
+
 // ------------------------------------------------ fully staged variant
 // The velocity half-step with every per-cell input staged in shared memory
 // by tensor-tile copies before any thread computes: the five stresses with
@@ -449,6 +616,17 @@ bool seismic3_staged_velocity_prepare(const S3Args<float>& a, S3XMaps* m) {
 
 void launch_seismic3_staged_velocity(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st) {
     s3x_velocity<<<dim3((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nz), dim3(BX, BY), XV_BYTES, st>>>(a, s, maps);
+}
+
+void launch_seismic3_pair_velocity(const S3Args<float>& a, const StepInfo& s, cudaStream_t st) {
+    const dim3 grd((a.nx + TPX - 1) / TPX, (a.ny + TPY - 1) / TPY, a.nz), blk(PX, PY);
+    switch (a.velocity_minb) {
+    case 5: s3p_velocity<5><<<grd, blk, 0, st>>>(a, s); break;
+    case 6: s3p_velocity<6><<<grd, blk, 0, st>>>(a, s); break;
+    case 7: s3p_velocity<7><<<grd, blk, 0, st>>>(a, s); break;
+    case 8: s3p_velocity<8><<<grd, blk, 0, st>>>(a, s); break;
+    default: s3p_velocity<4><<<grd, blk, 0, st>>>(a, s); break;
+    }
 }
 
 void launch_seismic3_cell_stress(const S3Args<float>& a, cudaStream_t st) {

@@ -406,6 +406,9 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
     } else if (velocity_kind == S3K_ZMARCH) {
         s3f_velocity<<<grd, blk, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 1, "s3f_velocity");
+    } else if (a.velocity_pair) {
+        launch_seismic3_pair_velocity(a, s, st);
+        if (h) h->fn(h->ctx, 1, "s3p_velocity");
     } else {
         launch_seismic3_cell_velocity(a, s, st);
         if (h) h->fn(h->ctx, 1, "s3c_velocity");

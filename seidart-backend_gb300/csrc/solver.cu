@@ -802,6 +802,17 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         auto split = [&](int d, int* o) { o[0] = d % gx; o[1] = (d / gx) % gy; o[2] = d / (gx * gy); };
         split(s->s3f.prefetch, s->s3f.pf_d);
         split(s->s3f.prefetch_v, s->s3f.pfv_d);
+        // cell-pair velocity kernel (two x-adjacent cells per thread, float2
+        // loads) when every pair is 8-byte aligned; SEIDART_S3_VPAIR=0 turns it off
+        t = getenv("SEIDART_S3_VPAIR");
+        s->s3f.velocity_pair = (s->dom.nx % 2 == 0) && !(t && *t == '0');
+        // the pair kernel holds two cells per thread: 4 CTAs per SM (352^3: 0.995 ms
+        // against 1.14 ms at 5 and 1.015 ms for the one-cell kernel at 6)
+        if (s->s3f.velocity_pair && !getenv("SEIDART_S3_VEL_MINB")) s->s3f.velocity_minb = 4;
+        t = getenv("SEIDART_S3_PFP");
+        const int pfp = (t && *t >= '0' && *t <= '9') ? atoi(t) : 608;
+        const int gy2 = (s->dom.ny + 15) / 16;
+        s->s3f.pfp_d[0] = pfp % gx; s->s3f.pfp_d[1] = (pfp / gx) % gy2; s->s3f.pfp_d[2] = pfp / (gx * gy2);
     }
     if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_BULK) {
         const char* t = getenv("SEIDART_S3_BULK");

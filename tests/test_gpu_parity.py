@@ -160,3 +160,21 @@ def test_electromag3_initial_fields_and_interior_box(oracle):
     for q, nm in enumerate(("Ex", "Ey", "Ez")):
         p.fields0[nm] = np.asfortranarray(rng.normal(0, 1e-3, p.shape))
     assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
+
+
+def test_seismic3_fp32_velocity_pair_kernel(oracle, monkeypatch):
+    """The cell-pair velocity kernel (two x-adjacent cells per thread, float2
+    loads on lean tiles) against the one-cell kernel and the oracle, on a grid
+    with lean tiles, a source inside and an odd tile tail in y."""
+    p = models.seismic3_layers(n=72, cpml=8, nt=30, nlayers=3, nrec_side=4, rec_z=3, src_z=30, ny=58)
+    p.src["x"] = 0.5 * p.src["z"]
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("SEIDART_S3_VPAIR", flag)
+        out[flag] = sg.run(p, sg.FP32)
+    for a, b in zip(out["0"]["fields"], out["1"]["fields"]):
+        assert rel_l2(b, a) <= 1e-6
+    assert rel_l2(out["1"]["norms"], out["0"]["norms"]) <= 1e-6
+    o = oracle.run_oracle(p)
+    for q in range(9):
+        assert rel_l2(out["1"]["fields"][q], o["fields"][q]) <= FP32_TOL, q
