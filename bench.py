@@ -478,27 +478,6 @@ def main():
     tr32, _ = s.traces()
     s.close()
 
-    extra = {}
-    if not args.no_fp64 and rank == 0:
-        # FP64 drop-in path on the same workload and the FP32-vs-FP64 error
-        s64 = sg.Solver(p, sg.FP64)
-        s64.step(args.warmup)
-        s64.sync()
-        k64 = min(args.steps, 40)
-        pr64 = s64.profile(k64)
-        s64.step(args.steps - k64)
-        s64.sync()
-        tr64, _ = s64.traces()
-        f64 = s64.get_fields()
-        s64.close()
-        extra["fp64_plain"] = {"value": p.ncell * k64 / (pr64["total_ms"] / 1e3) / 1e9, "unit": UNIT,
-                               "steps": k64}
-        extra["fp32_vs_fp64"] = {
-            "traces_rel_l2": float(np.linalg.norm(tr32 - tr64) / max(np.linalg.norm(tr64), 1e-300)),
-            "vz_rel_l2": float(np.linalg.norm(fp32_fields[2] - f64[2]) / max(np.linalg.norm(f64[2]), 1e-300)),
-            "steps": args.warmup + args.steps}
-        extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
-
     e2e = None
     if not args.no_e2e:
         # through the C ABI with host buffers: one full reference-length run
@@ -529,6 +508,27 @@ def main():
                "steps": pe.time_steps, "seconds": te, "phases": phases,
                "note": "Solver API on host FP64 buffers: upload and FP32 conversion of the model, sources and "
                        "initial fields, 1500 steps, copy-back of final fields, traces and norms"}
+
+    extra = {}
+    if not args.no_fp64 and rank == 0:
+        # FP64 drop-in path on the same workload and the FP32-vs-FP64 error
+        s64 = sg.Solver(p, sg.FP64)
+        s64.step(args.warmup)
+        s64.sync()
+        k64 = min(args.steps, 40)
+        pr64 = s64.profile(k64)
+        s64.step(args.steps - k64)
+        s64.sync()
+        tr64, _ = s64.traces()
+        f64 = s64.get_fields()
+        s64.close()
+        extra["fp64_plain"] = {"value": p.ncell * k64 / (pr64["total_ms"] / 1e3) / 1e9, "unit": UNIT,
+                               "steps": k64}
+        extra["fp32_vs_fp64"] = {
+            "traces_rel_l2": float(np.linalg.norm(tr32 - tr64) / max(np.linalg.norm(tr64), 1e-300)),
+            "vz_rel_l2": float(np.linalg.norm(fp32_fields[2] - f64[2]) / max(np.linalg.norm(f64[2]), 1e-300)),
+            "steps": args.warmup + args.steps}
+        extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
