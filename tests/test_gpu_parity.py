@@ -178,3 +178,36 @@ def test_seismic3_fp32_velocity_pair_kernel(oracle, monkeypatch):
     o = oracle.run_oracle(p)
     for q in range(9):
         assert rel_l2(out["1"]["fields"][q], o["fields"][q]) <= FP32_TOL, q
+
+
+def test_seismic3_fp32_odd_sizes(oracle):
+    """Odd nx and ny: the staged stress and the cell-pair velocity kernels
+    need nx % 4 == 0 and nx even, so the bulk-copy stress and the one-cell
+    velocity kernels run (ragged last tiles in x and y)."""
+    p = models.seismic3_layers(n=35, cpml=5, nt=30, nlayers=2, nrec_side=3, rec_z=3, src_z=6, ny=29)
+    assert p.nx % 2 == 1 and p.ny % 2 == 1
+    o = oracle.run_oracle(p)
+    g = sg.run(p, sg.FP32)
+    for q in range(9):
+        assert rel_l2(g["fields"][q], o["fields"][q]) <= FP32_TOL, q
+    assert rel_l2(g["norms"], o["norms"]) <= FP32_TOL
+
+
+@pytest.mark.parametrize("name", ["seismic2", "electromag3"])
+def test_zero_steps_is_a_clean_error(name):
+    """time_steps = 0 is refused with SEIDART_ERR_ARG (the reference would
+    loop zero times); the context stays usable."""
+    from dataclasses import replace
+    p = replace(PROBLEMS[name], time_steps=0, src={})
+    with pytest.raises(sg.SeidartError, match="time_steps"):
+        sg.run(p, sg.FP64)
+    g = sg.run(replace(PROBLEMS[name], time_steps=2, src={}), sg.FP64)
+    assert g["traces"].shape[0] == 2
+
+
+def test_electromag3_no_cpml_source_on_face(oracle):
+    """electromag3 with cpml = 0 (no PML; every cell inside the box) and the
+    source on a Dirichlet face: injected, then zeroed, as in the reference."""
+    p = models.electromag3_blocks(n=14, cpml=0, nt=20, nblocks=2, nrec_side=2, f0=8e8)
+    p.xind = 1  # source cell x = 1 (1-based): the low-x face
+    assert_exact(sg.run(p, sg.FP64), oracle.run_oracle(p))
