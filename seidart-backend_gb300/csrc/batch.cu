@@ -236,8 +236,11 @@ __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, in
     return vx * vx + vz * vz;
 }
 
-template <int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) s2b_persistent(BatchArgs B, int nsteps) {
+// MINB CTAs per SM bound the registers: 1024 threads per SM leave 64
+// registers per thread (capping them lower, 32 or 40, with 6 or 8 CTAs of
+// 256 threads, measured slower on the 64-model batch: spills)
+template <int TX, int TY, int MINB = 1024 / (TX * TY)>
+__global__ void __launch_bounds__(TX* TY, MINB) s2b_persistent(BatchArgs B, int nsteps) {
     __shared__ double red[TX * TY / 32];
     __shared__ float redf[TX * TY / 32];
     const int it0 = *B.step;
@@ -338,8 +341,8 @@ struct WarpNorm {
 // its tiles mostly share one model (descriptor stays in L1) and neighbouring
 // tile rows stay in L2; the rows of tile t+PD are prefetched while tile t
 // computes.
-template <int TX, int TY, int PD>
-__global__ void __launch_bounds__(TX* TY) s2b_chunked(BatchArgs B, int nsteps) {
+template <int TX, int TY, int PD, int MINB = 1024 / (TX * TY)>
+__global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nsteps) {
     const int tid = threadIdx.x + TX * threadIdx.y, lane = tid & 31;
     const int t0 = (int)((long long)B.ntiles * blockIdx.x / gridDim.x);
     const int t1 = (int)((long long)B.ntiles * (blockIdx.x + 1) / gridDim.x);
@@ -596,8 +599,11 @@ int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, 
             if (bps < 1 || (q == 1 && cand[1] == cand[0])) continue;
             const int ctl0[4] = {1, 0, 0, 0};
             cudaMemcpyAsync(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice, b->stream);
+            // an untimed two-step launch first (caches, descriptors, clocks), then the timed trial
+            int rc = launch_chunk(b, v, bps, std::min(2, trial_steps), 0);
+            cudaMemcpyAsync(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice, b->stream);
             cudaEventRecord(e0, b->stream);
-            int rc = launch_chunk(b, v, bps, trial_steps, 0);
+            if (rc == SEIDART_OK) rc = launch_chunk(b, v, bps, trial_steps, 0);
             cudaEventRecord(e1, b->stream);
             int st = 0;
             if (rc == SEIDART_OK) rc = read_status(b, &st);

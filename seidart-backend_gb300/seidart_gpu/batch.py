@@ -56,7 +56,7 @@ def _check(rc):
 
 
 class Batch:
-    def __init__(self, problems: list[Problem], autotune: bool = True, trial_steps: int = 8):
+    def __init__(self, problems: list[Problem], autotune: bool = True, trial_steps: int = 24):
         _declare()
         L = lib()
         if not problems or any(p.family != SEISMIC2 for p in problems):
