@@ -405,6 +405,10 @@ def main():
     ap.add_argument("--fwi-profile-case", action="store_true",
                     help="run one small misfit gradient (552^2 grid, 4 shots, 240 steps) and exit: the case "
                          "the FWI launch list in profiles/ is captured on")
+    ap.add_argument("--batch-profile-case", action="store_true",
+                    help="run a small ragged batch (16 models of the batch workload's distribution, 40 steps in "
+                         "launches of 20, the autotuned kernel) and exit: the case the batch profile in profiles/ "
+                         "is captured on")
     ap.add_argument("--grid", type=int, default=WORKLOAD["n"],
                     help="interior cells per axis (default 320: the 3D configuration)")
     args = ap.parse_args()
@@ -417,6 +421,15 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.batch_profile_case:
+        from seidart_gpu import models
+        from seidart_gpu.batch import Batch
+        ps = models.batch_layered_vti(nmodels=16, nt=40)
+        with Batch(ps, autotune=True) as b:
+            b.step(40, chunk=20)
+            b.sync()
+            print(json.dumps({"batch_profile_case": "ok", "config": b.config()}))
         return
     if args.fwi_profile_case:
         from seidart_gpu import models
