@@ -24,7 +24,8 @@ import numpy as np
 
 from ._lib import SeidartError, lib
 
-__all__ = ["seismic2", "seismic25", "electromag2", "electromag25", "electromag2c", "electromag25c"]
+__all__ = ["seismic2", "seismic25", "electromag2", "electromag25", "electromag2c", "electromag25c",
+           "permittivity_write", "permittivity_write_c", "stiffness_write", "attenuation_write"]
 
 _DECL = False
 
@@ -99,3 +100,40 @@ def electromag25(nx, ny, nz, dx, dy, dz, src, npoints_pml, nstep, single_output=
 
 def electromag25c(nx, ny, nz, dx, dy, dz, src, npoints_pml, nstep, single_output=True):
     _call3("electromag25c_", nx, ny, nz, dx, dy, dz, src, npoints_pml, nstep, single_output)
+
+
+# ---------------------------------------------------------- material writers
+# The binding's writers take (im, mlist, npoints_pml, nx, nz)
+# (legacy/cpmlfdtd_wrapper.c:19-137) and write the padded .dat records into
+# the working directory.  Fortran reads im(nx, nz) from the array's memory,
+# x fastest, so the image is taken the same way here; the table is the
+# (nmat, ncol) array.  The binding's prototypes drop stiffness_write's
+# gradient and attenuation_write's cpmlvalue; both are keyword arguments here.
+def _image(im, nx, nz):
+    a = np.ascontiguousarray(im, dtype=np.int32).reshape(-1)
+    if a.size != nx * nz:
+        raise ValueError(f"im holds {a.size} cells, expected nx * nz = {nx * nz}")
+    return a.reshape((nx, nz), order="F")
+
+
+def permittivity_write(im, mlist, npoints_pml, nx, nz):
+    from . import material
+    material.permittivity_write(".", _image(im, nx, nz), np.asarray(mlist, dtype=np.float64), int(npoints_pml))
+
+
+def permittivity_write_c(im, mlist, npoints_pml, nx, nz):
+    from . import material
+    material.permittivity_write(".", _image(im, nx, nz), np.asarray(mlist, dtype=np.complex128), int(npoints_pml),
+                                complex_valued=True)
+
+
+def stiffness_write(im, mlist, npoints_pml, nx, nz, gradient=None):
+    from . import material
+    g = None if gradient is None else np.asarray(gradient, dtype=np.float64).reshape((nx, nz), order="F")
+    material.stiffness_write(".", _image(im, nx, nz), np.asarray(mlist, dtype=np.float64), int(npoints_pml), g)
+
+
+def attenuation_write(im, alist, npoints_pml, nx, nz, cpmlvalue=0.0):
+    from . import material
+    material.attenuation_write(".", _image(im, nx, nz), np.asarray(alist, dtype=np.float64), int(npoints_pml),
+                               float(cpmlvalue))

@@ -108,3 +108,19 @@ def test_bad_material_id_is_rejected():
     im[2, 2] = 99
     with pytest.raises(SeidartError, match="not a table row"):
         material.stiffness_arrays(im, table, 2)
+
+
+def test_legacy_module_writers(tmp_path, monkeypatch):
+    """seidart_gpu.cpmlfdtd's writers take the binding's (im, mlist,
+    npoints_pml, nx, nz) and read im from memory x fastest, like Fortran."""
+    from seidart_gpu import cpmlfdtd, material
+    im, table = _case(8)
+    nx, nz = im.shape
+    monkeypatch.chdir(tmp_path)
+    cpmlfdtd.stiffness_write(np.asfortranarray(im).reshape(-1, order="F"), table, 2, nx, nz)
+    want = material.stiffness_arrays(im, table, 2)
+    rec = read_record(tmp_path / "c33.dat", np.float64).reshape(want["c33"].shape, order="F")
+    assert np.array_equal(rec, want["c33"])
+    cpmlfdtd.attenuation_write(np.asfortranarray(im).reshape(-1, order="F"), table[:, :3], 3, nx, nz, cpmlvalue=7.5)
+    g = read_record(tmp_path / "gamma_x.dat", np.float64).reshape((nx + 6, nz + 6), order="F")
+    assert g[0, 0] == 7.5
