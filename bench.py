@@ -14,6 +14,9 @@ grid (stress half-step + velocity half-step, source, Dirichlet faces, norms,
   roofline  dominant kernel: algorithmic bytes per launch / its CUDA-event time
   cpu_baseline  the CPU restatement (reference production flags, OpenMP) on a
             bounded sample of the same workload
+  configs_2d  the two 2D workloads at full length: seismic2 256^2 + 20 CPML
+            (2000 steps; FP64 plain, FP32 and the CPU restatement) and
+            electromag2 1024^2 + 20 CPML (4000 steps; FP64 and FP32)
   batched   the ragged multi-model 2D workload: 64 seismic2 models with nx, nz
             in [256, 1024], 3000 steps, one persistent launch per graph chunk
             with autotuned tiles; beside it the same models run one by one
@@ -200,6 +203,80 @@ def cpu_baseline_sample(p=None, budget_s: float = 20.0) -> dict:
     dt = time.perf_counter() - t0
     return {"value": p.ncell * n / dt / 1e9, "unit": UNIT, "cores": orc.load("omp").oracle_threads(), "kind": "port",
             "sample": f"{n} full time steps of the {p.nx}^3 grid after 1 untimed step (FP64, OpenMP, reference flags)"}
+
+
+def _timed_run(p, precision, warm: int = 10) -> dict:
+    """Whole run of problem p through the Solver API: `warm` untimed steps,
+    then the remaining steps timed with CUDA events on the solver's stream."""
+    import torch
+    import seidart_gpu as sg
+    st = torch.cuda.Stream()
+    with sg.Solver(p, precision) as s:
+        s.set_stream(st.cuda_stream)
+        s.step(warm)
+        s.sync()
+        l0 = s.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        s.step(p.time_steps - warm)
+        e1.record(st)
+        s.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        tr, _ = s.traces()
+        launches = s.launches - l0
+    return {"ms": ms, "steps": p.time_steps - warm, "traces": tr, "launches": launches}
+
+
+def bench_2d_configs() -> dict:
+    """The two 2D workloads, each run for its full length.
+
+    seismic2 two-layer (256^2 + 20 CPML, 2000 steps): FP64 plain and FP32 on
+    the GPU, and the OpenMP CPU restatement (reference flags, all host
+    cores) on the same 2000 steps.  electromag2 blocks (1024^2 + 20 CPML,
+    12 blocks, 4000 steps): FP64 and FP32.  Both also run the fast FP64 build
+    (FP64 fields, reciprocals and FMA contraction).  Bytes per step follow the
+    algorithmic count (seismic2: 20 words per cell + 30 per CPML cell;
+    electromag2: 12 + 14); both working sets fit in the 129 MB L2 (2.4 MB
+    and 59 MB per FP32 step), so the fraction of the HBM peak can pass 1."""
+    import seidart_gpu as sg
+    from oracle import oracle as orc
+    from seidart_gpu import models
+    hbm, _ = peaks()
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+    out = {}
+    cases = [("seismic2_256", models.seismic2_two_layer(), 256, 20, 30),
+             ("electromag2_1024", models.electromag2_blocks(nblocks=12), 1024, 12, 14)]
+    for name, p, n_int, w_cell, w_shell in cases:
+        shell = p.ncell - n_int * n_int
+        r = {"grid": [p.nx, p.nz], "cells": p.ncell, "steps": p.time_steps, "seed": p.meta.get("seed")}
+        runs = {}
+        for prec, word, key in ((sg.FP64, 8, "fp64_plain"), (sg.FP64_FAST, 8, "fp64_fast"), (sg.FP32, 4, "fp32")):
+            t = _timed_run(p, prec)
+            runs[key] = t
+            gbs = word * (w_cell * p.ncell + w_shell * shell) * t["steps"] / (t["ms"] / 1e3) / 1e9
+            r[key] = {"value": p.ncell * t["steps"] / (t["ms"] / 1e3) / 1e9, "unit": UNIT,
+                      "ms_per_step": t["ms"] / t["steps"], "algorithmic_gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
+                      "gpu_launches": t["launches"]}
+        r["fp32_vs_fp64_traces_rel_l2"] = rel(runs["fp32"]["traces"], runs["fp64_plain"]["traces"])
+        r["fp64_fast_vs_fp64_traces_rel_l2"] = rel(runs["fp64_fast"]["traces"], runs["fp64_plain"]["traces"])
+        r["fp32_speedup_vs_fp64"] = r["fp32"]["value"] / r["fp64_plain"]["value"]
+        if name.startswith("seismic2"):
+            st = orc.OracleState(p, kind="omp")
+            t0 = time.perf_counter()
+            st.step(p.time_steps)
+            dt = time.perf_counter() - t0
+            r["cpu_restatement"] = {"value": p.ncell * p.time_steps / dt / 1e9, "unit": UNIT,
+                                    "cores": orc.load("omp").oracle_threads(), "kind": "port", "seconds": dt,
+                                    "sample": f"all {p.time_steps} steps (FP64, OpenMP, reference flags)"}
+            r["fp64_vs_cpu_traces_rel_l2"] = rel(runs["fp64_plain"]["traces"], st.result()["traces"])
+            r["fp64_speedup_vs_cpu"] = r["fp64_plain"]["value"] / r["cpu_restatement"]["value"]
+        out[name] = r
+    return out
 
 
 def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
@@ -402,6 +479,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-fwi", action="store_true")
+    ap.add_argument("--no-2d", action="store_true", help="skip the seismic2 256^2 and electromag2 1024^2 runs")
     ap.add_argument("--fwi-profile-case", action="store_true",
                     help="run one small misfit gradient (552^2 grid, 4 shots, 240 steps) and exit: the case "
                          "the FWI launch list in profiles/ is captured on")
@@ -542,10 +620,24 @@ def main():
             "vz_rel_l2": float(np.linalg.norm(fp32_fields[2] - f64[2]) / max(np.linalg.norm(f64[2]), 1e-300)),
             "steps": args.warmup + args.steps}
         extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
+        # FP64 fields with the fast arithmetic (reciprocals, FMA): same steps, error against the exact path
+        sx = sg.Solver(p, sg.FP64_FAST)
+        sx.step(args.warmup)
+        sx.sync()
+        prx = sx.profile(k64)
+        sx.step(args.steps - k64)
+        sx.sync()
+        trx, _ = sx.traces()
+        sx.close()
+        extra["fp64_fast"] = {"value": p.ncell * k64 / (prx["total_ms"] / 1e3) / 1e9, "unit": UNIT, "steps": k64,
+                              "traces_rel_l2_vs_fp64": float(np.linalg.norm(trx - tr64) /
+                                                             max(np.linalg.norm(tr64), 1e-300))}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline_sample(p)
+    if not args.no_2d and rank == 0:
+        extra["configs_2d"] = bench_2d_configs()
     if not args.no_batch and rank == 0:
         extra["batched"] = bench_batch()
     if not args.no_fwi and rank == 0:

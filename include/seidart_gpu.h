@@ -50,6 +50,9 @@ extern "C" {
 /* precision of the field arrays and stencil arithmetic */
 #define SEIDART_FP64 0   /* drop-in path: same operation order as the reference */
 #define SEIDART_FP32 1   /* fast path: FP32 fields, FP64 set-up of coefficients */
+#define SEIDART_FP64_FAST 2  /* FP64 fields with the fast path's arithmetic (host reciprocals,
+                                FMA contraction): not bit-identical to the reference's operation
+                                order, within 1e-12 relative L2 of it */
 
 /* density face averaging, src/fortran/averaging.f08:5-25 (scalar_mean codes) */
 #define SEIDART_DENSITY_HARMONIC   1

@@ -1,9 +1,12 @@
 // common.cuh -- shared device helpers for the CPML-FDTD kernels.
 //
-// Each solver .cu file is compiled twice: with SEIDART_REAL=double and
+// Each solver .cu file is compiled three times: with SEIDART_REAL=double and
 // --fmad=false (the drop-in FP64 path, which keeps the reference's expression
-// trees so results are reproducible operation by operation), and with
-// SEIDART_REAL=float and FMA contraction on (the fast FP32 path).
+// trees so results are reproducible operation by operation), with
+// SEIDART_REAL=double, SEIDART_FAST64 and FMA contraction (FP64 fields with
+// the fast path's arithmetic: host-side reciprocals instead of divisions,
+// contracted multiply-adds, FP64 norms), and with SEIDART_REAL=float and FMA
+// contraction (the fast FP32 path).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -15,12 +18,20 @@ typedef SEIDART_REAL real;
 
 #define SD_CAT2(a, b) a##b
 #define SD_CAT(a, b) SD_CAT2(a, b)
+// SD_EXACT: the reference's divisions and operation order; SD_F32: FP32
+// storage and FP32 norm reductions
 #if defined(SEIDART_FP32)
 #define SD_SUFFIX _f32
 #define SD_EXACT 0
+#define SD_F32 1
+#elif defined(SEIDART_FAST64)
+#define SD_SUFFIX _f64x
+#define SD_EXACT 0
+#define SD_F32 0
 #else
 #define SD_SUFFIX _f64
 #define SD_EXACT 1
+#define SD_F32 0
 #endif
 // launcher names carry the precision suffix so both builds link into one library
 #define SD_NAME(n) SD_CAT(n, SD_SUFFIX)
@@ -56,6 +67,15 @@ __device__ __forceinline__ float inv_mean_f(float a, float b, int code) {
     case 2: return rsqrtf(a * b);
     case 3: return __fdividef(2.0f, a + b);
     default: return __frcp_rn(a);
+    }
+}
+// fast FP64 path: the same reciprocal forms in FP64 (one division per face)
+__device__ __forceinline__ double inv_mean_f(double a, double b, int code) {
+    switch (code) {
+    case 1: return (a + b) / (2.0 * a * b);
+    case 2: return 1.0 / sqrt(a * b);
+    case 3: return 2.0 / (a + b);
+    default: return 1.0 / a;
     }
 }
 

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(BX* BY) e2_e(E2Args<real> a, StepInfo si) {
         if (i == 1 || i == nx || j == 1 || j == nz) { ex = 0; ez = 0; }
         a.f[0][c] = ex;
         a.f[1][c] = ez;
-#if SD_EXACT
+#if !SD_F32
         nrm = sqrt((double)ex * (double)ex + (double)ez * (double)ez);
 #else
         sq = ex * ex + ez * ez; n0 = ex; n1 = ez;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(BX* BY) e2_e(E2Args<real> a, StepInfo si) {
         // plane-wave face cells: their norm is taken after the injection
         if (a.pw.on && pw_cell(a.pw, i - 1, 0, j - 1)) { nrm = 0.0; sq = 0.f; n0 = 0.f; n1 = 0.f; }
     }
-#if SD_EXACT
+#if !SD_F32
     nrm = block_max<BX * BY / 32>(nrm, red);
 #else
     __shared__ float redf[BX * BY / 32];

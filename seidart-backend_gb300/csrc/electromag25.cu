@@ -18,7 +18,7 @@ struct cx {
     real re, im;
 };
 __device__ __forceinline__ cx ld(const real* a, size_t c) {
-#if SD_EXACT
+#if !SD_F32
     const double2 v = reinterpret_cast<const double2*>(a)[c];
 #else
     const float2 v = reinterpret_cast<const float2*>(a)[c];
@@ -26,7 +26,7 @@ __device__ __forceinline__ cx ld(const real* a, size_t c) {
     return cx{v.x, v.y};
 }
 __device__ __forceinline__ void stc(real* a, size_t c, cx z) {
-#if SD_EXACT
+#if !SD_F32
     reinterpret_cast<double2*>(a)[c] = make_double2(z.re, z.im);
 #else
     reinterpret_cast<float2*>(a)[c] = make_float2(z.re, z.im);
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(BX* BY) e25_e(E25Args<real> a, StepInfo si) {
         stc(a.f[0], c, ex);
         stc(a.f[1], c, ey);
         stc(a.f[2], c, ez);
-#if SD_EXACT
+#if !SD_F32
         const double n1 = (double)ex.re * ex.re + (double)ex.im * ex.im;
         const double n2 = (double)ey.re * ey.re + (double)ey.im * ey.im;
         const double n3 = (double)ez.re * ez.re + (double)ez.im * ez.im;
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(BX* BY) e25_e(E25Args<real> a, StepInfo si) {
         w[0] = ex.re; w[1] = ex.im; w[2] = ey.re; w[3] = ey.im; w[4] = ez.re; w[5] = ez.im;
 #endif
     }
-#if SD_EXACT
+#if !SD_F32
     nrm = block_max<BX * BY / 32>(nrm, red);
 #else
     __shared__ float redf[BX * BY / 32];

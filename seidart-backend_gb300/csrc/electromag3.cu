@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(BX* BY) e3_e(E3Args<real> a, StepInfo si) {
         a.f[0][c] = ex;
         a.f[1][c] = ey;
         a.f[2][c] = ez;
-#if SD_EXACT
+#if !SD_F32
         nrm = sqrt((double)ex * (double)ex + (double)ey * (double)ey + (double)ez * (double)ez);
 #else
         sq = ex * ex + ey * ey + ez * ez; n0 = ex; n1 = ey; n2 = ez;
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(BX* BY) e3_e(E3Args<real> a, StepInfo si) {
         // plane-wave face cells: their norm is taken after the injection
         if (a.pw.on && pw_cell(a.pw, i - 1, j - 1, k - 1)) { nrm = 0.0; sq = 0.f; n0 = n1 = n2 = 0.f; }
     }
-#if SD_EXACT
+#if !SD_F32
     nrm = block_max<BX * BY / 32>(nrm, red);
 #else
     __shared__ float redf[BX * BY / 32];

@@ -843,7 +843,7 @@ void electromag25c_(int nx, int ny, int nz, double dx, double dy, double dz, int
 
 // ------------------------------------------------------------------- CLI
 // seidartfdtd <input.json> [seismic=true|false] [density_method=...]
-// (src/fortran/main.f08:31-119); extra flags precision=fp64|fp32 and
+// (src/fortran/main.f08:31-119); extra flags precision=fp64|fp64fast|fp32 and
 // snapshots=true|false are accepted, defaults keep the reference behaviour.
 int seidart_cli_main(int argc, char** argv) {
     if (argc < 2) {
@@ -871,7 +871,8 @@ int seidart_cli_main(int argc, char** argv) {
         const std::string k = trim(arg.substr(0, eq)), v = trim(arg.substr(eq + 1));
         if (k == "seismic") { if (v == "true") seismic = true; else if (v == "false") seismic = false; }
         else if (k == "density_method") density = v;
-        else if (k == "precision") precision = (v == "fp32") ? SEIDART_FP32 : SEIDART_FP64;
+        else if (k == "precision")
+            precision = v == "fp32" ? SEIDART_FP32 : v == "fp64fast" ? SEIDART_FP64_FAST : SEIDART_FP64;
         else if (k == "snapshots") snaps = v != "false";
     }
     int code = 0;

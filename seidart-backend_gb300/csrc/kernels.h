@@ -72,6 +72,7 @@ struct S2Args {
     PwDev pw;              // plane-wave source (pw.on = 0: point sources)
 };
 void launch_seismic2_f64(const S2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic2_f64x(const S2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic2_f32(const S2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // ----------------------------------------------------------- electromag2
@@ -93,6 +94,7 @@ struct E2Args {
     PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag2_f64(const E2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag2_f64x(const E2Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag2_f32(const E2Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // Adjoint of one FP32 electromag2 step (adjoint_em.cu).  State arrays, N
@@ -151,6 +153,7 @@ struct S25Args {
     PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_seismic25_f64(const S25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic25_f64x(const S25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic25_f32(const S25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // ----------------------------------------------------------- electromag25
@@ -172,6 +175,7 @@ struct E25Args {
     PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag25_f64(const E25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag25_f64x(const E25Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag25_f32(const E25Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // ----------------------------------------------------------- electromag3
@@ -197,6 +201,7 @@ struct E3Args {
     PwDev pw;         // plane-wave source (pw.on = 0: point sources)
 };
 void launch_electromag3_f64(const E3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_electromag3_f64x(const E3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_electromag3_f32(const E3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // -------------------------------------------------------------- seismic3
@@ -279,6 +284,7 @@ template <typename T> void pw_seismic3(const S3Args<T>& a, const StepInfo& s, cu
 template <typename T> void pw_electromag2(const E2Args<T>& a, const StepInfo& s, cudaStream_t st);
 template <typename T> void pw_electromag3(const E3Args<T>& a, const StepInfo& s, cudaStream_t st);
 void launch_seismic3_f64(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
+void launch_seismic3_f64x(const S3Args<double>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 void launch_seismic3_f32(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h = nullptr);
 
 // Number of kernel launches one step of each family issues (for accounting).

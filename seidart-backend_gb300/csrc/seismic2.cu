@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(BX* BY) s2_velocity(S2Args<real> a, StepInfo s
         if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0; vz = 0; }
         a.f[0][c] = vx;
         a.f[1][c] = vz;
-#if SD_EXACT
+#if !SD_F32
         nrm = sqrt((double)vx * (double)vx + (double)vz * (double)vz);
 #else
         sq = vx * vx + vz * vz; n0 = vx; n1 = vz;
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(BX* BY) s2_velocity(S2Args<real> a, StepInfo s
         // plane-wave face cells: their norm is taken after the injection
         if (a.pw.on && pw_cell(a.pw, i - 1, 0, j - 1)) { nrm = 0.0; sq = 0.f; n0 = 0.f; n1 = 0.f; }
     }
-#if SD_EXACT
+#if !SD_F32
     nrm = block_max<BX * BY / 32>(nrm, red);
 #else
     __shared__ float redf[BX * BY / 32];

@@ -18,7 +18,7 @@ struct cx {
     real re, im;
 };
 __device__ __forceinline__ cx ld(const real* a, size_t c) {
-#if SD_EXACT
+#if !SD_F32
     const double2 v = reinterpret_cast<const double2*>(a)[c];
 #else
     const float2 v = reinterpret_cast<const float2*>(a)[c];
@@ -26,7 +26,7 @@ __device__ __forceinline__ cx ld(const real* a, size_t c) {
     return cx{v.x, v.y};
 }
 __device__ __forceinline__ void stc(real* a, size_t c, cx z) {
-#if SD_EXACT
+#if !SD_F32
     reinterpret_cast<double2*>(a)[c] = make_double2(z.re, z.im);
 #else
     reinterpret_cast<float2*>(a)[c] = make_float2(z.re, z.im);
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(BX* BY) s25_velocity(S25Args<real> a, StepInfo
         stc(a.f[0], c, vx);
         stc(a.f[1], c, vy);
         stc(a.f[2], c, vz);
-#if SD_EXACT
+#if !SD_F32
         const double n1 = (double)vx.re * vx.re + (double)vx.im * vx.im;
         const double n2 = (double)vy.re * vy.re + (double)vy.im * vy.im;
         const double n3 = (double)vz.re * vz.re + (double)vz.im * vz.im;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(BX* BY) s25_velocity(S25Args<real> a, StepInfo
             for (float& x : w) x = 0.f;
         }
     }
-#if SD_EXACT
+#if !SD_F32
     nrm = block_max<BX * BY / 32>(nrm, red);
 #else
     __shared__ float redf[BX * BY / 32];

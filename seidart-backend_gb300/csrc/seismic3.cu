@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) s3_velocity(S3Args<real> a, StepIn
         // handled by s3_stress_source
         const bool src_cell = a.stress_src && ((i == is && j == js && k == ks) || (i == is + 1 && j == js + 1 && k == ks) ||
                                                (i == is + 1 && j == js && k == ks + 1) || (i == is && j == js + 1 && k == ks + 1));
-#if SD_EXACT
+#if !SD_F32
         vn = sqrt((double)vx * vx + (double)vy * vy + (double)vz * vz);
         if (!src_cell) {
             const double s1 = sxx[c], s2 = syy[c], s3 = szz[c], s4 = sxy[c], s5 = syz[c], s6 = sxz[c];
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) s3_velocity(S3Args<real> a, StepIn
             for (float& x : w) x = 0.f;
         }
     }
-#if SD_EXACT
+#if !SD_F32
     vn = block_max<BX * BY * BZ / 32>(vn, red);
     sn = block_max<BX * BY * BZ / 32>(sn, red2);
 #else

@@ -197,6 +197,13 @@ __global__ void convert_to_f32(float* __restrict__ d, const double* __restrict__
         d[q] = __double2float_rn(x);
     }
 }
+// the same derived forms in place on FP64 arrays (fast FP64 solvers)
+__global__ void derive_f64(double* __restrict__ d, size_t n, int mode, double dt) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const double x = d[q];
+        d[q] = mode == 1 ? __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(x, dt))) : __ddiv_rn(1.0, x);
+    }
+}
 __global__ void convert_to_f64(double* __restrict__ d, const float* __restrict__ s, size_t n) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         d[q] = (double)s[q];
@@ -220,6 +227,10 @@ int upload(SeidartSolver& s, void* d, const double* h, size_t n, int mode = 0) {
     cudaStream_t st = s.stream;
     if (sizeof(T) == sizeof(double)) {
         CUDA_TRY(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (mode != 0 && n > 0) {
+            derive_f64<<<4 * 152, 256, 0, st>>>((double*)d, n, mode, s.src.dt);
+            CUDA_TRY(cudaGetLastError());
+        }
         CUDA_TRY(cudaStreamSynchronize(st));
         return SEIDART_OK;
     }
@@ -310,14 +321,15 @@ template <typename T>
 int setup_model(SeidartSolver& s, const double* const* model, const double* const* srcfn,
                 const double** dev_src, std::vector<std::vector<double>>& derived) {
     const size_t N = s.ncell;
-    const bool f32 = sizeof(T) == sizeof(float);
+    // reciprocal forms of the fast arithmetic (FP32 and fast FP64 solvers)
+    const bool recip = sizeof(T) == sizeof(float) || s.precision == SEIDART_FP64_FAST;
     const double dt = s.src.dt;
     auto arr = [&](const double* h) -> const T* {
         T* d = (T*)s.carve(N * sizeof(T));
         if (d && upload<T>(s, d, h, N) != SEIDART_OK) return nullptr;
         return d;
     };
-    // FP32 arrays of a derived form, converted on the device (mode of convert_to_f32)
+    // arrays of a derived form, converted on the device (mode of convert_to_f32 / derive_f64)
     auto arr_mode = [&](const double* h, int mode) -> const T* {
         T* d = (T*)s.carve(N * sizeof(T));
         if (d && upload<T>(s, d, h, N, mode) != SEIDART_OK) return nullptr;
@@ -332,9 +344,9 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
         for (size_t q = 0; q < N; ++q) v[q] = fn(q);
         return v.data();
     };
-    // FP32: gamma -> 1/(1+gamma dt), kappa -> 1/kappa (same memory traffic)
-    auto gam = [&](const double* g) { return f32 ? arr_mode(g, 1) : arr(g); };
-    auto kap = [&](const double* k) { return f32 ? arr_mode(k, 2) : arr(k); };
+    // fast arithmetic: gamma -> 1/(1+gamma dt), kappa -> 1/kappa (same memory traffic)
+    auto gam = [&](const double* g) { return recip ? arr_mode(g, 1) : arr(g); };
+    auto kap = [&](const double* k) { return recip ? arr_mode(k, 2) : arr(k); };
     (void)dt;
     const int cs = cpml_slot(s.family);
     const T* cp[6];
@@ -390,17 +402,17 @@ int setup_model(SeidartSolver& s, const double* const* model, const double* cons
         for (int q = 0; q < 21; ++q) a.C[q] = arr(model[q]);
         for (int q = 0; q < 6; ++q) a.g[q] = gam(model[SEIDART_GX3 + q]);
         for (int q = 0; q < 6; ++q) a.cpml[q] = cp[q];
-        // density averaging, cpmlfdtd.f08:889-898 (FP32: stored as 1/rho)
+        // density averaging, cpmlfdtd.f08:889-898 (fast arithmetic: stored as 1/rho)
         const double* rho = model[SEIDART_RHO3];
         const int dirs[9] = {0, -1, 2, 1, -1, 2, 1, -1, 3};  // -1: plain rho
         for (int q = 0; q < 9; ++q) {
             if (!s.arena) { a.rho9[q] = arr(rho); continue; }
             derived.emplace_back(rho, rho + N);
             if (dirs[q] >= 0) averaging2d(derived.back().data(), s.dom.nx, s.dom.nz, s.density, dirs[q]);
-            if (f32) for (double& v : derived.back()) v = 1.0 / v;
+            if (recip) for (double& v : derived.back()) v = 1.0 / v;
             a.rho9[q] = arr(derived.back().data());
         }
-        a.rho = f32 ? arr_mode(rho, 2) : arr(rho);
+        a.rho = recip ? arr_mode(rho, 2) : arr(rho);
         for (int q = 0; q < 9; ++q) a.src[q] = dev_src[q];
         if constexpr (sizeof(T) == 8) s.s25d = a; else s.s25f = a;
         break;
@@ -494,6 +506,7 @@ template <typename T>
 void finish_args(SeidartSolver& s) {
     const int is = s.src.xind + s.dom.cpml - 1, js = s.src.yind + s.dom.cpml - 1, ks = s.src.zind + s.dom.cpml - 1;
     const bool f32 = sizeof(T) == sizeof(float);
+    const bool recip = f32 || s.precision == SEIDART_FP64_FAST;
     switch (s.family) {
     case SEIDART_SEISMIC2: {
         S2Args<T>& a = *(S2Args<T>*)(f32 ? (void*)&s.s2f : (void*)&s.s2d);
@@ -505,9 +518,9 @@ void finish_args(SeidartSolver& s) {
     case SEIDART_ELECTROMAG2: {
         E2Args<T>& a = *(E2Args<T>*)(f32 ? (void*)&s.e2f : (void*)&s.e2d);
         fill_common2<T>(s, a);
-        // the FP32 build multiplies by 1/dx, 1/dz
-        a.dx = f32 ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
-        a.dz = f32 ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
+        // the fast builds multiply by 1/dx, 1/dz
+        a.dx = recip ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
+        a.dz = recip ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
         a.dbHy = (T)(s.src.dt / kMu0);
         a.isrc = is; a.jsrc = ks;
         break;
@@ -531,10 +544,10 @@ void finish_args(SeidartSolver& s) {
         E3Args<T>& a = *(E3Args<T>*)(f32 ? (void*)&s.e3f : (void*)&s.e3d);
         fill_common2<T>(s, a);
         a.ny = s.dom.ny;
-        // the FP32 build multiplies by 1/dx, 1/dy, 1/dz
-        a.dx = f32 ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
-        a.dy = f32 ? (T)(1.0 / s.dom.dy) : (T)s.dom.dy;
-        a.dz = f32 ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
+        // the fast builds multiply by 1/dx, 1/dy, 1/dz
+        a.dx = recip ? (T)(1.0 / s.dom.dx) : (T)s.dom.dx;
+        a.dy = recip ? (T)(1.0 / s.dom.dy) : (T)s.dom.dy;
+        a.dz = recip ? (T)(1.0 / s.dom.dz) : (T)s.dom.dz;
         a.dbH = (T)(s.src.dt / kMu0);
         a.isrc = is; a.jsrc = js; a.ksrc = ks;
         break;
@@ -574,20 +587,23 @@ int launches_per_step(const SeidartSolver& s) {
 
 void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nullptr) {
     StepInfo si{s.step_dev, s.nrec, s.rec_dev};
-    const bool f32 = s.precision == SEIDART_FP32;
+    const bool f32 = s.precision == SEIDART_FP32, fx = s.precision == SEIDART_FP64_FAST;
+    // FP64 solvers: the exact build, or the fast-arithmetic FP64 build
+#define SD_F64(fam, args) (fx ? launch_##fam##_f64x(args, si, st, h) : launch_##fam##_f64(args, si, st, h))
     switch (s.family) {
-    case SEIDART_SEISMIC2: f32 ? launch_seismic2_f32(s.s2f, si, st, h) : launch_seismic2_f64(s.s2d, si, st, h); break;
-    case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : launch_electromag2_f64(s.e2d, si, st, h); break;
-    case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : launch_seismic25_f64(s.s25d, si, st, h); break;
-    case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : launch_electromag25_f64(s.e25d, si, st, h); break;
-    case SEIDART_ELECTROMAG3: f32 ? launch_electromag3_f32(s.e3f, si, st, h) : launch_electromag3_f64(s.e3d, si, st, h); break;
+    case SEIDART_SEISMIC2: f32 ? launch_seismic2_f32(s.s2f, si, st, h) : SD_F64(seismic2, s.s2d); break;
+    case SEIDART_ELECTROMAG2: f32 ? launch_electromag2_f32(s.e2f, si, st, h) : SD_F64(electromag2, s.e2d); break;
+    case SEIDART_SEISMIC25: f32 ? launch_seismic25_f32(s.s25f, si, st, h) : SD_F64(seismic25, s.s25d); break;
+    case SEIDART_ELECTROMAG25: f32 ? launch_electromag25_f32(s.e25f, si, st, h) : SD_F64(electromag25, s.e25d); break;
+    case SEIDART_ELECTROMAG3: f32 ? launch_electromag3_f32(s.e3f, si, st, h) : SD_F64(electromag3, s.e3d); break;
     case SEIDART_SEISMIC3:
-        if (!f32) launch_seismic3_f64(s.s3d, si, st, h);
+        if (!f32) SD_F64(seismic3, s.s3d);
         else if (s.s3f.pw.on) launch_seismic3_f32(s.s3f, si, st, h);  // plane waves: the one-cell kernels
         else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr, s.s3_stress_kind,
                                   s.s3_velocity_kind);
         break;
     }
+#undef SD_F64
 }
 
 // Event recorder for seidart_solver_profile: one event after every kernel.
@@ -663,8 +679,8 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     *out = nullptr;
     Layout L;
     if (!layout_of(family, &L)) return set_err(SEIDART_ERR_ARG, "unknown solver family %d", family);
-    if (precision != SEIDART_FP64 && precision != SEIDART_FP32)
-        return set_err(SEIDART_ERR_ARG, "precision must be SEIDART_FP64 or SEIDART_FP32");
+    if (precision != SEIDART_FP64 && precision != SEIDART_FP32 && precision != SEIDART_FP64_FAST)
+        return set_err(SEIDART_ERR_ARG, "precision must be SEIDART_FP64, SEIDART_FP32 or SEIDART_FP64_FAST");
     if (density_code < 1 || density_code > 4)
         return set_err(SEIDART_ERR_ARG, "density_code %d: must be 1 harmonic, 2 geometric, 3 arithmetic, 4 none",
                        density_code);

@@ -1,8 +1,9 @@
 """Build recipe for libseidart_gpu.so (sm_103a only).
 
-Every kernel file is compiled twice: the FP64 drop-in build with
+Every kernel file is compiled three times: the FP64 drop-in build with
 ``--fmad=false`` (so each FP64 expression keeps the reference's rounding
-sequence) and the FP32 fast build with FMA contraction.  Host code is built
+sequence), the fast FP64 build (FP64 fields, reciprocals and FMA
+contraction) and the FP32 fast build with FMA contraction.  Host code is built
 with ``-ffp-contract=off`` so host-side coefficient set-up matches the CPU
 restatement bit for bit on x86 and on Arm.  Objects compile in parallel; the
 library is linked in-tree next to this file.
@@ -41,10 +42,11 @@ def _jobs() -> list[tuple[list[str], Path]]:
     nvcc = _nvcc()
     jobs = []
     for src in DUAL:
-        for prec in ("f64", "f32"):
+        for prec in ("f64", "f64x", "f32"):
             obj = BUILD / f"{Path(src).stem}.{prec}.o"
-            flags = (["--fmad=false", "-DSEIDART_REAL=double"] if prec == "f64"
-                     else ["-DSEIDART_REAL=float", "-DSEIDART_FP32"])
+            flags = {"f64": ["--fmad=false", "-DSEIDART_REAL=double"],
+                     "f64x": ["-DSEIDART_REAL=double", "-DSEIDART_FAST64"],
+                     "f32": ["-DSEIDART_REAL=float", "-DSEIDART_FP32"]}[prec]
             jobs.append(([nvcc, *ARCH, *COMMON, *flags, "-c", str(CSRC / src), "-o", str(obj)], obj))
     for src in SINGLE:
         if not (CSRC / src).exists():

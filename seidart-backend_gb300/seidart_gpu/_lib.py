@@ -22,7 +22,7 @@ ERRORS = {
 }
 
 SEISMIC2, SEISMIC25, SEISMIC3, ELECTROMAG2, ELECTROMAG25, ELECTROMAG3 = 1, 2, 3, 4, 5, 6
-FP64, FP32 = 0, 1
+FP64, FP32, FP64_FAST = 0, 1, 2
 
 
 class SeidartError(RuntimeError):

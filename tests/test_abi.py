@@ -56,3 +56,13 @@ def test_no_unresolved_internal_symbols():
     unversioned = [ln.split()[-1] for ln in out.splitlines() if ln.strip() and "@" not in ln]
     unversioned = [s for s in unversioned if not s.startswith(("__gmon_start__", "_ITM_", "__cxa_finalize"))]
     assert not unversioned, unversioned
+
+
+def test_python_constants_match_the_header():
+    """Family and precision codes of the Python package are the header's."""
+    import seidart_gpu as sg
+    text = HEADER.read_text()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(SEIDART_[A-Z0-9_]+)\s+(-?\d+)", text)}
+    for name in ("FP64", "FP32", "FP64_FAST", "SEISMIC2", "SEISMIC25", "SEISMIC3", "ELECTROMAG2", "ELECTROMAG25",
+                 "ELECTROMAG3"):
+        assert defs["SEIDART_" + name] == getattr(sg, name), name
