@@ -102,7 +102,7 @@ class Batch:
             _check(L.seidart_batch_tuning(self.handle, v, C.byref(tx), C.byref(ty), C.addressof(bps), C.addressof(ms)))
             for q in range(2):
                 if ms[q] >= 0:
-                    out.append({"tile": [tx.value, ty.value], "ctas_per_sm": bps[q], "ms": ms[q]})
+                    out.append({"variant": v, "tile": [tx.value, ty.value], "ctas_per_sm": bps[q], "ms": ms[q]})
         return out
 
     def config(self) -> dict:
