@@ -154,6 +154,19 @@ class Problem:
                        else np.asfortranarray(f, dtype=dt).copy(order="F"))
         return out
 
+    def given_fields(self) -> list:
+        """Initial fields the problem sets, None for the ones it leaves at zero."""
+        dt = np.complex128 if self.is_complex else np.float64
+        out = []
+        for name in FIELD_SLOTS[self.family]:
+            f = self.fields0.get(name)
+            if f is not None:
+                f = np.asfortranarray(f, dtype=dt)
+                if f.shape != self.shape:
+                    raise ValueError(f"initial field {name} has shape {f.shape}, expected {self.shape}")
+            out.append(f)
+        return out
+
     def receiver_array(self) -> np.ndarray:
         if self.receivers is None:
             return np.zeros(0, dtype=np.int32)
@@ -184,7 +197,8 @@ class Solver:
                                           ptr_array(self._model), ptr_array(self._src), len(rec),
                                           rec.ctypes.data if len(rec) else None))
         self.handle = h
-        self.set_fields(problem.field_list())
+        # the device state starts at zero: only the initial fields the problem sets travel
+        self.set_fields(problem.given_fields())
         pw = problem.plane_wave_struct()
         if pw is not None:
             check(lib().seidart_solver_set_plane_wave(self.handle, C.byref(pw), ptr_array(self._model)))
