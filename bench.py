@@ -312,7 +312,12 @@ def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
             s1.sync()
             seq_t += time.perf_counter() - t1
             seq_cells += q.ncell * 280
+    # algorithmic bytes per step: 20 words per cell + 30 per CPML cell (FP32)
+    hbm, _ = peaks()
+    step_b = sum(4 * (20 * p.ncell + 30 * (p.ncell - (p.nx - 2 * p.cpml) * (p.nz - 2 * p.cpml))) for p in ps)
+    gbs = step_b * (nt - warm) / dt / 1e9
     return {"value": cells * (nt - warm) / dt / 1e9, "unit": UNIT, "models": nmodels, "cells": cells,
+            "algorithmic_gbs": gbs, "frac_of_measured_hbm": gbs / hbm, "bytes_per_step": step_b,
             "steps_timed": nt - warm, "seconds": dt, "setup_s": setup, "tuned": cfg, "gpu_launches": launches,
             "one_by_one": {"value": seq_cells / seq_t / 1e9, "unit": UNIT,
                            "sample": "first 8 models, 280 timed steps each, single-model FP32 solver"},
