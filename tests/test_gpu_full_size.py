@@ -85,3 +85,25 @@ def test_electromag2_full_size_full_length():
     assert np.max(np.abs(g64["traces"])) > 0
     assert rel_l2(g32["traces"], g64["traces"]) <= 1e-4
     assert rel_l2(gx["traces"], g64["traces"]) <= 1e-12
+
+
+def test_ragged_batch_full_size():
+    """The 64-model ragged batch (nx, nz in [256, 1024] + 20 CPML, 29.4 M
+    cells) for 200 steps in chunks, against single-model FP32 runs of a
+    sample of its models (smallest, largest, two in between)."""
+    from seidart_gpu.batch import Batch
+    ps = models.batch_layered_vti(nmodels=64, nt=200)
+    with Batch(ps, autotune=True, trial_steps=8) as b:
+        b.step(50, chunk=25)
+        b.step(150, chunk=100)
+        b.sync()
+        order = np.argsort([p.ncell for p in ps])
+        for m in (order[0], order[21], order[42], order[-1]):
+            single = sg.run(ps[m], sg.FP32)
+            tr, nrm = b.traces(m)
+            assert np.max(np.abs(single["fields"][1])) > 0
+            assert rel_l2(tr, single["traces"]) <= 1e-6, m
+            assert rel_l2(nrm, single["norms"]) <= 1e-6, m
+            f = b.fields(m)
+            for q in range(5):
+                assert rel_l2(f[q], single["fields"][q]) <= 1e-6, (m, q)
