@@ -492,6 +492,9 @@ def main():
                     help="run a small ragged batch (16 models of the batch workload's distribution, 40 steps in "
                          "launches of 20, the autotuned kernel) and exit: the case the batch profile in profiles/ "
                          "is captured on")
+    ap.add_argument("--batch-variant", default=None,
+                    help="with --batch-profile-case: 'V,B' runs kernel variant V with B CTAs per SM instead of "
+                         "the autotuned choice (so a profiler can capture its first launch)")
     ap.add_argument("--grid", type=int, default=WORKLOAD["n"],
                     help="interior cells per axis (default 320: the 3D configuration)")
     args = ap.parse_args()
@@ -509,7 +512,10 @@ def main():
         from seidart_gpu import models
         from seidart_gpu.batch import Batch
         ps = models.batch_layered_vti(nmodels=16, nt=40)
-        with Batch(ps, autotune=True) as b:
+        with Batch(ps, autotune=args.batch_variant is None) as b:
+            if args.batch_variant is not None:
+                v, bps = (int(x) for x in args.batch_variant.split(","))
+                b.set_config(v, bps)
             b.step(40, chunk=20)
             b.sync()
             print(json.dumps({"batch_profile_case": "ok", "config": b.config()}))

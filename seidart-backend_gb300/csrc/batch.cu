@@ -290,22 +290,37 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_persistent(BatchArgs B, int 
 
 __device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-// L2 prefetch of every row tile t will read: velocities and stresses, the ten
-// per-cell coefficients (C, rho, gamma) and, on tiles reaching outside the
-// inert box, the 12 memories and 6 CPML coefficients.  A hint: nothing stays
+// L2 prefetch of the rows tile t will read in one phase of the step -- the
+// stress half-step (PHASE 1: velocities, old stresses, the nine stress
+// coefficients; on tiles reaching outside the inert box the eight stress
+// CPML memories and the six CPML coefficients) or the velocity half-step
+// (PHASE 2: stresses, velocities, density; outside the box the four
+// velocity memories and the CPML coefficients).  A hint: nothing stays
 // allocated for it.
-template <int TX, int TY>
+template <int PHASE>
+__device__ __forceinline__ const float* pf_array(const BModel& M, int a) {
+    if (a < 5) return M.f[a];  // vx vz sxx szz sxz
+    if (PHASE == 1) {
+        if (a < 14) return M.m[a - 5 + (a >= 11 ? 1 : 0)];  // c11 c13 c15 c33 c35 c55, gx gz gxz (skip rho)
+        if (a < 22) return M.mem[a - 14];                     // memories 0..7
+        return M.m[10 + a - 22];                              // kappa .. bcoef_half
+    }
+    if (a == 5) return M.m[6];                                // rho
+    if (a < 10) return M.mem[8 + a - 6];                      // memories 8..11
+    return M.m[10 + a - 10];
+}
+
+template <int TX, int TY, int PHASE>
 __device__ __forceinline__ void tile_prefetch(const BatchArgs& B, int t, int tid) {
     const BModel& M = B.models[B.tile_model[t]];
     const int lt = t - M.tile0, tx = lt % M.tiles_x, tz = lt / M.tiles_x;
     const int x0 = tx * TX, x1 = min(x0 + TX, M.nx) - 1, z0 = tz * TY, z1 = min(z0 + TY, M.nz);
     const bool shell = !(x0 >= M.box.i0 && x1 < M.box.i1 && z0 >= M.box.k0 && z1 <= M.box.k1);
-    const int narr = shell ? 33 : 15;
+    const int narr = PHASE == 1 ? (shell ? 28 : 14) : (shell ? 16 : 6);
     for (int q = tid; q < narr * TY; q += TX * TY) {
         const int a = q / TY, y = z0 + q % TY;
         if (y >= z1) continue;
-        const float* base = a < 5 ? M.f[a] : a < 15 ? M.m[a - 5] : a < 27 ? M.mem[a - 15] : M.m[10 + a - 27];
-        const float* row = base + (size_t)y * M.nx;
+        const float* row = pf_array<PHASE>(M, a) + (size_t)y * M.nx;
         pf_l2(row + x0);
         if (TX > 32 && x0 + 32 <= x1) pf_l2(row + x0 + 32);
         pf_l2(row + x1);
@@ -351,17 +366,17 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nst
         const int it = it0 + s;
         // phase 1: stress
         for (int t = t0; t < t1; ++t) {
-            if (t + PD < t1) tile_prefetch<TX, TY>(B, t + PD, tid);
+            if (t + PD < t1) tile_prefetch<TX, TY, 1>(B, t + PD, tid);
             const BModel* M;
             int i, j;
             if (tile_cell<TX, TY>(B, t, M, i, j)) cell_stress(*M, i, j);
         }
-        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY>(B, t, tid);
+        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY, 2>(B, t, tid);
         if (!grid_barrier(B)) return;
         // phase 2: velocity, force source, Dirichlet, norms
         WarpNorm wn;
         for (int t = t0; t < t1; ++t) {
-            if (t + PD < t1) tile_prefetch<TX, TY>(B, t + PD, tid);
+            if (t + PD < t1) tile_prefetch<TX, TY, 2>(B, t + PD, tid);
             const int m = B.tile_model[t];
             if (m != wn.model) {
                 wn.flush(B, it, lane);
@@ -392,7 +407,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nst
                 a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
             }
         }
-        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY>(B, t, tid);
+        for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY, 1>(B, t, tid);
         if (!grid_barrier(B)) return;
     }
     if (blockIdx.x == 0 && tid == 0) *B.step = it0 + nsteps;
