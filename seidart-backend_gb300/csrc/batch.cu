@@ -321,8 +321,9 @@ __device__ __forceinline__ void tile_prefetch(const BatchArgs& B, int t, int tid
         const int a = q / TY, y = z0 + q % TY;
         if (y >= z1) continue;
         const float* row = pf_array<PHASE>(M, a) + (size_t)y * M.nx;
-        pf_l2(row + x0);
-        if (TX > 32 && x0 + 32 <= x1) pf_l2(row + x0 + 32);
+#pragma unroll
+        for (int xo = 0; xo < TX; xo += 32)
+            if (x0 + xo <= x1) pf_l2(row + x0 + xo);
         pf_l2(row + x1);
     }
 }
@@ -429,6 +430,8 @@ const Variant kVariants[] = {
     {64, 4, (const void*)s2b_chunked<64, 4, 2>, "chunked"},
     {32, 4, (const void*)s2b_chunked<32, 4, 2>, "chunked"},
     {32, 16, (const void*)s2b_chunked<32, 16, 1>, "chunked"},
+    {32, 16, (const void*)s2b_chunked<32, 16, 2>, "chunked"},
+    {64, 8, (const void*)s2b_chunked<64, 8, 1>, "chunked"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

@@ -39,7 +39,7 @@ def test_batch_matches_single_model_runs(oracle):
             assert rel_l2(nrm, o["norms"]) <= 1e-4
 
 
-@pytest.mark.parametrize("variant", range(10))
+@pytest.mark.parametrize("variant", range(12))
 def test_every_kernel_variant_matches_single_runs(variant):
     if variant >= Batch.num_variants():
         pytest.skip("variant not built")
