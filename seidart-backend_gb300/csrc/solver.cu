@@ -155,6 +155,8 @@ struct SeidartSolver {
     float* s3_packed = nullptr;  // tile-packed coefficients of the bulk stress kernel
     double* stage = nullptr;     // FP64 staging buffer for on-device precision conversion (FP32 solvers)
     size_t stage_n = 0;          // its capacity in doubles
+    float* pin = nullptr;        // pinned host double buffer of FP32 read-backs (2 x kPinChunk floats)
+    cudaEvent_t pin_ev[2] = {nullptr, nullptr};
     S3XMaps s3_staged{};         // tensor maps of the staged stress kernel (when s3f.staged is set)
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
@@ -224,6 +226,88 @@ int ensure_stage(SeidartSolver& s, size_t n) {
     return SEIDART_OK;
 }
 
+// FP32 transfers of large arrays go through a pinned double buffer: on the
+// way in, host threads round chunk k of the caller's FP64 array (in the
+// derived form of `mode`, the same FP64 operations as convert_to_f32) into
+// one half while chunk k-1 is copied from the other; on the way out, chunk
+// k is widened into the caller's array while chunk k+1 is copied.  Half the
+// bytes of FP64 cross the link, and no staging kernel runs.
+constexpr size_t kPinChunk = size_t(1) << 23;  // floats per chunk (32 MiB)
+
+int ensure_pin(SeidartSolver& s) {
+    if (s.pin) return SEIDART_OK;
+    if (cudaMallocHost((void**)&s.pin, 2 * kPinChunk * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        s.pin = nullptr;
+        return SEIDART_ERR_NOMEM;
+    }
+    for (int b = 0; b < 2; ++b) CUDA_TRY(cudaEventCreateWithFlags(&s.pin_ev[b], cudaEventDisableTiming));
+    return SEIDART_OK;
+}
+
+// run body(lo, hi) over [0, m) on up to 16 host threads
+template <typename F>
+void host_parallel(size_t m, F body) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t nth = std::max<size_t>(1, std::min<size_t>(std::min(hw, 16u), m >> 18));
+    std::vector<std::thread> pool;
+    for (size_t w = 1; w < nth; ++w) pool.emplace_back([&, w] { body(m * w / nth, m * (w + 1) / nth); });
+    body(0, m / nth);
+    for (auto& t : pool) t.join();
+}
+
+void widen(double* dst, const float* src, size_t m) {
+    host_parallel(m, [&](size_t lo, size_t hi) {
+        for (size_t q = lo; q < hi; ++q) dst[q] = (double)src[q];
+    });
+}
+
+void narrow(float* dst, const double* src, size_t m, int mode, double dt) {
+    host_parallel(m, [&](size_t lo, size_t hi) {
+        for (size_t q = lo; q < hi; ++q) {
+            double x = src[q];
+            if (mode == 1) x = 1.0 / (1.0 + x * dt);
+            else if (mode == 2) x = 1.0 / x;
+            dst[q] = (float)x;
+        }
+    });
+}
+
+int upload_f32_pinned(SeidartSolver& s, float* d, const double* h, size_t n, int mode) {
+    cudaStream_t st = s.stream;
+    if (const int rc = ensure_pin(s)) return rc;
+    const size_t nch = (n + kPinChunk - 1) / kPinChunk;
+    for (size_t k = 0; k < nch; ++k) {
+        const int b = (int)(k & 1);
+        if (k >= 2) CUDA_TRY(cudaEventSynchronize(s.pin_ev[b]));  // the copy that last read this half
+        const size_t o = k * kPinChunk, m = std::min(kPinChunk, n - o);
+        narrow(s.pin + b * kPinChunk, h + o, m, mode, s.src.dt);
+        CUDA_TRY(cudaMemcpyAsync(d + o, s.pin + b * kPinChunk, m * sizeof(float), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaEventRecord(s.pin_ev[b], st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SEIDART_OK;
+}
+
+int download_f32_pinned(SeidartSolver& s, double* h, const float* d, size_t n) {
+    cudaStream_t st = s.stream;
+    if (const int rc = ensure_pin(s)) return rc;
+    const size_t nch = (n + kPinChunk - 1) / kPinChunk;
+    auto issue = [&](size_t k) -> cudaError_t {
+        const size_t o = k * kPinChunk, m = std::min(kPinChunk, n - o);
+        cudaError_t e = cudaMemcpyAsync(s.pin + (k & 1) * kPinChunk, d + o, m * sizeof(float), cudaMemcpyDeviceToHost, st);
+        return e == cudaSuccess ? cudaEventRecord(s.pin_ev[k & 1], st) : e;
+    };
+    if (nch > 0) CUDA_TRY(issue(0));
+    for (size_t k = 0; k < nch; ++k) {
+        if (k + 1 < nch) CUDA_TRY(issue(k + 1));
+        CUDA_TRY(cudaEventSynchronize(s.pin_ev[k & 1]));
+        const size_t o = k * kPinChunk, m = std::min(kPinChunk, n - o);
+        widen(h + o, s.pin + (k & 1) * kPinChunk, m);
+    }
+    return SEIDART_OK;
+}
+
 template <typename T>
 int upload(SeidartSolver& s, void* d, const double* h, size_t n, int mode = 0) {
     cudaStream_t st = s.stream;
@@ -235,6 +319,10 @@ int upload(SeidartSolver& s, void* d, const double* h, size_t n, int mode = 0) {
         }
         CUDA_TRY(cudaStreamSynchronize(st));
         return SEIDART_OK;
+    }
+    if (n >= kPinChunk / 4) {  // large arrays: pinned FP32 path (falls through if no pinned memory)
+        const int rc = upload_f32_pinned(s, (float*)d, h, n, mode);
+        if (rc != SEIDART_ERR_NOMEM) return rc;
     }
     const size_t chunk = std::max<size_t>(s.ncell, 1 << 20);
     if (ensure_stage(s, std::min(n, chunk)) != SEIDART_OK) return set_err(SEIDART_ERR_NOMEM, "staging buffer");
@@ -254,6 +342,10 @@ int download(SeidartSolver& s, double* h, const void* d, size_t n) {
         CUDA_TRY(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         return SEIDART_OK;
+    }
+    if (n >= kPinChunk / 4) {  // large arrays: pinned FP32 path (falls through if no pinned memory)
+        const int rc = download_f32_pinned(s, h, (const float*)d, n);
+        if (rc != SEIDART_ERR_NOMEM) return rc;
     }
     const size_t chunk = std::max<size_t>(s.ncell, 1 << 20);
     if (ensure_stage(s, std::min(n, chunk)) != SEIDART_OK) return set_err(SEIDART_ERR_NOMEM, "staging buffer");
@@ -1081,6 +1173,9 @@ int seidart_solver_destroy(SeidartSolver* s) {
     if (s->arena) cudaFree(s->arena);
     if (s->s3_packed) cudaFree(s->s3_packed);
     if (s->stage) cudaFree(s->stage);
+    if (s->pin) cudaFreeHost(s->pin);
+    for (int b = 0; b < 2; ++b)
+        if (s->pin_ev[b]) cudaEventDestroy(s->pin_ev[b]);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return SEIDART_OK;
