@@ -17,6 +17,8 @@ grid (stress half-step + velocity half-step, source, Dirichlet faces, norms,
   configs_2d  the two 2D workloads at full length: seismic2 256^2 + 20 CPML
             (2000 steps; FP64 plain, FP32 and the CPU restatement) and
             electromag2 1024^2 + 20 CPML (4000 steps; FP64 and FP32)
+  families  seismic25, electromag25 (1024^2) and electromag3 (256^3) in the
+            three precisions
   batched   the ragged multi-model 2D workload: 64 seismic2 models with nx, nz
             in [256, 1024], 3000 steps, one persistent launch per graph chunk
             with autotuned tiles; beside it the same models run one by one
@@ -205,7 +207,7 @@ def cpu_baseline_sample(p=None, budget_s: float = 20.0) -> dict:
             "sample": f"{n} full time steps of the {p.nx}^3 grid after 1 untimed step (FP64, OpenMP, reference flags)"}
 
 
-def _timed_run(p, precision, warm: int = 10) -> dict:
+def _timed_run(p, precision, warm: int = 10, want_fields: bool = False) -> dict:
     """Whole run of problem p through the Solver API: `warm` untimed steps,
     then the remaining steps timed with CUDA events on the solver's stream."""
     import torch
@@ -226,7 +228,8 @@ def _timed_run(p, precision, warm: int = 10) -> dict:
         ms = e0.elapsed_time(e1)
         tr, _ = s.traces()
         launches = s.launches - l0
-    return {"ms": ms, "steps": p.time_steps - warm, "traces": tr, "launches": launches}
+        fields = s.get_fields() if want_fields else None
+    return {"ms": ms, "steps": p.time_steps - warm, "traces": tr, "launches": launches, "fields": fields}
 
 
 def bench_2d_configs() -> dict:
@@ -275,6 +278,41 @@ def bench_2d_configs() -> dict:
                                     "sample": f"all {p.time_steps} steps (FP64, OpenMP, reference flags)"}
             r["fp64_vs_cpu_traces_rel_l2"] = rel(runs["fp64_plain"]["traces"], st.result()["traces"])
             r["fp64_speedup_vs_cpu"] = r["fp64_plain"]["value"] / r["cpu_restatement"]["value"]
+        out[name] = r
+    return out
+
+
+def bench_families() -> dict:
+    """The solvers the headline and 2D legs do not time: seismic25 and
+    electromag25 (2.5D, complex fields) on 1024^2 + 20 CPML for 400 steps
+    and electromag3 on 256^3 + 10 CPML for 200 steps, each in FP64 exact,
+    fast FP64 and FP32, with the FP32 and fast-FP64 errors against exact FP64
+    on the final fields (on these grids and step counts the wave has not yet
+    reached the receiver lines, whose FP64 samples are leading-edge values
+    far below FP32's range)."""
+    import seidart_gpu as sg
+    from seidart_gpu import models
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+    cases = [("seismic25_1024", models.seismic25_two_layer(n=1024, cpml=20, nt=400)),
+             ("electromag25_1024", models.electromag25_blocks(n=1024, cpml=20, nt=400)),
+             ("electromag3_256", models.electromag3_blocks(n=256, cpml=10, nt=200))]
+    out = {}
+    for name, p in cases:
+        r = {"grid": list(p.shape), "cells": p.ncell, "steps": p.time_steps}
+        runs = {}
+        for prec, key in ((sg.FP64, "fp64_plain"), (sg.FP64_FAST, "fp64_fast"), (sg.FP32, "fp32")):
+            t = _timed_run(p, prec, want_fields=True)
+            runs[key] = t
+            r[key] = {"value": p.ncell * t["steps"] / (t["ms"] / 1e3) / 1e9, "unit": UNIT,
+                      "ms_per_step": t["ms"] / t["steps"], "gpu_launches": t["launches"]}
+        ref = np.concatenate([np.asarray(f).ravel() for f in runs["fp64_plain"]["fields"]])
+        for key in ("fp32", "fp64_fast"):
+            got = np.concatenate([np.asarray(f).ravel() for f in runs[key]["fields"]])
+            r[f"{key}_vs_fp64_fields_rel_l2"] = rel(got, ref)
+        r["fp64_max_abs_trace"] = float(np.max(np.abs(runs["fp64_plain"]["traces"])))
         out[name] = r
     return out
 
@@ -650,6 +688,7 @@ def main():
         cpu = cpu_baseline_sample(p)
     if not args.no_2d and rank == 0:
         extra["configs_2d"] = bench_2d_configs()
+        extra["families"] = bench_families()
     if not args.no_batch and rank == 0:
         extra["batched"] = bench_batch()
     if not args.no_fwi and rank == 0:
