@@ -22,6 +22,16 @@ def shard(items: list, rank: int, world: int) -> list:
     return items[rank::world]
 
 
+def sharded_batch(problems: list, rank: int, world: int, **batch_kw):
+    """This rank's share of a ragged batch (models round-robin over ranks) as
+    one ``Batch`` on this rank's GPU, or None when the rank owns no model.
+    Model m of ``problems`` is model ``m // world`` of rank ``m % world``'s
+    batch; no collective is needed while the batches step."""
+    from .batch import Batch
+    mine = shard(problems, rank, world)
+    return Batch(mine, **batch_kw) if mine else None
+
+
 def _dist():
     import torch.distributed as dist
     return dist if dist.is_available() and dist.is_initialized() else None

@@ -67,3 +67,23 @@ def test_bounded_barrier_timeout_reports_status():
     with Batch(small_batch(nt=10), autotune=False) as b2:
         b2.step(10)
         b2.sync()
+
+
+def test_sharded_batch_covers_every_model_once():
+    """Two ranks' shares of one ragged batch (built one after the other on
+    this GPU; the shares never wait on each other) reproduce every model."""
+    from seidart_gpu.distributed import sharded_batch
+    probs = small_batch(nt=30)
+    seen = []
+    for rank in range(2):
+        b = sharded_batch(probs, rank, 2, autotune=False)
+        with b:
+            b.step(probs[0].time_steps)
+            b.sync()
+            for k in range(len(probs[rank::2])):
+                m = rank + 2 * k
+                single = sg.run(probs[m], sg.FP32)
+                tr, _ = b.traces(k)
+                assert rel_l2(tr, single["traces"]) <= 1e-6, m
+                seen.append(m)
+    assert sorted(seen) == list(range(len(probs)))
