@@ -69,15 +69,16 @@ class Clocks:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, interval_ms: int = 20):
         self.gpu = gpu
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines = []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -114,16 +115,27 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def bench_config(p, world: int = 1) -> dict:
+    """The workload description both arms print (same keys and values; the
+    arithmetic type is the line's own ``dtype``)."""
+    return {"workload": f"seismic3 anisotropic elastic, {WORKLOAD['n']}^3 interior + {WORKLOAD['cpml']} CPML "
+                        f"({p.nx}^3 padded cells), 5 rotated orthotropic layers",
+            "grid": [p.nx, p.ny, p.nz], "cells": p.ncell, "receivers": 1024, "seed": WORKLOAD["seed"],
+            "l2": "inputs larger than L2 (about 14 GB moved per step vs 129 MB L2)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def make_problem(nt=None):
     from seidart_gpu import models
     w = WORKLOAD
     return models.seismic3_layers(n=w["n"], cpml=w["cpml"], nt=nt or w["nt"], seed=w["seed"])
 
 
-# DRAM traffic / algorithmic bytes of one launch, from one ncu capture of the
-# 224^3 case (profiles/s3x_stress_224cube.md, profiles/s3b_stress_224cube.md,
-# profiles/s3c_velocity_224cube.md, profiles/s3p_velocity_224cube.md); the
-# bench scales it to its own launch by the algorithmic bytes.
+# DRAM traffic / algorithmic bytes of one launch: ncu's dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch of each kernel on the 224^3 case (a
+# full-size launch is too large for a multi-pass capture), divided by that
+# launch's algorithmic bytes; the bench scales it to its own launch by the
+# algorithmic bytes.
 TRAFFIC_RATIO = {"s3x_stress": 1.121, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.205}
 
 
@@ -135,10 +147,11 @@ def kernel_bytes(p, box_cells: int) -> dict:
     shell = n - box_cells
     stress = WORD * (42 * n + 78 * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12; shell: 36 memories R+W + 6 coefficients
     velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
-    # z-marching kernels (default) and one-thread-per-cell kernels
+    # the fused step does both half-steps: the whole step's algorithmic bytes
     return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3p_velocity": velocity,
             "s3f_stress": stress, "s3f_velocity": velocity,
-            "s3t_stress": stress, "s3b_stress": stress, "s3x_stress": stress}
+            "s3t_stress": stress, "s3b_stress": stress, "s3x_stress": stress,
+            "s3w_step": step_bytes(p, box_cells)}
 
 
 def step_bytes(p, box_cells: int) -> int:
@@ -182,8 +195,7 @@ def run_reference(args, rank: int) -> None:
             "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * dt / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded layered orthotropic model)",
-            "config": {"workload": f"seismic3 {WORKLOAD['n']}^3+16 CPML ({p.nx}^3 padded), reference CPU loops",
-                       "grid": [p.nx, p.ny, p.nz], "seed": WORKLOAD["seed"]},
+            "config": bench_config(p, args.gpus),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": orc.load("omp").oracle_threads(), "kind": "port",
                              "sample": f"{k} of {args.steps} requested full time steps of the {p.nx}^3 grid after {args.warmup} warm-up steps (FP64, OpenMP)"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -614,16 +626,21 @@ def main():
     sb = step_bytes(p, box_cells)
     step_gbs = sb * args.steps / (ms_total / 1e3) / 1e9
     launches = sum(v["launches"] for v in kernels.values())
-    fp32_fields = s.get_fields()
-    tr32, _ = s.traces()
     s.close()
 
-    e2e = None
+    def rel(a, b):
+        a, b = np.asarray(a), np.asarray(b)
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+    # the full-length problem: the configuration's 1500 steps from the zero state
+    pe = dataclasses.replace(p, time_steps=WORKLOAD["nt"], src={k: v[:WORKLOAD["nt"]] for k, v in p.src.items()})
+    e2e, clk_e2e, full32 = None, None, None
     if not args.no_e2e:
         # through the C ABI with host buffers: one full reference-length run
-        pe = dataclasses.replace(p, time_steps=WORKLOAD["nt"], src={k: v[:WORKLOAD["nt"]] for k, v in p.src.items()})
         torch.cuda.synchronize()
         barrier()
+        ce = Clocks(local, interval_ms=100)
+        ce.start()
         t0 = time.perf_counter()
         with sg.Solver(pe, sg.FP32) as se:   # host FP64 model, sources and initial fields in
             torch.cuda.synchronize()
@@ -636,6 +653,8 @@ def main():
             t3 = time.perf_counter()
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
+        clk_e2e = ce.stop()
+        full32 = {"traces": tr_out, "fields": f_out}
         phases = {"setup_s": t1 - t0, "steps_s": t2 - t1, "readback_s": t3 - t2, "teardown_s": t0 + te - t3}
         barrier()
         model_bytes = sum(a.nbytes for a in pe.model_list())
@@ -646,54 +665,60 @@ def main():
         e2e = {"value": world * pe.ncell * pe.time_steps / te / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int((model_bytes + src_bytes + f0_bytes) / pe.time_steps),
                "d2h_bytes_per_step": int((f_bytes + tr_bytes) / pe.time_steps),
-               "steps": pe.time_steps, "seconds": te, "phases": phases,
+               "steps": pe.time_steps, "seconds": te, "phases": phases, "clocks": clk_e2e,
                "note": "Solver API on host FP64 buffers: upload and FP32 conversion of the model and sources "
                        "(zero initial state), 1500 steps, copy-back of final fields, traces and norms"}
 
     extra = {}
     if not args.no_fp64 and rank == 0:
-        # FP64 drop-in path on the same workload and the FP32-vs-FP64 error
-        s64 = sg.Solver(p, sg.FP64)
+        if full32 is None:
+            g = _timed_run(pe, sg.FP32, want_fields=True)
+            full32 = {"traces": g["traces"], "fields": g["fields"]}
+        # FP64 fields with the fast arithmetic (reciprocals, FMA; within 1e-12
+        # of the exact FP64 build): all 1500 steps of the configuration, the
+        # FP64 reference the FP32 result is held to
+        fx = _timed_run(pe, sg.FP64_FAST, want_fields=True)
+        # the exact FP64 drop-in path: its rate over a sample of steps, and its
+        # traces against the fast FP64 run's over the same steps
+        s64 = sg.Solver(pe, sg.FP64)
         s64.step(args.warmup)
         s64.sync()
         k64 = min(args.steps, 40)
         pr64 = s64.profile(k64)
-        s64.step(args.steps - k64)
         s64.sync()
         tr64, _ = s64.traces()
-        f64 = s64.get_fields()
         s64.close()
+        n64 = args.warmup + k64
         extra["fp64_plain"] = {"value": p.ncell * k64 / (pr64["total_ms"] / 1e3) / 1e9, "unit": UNIT,
-                               "steps": k64}
+                               "steps": k64, "ms_per_step": pr64["total_ms"] / k64, "dtype": "f64",
+                               "build": "exact (IEEE divisions, no FMA contraction; bit-exact with the CPU "
+                                        "restatement)"}
+        extra["fp64_fast"] = {"value": pe.ncell * fx["steps"] / (fx["ms"] / 1e3) / 1e9, "unit": UNIT,
+                              "steps": fx["steps"], "ms_per_step": fx["ms"] / fx["steps"], "dtype": "f64",
+                              "traces_rel_l2_vs_fp64": rel(fx["traces"][:n64], tr64),
+                              "steps_vs_fp64": n64}
+        per_field = [rel(a, b) for a, b in zip(full32["fields"], fx["fields"])]
         extra["fp32_vs_fp64"] = {
-            "traces_rel_l2": float(np.linalg.norm(tr32 - tr64) / max(np.linalg.norm(tr64), 1e-300)),
-            "vz_rel_l2": float(np.linalg.norm(fp32_fields[2] - f64[2]) / max(np.linalg.norm(f64[2]), 1e-300)),
-            "steps": args.warmup + args.steps}
+            "steps": pe.time_steps, "reference": "fast FP64 build, all steps of the configuration",
+            "traces_rel_l2": rel(full32["traces"], fx["traces"]),
+            "fields_rel_l2_max": max(per_field),
+            "fields_rel_l2": dict(zip(["vx", "vy", "vz", "sxx", "sxy", "sxz", "syy", "syz", "szz"], per_field)),
+            "bound": 1e-4}
         extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
-        # FP64 fields with the fast arithmetic (reciprocals, FMA): same steps, error against the exact path
-        sx = sg.Solver(p, sg.FP64_FAST)
-        sx.step(args.warmup)
-        sx.sync()
-        prx = sx.profile(k64)
-        sx.step(args.steps - k64)
-        sx.sync()
-        trx, _ = sx.traces()
-        sx.close()
-        extra["fp64_fast"] = {"value": p.ncell * k64 / (prx["total_ms"] / 1e3) / 1e9, "unit": UNIT, "steps": k64,
-                              "traces_rel_l2_vs_fp64": float(np.linalg.norm(trx - tr64) /
-                                                             max(np.linalg.norm(tr64), 1e-300))}
+        extra["fp32_speedup_vs_fp64_fast"] = value / world / extra["fp64_fast"]["value"]
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline_sample(p)
+    legs = {}
     if not args.no_2d and rank == 0:
-        extra["configs_2d"] = bench_2d_configs()
-        extra["families"] = bench_families()
+        legs["configs_2d"] = bench_2d_configs()
+        legs["families"] = bench_families()
     if not args.no_batch and rank == 0:
-        extra["batched"] = bench_batch()
+        legs["batched"] = bench_batch()
     if not args.no_fwi and rank == 0:
-        extra["fwi"] = bench_fwi()
-        extra["fwi_em"] = bench_fwi_em()
+        legs["fwi"] = bench_fwi()
+        legs["fwi_em"] = bench_fwi_em()
 
     if rank == 0:
         line = {
@@ -701,23 +726,21 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded 5-layer rotated-orthotropic model, Ricker force source)",
-            "config": {"workload": f"seismic3 anisotropic elastic, {WORKLOAD['n']}^3 interior + 16 CPML ({p.nx}^3 padded), FP32",
-                       "grid": [p.nx, p.ny, p.nz], "cells": p.ncell, "receivers": 1024, "seed": WORKLOAD["seed"],
-                       "l2": "inputs larger than L2 (about 14 GB moved per step vs 129 MB L2)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(p, world),
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": TRAFFIC_RATIO[dom] * kb[dom] if dom in TRAFFIC_RATIO else None,
                          "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
                          "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms},
             "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb},
-            "kernels": kernels,
-            "gpu_launches": launches,
-            "clocks": clk,
-            "e2e": e2e,
-            "cpu_baseline": cpu,
-            "wall_s_timed": wall,
             **extra,
+            "kernels": kernels,
+            "wall_s_timed": wall,
+            **legs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -243,6 +243,15 @@ int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, doubl
                            int* kernel_launches, char* names, int names_len);
 /* Number of kernel launches the last seidart_solver_step call issued. */
 long long seidart_solver_launches(const SeidartSolver* s);
+/* Diagnostic, no counterpart in the reference (its only failure channel is
+ * the blow-up stop, cpmlfdtd.f08:2263): the FP32 3D kernels' bound on each
+ * device wait (shared-memory copies, and the fused step's wait for finished
+ * planes), in polls; default 2^20.  probe_bytes > 0 (a multiple of 16) is a
+ * test hook: one CTA arms its copy barrier with that many bytes more than its
+ * copies bring, and one item of the fused step waits for a plane count that
+ * is never reached, so those waits run out; the next seidart_solver_sync
+ * returns SEIDART_ERR_TIMEOUT once and the solver stays usable. */
+int seidart_solver_set_wait(SeidartSolver* s, int limit, int probe_bytes);
 int seidart_solver_destroy(SeidartSolver* s);
 /* Device pointer, element type and stream of field slot `slot` (for callers
  * that read the live fields on the device, e.g. snapshot writers). */
@@ -426,7 +435,10 @@ int seidart_attenuation_write(const char* dir, const int* im, int nx, int nz, co
  * per-trace accumulators must start at zero: each call clears them on
  * `stream` before use.  The first call on each device looks the array up
  * (cudaGetSymbolAddress with that device current, which may load the
- * module); make that first call before any stream capture begins.  Calls
+ * module); make that first call before any stream capture begins.  Every
+ * call waits for `stream` to finish before it returns, because it copies
+ * the results into host memory.  The looked-up address is kept for the life
+ * of the process, so cudaDeviceReset between calls is not supported.  Calls
  * that overlap on one device share the scratch and race: serialise them. */
 #define SEIDART_NOALLOC_MAX_TRACES 8192
 int seidart_trace_misfit_noalloc(const float* syn, const float* obs, float* residual, int nsteps, int ntraces,

@@ -236,7 +236,13 @@ struct S3Args {
     const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
     const void* staged_v;  // the same for the staged velocity kernel
     int velocity_minb;     // FP32: CTAs per SM the cell velocity kernel is compiled for (4 .. 8)
+    int wait_limit;        // FP32: polls of a bounded mbarrier or plane wait before the kernel gives up
+    int wait_probe;        // test hook: bytes armed beyond a copy's size on one CTA (0 = off)
+    int* wave_ctl;         // FP32 fused step: [0] work ticket, [WAVE_DONE0 + k] tiles of plane k done; NULL = two kernels
+    int wave_n;            // ints of wave_ctl the epilogue clears
 };
+// layout of S3Args::wave_ctl
+constexpr int WAVE_DONE0 = 32;
 // TMA tensor maps of the staged FP32 3D stress kernel: old stresses (32 x 8
 // boxes), velocities with a 4/2-cell x/y halo (40 x 12 boxes) and without
 // (32 x 8 boxes, for the z neighbours)
@@ -252,6 +258,9 @@ void launch_seismic3_staged_velocity(const S3Args<float>& a, const S3XMaps& maps
 bool seismic3_make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz, int bx, int by);
 bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* maps);
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st);
+// fused step: both half-steps of one time step in one launch (wavefront over z planes)
+bool seismic3_wave_prepare(const S3Args<float>& a);
+void launch_seismic3_wave(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st);
 // TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
 // (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes
 struct S3Maps {

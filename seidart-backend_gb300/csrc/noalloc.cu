@@ -17,6 +17,10 @@
 // Calls that overlap on one device (two host threads, or two streams
 // without ordering between them) share the accumulators and corrupt each
 // other's results: callers serialise calls per device.
+// The device address of the array and the SM count are looked up once per
+// device and kept for the life of the process; cudaDeviceReset between
+// calls is not supported (it unloads the module, and the kept address would
+// then point at freed memory).
 #include <cuda_runtime.h>
 #include <stdio.h>
 
@@ -34,6 +38,7 @@ constexpr int MAX_DEVICES = 64;
 static __device__ __align__(256) double g_misfit_scratch[MAXT + 32];
 
 std::atomic<double*> g_scratch_ptr[MAX_DEVICES];
+std::atomic<int> g_sm_count[MAX_DEVICES];
 
 }  // namespace
 
@@ -98,14 +103,19 @@ int seidart_trace_misfit_noalloc(const float* syn, const float* obs, float* resi
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_misfit_scratch);
         if (e != cudaSuccess || !p) return nerr(SEIDART_ERR_CUDA, cudaGetErrorString(e));
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            return nerr(SEIDART_ERR_CUDA, "cannot read the SM count of the current device");
+        g_sm_count[dev].store(sms, std::memory_order_relaxed);
         acc = (double*)p;
         g_scratch_ptr[dev].store(acc, std::memory_order_release);
     }
+    const int sms = g_sm_count[dev].load(std::memory_order_relaxed);
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(acc, 0, sizeof(double) * ntraces, st) != cudaSuccess)
         return nerr(SEIDART_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     const int gx = (ntraces + TB - 1) / TB;
-    const int want_y = (4 * 152 + gx - 1) / gx;  // about four CTAs per SM in all
+    const int want_y = (4 * sms + gx - 1) / gx;  // about four CTAs per SM in all
     const int spb = (nsteps + want_y - 1) / want_y;
     const int gy = (nsteps + spb - 1) / spb;
     misfit_partial<<<dim3(gx, gy), TB, 0, st>>>(syn, obs, residual, nsteps, ntraces, spb, acc);

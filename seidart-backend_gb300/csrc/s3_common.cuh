@@ -78,6 +78,11 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
         : "memory");
     return ok != 0;
 }
+// complete `bytes` of the barrier's pending transaction count from this
+// thread (the test hook's stand-in for bytes that never arrive)
+__device__ __forceinline__ void mbar_complete_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
 // bounded wait: false when the phase did not complete within `limit` polls
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity, int limit) {
     for (int it = 0; it < limit; ++it)

@@ -16,7 +16,7 @@
 // what the register-bound one-cell kernels lack: they stall on load latency
 // with HBM a third busy.  A wait that gives up sets the solver's error word
 // and skips the update; the CTA still lets its copy land before exiting.
-#include "s3_common.cuh"
+#include "s3_velocity.cuh"
 
 namespace {
 
@@ -24,7 +24,34 @@ using namespace s3;
 
 constexpr int BX = 32, BY = 8, NT = BX * BY, NCOEF = 27;
 constexpr unsigned TILE_BYTES = NCOEF * NT * sizeof(float);
-constexpr int WAIT_LIMIT = 1 << 20;
+
+// stress store: streaming (evict-first) when the next reader is the next
+// launch, plain when other CTAs of the same launch read it back from L2
+template <bool STREAM>
+__device__ __forceinline__ void st_sig(float* p, float v) {
+    if constexpr (STREAM) __stcs(p, v);
+    else *p = v;
+}
+
+// The bounded wait of a staged CTA.  On give-up the CTA sets the solver's
+// error word and its first thread waits again, with the far larger bound
+// WAIT_LAND, for the copies it issued to land, so that no copy writes into
+// shared memory after the CTA has retired (the copies read this GPU's own
+// HBM, so they finish within microseconds whenever the GPU makes progress).
+// `probe` > 0 (a test hook, one CTA): the barrier was armed with that many
+// bytes more than the copies bring, so the first wait runs out; the give-up
+// path then completes the missing bytes itself before it drains.
+constexpr int WAIT_LAND = 1 << 26;
+__device__ __forceinline__ bool staged_wait(const S3Args<float>& A, unsigned long long* bar, int tid, int probe) {
+    if (mbar_wait_bounded(bar, 0, A.wait_limit)) return true;
+    if (tid == 0) {
+        if (A.err) atomicExch(A.err, 1);
+        if (probe > 0) mbar_complete_tx(bar, (unsigned)probe);
+        mbar_wait_bounded(bar, 0, WAIT_LAND);
+    }
+    return false;
+}
+
 
 __global__ void __launch_bounds__(NT) s3b_pack(S3Args<float> A, float* P) {
     const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
@@ -105,14 +132,7 @@ __device__ __forceinline__ void stress_tile(const S3Args<float>& A, const float*
             bz[f] = (27.0f * (a0 - zm1) - (zp1 - zm2)) * hz;
         }
     }
-    const bool ok = mbar_wait_bounded(bar, 0, WAIT_LIMIT);
-    if (!ok) {
-        if (A.err) atomicExch(A.err, 1);
-        // the copy may still be in flight: keep the CTA (and its shared
-        // memory) alive until it lands, again with a bounded wait
-        if (tid == 0) mbar_wait_bounded(bar, 0, WAIT_LIMIT);
-        return;
-    }
+    if (!staged_wait(A, bar, tid, 0)) return;
     if (!active) return;
     const auto CR = [&](int q) { return coef[q * NT + tid]; };
     const auto GM = [&](int q) { return coef[(21 + q) * NT + tid]; };
@@ -190,11 +210,11 @@ constexpr int XS_VZ = XS_VH + 3 * VHW * VHH;    // [3][4][NT]: z = k-2, k-1, k+1
 constexpr int XS_TOTAL = XS_VZ + 12 * NT;
 constexpr unsigned XS_BYTES = XS_TOTAL * sizeof(float);  // 51,840
 
-template <bool LEAN>
+template <bool LEAN, bool STREAM = true>
 __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float* sm, unsigned long long* bar, int tid,
-                                            int k) {
+                                            int x0, int y0, int k, int probe) {
     const int nx = A.nx, ny = A.ny, nz = A.nz;
-    const int gx = blockIdx.x * BX + threadIdx.x, gy = blockIdx.y * BY + threadIdx.y;
+    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
     bool L1 = true, L2 = true, L3 = true, L4 = true, active = true;
     if (!LEAN) {
         const bool x14 = gx >= 1 && gx <= nx - 3, x23 = gx >= 2 && gx <= nx - 2;
@@ -203,14 +223,7 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
         L1 = x14 && y13 && z12; L2 = x23 && y24 && z12; L3 = x23 && y13 && z34; L4 = x14 && y24 && z34;
         active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
     }
-    const bool ok = mbar_wait_bounded(bar, 0, WAIT_LIMIT);
-    if (!ok) {
-        if (A.err) atomicExch(A.err, 1);
-        // copies may still be in flight: keep the CTA (and its shared
-        // memory) alive until they land, again with a bounded wait
-        if (tid == 0) mbar_wait_bounded(bar, 0, WAIT_LIMIT);
-        return;
-    }
+    if (!staged_wait(A, bar, tid, probe)) return;
     if (!active) return;
     const size_t c = (size_t)gx + (size_t)nx * ((size_t)gy + (size_t)ny * k);
     const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
@@ -243,60 +256,212 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
     if (L1) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) loop_cpml<1>(A, c, ex, ey, ez);
-        __stcs(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
-        __stcs(A.f[6] + c, stress_new(CR, so[3 * NT], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
-        __stcs(A.f[8] + c, stress_new(CR, so[5 * NT], GM(2), 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[6] + c, stress_new(CR, so[3 * NT], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[8] + c, stress_new(CR, so[5 * NT], GM(2), 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
     }
     if (L2) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) loop_cpml<2>(A, c, ex, ey, ez);
-        __stcs(A.f[4] + c, stress_new(CR, so[NT], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[4] + c, stress_new(CR, so[NT], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
     }
     if (L3) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
         if (pml) loop_cpml<3>(A, c, ex, ey, ez);
-        __stcs(A.f[5] + c, stress_new(CR, so[2 * NT], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[5] + c, stress_new(CR, so[2 * NT], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
     }
     if (L4) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
         if (pml) loop_cpml<4>(A, c, ex, ey, ez);
-        __stcs(A.f[7] + c, stress_new(CR, so[4 * NT], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+        st_sig<STREAM>(A.f[7] + c, stress_new(CR, so[4 * NT], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
     }
+}
+
+// Arm the CTA's barrier and issue the 22 copies of one staged stress tile
+// (tile tx, ty of plane k; `lin` its index in the packed coefficient array),
+// one per lane of warp 0.  `probe` extra bytes are armed on top (test hook).
+__device__ __forceinline__ void stress_copies(const S3Args<float>& A, const S3XMaps& M, float* sm,
+                                              unsigned long long* bar, int tid, int x0, int y0, int k, size_t lin,
+                                              int probe) {
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_expect_tx(bar, XS_BYTES + (unsigned)probe);
+    }
+    __syncthreads();
+    if (tid < 22) {
+        if (tid == 0) {
+            bulk_g2s(sm, A.packed + lin * (NCOEF * NT), TILE_BYTES, bar);
+        } else if (tid <= 6) {
+            tma_load3(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, bar);
+        } else if (tid <= 9) {
+            tma_load3(sm + XS_VH + (tid - 7) * VHW * VHH, &M.vh[tid - 7], x0 - 4, y0 - 2, k, bar);
+        } else {
+            const int q = tid - 10, f = q >> 2, zi = q & 3;
+            const int dz = zi < 2 ? zi - 2 : zi - 1;
+            tma_load3(sm + XS_VZ + q * NT, &M.vp[f], x0, y0, k + dz, bar);
+        }
+    }
+}
+
+__device__ __forceinline__ bool lean_stress_tile(const S3Args<float>& A, int x0, int y0, int k) {
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    return x0 >= 2 && x0 + BX - 1 <= nx - 3 && y0 >= 2 && y0 + BY - 1 <= ny - 3 && k >= 2 && k <= nz - 3 &&
+           x0 >= A.box.i0 && x0 + BX <= A.box.i1 && y0 >= A.box.j0 && y0 + BY <= A.box.j1 && k >= A.box.k0 &&
+           k < A.box.k1;
+}
+
+// the test hook arms extra bytes on one CTA: the first tile of plane 2
+__device__ __forceinline__ int probe_bytes(const S3Args<float>& A, int tx, int ty, int k) {
+    return (A.wait_probe > 0 && tx == 0 && ty == 0 && k == 2) ? A.wait_probe : 0;
 }
 
 template <int MINB>
 __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __grid_constant__ S3XMaps M) {
     extern __shared__ __align__(128) float sm[];
     __shared__ __align__(8) unsigned long long bar;
-    const int k = blockIdx.z, nx = A.nx, ny = A.ny, nz = A.nz;
+    const int k = blockIdx.z, nz = A.nz;
     const int tid = threadIdx.y * BX + threadIdx.x;
     if (A.prefetch > 0) s3b_prefetch(A, A.prefetch, tid);
     if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
-    if (tid == 0) {
-        mbar_init(&bar, 1);
-        mbar_expect_tx(&bar, XS_BYTES);
-    }
-    __syncthreads();
-    if (tid < 22) {  // one copy per lane of warp 0
-        if (tid == 0) {
-            const size_t t = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k);
-            bulk_g2s(sm, A.packed + t * (NCOEF * NT), TILE_BYTES, &bar);
-        } else if (tid <= 6) {
-            tma_load3(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, &bar);
-        } else if (tid <= 9) {
-            tma_load3(sm + XS_VH + (tid - 7) * VHW * VHH, &M.vh[tid - 7], x0 - 4, y0 - 2, k, &bar);
-        } else {
-            const int q = tid - 10, f = q >> 2, zi = q & 3;
-            const int dz = zi < 2 ? zi - 2 : zi - 1;
-            tma_load3(sm + XS_VZ + q * NT, &M.vp[f], x0, y0, k + dz, &bar);
+    const int probe = probe_bytes(A, blockIdx.x, blockIdx.y, k);
+    stress_copies(A, M, sm, &bar, tid, x0, y0, k, blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k),
+                  probe);
+    if (lean_stress_tile(A, x0, y0, k)) staged_tile<true>(A, sm, &bar, tid, x0, y0, k, probe);
+    else staged_tile<false>(A, sm, &bar, tid, x0, y0, k, probe);
+}
+
+// ------------------------------------------------ fused step (wavefront)
+// Both half-steps of one time step in one launch.  Work items are (plane p,
+// tile) in plane-major order and are handed out by an atomic ticket, so an
+// item is only ever started after every item before it has been started:
+//   * stress half-step of the tile at plane p (the staged tile above, its
+//     stresses stored with plain stores so they stay in L2), then the item
+//     counts itself done for plane p;
+//   * velocity half-step of the same tile at plane m = p - WAVE_LAG, after
+//     the stresses of planes m-2 .. m+2 are done everywhere: those are all
+//     the stresses the velocity loops read (x/y neighbours at plane m, z
+//     neighbours of the tile's own columns), and all the stress updates that
+//     read the old velocities of plane m.
+// The items waited for have lower tickets, so they were claimed by CTAs that
+// are running or done and whose stress half-steps wait for nothing: every
+// wait ends.  The waits are still bounded (WAVE_SPIN polls of 32-ns sleeps
+// scaled by the runtime limit); a wait that runs out raises the solver's
+// error word and skips the tile.  Velocity-loop reads of stresses go through
+// the coherent path (they were written in this launch); the stresses written
+// here and read back a few planes later come from L2, so the step moves each
+// array to or from DRAM about once: the 46 words per interior cell of the
+// whole step, against 55 for the two-kernel step (stresses written and read
+// back, velocities read twice).
+constexpr int WAVE_LAG = 4;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// wait until every tile of planes q0..q1 has finished its stress half-step
+__device__ __forceinline__ bool wave_wait(const int* done, int q0, int q1, int need, int limit) {
+    for (int q = q0; q <= q1; ++q) {
+        int it = 0;
+        while (ld_acquire(done + q) < need) {
+            if (++it > limit) return false;
+            __nanosleep(32);
         }
     }
-    const bool lean = x0 >= 2 && x0 + BX - 1 <= nx - 3 && y0 >= 2 && y0 + BY - 1 <= ny - 3 && k >= 2 && k <= nz - 3 &&
-                      x0 >= A.box.i0 && x0 + BX <= A.box.i1 && y0 >= A.box.j0 && y0 + BY <= A.box.j1 &&
-                      k >= A.box.k0 && k < A.box.k1;
-    if (lean) staged_tile<true>(A, sm, &bar, tid, k);
-    else staged_tile<false>(A, sm, &bar, tid, k);
+    return true;
+}
+
+struct WaveGeom {
+    int gxt, gyt, tpp;  // tiles per row, tile rows, tiles per plane
+};
+
+// L2 prefetch: the stress inputs of the item `ahead` tickets later, and the
+// velocity-phase inputs of this item that nothing has pulled into L2 yet
+// (density of plane m+1, and on shell tiles the velocity-loop memories and
+// the CPML coefficients of plane m)
+__device__ __forceinline__ void wave_prefetch(const S3Args<float>& A, const WaveGeom& G, int t_ahead, int m, int tx,
+                                              int ty, int tid) {
+    const int nz = A.nz;
+    const int pa = t_ahead / G.tpp, ra = t_ahead - pa * G.tpp, tya = ra / G.gxt, txa = ra - tya * G.gxt;
+    if (pa >= 1 && pa <= nz - 2) {
+        const size_t lin = (size_t)txa + (size_t)G.gxt * ((size_t)tya + (size_t)G.gyt * pa);
+        if (tid < NCOEF * NT / 32) pf_l2(A.packed + lin * (NCOEF * NT) + tid * 32);
+        pf_tile_rows(A.f, 9, txa, tya, pa, A.nx, A.ny, tid, NT);
+        if (!tile_in_box(A.box, txa, tya, pa, A.nx, A.ny)) {
+            pf_tile_rows(A.mem, 36, txa, tya, pa, A.nx, A.ny, tid, NT);
+            pf_tile_rows(A.cpml, 6, txa, tya, pa, A.nx, A.ny, tid, NT);
+        }
+    }
+    if (m >= 0 && m < nz) {
+        if (m + 1 < nz) pf_tile_rows(&A.rho, 1, tx, ty, m + 1, A.nx, A.ny, tid, NT);
+        if (!tile_in_box(A.box, tx, ty, m, A.nx, A.ny)) {
+            pf_tile_rows(A.mem + 36, 9, tx, ty, m, A.nx, A.ny, tid, NT);
+            pf_tile_rows(A.cpml, 6, tx, ty, m, A.nx, A.ny, tid, NT);
+        }
+    }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(NT, MINB) s3w_step(S3Args<float> A, StepInfo si, const __grid_constant__ S3XMaps M,
+                                                     WaveGeom G) {
+    extern __shared__ __align__(128) float sm[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int s_ticket, s_ok;
+    __shared__ unsigned redu[2 * NT / 32];
+    __shared__ double redd[2][NT / 32];
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    int* ctl = A.wave_ctl;
+    if (tid == 0) s_ticket = atomicAdd(ctl, 1);
+    __syncthreads();
+    const int t = s_ticket;
+    const int p = t / G.tpp, r = t - p * G.tpp, ty = r / G.gxt, tx = r - ty * G.gxt;
+    const int nx = A.nx, ny = A.ny, nz = A.nz;
+    const int x0 = tx * BX, y0 = ty * BY;
+    const int m = p - WAVE_LAG;
+    if (A.prefetch > 0) wave_prefetch(A, G, t + A.prefetch, m, tx, ty, tid);
+    // ---- stress half-step of plane p
+    if (p >= 1 && p <= nz - 2) {
+        const int probe = probe_bytes(A, tx, ty, p);
+        stress_copies(A, M, sm, &bar, tid, x0, y0, p, (size_t)tx + (size_t)G.gxt * ((size_t)ty + (size_t)G.gyt * p),
+                      probe);
+        if (lean_stress_tile(A, x0, y0, p)) staged_tile<true, false>(A, sm, &bar, tid, x0, y0, p, probe);
+        else staged_tile<false, false>(A, sm, &bar, tid, x0, y0, p, probe);
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(ctl + WAVE_DONE0 + p, 1);
+        }
+    }
+    if (m < 0 || m >= nz) return;
+    // ---- velocity half-step of plane m
+    if (tid == 0) {
+        // test hook: one item waits for a count no plane reaches
+        const int need = G.tpp + ((A.wait_probe > 0 && t == WAVE_LAG * G.tpp) ? 1 : 0);
+        s_ok = wave_wait(ctl + WAVE_DONE0, max(1, m - 2), min(nz - 2, m + 2), need, A.wait_limit);
+        if (!s_ok && A.err) atomicExch(A.err, 1);
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const int it = *si.step;
+    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
+    float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lean_tile(A, x0, y0, m, true)) velocity_cell<true, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
+    else if (gx < nx && gy < ny) velocity_cell<false, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
+    double vn, sn;
+    block_norm2_f32<NT / 32>(
+        vsq, ssq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); },
+        [&] {
+            const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
+            return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+        },
+        redu, &redd[0][0], vn, sn);
+    if (tid == 0) {
+        const int slot = (tx + 7 * ty + 13 * m) % 64;
+        atomic_max_nonneg(A.norms_part + slot, vn);
+        atomic_max_nonneg(A.norms_part + 64 + slot, sn);
+    }
 }
 
 using StressFn = void (*)(S3Args<float>);
@@ -342,6 +507,25 @@ bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* m) {
 
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st) {
     s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
+}
+
+bool seismic3_wave_prepare(const S3Args<float>& a) {
+    if (!a.staged || !a.wave_ctl) return false;
+    if (cudaFuncSetAttribute((const void*)s3w_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_BYTES) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+void launch_seismic3_wave(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st) {
+    WaveGeom G;
+    G.gxt = (a.nx + BX - 1) / BX;
+    G.gyt = (a.ny + BY - 1) / BY;
+    G.tpp = G.gxt * G.gyt;
+    const unsigned items = (unsigned)(G.tpp * (a.nz + WAVE_LAG));
+    s3w_step<4><<<items, dim3(BX, BY), XS_BYTES, st>>>(a, s, maps, G);
 }
 
 void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st) {

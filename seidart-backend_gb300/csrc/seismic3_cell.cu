@@ -14,7 +14,7 @@
 // Stencil neighbours are read through the read-only path (ld.global.nc), so
 // a value shared by adjacent cells comes from L1/L2, not HBM, after the first
 // read.
-#include "s3_common.cuh"
+#include "s3_velocity.cuh"
 
 namespace {
 
@@ -119,120 +119,6 @@ __device__ __forceinline__ void s3c_velocity_prefetch(const S3Args<float>& A, in
         pf_tile_rows(A.mem + 36, 9, tx, ty, k, A.nx, A.ny, tid, BX * BY);
         pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, BX * BY);
     }
-}
-
-// One cell of the velocity half-step.  LEAN: the CTA's whole tile lies
-// inside the inert interior box, at least two cells from every face and away
-// from the source cells, so every update applies, no index needs clamping and
-// no CPML, source or Dirichlet test is made.
-template <bool LEAN>
-__device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, int gx, int gy, int k, float& vsq,
-                                              float& ssq, float (&w)[9]) {
-    const int nx = A.nx, ny = A.ny, nz = A.nz;
-    const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
-    const size_t c = (size_t)gx + sy * gy + sz * k;
-    long xm2 = -2, xm1 = -1, xp1 = 1, xp2 = 2;
-    long ym2 = -2 * (long)sy, ym1 = -(long)sy, yp1 = (long)sy, yp2 = 2 * (long)sy;
-    long zm2 = -2 * (long)sz, zm1 = -(long)sz, zp1 = (long)sz, zp2 = 2 * (long)sz;
-    if (!LEAN) {
-        xm2 = (long)cl(gx - 2, 0, nx - 1) - gx; xm1 = (long)cl(gx - 1, 0, nx - 1) - gx;
-        xp1 = (long)cl(gx + 1, 0, nx - 1) - gx; xp2 = (long)cl(gx + 2, 0, nx - 1) - gx;
-        ym2 = ((long)cl(gy - 2, 0, ny - 1) - gy) * (long)sy; ym1 = ((long)cl(gy - 1, 0, ny - 1) - gy) * (long)sy;
-        yp1 = ((long)cl(gy + 1, 0, ny - 1) - gy) * (long)sy; yp2 = ((long)cl(gy + 2, 0, ny - 1) - gy) * (long)sy;
-        zm2 = ((long)cl(k - 2, 0, nz - 1) - k) * (long)sz; zm1 = ((long)cl(k - 1, 0, nz - 1) - k) * (long)sz;
-        zp1 = ((long)cl(k + 1, 0, nz - 1) - k) * (long)sz; zp2 = ((long)cl(k + 2, 0, nz - 1) - k) * (long)sz;
-    }
-    const float *Sxx = A.f[3] + c, *Sxy = A.f[4] + c, *Sxz = A.f[5] + c, *Syy = A.f[6] + c, *Syz = A.f[7] + c,
-                *Szz = A.f[8] + c, *R = A.rho + c;
-    // ---- loads
-    const float sxx0 = __ldg(Sxx), sxxm1 = __ldg(Sxx + xm1), sxxm2 = __ldg(Sxx + xm2);
-    const float sxy0 = __ldg(Sxy), sxyp1 = __ldg(Sxy + xp1), sxyp2 = __ldg(Sxy + xp2);
-    const float sxyym1 = __ldg(Sxy + ym1), sxyym2 = __ldg(Sxy + ym2);
-    const float syy0 = __ldg(Syy), syyp1 = __ldg(Syy + yp1), syyp2 = __ldg(Syy + yp2);
-    const float sxz0 = __ldg(Sxz), sxzp1 = __ldg(Sxz + xp1), sxzp2 = __ldg(Sxz + xp2);
-    const float sxzzm1 = __ldg(Sxz + zm1), sxzzm2 = __ldg(Sxz + zm2);
-    const float syz0 = __ldg(Syz), syzym1 = __ldg(Syz + ym1), syzym2 = __ldg(Syz + ym2);
-    const float syzzm1 = __ldg(Syz + zm1), syzzm2 = __ldg(Syz + zm2);
-    const float szz0 = __ldg(Szz), szzp1 = __ldg(Szz + zp1), szzp2 = __ldg(Szz + zp2);
-    const float r0 = __ldg(R), rxm = __ldg(R + xm1), rxp = __ldg(R + xp1), rzm = __ldg(R + zm1), rzp = __ldg(R + zp1);
-    float vx = A.f[0][c], vy = A.f[1][c], vz = A.f[2][c];
-    const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
-    const float dt = A.dt;
-    const int code = A.density_code;
-    const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
-                                k < A.box.k1);
-    const float byy = inv_mean_f(r0, r0, code);
-    if (LEAN || (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2)) {  // vx
-        float d1 = (27.0f * (sxx0 - sxxm1) + sxxm2) * hx;
-        float d2 = (27.0f * (sxy0 - sxyym1) + sxyym2) * hy;
-        float d3 = (27.0f * (sxz0 - sxzzm1) + sxzzm2) * hz;
-        if (pml) {
-            const CpmlC p = cpml_at(A, c, true);
-            d1 = cpml_apply(A.mem[36], c, p, d1);
-            d2 = cpml_apply(A.mem[40], c, p, d2);
-            d3 = cpml_apply(A.mem[42], c, p, d3);
-        }
-        vx = vx + (d1 * inv_mean_f(r0, rxm, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
-    }
-    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 1 && gy <= ny - 3 && k >= 2 && k <= nz - 2)) {  // vy
-        float d1 = (27.0f * (sxyp1 - sxy0) - sxyp2) * hx;
-        float d2 = (27.0f * (syyp1 - syy0) - syyp2) * hy;
-        float d3 = (27.0f * (syz0 - syzzm1) + syzzm2) * hz;
-        if (pml) {
-            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
-            d1 = cpml_apply(A.mem[39], c, ph, d1);
-            d2 = cpml_apply(A.mem[37], c, ph, d2);
-            d3 = cpml_apply(A.mem[44], c, pf, d3);
-        }
-        vy = vy + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
-    }
-    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 2 && gy <= ny - 2 && k >= 1 && k <= nz - 3)) {  // vz
-        float d1 = (27.0f * (sxzp1 - sxz0) - sxzp2) * hx;
-        float d2 = (27.0f * (syz0 - syzym1) + syzym2) * hy;
-        float d3 = (27.0f * (szzp1 - szz0) - szzp2) * hz;
-        if (pml) {
-            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
-            d1 = cpml_apply(A.mem[41], c, ph, d1);
-            d2 = cpml_apply(A.mem[43], c, pf, d2);
-            d3 = cpml_apply(A.mem[38], c, ph, d3);
-        }
-        vz = vz + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzp, code)) * dt;
-    }
-    bool src_cell = false;
-    if (!LEAN) {
-        // force source (cpmlfdtd.f08:2214-2219)
-        const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
-        if (gx == is + 1 && gy == js && k == ks && A.src[0]) vx = vx + (float)A.src[0][it - 1] * dt / r0;
-        if (gx == is && gy == js + 1 && k == ks && A.src[1])
-            vy = vy + (float)A.src[1][it - 1] * dt / A.rho[(size_t)is + sy * js + sz * ks];
-        if (gx == is && gy == js && k == ks + 1 && A.src[2]) vz = vz + (float)A.src[2][it - 1] * dt / r0;
-        if (gx == 0 || gx == nx - 1 || gy == 0 || gy == ny - 1 || k == 0 || k == nz - 1) { vx = 0.f; vy = 0.f; vz = 0.f; }
-        src_cell = A.stress_src && ((gx == is && gy == js && k == ks) || (gx == is + 1 && gy == js + 1 && k == ks) ||
-                                    (gx == is + 1 && gy == js && k == ks + 1) || (gx == is && gy == js + 1 && k == ks + 1));
-    }
-    __stcs(A.f[0] + c, vx);
-    __stcs(A.f[1] + c, vy);
-    __stcs(A.f[2] + c, vz);
-    w[0] = vx; w[1] = vy; w[2] = vz;
-    vsq = vx * vx + vy * vy + vz * vz;
-    if (!src_cell) {
-        w[3] = sxx0; w[4] = syy0; w[5] = szz0; w[6] = sxy0; w[7] = syz0; w[8] = sxz0;
-        ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
-    }
-}
-
-// true when the whole 32 x 8 tile of plane k qualifies for the lean path
-__device__ __forceinline__ bool lean_tile(const S3Args<float>& A, int x0, int y0, int k, bool sources) {
-    const int nx = A.nx, ny = A.ny, nz = A.nz;
-    if (!(x0 >= 2 && x0 + BX - 1 <= nx - 3 && y0 >= 2 && y0 + BY - 1 <= ny - 3 && k >= 2 && k <= nz - 3)) return false;
-    if (!(x0 >= A.box.i0 && x0 + BX <= A.box.i1 && y0 >= A.box.j0 && y0 + BY <= A.box.j1 && k >= A.box.k0 &&
-          k < A.box.k1))
-        return false;
-    if (sources) {  // the source cells sit at (is..is+1, js..js+1, ks..ks+1)
-        const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
-        if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + BX && js + 1 >= y0 && js < y0 + BY) return false;
-    }
-    return true;
 }
 
 template <int MINB>
@@ -448,7 +334,7 @@ constexpr int NTV = BX * BY;
 constexpr int P_SZZ = 0, P_XZ1 = 1, P_XZ2 = 2, P_YZ1 = 3, P_YZ2 = 4, P_ZZ1 = 5, P_ZZ2 = 6, P_RM = 7, P_RP = 8, P_V = 9;
 constexpr int XV_TOTAL = XV_P + 12 * NTV;
 constexpr unsigned XV_BYTES = XV_TOTAL * sizeof(float);  // 23,808
-constexpr int WAIT_LIMIT_V = 1 << 20;
+constexpr int WAIT_LAND_V = 1 << 26;  // drain bound on the give-up path (copies read local HBM)
 
 template <bool LEAN>
 __device__ __forceinline__ void staged_velocity_cell(const S3Args<float>& A, const float* sm, int it, int gx, int gy,
@@ -575,10 +461,10 @@ __global__ void __launch_bounds__(BX* BY) s3x_velocity(S3Args<float> A, StepInfo
         }
     }
     float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const bool ok = mbar_wait_bounded(&bar, 0, WAIT_LIMIT_V);
+    const bool ok = mbar_wait_bounded(&bar, 0, A.wait_limit);
     if (!ok) {
         if (A.err) atomicExch(A.err, 1);
-        if (tid == 0) mbar_wait_bounded(&bar, 0, WAIT_LIMIT_V);
+        if (tid == 0) mbar_wait_bounded(&bar, 0, WAIT_LAND_V);
     } else if (lean_tile(A, x0, y0, k, true)) {
         staged_velocity_cell<true>(A, sm, it, gx, gy, k, tid, vsq, ssq, w);
     } else if (gx < nx && gy < ny) {

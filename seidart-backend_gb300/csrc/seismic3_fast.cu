@@ -372,6 +372,9 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
         A.norms_part[threadIdx.x] = 0.0;
         A.norms_part[NSLOT + threadIdx.x] = 0.0;
     }
+    // the fused step's work ticket and plane counters start the next step at zero
+    if (A.wave_ctl)
+        for (int q = threadIdx.x; q < A.wave_n; q += blockDim.x) A.wave_ctl[q] = 0;
     if (threadIdx.x == 0) {
         A.norms[it - 1] = v;
         A.norms[A.nt + it - 1] = w;
@@ -384,6 +387,18 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
 void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
                           const S3Maps* maps, int stress_kind, int velocity_kind) {
     const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
+    if (a.wave_ctl && a.staged) {
+        // both half-steps in one launch
+        launch_seismic3_wave(a, *(const S3XMaps*)a.staged, s, st);
+        if (h) h->fn(h->ctx, 0, "s3w_step");
+        if (a.stress_src) {
+            s3f_stress_source<<<1, 1, 0, st>>>(a, s);
+            if (h) h->fn(h->ctx, 2, "s3f_stress_source");
+        }
+        s3f_epilogue<<<1, 256, 0, st>>>(a, s);
+        if (h) h->fn(h->ctx, 3, "s3f_epilogue");
+        return;
+    }
     if (stress_kind == S3K_BULK && a.packed && a.staged) {
         launch_seismic3_staged_stress(a, *(const S3XMaps*)a.staged, st);
         if (h) h->fn(h->ctx, 0, "s3x_stress");

@@ -26,7 +26,7 @@ namespace {
 
 constexpr int NCOEF = 33;                  // C 21 + gamma 6 + sigma 6
 constexpr int ZCH = 32;                    // planes per CTA
-constexpr long long WAIT_LIMIT = 1 << 20;  // bounded mbarrier polling
+constexpr long long WAIT_LAND = 1 << 26;   // drain bound on the give-up path (copies read local HBM)
 
 // Tile shape TX x TY, SC coefficient stages, RV velocity ring planes (5 in use
 // plus RV-5 ahead), MINB CTAs per SM.  The velocity box starts at x0-4 so
@@ -64,11 +64,14 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
         : "memory");
     return ok != 0;
 }
-// bounded wait; false if the copy did not land within the budget
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
-    for (long long it = 0; it < WAIT_LIMIT; ++it)
+// bounded wait; false if the copy did not land within `limit` polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity, long long limit) {
+    for (long long it = 0; it < limit; ++it)
         if (mbar_try_wait(b, parity)) return true;
     return false;
+}
+__device__ __forceinline__ void mbar_complete_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(sa(b)), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void tma3(void* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
     asm volatile(
@@ -147,9 +150,14 @@ __global__ void __launch_bounds__(K::TX* K::TY, K::MINB) s3t_stress(S3Args<float
     // producer state (thread 0): copies in flight and the phase parity each
     // will complete, for the bounded drain on the error path
     unsigned pend_c = 0, pend_v = 0, par_c = 0, par_v = 0;
+    // test hook: the first CTA arms its first coefficient stage with extra
+    // bytes that no copy brings, so its bounded wait runs out
+    const unsigned probe = (A.wait_probe > 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0)
+                               ? (unsigned)A.wait_probe : 0u;
+    const long long limit = A.wait_limit;
     auto issue_coef = [&](int p) {
         const int s = (p - kb) % SC;
-        mbar_expect_tx(&S.full_c[s], coef_bytes);
+        mbar_expect_tx(&S.full_c[s], coef_bytes + (p == kb ? probe : 0u));
         for (int a = 0; a < NCOEF; ++a) tma3(&S.coef[s][a][0][0], &maps.coef[a], x0, y0, p, &S.full_c[s]);
         pend_c |= 1u << s;
         par_c = (par_c & ~(1u << s)) | ((((unsigned)(p - kb) / SC) & 1u) << s);
@@ -171,12 +179,12 @@ __global__ void __launch_bounds__(K::TX* K::TY, K::MINB) s3t_stress(S3Args<float
     __syncthreads();
     bool fail = false;
     // the first four velocity planes (kb-2 .. kb+1)
-    for (int p = kb - 2; p <= kb + 1 && !fail; ++p) fail = !mbar_wait(&S.full_v[(p - (kb - 2)) % RV], 0);
+    for (int p = kb - 2; p <= kb + 1 && !fail; ++p) fail = !mbar_wait(&S.full_v[(p - (kb - 2)) % RV], 0, limit);
 
     for (int k = kb; k < ke; ++k) {
         const int sc = (k - kb) % SC, sv2 = (k + 2 - (kb - 2)) % RV;
-        if (!fail) fail = !mbar_wait(&S.full_c[sc], ((k - kb) / SC) & 1);
-        if (!fail) fail = !mbar_wait(&S.full_v[sv2], ((k + 2 - (kb - 2)) / RV) & 1);
+        if (!fail) fail = !mbar_wait(&S.full_c[sc], ((k - kb) / SC) & 1, limit);
+        if (!fail) fail = !mbar_wait(&S.full_v[sv2], ((k + 2 - (kb - 2)) / RV) & 1, limit);
         if (__syncthreads_or(fail)) { fail = true; break; }
         if (tid == 0) pend_c &= ~(1u << sc);
         if (tid == 0) pend_v &= ~(1u << sv2);
@@ -242,11 +250,13 @@ __global__ void __launch_bounds__(K::TX* K::TY, K::MINB) s3t_stress(S3Args<float
     }
     if (fail && tid == 0) {
         atomicExch(A.err, 1);
-        // wait (bounded) for this CTA's copies in flight before shared memory is released
+        if (probe) mbar_complete_tx(&S.full_c[0], probe);  // the bytes the test hook held back
+        // wait, with the far larger bound WAIT_LAND, for this CTA's copies in
+        // flight before its shared memory is released
         for (int s = 0; s < SC; ++s)
-            if (pend_c >> s & 1) mbar_wait(&S.full_c[s], par_c >> s & 1);
+            if (pend_c >> s & 1) mbar_wait(&S.full_c[s], par_c >> s & 1, WAIT_LAND);
         for (int s = 0; s < RV; ++s)
-            if (pend_v >> s & 1) mbar_wait(&S.full_v[s], par_v >> s & 1);
+            if (pend_v >> s & 1) mbar_wait(&S.full_v[s], par_v >> s & 1, WAIT_LAND);
     }
 }
 

@@ -162,6 +162,8 @@ struct SeidartSolver {
     int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
     int* err_dev = nullptr;  // error word raised by bounded device waits
+    int* wave_ctl = nullptr; // FP32 3D fused step: work ticket and per-plane counters (arena)
+    int wave_n = 0;
     int nnorm = 1;
     int steps_done = 0;
     int stress_src = 0;
@@ -666,6 +668,10 @@ void finish_args(SeidartSolver& s) {
         a.nt = s.src.time_steps;
         a.norms_part = s.norms_part;
         a.err = s.err_dev;
+        a.wait_limit = 1 << 20;
+        a.wait_probe = 0;
+        a.wave_ctl = nullptr;  // set once the fused step is prepared
+        a.wave_n = 0;
         break;
     }
     }
@@ -687,7 +693,10 @@ const PwDev& solver_pw(const SeidartSolver& s) {
 // plane wave's face launches plus its norm launch
 int launches_per_step(const SeidartSolver& s) {
     const PwDev& pw = solver_pw(s);
-    return 3 + (s.stress_src ? 1 : 0) + (pw.on && pw.nface > 0 ? pw.nface + 1 : 0);
+    // the fused 3D step replaces the two half-step kernels by one
+    const bool wave = s.family == SEIDART_SEISMIC3 && s.precision == SEIDART_FP32 && !pw.on && s.s3f.wave_ctl &&
+                      s.s3f.staged;
+    return (wave ? 2 : 3) + (s.stress_src ? 1 : 0) + (pw.on && pw.nface > 0 ? pw.nface + 1 : 0);
 }
 
 void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nullptr) {
@@ -860,6 +869,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->norms = (double*)s->carve(sizeof(double) * src->time_steps * s->nnorm);
         s->norms_part = (double*)s->carve(sizeof(double) * 2 * 64);
         s->err_dev = (int*)s->carve(sizeof(int));
+        if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32) {
+            s->wave_n = WAVE_DONE0 + s->dom.nz;
+            s->wave_ctl = (int*)s->carve(sizeof(int) * s->wave_n);
+        }
         if (pass == 0) {
             // model arrays: measured by running the set-up against a null arena
             derived.clear();
@@ -961,6 +974,20 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         if (s->s3f.staged && (sv && *sv == '1') && s->s3_velocity_kind == S3K_CELL &&
             seismic3_staged_velocity_prepare(s->s3f, &s->s3_staged))
             s->s3f.staged_v = &s->s3_staged;
+        // fused step (both half-steps in one wavefront launch) on top of the
+        // staged stress tiles, on request (SEIDART_S3_WAVE=1)
+        const char* wv = getenv("SEIDART_S3_WAVE");
+        if (s->s3f.staged && !s->s3f.staged_v && (wv && *wv == '1') && s->s3_velocity_kind == S3K_CELL &&
+            s->wave_ctl) {
+            s->s3f.wave_ctl = s->wave_ctl;
+            s->s3f.wave_n = s->wave_n;
+            if (cudaMemsetAsync(s->wave_ctl, 0, sizeof(int) * s->wave_n, s->stream) != cudaSuccess ||
+                !seismic3_wave_prepare(s->s3f)) {
+                cudaGetLastError();
+                s->s3f.wave_ctl = nullptr;
+                s->s3f.wave_n = 0;
+            }
+        }
     }
     *out = s;
     return SEIDART_OK;
@@ -1071,7 +1098,11 @@ int seidart_solver_sync(SeidartSolver* s) {
     if (s->err_dev) {
         int err = 0;
         CUDA_TRY(cudaMemcpy(&err, s->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
-        if (err) return set_err(SEIDART_ERR_TIMEOUT, "a bounded device wait (TMA copy) did not complete");
+        if (err) {
+            // report it once: clear the word so later steps start clean
+            CUDA_TRY(cudaMemset(s->err_dev, 0, sizeof(int)));
+            return set_err(SEIDART_ERR_TIMEOUT, "a bounded device wait (copy or plane wait) did not complete");
+        }
     }
     if (s->steps_done == 0) return SEIDART_OK;
     std::vector<double> nrm(s->steps_done);
@@ -1164,6 +1195,19 @@ void* seidart_solver_field_ptr(SeidartSolver* s, int slot) {
 }
 
 long long seidart_solver_launches(const SeidartSolver* s) { return s ? s->launches : -1; }
+
+int seidart_solver_set_wait(SeidartSolver* s, int limit, int probe_bytes) {
+    if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
+    if (limit < 1 || probe_bytes < 0 || probe_bytes % 16 != 0)
+        return set_err(SEIDART_ERR_ARG, "wait limit must be >= 1 and probe bytes a non-negative multiple of 16");
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->s3f.wait_limit = limit;
+    s->s3f.wait_probe = probe_bytes;
+    // the launch arguments are baked into the captured step graphs
+    for (int q = 0; q < 2; ++q)
+        if (s->graph_exec[q]) { cudaGraphExecDestroy(s->graph_exec[q]); s->graph_exec[q] = nullptr; s->graph_len[q] = 0; }
+    return SEIDART_OK;
+}
 
 int seidart_solver_destroy(SeidartSolver* s) {
     if (!s) return SEIDART_OK;

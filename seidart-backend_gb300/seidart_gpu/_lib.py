@@ -79,6 +79,7 @@ _SIGS = {
                                          C.c_int]),
     "seidart_solver_field_ptr": (C.c_void_p, [C.c_void_p, C.c_int]),
     "seidart_solver_launches": (C.c_longlong, [C.c_void_p]),
+    "seidart_solver_set_wait": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "seidart_solver_destroy": (C.c_int, [C.c_void_p]),
     "seidart_last_error": (C.c_char_p, []),
 }

@@ -249,6 +249,12 @@ class Solver:
     def launches(self) -> int:
         return lib().seidart_solver_launches(self.handle)
 
+    def set_wait(self, limit: int, probe_bytes: int = 0) -> None:
+        """Bound (in polls) of the FP32 3D kernels' device waits; probe_bytes > 0
+        is the test hook that makes one CTA's waits run out (see
+        seidart_solver_set_wait in include/seidart_gpu.h)."""
+        check(lib().seidart_solver_set_wait(self.handle, int(limit), int(probe_bytes)))
+
     def field_ptr(self, slot: int) -> int:
         return lib().seidart_solver_field_ptr(self.handle, slot)
 

@@ -91,8 +91,10 @@ def sharded_gradient(problem, shots: list, observed: list, rank: int, world: int
     if idx:
         loss, g = gradient(problem, [shots[i] for i in idx], [observed[i] for i in idx])
     else:
-        from .fwi import GRAD_KEYS
-        loss, g = 0.0, {k: np.zeros(problem.shape, order="F") for k in GRAD_KEYS}
+        # a rank without shots still joins every collective: it sends zeros
+        # under the same keys the busy ranks send for this problem family
+        from .fwi import grad_keys
+        loss, g = 0.0, {k: np.zeros(problem.shape, order="F") for k in grad_keys(problem.family)}
     arrays = {k: np.asarray(v, dtype=np.float64) for k, v in g.items()}
     arrays["__loss__"] = np.array([loss], dtype=np.float64)
     tot = allreduce_sum(arrays)

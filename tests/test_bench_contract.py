@@ -18,3 +18,7 @@ def test_reference_arm_prints_one_json_line():
     assert d["warmup"] == 3 and d["steps"] >= 2 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    # both arms describe the workload with the same dict
+    import bench
+    bench.WORKLOAD["n"] = 8
+    assert d["config"] == bench.bench_config(bench.make_problem(nt=5), 1)

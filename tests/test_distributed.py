@@ -15,6 +15,32 @@ import torch.multiprocessing as mp  # noqa: E402
 
 class _P:
     shape = (6, 5)
+    family = 1  # seismic2
+
+
+class _PEm:
+    shape = (6, 5)
+    family = 4  # electromag2
+
+
+def _fake_gradient_em(p, shots, observed):
+    loss = float(sum(s for s in shots))
+    g = {k: sum((s + 1.0) * (q + 1) * np.ones(p.shape) for s in shots) for q, k in
+         enumerate(("e11", "e13", "e33", "s11", "s13", "s33"))}
+    return loss, g
+
+
+def _worker_idle(rank, world, port, out):
+    """One shot over `world` ranks: every rank but rank 0 owns no shot."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from seidart_gpu.distributed import sharded_gradient
+        loss, g = sharded_gradient(_PEm(), [0], [None], rank, world, gradient=_fake_gradient_em)
+        out.put((rank, loss, sorted(g), {k: float(v.sum()) for k, v in g.items()}))
+    finally:
+        dist.destroy_process_group()
 
 
 def _fake_gradient(p, shots, observed):
@@ -67,6 +93,29 @@ def test_sharded_gradient_and_max_time_world2():
         for k, v in full_g.items():
             assert gsum[k] == pytest.approx(v.sum())
         assert t == 2.0                                  # slowest rank
+
+
+def test_sharded_gradient_idle_rank_electromag2():
+    """More ranks than shots on an electromag2 inversion: the idle rank must
+    contribute zeros under the EM gradient keys, so both ranks make the same
+    collectives and return the one shot's loss and gradient."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker_idle, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    full_loss, full_g = _fake_gradient_em(_PEm(), [0], None)
+    for rank, loss, keys, gsum in res:
+        assert keys == sorted(full_g)
+        assert loss == full_loss
+        for k, v in full_g.items():
+            assert gsum[k] == pytest.approx(v.sum())
 
 
 def test_shard_rejects_bad_rank():

@@ -8,6 +8,12 @@ need an oracle run of that size.
   doubles every field, memory, trace and norm (scaling by 2 commutes with
   rounding, so the FP64 run must match bit for bit and the FP32 run to
   within its subnormal far field).
+* the same seismic3 workload for all 1500 steps of its configuration: FP32
+  traces and final fields within 1e-4 relative L2 of the fast FP64 build
+  (itself within 1e-12 of exact FP64, checked above and in the bench).
+* seismic2 two-layer (256^2 + 20 CPML, 2000 steps, the 2D elastic
+  configuration): the exact FP64 build bit for bit against the CPU
+  restatement over all 2000 steps.
 * electromag2 at 1024^2 + 20 CPML (1064^2 cells) for the full 4000 steps:
   FP32 against FP64 and fast FP64 against FP64.
 """
@@ -75,6 +81,36 @@ def test_seismic3_full_size_linearity(cube):
     assert rel_l2(b32["traces"], 2.0 * a32["traces"]) <= 1e-6
     for q in range(9):
         assert rel_l2(b32["fields"][q], 2.0 * a32["fields"][q]) <= 1e-6, q
+
+
+def test_seismic3_full_length_fp32_vs_fp64():
+    """All 1500 steps of the 3D configuration from the zero state: by then the
+    wavefront from the centre-top source has crossed the receiver grid and
+    reached the CPML, so traces and fields carry the whole propagation."""
+    p = models.seismic3_layers(n=320, cpml=16, nt=1500, seed=2)
+    g32 = _run(p, sg.FP32)
+    gx = _run(p, sg.FP64_FAST)
+    assert np.max(np.abs(gx["traces"])) > 0
+    assert rel_l2(g32["traces"], gx["traces"]) <= 1e-4
+    assert rel_l2(g32["norms"], gx["norms"]) <= 1e-4
+    for q in range(9):
+        assert rel_l2(g32["fields"][q], gx["fields"][q]) <= 1e-4, q
+
+
+def test_seismic2_config0_full_length_bit_exact(oracle):
+    """The 2D elastic configuration for all 2000 steps: exact FP64 on the GPU
+    equals the CPU restatement bit for bit (fields, CPML memories, traces,
+    norms)."""
+    p = models.seismic2_two_layer()  # 256^2 + 20 CPML, 2000 steps
+    ref = oracle.run_oracle(p)
+    got = sg.run(p, sg.FP64)
+    assert np.max(np.abs(ref["traces"])) > 0
+    assert np.array_equal(got["traces"], ref["traces"])
+    assert np.array_equal(got["norms"], ref["norms"])
+    for a, b in zip(got["fields"], ref["fields"]):
+        assert np.array_equal(a, b)
+    for a, b in zip(got["memory"], ref["memory"]):
+        assert np.array_equal(a, b)
 
 
 def test_electromag2_full_size_full_length():
