@@ -349,6 +349,7 @@ def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
     dt = time.perf_counter() - t0
     cfg = b.config()
     launches = b.launches
+    graph_launches = b.graph_launches
     b.close()
     # the same models one by one (single-model FP32 solver), a bounded sample
     seq_cells, seq_t = 0, 0.0
@@ -369,6 +370,7 @@ def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
     return {"value": cells * (nt - warm) / dt / 1e9, "unit": UNIT, "models": nmodels, "cells": cells,
             "algorithmic_gbs": gbs, "frac_of_measured_hbm": gbs / hbm, "bytes_per_step": step_b,
             "steps_timed": nt - warm, "seconds": dt, "setup_s": setup, "tuned": cfg, "gpu_launches": launches,
+            "graph_replays": graph_launches,
             "one_by_one": {"value": seq_cells / seq_t / 1e9, "unit": UNIT,
                            "sample": "first 8 models, 280 timed steps each, single-model FP32 solver"},
             "dtype": "f32"}
@@ -542,6 +544,9 @@ def main():
                     help="run a small ragged batch (16 models of the batch workload's distribution, 40 steps in "
                          "launches of 20, the autotuned kernel) and exit: the case the batch profile in profiles/ "
                          "is captured on")
+    ap.add_argument("--s3-profile-case", action="store_true",
+                    help="run 4 FP32 steps of the 3D workload at --grid (e.g. 192: 224^3 padded cells) through "
+                         "the default kernels and exit: the case the 3D kernel profiles in profiles/ are captured on")
     ap.add_argument("--batch-variant", default=None,
                     help="with --batch-profile-case: 'V,B' runs kernel variant V with B CTAs per SM instead of "
                          "the autotuned choice (so a profiler can capture its first launch)")
@@ -569,6 +574,15 @@ def main():
             b.step(40, chunk=20)
             b.sync()
             print(json.dumps({"batch_profile_case": "ok", "config": b.config()}))
+        return
+    if args.s3_profile_case:
+        import seidart_gpu as sg
+        p = make_problem(nt=4)
+        with sg.Solver(p, sg.FP32) as s:
+            s.step(4)
+            s.sync()
+            tr, _ = s.traces()
+        print(json.dumps({"s3_profile_case": "ok", "grid": [p.nx, p.ny, p.nz], "trace_max": float(np.abs(tr).max())}))
         return
     if args.fwi_profile_case:
         from seidart_gpu import models

@@ -332,6 +332,11 @@ int seidart_batch_force_timeout(SeidartBatch* b, long long spin_limit);
 SeidartSolver* seidart_batch_model(SeidartBatch* b, int m);
 int seidart_batch_steps_done(const SeidartBatch* b);
 long long seidart_batch_launches(const SeidartBatch* b);
+/* How many of the last seidart_batch_step call's launches were replays of a
+ * captured CUDA graph (each chunk's persistent launch is captured once per
+ * chunk length and configuration; the device may refuse capture of a
+ * cooperative launch, in which case the chunks launch directly). */
+long long seidart_batch_graph_launches(const SeidartBatch* b);
 int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid);
 int seidart_batch_num_variants(void);
 int seidart_batch_destroy(SeidartBatch* b);

@@ -456,6 +456,13 @@ struct SeidartBatch {
     double tune_ms[kNumVariants][2] = {{0}};
     int tune_bps[kNumVariants][2] = {{0}};
     long long launches = 0;
+    // chunk graphs: one captured persistent launch of `len` steps per
+    // (variant, CTAs per SM, len); at most two cached (the chunk and a tail)
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int glen[2] = {0, 0}, gvar[2] = {-1, -1}, gbps[2] = {0, 0};
+    int gnext = 0;
+    bool graphs_ok = true;   // false once capture of the cooperative launch failed
+    long long graph_launches = 0;
 };
 
 namespace {
@@ -494,6 +501,41 @@ int launch_chunk(SeidartBatch* b, int var, int bps, int nsteps, int force_timeou
     return SEIDART_OK;
 }
 
+// The graph holding one persistent launch of `n` steps with (var, bps),
+// captured on first use.  A capture that fails leaves *out NULL and turns
+// graphs off for this batch (the caller then launches directly).
+int chunk_graph(SeidartBatch* b, int var, int bps, int n, cudaGraphExec_t* out) {
+    *out = nullptr;
+    for (int q = 0; q < 2; ++q)
+        if (b->gexec[q] && b->glen[q] == n && b->gvar[q] == var && b->gbps[q] == bps) { *out = b->gexec[q]; return SEIDART_OK; }
+    if (!b->graphs_ok) return SEIDART_OK;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        b->graphs_ok = false;
+        return SEIDART_OK;
+    }
+    const long long keep = b->launches;
+    const int rc = launch_chunk(b, var, bps, n, 0);
+    b->launches = keep;  // captured, not launched
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (rc != SEIDART_OK || e != cudaSuccess || !g || cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        b->graphs_ok = false;
+        return rc == SEIDART_ERR_ARG ? rc : SEIDART_OK;
+    }
+    cudaGraphDestroy(g);
+    const int slot = b->gnext;
+    b->gnext ^= 1;
+    if (b->gexec[slot]) cudaGraphExecDestroy(b->gexec[slot]);
+    b->gexec[slot] = ex;
+    b->glen[slot] = n; b->gvar[slot] = var; b->gbps[slot] = bps;
+    *out = ex;
+    return SEIDART_OK;
+}
+
 int read_status(SeidartBatch* b, int* status) {
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return berr(SEIDART_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     int st = 0;
@@ -515,6 +557,8 @@ int seidart_batch_destroy(SeidartBatch* b) {
         if (b->dev_models[v]) cudaFree(b->dev_models[v]);
         if (b->dev_tile_model[v]) cudaFree(b->dev_tile_model[v]);
     }
+    for (int q = 0; q < 2; ++q)
+        if (b->gexec[q]) cudaGraphExecDestroy(b->gexec[q]);
     if (b->ctl) cudaFree(b->ctl);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -666,15 +710,27 @@ int seidart_batch_set_config(SeidartBatch* b, int variant, int bps) {
 }
 
 // Advance every model `nsteps` steps: one persistent cooperative launch per
-// chunk of steps.
+// chunk of steps, each launch captured once in a CUDA graph and replayed
+// (the device step counter lets one graph serve any starting step).
 int seidart_batch_step(SeidartBatch* b, int nsteps, int chunk) {
     if (!b || nsteps < 0 || b->steps_done + nsteps > b->time_steps) return berr(SEIDART_ERR_ARG, "steps exceed time_steps");
     if (chunk < 1) chunk = nsteps > 0 ? nsteps : 1;
     b->launches = 0;
+    b->graph_launches = 0;
     for (int left = nsteps; left > 0;) {
         const int n = std::min(left, chunk);
-        const int rc = launch_chunk(b, b->variant, b->bps, n, 0);
+        cudaGraphExec_t ex = nullptr;
+        int rc = chunk_graph(b, b->variant, b->bps, n, &ex);
         if (rc != SEIDART_OK) return rc;
+        if (ex) {
+            if (cudaGraphLaunch(ex, b->stream) != cudaSuccess)
+                return berr(SEIDART_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(cudaGetLastError()));
+            ++b->launches;
+            ++b->graph_launches;
+        } else {
+            rc = launch_chunk(b, b->variant, b->bps, n, 0);
+            if (rc != SEIDART_OK) return rc;
+        }
         left -= n;
     }
     b->steps_done += nsteps;
@@ -720,6 +776,7 @@ SeidartSolver* seidart_batch_model(SeidartBatch* b, int m) {
 }
 int seidart_batch_steps_done(const SeidartBatch* b) { return b ? b->steps_done : -1; }
 long long seidart_batch_launches(const SeidartBatch* b) { return b ? b->launches : -1; }
+long long seidart_batch_graph_launches(const SeidartBatch* b) { return b ? b->graph_launches : -1; }
 int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid) {
     if (!b) return berr(SEIDART_ERR_ARG, "NULL batch");
     if (tx) *tx = kVariants[b->variant].tx;

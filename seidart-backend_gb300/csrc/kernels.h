@@ -240,6 +240,8 @@ struct S3Args {
     int wait_probe;        // test hook: bytes armed beyond a copy's size on one CTA (0 = off)
     int* wave_ctl;         // FP32 fused step: [0] work ticket, [WAVE_DONE0 + k] tiles of plane k done; NULL = two kernels
     int wave_n;            // ints of wave_ctl the epilogue clears
+    int wave_ctas;         // CTAs of the persistent fused step (resident slots)
+    int wave_lag;          // planes between the fused step's stress and velocity fronts (0: default)
 };
 // layout of S3Args::wave_ctl
 constexpr int WAVE_DONE0 = 32;
@@ -259,7 +261,8 @@ bool seismic3_make_map(CUtensorMap* m, const float* base, int nx, int ny, int nz
 bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* maps);
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st);
 // fused step: both half-steps of one time step in one launch (wavefront over z planes)
-bool seismic3_wave_prepare(const S3Args<float>& a);
+// resident CTAs of the fused step on this device (0: not available)
+int seismic3_wave_prepare(const S3Args<float>& a);
 void launch_seismic3_wave(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st);
 // TMA tensor maps of the FP32 3D stress kernel: 33 plane tiles per cell
 // (21 C_ij, 6 attenuation factors, 6 old stresses) and the 3 velocity planes

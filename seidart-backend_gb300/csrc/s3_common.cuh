@@ -78,6 +78,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
         : "memory");
     return ok != 0;
 }
+// plain arrival (release at CTA scope) on a barrier counting warps or threads
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
 // complete `bytes` of the barrier's pending transaction count from this
 // thread (the test hook's stand-in for bytes that never arrive)
 __device__ __forceinline__ void mbar_complete_tx(unsigned long long* b, unsigned bytes) {

@@ -16,6 +16,8 @@
 // what the register-bound one-cell kernels lack: they stall on load latency
 // with HBM a third busy.  A wait that gives up sets the solver's error word
 // and skips the update; the CTA still lets its copy land before exiting.
+#include <algorithm>
+
 #include "s3_velocity.cuh"
 
 namespace {
@@ -42,12 +44,13 @@ __device__ __forceinline__ void st_sig(float* p, float v) {
 // bytes more than the copies bring, so the first wait runs out; the give-up
 // path then completes the missing bytes itself before it drains.
 constexpr int WAIT_LAND = 1 << 26;
-__device__ __forceinline__ bool staged_wait(const S3Args<float>& A, unsigned long long* bar, int tid, int probe) {
-    if (mbar_wait_bounded(bar, 0, A.wait_limit)) return true;
+__device__ __forceinline__ bool staged_wait(const S3Args<float>& A, unsigned long long* bar, int tid, int probe,
+                                            unsigned parity = 0) {
+    if (mbar_wait_bounded(bar, parity, A.wait_limit)) return true;
     if (tid == 0) {
         if (A.err) atomicExch(A.err, 1);
         if (probe > 0) mbar_complete_tx(bar, (unsigned)probe);
-        mbar_wait_bounded(bar, 0, WAIT_LAND);
+        mbar_wait_bounded(bar, parity, WAIT_LAND);
     }
     return false;
 }
@@ -212,7 +215,7 @@ constexpr unsigned XS_BYTES = XS_TOTAL * sizeof(float);  // 51,840
 
 template <bool LEAN, bool STREAM = true>
 __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float* sm, unsigned long long* bar, int tid,
-                                            int x0, int y0, int k, int probe) {
+                                            int x0, int y0, int k, int probe, unsigned parity = 0) {
     const int nx = A.nx, ny = A.ny, nz = A.nz;
     const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
     bool L1 = true, L2 = true, L3 = true, L4 = true, active = true;
@@ -223,7 +226,7 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
         L1 = x14 && y13 && z12; L2 = x23 && y24 && z12; L3 = x23 && y13 && z34; L4 = x14 && y24 && z34;
         active = gx < nx && gy < ny && (L1 || L2 || L3 || L4);
     }
-    if (!staged_wait(A, bar, tid, probe)) return;
+    if (!staged_wait(A, bar, tid, probe, parity)) return;
     if (!active) return;
     const size_t c = (size_t)gx + (size_t)nx * ((size_t)gy + (size_t)ny * k);
     const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
@@ -280,6 +283,25 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
 // Arm the CTA's barrier and issue the 22 copies of one staged stress tile
 // (tile tx, ty of plane k; `lin` its index in the packed coefficient array),
 // one per lane of warp 0.  `probe` extra bytes are armed on top (test hook).
+// the 22 copies alone (lanes 0..21 of warp 0), on a barrier already armed
+__device__ __forceinline__ void stress_copies_issue(const S3Args<float>& A, const S3XMaps& M, float* sm,
+                                                    unsigned long long* bar, int tid, int x0, int y0, int k,
+                                                    size_t lin) {
+    if (tid < 22) {
+        if (tid == 0) {
+            bulk_g2s(sm, A.packed + lin * (NCOEF * NT), TILE_BYTES, bar);
+        } else if (tid <= 6) {
+            tma_load3(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, bar);
+        } else if (tid <= 9) {
+            tma_load3(sm + XS_VH + (tid - 7) * VHW * VHH, &M.vh[tid - 7], x0 - 4, y0 - 2, k, bar);
+        } else {
+            const int q = tid - 10, f = q >> 2, zi = q & 3;
+            const int dz = zi < 2 ? zi - 2 : zi - 1;
+            tma_load3(sm + XS_VZ + q * NT, &M.vp[f], x0, y0, k + dz, bar);
+        }
+    }
+}
+
 __device__ __forceinline__ void stress_copies(const S3Args<float>& A, const S3XMaps& M, float* sm,
                                               unsigned long long* bar, int tid, int x0, int y0, int k, size_t lin,
                                               int probe) {
@@ -353,7 +375,7 @@ __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __
 // array to or from DRAM about once: the 46 words per interior cell of the
 // whole step, against 55 for the two-kernel step (stresses written and read
 // back, velocities read twice).
-constexpr int WAVE_LAG = 4;
+constexpr int WAVE_LAG = 4;  // default lag
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
@@ -375,6 +397,7 @@ __device__ __forceinline__ bool wave_wait(const int* done, int q0, int q1, int n
 
 struct WaveGeom {
     int gxt, gyt, tpp;  // tiles per row, tile rows, tiles per plane
+    int lag;            // velocity plane = stress plane - lag (>= 3)
 };
 
 // L2 prefetch: the stress inputs of the item `ahead` tickets later, and the
@@ -403,62 +426,185 @@ __device__ __forceinline__ void wave_prefetch(const S3Args<float>& A, const Wave
     }
 }
 
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Persistent form: every CTA loops over tickets.  Per item, after the stress
+// tile is computed (its shared-memory inputs consumed), the CTA claims its
+// next ticket and starts that item's stress copies into the same shared
+// memory before it runs the current item's velocity half-step, so the
+// coefficient and field stream from DRAM continues while the velocity tile
+// works from L2.  The plane counters of a velocity tile are polled by five
+// lanes at once.  The deadlock argument of the one-item form holds: the
+// owner of the lowest unfinished stress item is either computing it or
+// waiting for planes whose items all hold lower tickets, so it never waits
+// on itself or on a later item.
+// Per-warp norm contribution of the velocity tile into the CTA's running
+// maxima (shared memory): FP32 squares as bit patterns (non-negative floats
+// order like them, inf and NaN above all finite values), and for a warp with
+// a square at or above 3e38 the exact FP64 norms of its cells.
+template <typename FA, typename FB>
+__device__ __forceinline__ void warp_norm2(float sa, float sb, FA exa, FB exb, unsigned* shu,
+                                           unsigned long long* shd) {
+    const unsigned ua = __reduce_max_sync(0xffffffffu, __float_as_uint(sa));
+    const unsigned ub = __reduce_max_sync(0xffffffffu, __float_as_uint(sb));
+    const unsigned big = __float_as_uint(3.0e38f);
+    const int lane = threadIdx.x & 31;
+    if (ua >= big || ub >= big) {
+        double a = exa(), b = exb();
+        for (int o = 16; o > 0; o >>= 1) {
+            a = nanmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = nanmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+        if (lane == 0) {
+            atomicMax(shd, (unsigned long long)__double_as_longlong(a));
+            atomicMax(shd + 1, (unsigned long long)__double_as_longlong(b));
+        }
+    } else if (lane == 0) {
+        atomicMax(shu, ua);
+        atomicMax(shu + 1, ub);
+    }
+}
+
+// Persistent form: every CTA loops over tickets, and no CTA-wide barrier
+// sits in the loop.  Per item:
+//   * each warp computes its rows of the stress tile from the staged copies
+//     and arrives on `freed` once its stores are issued;
+//   * warp 0 waits for all eight arrivals, counts the tile done for plane p,
+//     claims the next ticket (published through the `ticket` barrier) and
+//     starts the next item's copies into the same shared memory, so the DRAM
+//     stream goes on while the velocity tile runs;
+//   * each warp polls the five plane counters its velocity rows need, runs
+//     its rows of the velocity tile from L2, folds its norms into the CTA's
+//     running maxima, then reads the next ticket.
+// Norm maxima go to the step's slots once, when the CTA runs out of work.
+// Deadlock freedom is the one-item argument: the owner of the lowest
+// unfinished stress item is either computing it or waiting for planes whose
+// items all hold lower tickets.
 template <int MINB>
 __global__ void __launch_bounds__(NT, MINB) s3w_step(S3Args<float> A, StepInfo si, const __grid_constant__ S3XMaps M,
-                                                     WaveGeom G) {
+                                                     WaveGeom G, int total) {
     extern __shared__ __align__(128) float sm[];
-    __shared__ __align__(8) unsigned long long bar;
-    __shared__ int s_ticket, s_ok;
-    __shared__ unsigned redu[2 * NT / 32];
-    __shared__ double redd[2][NT / 32];
+    __shared__ __align__(8) unsigned long long bar, freed, ticket_bar;
+    __shared__ int s_ticket[2];
+    __shared__ unsigned s_nu[2];
+    __shared__ unsigned long long s_nd[2];
     const int tid = threadIdx.y * BX + threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     int* ctl = A.wave_ctl;
-    if (tid == 0) s_ticket = atomicAdd(ctl, 1);
-    __syncthreads();
-    const int t = s_ticket;
-    const int p = t / G.tpp, r = t - p * G.tpp, ty = r / G.gxt, tx = r - ty * G.gxt;
-    const int nx = A.nx, ny = A.ny, nz = A.nz;
-    const int x0 = tx * BX, y0 = ty * BY;
-    const int m = p - WAVE_LAG;
-    if (A.prefetch > 0) wave_prefetch(A, G, t + A.prefetch, m, tx, ty, tid);
-    // ---- stress half-step of plane p
-    if (p >= 1 && p <= nz - 2) {
-        const int probe = probe_bytes(A, tx, ty, p);
-        stress_copies(A, M, sm, &bar, tid, x0, y0, p, (size_t)tx + (size_t)G.gxt * ((size_t)ty + (size_t)G.gyt * p),
-                      probe);
-        if (lean_stress_tile(A, x0, y0, p)) staged_tile<true, false>(A, sm, &bar, tid, x0, y0, p, probe);
-        else staged_tile<false, false>(A, sm, &bar, tid, x0, y0, p, probe);
-        __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(ctl + WAVE_DONE0 + p, 1);
-        }
-    }
-    if (m < 0 || m >= nz) return;
-    // ---- velocity half-step of plane m
+    int* done = ctl + WAVE_DONE0;
+    const int nx = A.nx, ny = A.ny, nz = A.nz, lag = G.lag;
+    auto decode = [&](int t, int& p, int& tx, int& ty) {
+        p = t / G.tpp;
+        const int r = t - p * G.tpp;
+        ty = r / G.gxt;
+        tx = r - ty * G.gxt;
+    };
+    auto has_stress = [&](int t) { return t < total && t / G.tpp >= 1 && t / G.tpp <= nz - 2; };
+    // arm the copy barrier's next phase and start item t's copies (warp 0)
+    auto start_copies = [&](int t) {
+        int p, tx, ty;
+        decode(t, p, tx, ty);
+        if (lane == 0) mbar_expect_tx(&bar, XS_BYTES + (unsigned)probe_bytes(A, tx, ty, p));
+        __syncwarp();
+        stress_copies_issue(A, M, sm, &bar, tid, tx * BX, ty * BY, p,
+                            (size_t)tx + (size_t)G.gxt * ((size_t)ty + (size_t)G.gyt * p));
+    };
     if (tid == 0) {
-        // test hook: one item waits for a count no plane reaches
-        const int need = G.tpp + ((A.wait_probe > 0 && t == WAVE_LAG * G.tpp) ? 1 : 0);
-        s_ok = wave_wait(ctl + WAVE_DONE0, max(1, m - 2), min(nz - 2, m + 2), need, A.wait_limit);
-        if (!s_ok && A.err) atomicExch(A.err, 1);
+        mbar_init(&bar, 1);
+        mbar_init(&freed, NT / 32);
+        mbar_init(&ticket_bar, 1);
+        s_ticket[0] = atomicAdd(ctl, 1);
+        s_nu[0] = s_nu[1] = 0u;
+        s_nd[0] = s_nd[1] = 0ull;
     }
     __syncthreads();
-    if (!s_ok) return;
+    int t = s_ticket[0];
+    if (has_stress(t) && warp == 0) start_copies(t);
+    unsigned phase = 0;  // parity of the copy barrier's pending phase
     const int it = *si.step;
-    const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
-    float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (lean_tile(A, x0, y0, m, true)) velocity_cell<true, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
-    else if (gx < nx && gy < ny) velocity_cell<false, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
-    double vn, sn;
-    block_norm2_f32<NT / 32>(
-        vsq, ssq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); },
-        [&] {
-            const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
-            return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
-        },
-        redu, &redd[0][0], vn, sn);
+    for (int iter = 0; t < total; ++iter) {
+        int p, tx, ty;
+        decode(t, p, tx, ty);
+        const int x0 = tx * BX, y0 = ty * BY;
+        const int m = p - lag;
+        if (A.prefetch > 0) wave_prefetch(A, G, t + A.prefetch, m, tx, ty, tid);
+        // ---- stress half-step of plane p (each warp: its row of the tile)
+        const bool st = has_stress(t);
+        if (st) {
+            const int probe = probe_bytes(A, tx, ty, p);
+            if (lean_stress_tile(A, x0, y0, p)) staged_tile<true, false>(A, sm, &bar, tid, x0, y0, p, probe, phase);
+            else staged_tile<false, false>(A, sm, &bar, tid, x0, y0, p, probe, phase);
+            phase ^= 1u;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&freed);  // this warp's reads of the staging buffer and its stores are done
+        if (warp == 0) {
+            mbar_wait_bounded(&freed, iter & 1, WAIT_LAND);
+            int tn = 0;
+            if (lane == 0) {
+                if (st) red_release_add(done + p, 1);
+                tn = atomicAdd(ctl, 1);
+                s_ticket[iter & 1] = tn;
+                mbar_arrive(&ticket_bar);
+            }
+            tn = __shfl_sync(0xffffffffu, tn, 0);
+            if (has_stress(tn)) {
+                // the generic-proxy reads of the tile just computed come before
+                // the asynchronous copies that overwrite it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                start_copies(tn);
+            }
+        }
+        // ---- velocity half-step of plane m (each warp: its row of the tile)
+        if (m >= 0 && m < nz) {
+            const int q0 = max(1, m - 2), q1 = min(nz - 2, m + 2);
+            const int q = q0 + lane;
+            // test hook: one item waits for a count no plane reaches
+            const int need = G.tpp + ((A.wait_probe > 0 && t == lag * G.tpp) ? 1 : 0);
+            bool ok = true;
+            if (q <= q1) {
+                int n = 0;
+                while (ld_relaxed(done + q) < need) {
+                    if (++n > A.wait_limit) { ok = false; break; }
+                    __nanosleep(32);
+                }
+                // the lane that saw the count orders the warp's later reads
+                // after the stores the count releases
+                asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            }
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0 && A.err) atomicExch(A.err, 1);
+            } else {
+                const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
+                float vsq = 0.f, ssq = 0.f, w[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (lean_tile(A, x0, y0, m, true)) velocity_cell<true, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
+                else if (gx < nx && gy < ny) velocity_cell<false, LD_CA>(A, it, gx, gy, m, vsq, ssq, w);
+                warp_norm2(
+                    vsq, ssq, [&] { return sqrt((double)w[0] * w[0] + (double)w[1] * w[1] + (double)w[2] * w[2]); },
+                    [&] {
+                        const double s1 = w[3], s2 = w[4], s3 = w[5], s4 = w[6], s5 = w[7], s6 = w[8];
+                        return sqrt(s1 * s1 + s2 * s2 + s3 * s3 + 2.0 * (s4 * s4 + s5 * s5 + s6 * s6));
+                    },
+                    s_nu, s_nd);
+            }
+        }
+        // the next ticket (published by warp 0 once every warp had arrived)
+        mbar_wait_bounded(&ticket_bar, iter & 1, WAIT_LAND);
+        t = s_ticket[iter & 1];
+    }
+    __syncthreads();
     if (tid == 0) {
-        const int slot = (tx + 7 * ty + 13 * m) % 64;
+        const double vn = nanmax(sqrt((double)__uint_as_float(s_nu[0])), __longlong_as_double((long long)s_nd[0]));
+        const double sn = nanmax(sqrt((double)__uint_as_float(s_nu[1])), __longlong_as_double((long long)s_nd[1]));
+        const int slot = blockIdx.x % 64;
         atomic_max_nonneg(A.norms_part + slot, vn);
         atomic_max_nonneg(A.norms_part + 64 + slot, sn);
     }
@@ -509,14 +655,21 @@ void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, 
     s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
 }
 
-bool seismic3_wave_prepare(const S3Args<float>& a) {
-    if (!a.staged || !a.wave_ctl) return false;
+int seismic3_wave_prepare(const S3Args<float>& a) {
+    if (!a.staged || !a.wave_ctl) return 0;
     if (cudaFuncSetAttribute((const void*)s3w_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_BYTES) !=
         cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return true;
+    int per_sm = 0, dev = 0, nsm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)s3w_step<4>, NT, XS_BYTES) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm * nsm;
 }
 
 void launch_seismic3_wave(const S3Args<float>& a, const S3XMaps& maps, const StepInfo& s, cudaStream_t st) {
@@ -524,8 +677,11 @@ void launch_seismic3_wave(const S3Args<float>& a, const S3XMaps& maps, const Ste
     G.gxt = (a.nx + BX - 1) / BX;
     G.gyt = (a.ny + BY - 1) / BY;
     G.tpp = G.gxt * G.gyt;
-    const unsigned items = (unsigned)(G.tpp * (a.nz + WAVE_LAG));
-    s3w_step<4><<<items, dim3(BX, BY), XS_BYTES, st>>>(a, s, maps, G);
+    G.lag = a.wave_lag >= 3 ? a.wave_lag : WAVE_LAG;
+    const int items = G.tpp * (a.nz + G.lag);
+    // one CTA per resident slot (4 per SM); each loops over tickets
+    const int grid = std::min(items, a.wave_ctas > 0 ? a.wave_ctas : items);
+    s3w_step<4><<<grid, dim3(BX, BY), XS_BYTES, st>>>(a, s, maps, G, items);
 }
 
 void launch_seismic3_bulk_stress(const S3Args<float>& a, int variant, cudaStream_t st) {

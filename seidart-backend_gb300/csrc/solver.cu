@@ -981,8 +981,11 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->wave_ctl) {
             s->s3f.wave_ctl = s->wave_ctl;
             s->s3f.wave_n = s->wave_n;
+            s->s3f.wave_ctas = seismic3_wave_prepare(s->s3f);
+            const char* lg = getenv("SEIDART_S3_WAVE_LAG");
+            s->s3f.wave_lag = (lg && *lg >= '0' && *lg <= '9') ? atoi(lg) : 0;
             if (cudaMemsetAsync(s->wave_ctl, 0, sizeof(int) * s->wave_n, s->stream) != cudaSuccess ||
-                !seismic3_wave_prepare(s->s3f)) {
+                s->s3f.wave_ctas < 1) {
                 cudaGetLastError();
                 s->s3f.wave_ctl = nullptr;
                 s->s3f.wave_n = 0;

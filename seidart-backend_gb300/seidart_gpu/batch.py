@@ -36,6 +36,7 @@ def _declare():
         "seidart_batch_model": (vp, [vp, i]),
         "seidart_batch_steps_done": (i, [vp]),
         "seidart_batch_launches": (ll, [vp]),
+        "seidart_batch_graph_launches": (ll, [vp]),
         "seidart_batch_config": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "seidart_batch_num_variants": (i, []),
         "seidart_batch_destroy": (i, [vp]),
@@ -142,6 +143,11 @@ class Batch:
     @property
     def launches(self) -> int:
         return lib().seidart_batch_launches(self.handle)
+
+    @property
+    def graph_launches(self) -> int:
+        """Launches of the last step() that were CUDA graph replays."""
+        return lib().seidart_batch_graph_launches(self.handle)
 
     def fields(self, m: int) -> list:
         out = self.problems[m].field_list()

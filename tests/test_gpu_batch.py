@@ -25,6 +25,9 @@ def test_batch_matches_single_model_runs(oracle):
     with Batch(probs, autotune=True, trial_steps=4) as b:
         assert b.tuning and len(b.tuning) >= 5
         b.step(25, chunk=10)
+        # three chunks (10, 10, 5 steps): each a replay of a captured graph
+        # holding one persistent launch
+        assert b.launches == 3 and b.graph_launches == 3
         b.step(probs[0].time_steps - 25)
         b.sync()
         for m, p in enumerate(probs):
