@@ -193,6 +193,11 @@ int seidart_run(int family, int precision, const SeidartDomain* dom,
  * stream; steps are asynchronous on that stream.                           */
 typedef struct SeidartSolver SeidartSolver;
 
+/* model[q] are host FP64 grids, except that for seismic2 and seismic3 the
+ * stiffness, density and attenuation slots (every slot before the CPML
+ * ones) may be DEVICE FP64 grids, e.g. from seidart_stiffness_arrays_dev:
+ * those are copied (FP64) or converted (FP32) device to device into the
+ * solver's arena.  Any other slot in device memory returns SEIDART_ERR_ARG. */
 int seidart_solver_create(SeidartSolver** out, int family, int precision,
                           const SeidartDomain* dom, const SeidartSource* src,
                           int density_code, const double* const* model,
@@ -377,6 +382,12 @@ int seidart_fwi_model_traces(SeidartFwi* f, double* traces);
 int seidart_fwi_forward_step_host(SeidartFwi* f, float* x);
 int seidart_fwi_adjoint_step_host(SeidartFwi* f, const float* xprev, const float* xcur, float* lam);
 long long seidart_fwi_launches(const SeidartFwi* f);
+/* seismic2 only: on != 0 makes seidart_fwi_gradient also return dL/dc15 and
+ * dL/dc35 after the five above ([7][nx*nz]: c11 c13 c33 c55 rho c15 c35).
+ * Both coefficients enter the normal and shear stress updates
+ * (cpmlfdtd.f08:342-351, :380-383); their sums cost two more FP32
+ * accumulators per cell and adjoint step, so they are off by default. */
+int seidart_fwi_set_full_tensor(SeidartFwi* f, int on);
 int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count);
 int seidart_fwi_destroy(SeidartFwi* f);
 const char* seidart_fwi_last_error(void);
@@ -419,6 +430,24 @@ int seidart_attenuation_arrays(const int* im, int nx, int nz, const double* alis
                                double cpmlvalue, double* const* out);
 int seidart_attenuation_write(const char* dir, const int* im, int nx, int nz, const double* alist, int nmat, int ncol,
                               int npml, double cpmlvalue);
+/* The same pre-pass on the device (legacy/cpmlfdtd_cbindings.f95:60-611, as
+ * above): dev_out[q] are DEVICE buffers of the padded FP64 grids (every one
+ * of the 22 / 12 / 3 is required, since the carry reads them; complex eps
+ * grids hold interleaved pairs); im, the table and gradient are host arrays
+ * (uploaded to scratch the call allocates and frees).  A fill kernel and one
+ * row and one column kernel per carry iteration run on `stream` (a
+ * cudaStream_t, NULL = legacy default); the call returns after the stream
+ * has finished them.  The grids equal the host pass's bit for bit; a
+ * seismic2 / seismic3 solver can take them directly as model arrays (see
+ * seidart_solver_create). */
+int seidart_stiffness_arrays_dev(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                                 const double* gradient, double* const* dev_out, void* stream);
+int seidart_permittivity_arrays_dev(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                                    double* const* dev_out, void* stream);
+int seidart_permittivity_arrays_c_dev(const int* im, int nx, int nz, const double* mlist_c, int nmat, int ncol,
+                                      int npml, double* const* dev_out, void* stream);
+int seidart_attenuation_arrays_dev(const int* im, int nx, int nz, const double* alist, int nmat, int ncol, int npml,
+                                   double cpmlvalue, double* const* dev_out, void* stream);
 
 /* ---- trace misfit without device allocation.  No counterpart in the
  * reference (SeidarT-Backend computes no misfit); it is the no-allocation

@@ -143,10 +143,11 @@ def forward_traces(m: dict, dx: float, dz: float, dt: float, nt: int, src_cell: 
     return torch.stack(out)
 
 
-def misfit_and_gradient(problem, shots, observed, density_code: int):
-    """FP64 L and dL/d{c11, c13, c33, c55, rho} ((nx, nz) numpy arrays) for a
-    seismic2 Problem and the same shot list the GPU adjoint takes."""
-    keys = ("c11", "c13", "c33", "c55", "rho")
+def misfit_and_gradient(problem, shots, observed, density_code: int,
+                        keys=("c11", "c13", "c33", "c55", "rho")):
+    """FP64 L and dL/d{keys} ((nx, nz) numpy arrays; any seismic2 model slot,
+    e.g. c15 and c35 as well) for a seismic2 Problem and the same shot list
+    the GPU adjoint takes."""
     m = {k: torch.tensor(np.asarray(v, dtype=np.float64), requires_grad=k in keys) for k, v in problem.model.items()}
     rec = np.asarray(problem.receivers, dtype=np.int64)
     loss = torch.zeros((), dtype=torch.float64)

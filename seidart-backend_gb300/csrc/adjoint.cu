@@ -62,7 +62,9 @@ struct AdjArgs {
     const float* xc;     // x_n
     float* lam;          // adjoint state, NS arrays
     float* scr;          // 12 scratch arrays: lf1..lf4, ld1..ld4, le1..le4
-    float* grad;         // 8 FP32 accumulators of the current segment: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
+    float* grad;         // FP32 accumulators of the current segment: c11 c13 c33 c55 Bxx Bzx Bxz Bzz
+                         // (and c15 c35 when `full`)
+    int full;            // 1: also dL/dc15 and dL/dc35 (slots 8, 9)
     size_t N;
     int isrc, jsrc;
     const double* srcz;  // force series of the shot (device), NULL = none
@@ -259,6 +261,19 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
         A.grad[c] += px * D1;
         A.grad[N + c] += px * D2 + pz * D1;
         A.grad[2 * N + c] += pz * D2;
+        if (A.full) {
+            // c15 and c35 multiply dvz_dx + dvx_dz of the normal-stress loop
+            // (cpmlfdtd.f08:342-351): forward x (full coefficients) and
+            // backward z (half coefficients), C-PML rescaled as the step did
+            float D3 = (27.0f * (vz[c + 1] - vz[c]) - (vz[c + 2] - vz[c - 1])) * hx;
+            float D4 = (27.0f * (vx[c] - vx[c - nx]) - (vx[c + nx] - vx[c - 2 * nx])) * hz;
+            if (pml) {
+                D3 = D3 * m[10][c] + xc[(5 + 2) * N + c];
+                D4 = D4 * m[11][c] + xc[(5 + 1) * N + c];
+            }
+            A.grad[8 * N + c] += px * (D3 + D4);
+            A.grad[9 * N + c] += pz * (D3 + D4);
+        }
     }
     if (inS(i, k, nx, nz)) {
         const float gxz = m[9][c];
@@ -290,6 +305,19 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
             le4 = lE34;
         }
         A.grad[3 * N + c] += pxz * (E3 + E4);
+        if (A.full) {
+            // sigma_xz's c15 dvx_dx (backward x) and c35 dvz_dz (forward z),
+            // half coefficients (cpmlfdtd.f08:380-383)
+            float E1 = (27.0f * (vx[c] - vx[c - 1]) - (vx[c + 1] - vx[c - 2])) * hx;
+            float E2 = (27.0f * (vz[c + nx] - vz[c]) - (vz[c + 2 * nx] - vz[c - nx])) * hz;
+            if (pml) {
+                const float ikh = m[11][c];
+                E1 = E1 * ikh + xc[(5 + 4) * N + c];
+                E2 = E2 * ikh + xc[(5 + 7) * N + c];
+            }
+            A.grad[8 * N + c] += pxz * E1;
+            A.grad[9 * N + c] += pxz * E2;
+        }
     }
     lam[2 * N + c] = nsxx;
     lam[3 * N + c] = nszz;
@@ -511,8 +539,8 @@ struct FwiLane {
     float* lam = nullptr;       // [ns][N]
     float* scr = nullptr;       // [12][N]
     float* dres = nullptr;      // [nt][2][nrec] residual of the lane's shot
-    double* grad = nullptr;     // [8][N] FP64 gradient sums over segments and shots
-    float* grad32 = nullptr;    // [8][N] FP32 sums within the current segment
+    double* grad = nullptr;     // [kGradSlots][N] FP64 gradient sums over segments and shots
+    float* grad32 = nullptr;    // [kGradSlots][N] FP32 sums within the current segment
     double* dscal = nullptr;    // [0] misfit of the lane's shots
     int* dbase = nullptr;       // device segment base (steps before the segment)
     // [0] full segments of K steps, [1] the shorter last one
@@ -520,8 +548,15 @@ struct FwiLane {
     long long launches = 0;
 };
 
+// gradient accumulator slots per cell: 8 (electromag2: aEx..eEz; seismic2:
+// c11 c13 c33 c55 and four face buoyancies) plus c15, c35 for seismic2 with
+// the full tensor on
+constexpr int kGradSlots = 10;
+
 struct SeidartFwi {
     std::vector<FwiLane> lanes;
+    bool full = false;  // seismic2: also dL/dc15, dL/dc35
+    int ng() const { return full ? 10 : 8; }  // slots in use
     int family = SEIDART_SEISMIC2, ns = NS;  // solver family and state arrays per cell
     int nrec = 0, nt = 0, nshots = 0, K = 1, G = 1, density = 3;
     size_t N = 0;
@@ -567,6 +602,7 @@ AdjArgs adj_args(SeidartFwi* f, FwiLane& L, const float* xp, const float* xc, co
     A.base = L.dbase; A.j = j;
     A.rfirst = f->rfirst; A.rnext = f->rnext; A.nrec = f->nrec;
     A.dres = f->nrec > 0 ? L.dres : nullptr;
+    A.full = f->full ? 1 : 0;
     return A;
 }
 
@@ -701,7 +737,7 @@ int capture_segment(SeidartFwi* f, FwiLane& L, int len, bool adjoint, cudaGraphE
     } else {
         for (int j = len; j >= 1; --j)
             adjoint_step(f, L, j, L.seg + (size_t)(j - 1) * state, L.seg + (size_t)j * state, srcz, true);
-        fold_grad<<<4 * 152, 256, 0, L.st>>>(L.grad, L.grad32, 8 * f->N);
+        fold_grad<<<4 * 152, 256, 0, L.st>>>(L.grad, L.grad32, (size_t)f->ng() * f->N);
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(L.st, &g);
@@ -805,7 +841,8 @@ int sync_lanes(SeidartFwi* f) {
 }
 
 size_t lane_bytes(size_t N, int ns, int K, int G, int nt, int nrec) {
-    return sizeof(float) * ((size_t)G + K + 1 + 1 + 0) * ns * N + sizeof(float) * 12 * N + sizeof(double) * 8 * N +
+    return sizeof(float) * ((size_t)G + K + 1 + 1 + 0) * ns * N + sizeof(float) * 12 * N +
+           (sizeof(double) + sizeof(float)) * kGradSlots * N +
            sizeof(float) * (size_t)nt * 2 * (nrec > 0 ? nrec : 1) + sizeof(float) * 40 * N;  // + solver arena
 }
 
@@ -990,8 +1027,8 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
             cudaMalloc((void**)&L.lam, sizeof(float) * f->ns * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.scr, sizeof(float) * 12 * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.dres, sizeof(float) * (nobs ? nobs : 1)) != cudaSuccess ||
-            cudaMalloc((void**)&L.grad, sizeof(double) * 8 * f->N) != cudaSuccess ||
-            cudaMalloc((void**)&L.grad32, sizeof(float) * 8 * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.grad, sizeof(double) * kGradSlots * f->N) != cudaSuccess ||
+            cudaMalloc((void**)&L.grad32, sizeof(float) * kGradSlots * f->N) != cudaSuccess ||
             cudaMalloc((void**)&L.dscal, sizeof(double) * 2) != cudaSuccess ||
             cudaMalloc((void**)&L.dbase, sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
@@ -1000,7 +1037,7 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
         }
         // segment states are written only where a step updates them: start from zeros
         if (cudaMemset(L.seg, 0, sizeof(float) * (f->K + 1) * f->ns * f->N) != cudaSuccess ||
-            cudaMemset(L.grad32, 0, sizeof(float) * 8 * f->N) != cudaSuccess) {
+            cudaMemset(L.grad32, 0, sizeof(float) * kGradSlots * f->N) != cudaSuccess) {
             cudaGetLastError();
             seidart_fwi_destroy(f);
             return ferr(SEIDART_ERR_CUDA, "FWI lane initialisation failed");
@@ -1022,7 +1059,8 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
 }
 
 // Loss and gradient over all shots.  grad (host, may be NULL) receives FP64
-// per cell: seismic2 [5][ncell] dL/dc11, dL/dc13, dL/dc33, dL/dc55, dL/drho;
+// per cell: seismic2 [5][ncell] dL/dc11, dL/dc13, dL/dc33, dL/dc55, dL/drho
+// (and [7][ncell] with dL/dc15, dL/dc35 after them when the full tensor is on);
 // electromag2 [6][ncell] dL/deps11, dL/deps13, dL/deps33 (relative
 // permittivities, as in e11.dat ...), dL/dsig11, dL/dsig13, dL/dsig33.
 int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
@@ -1030,8 +1068,8 @@ int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
     f->launches = 0;
     for (auto& L : f->lanes) {
         L.launches = 0;
-        FCUDA(cudaMemsetAsync(L.grad, 0, sizeof(double) * 8 * f->N, L.st));
-        FCUDA(cudaMemsetAsync(L.grad32, 0, sizeof(float) * 8 * f->N, L.st));
+        FCUDA(cudaMemsetAsync(L.grad, 0, sizeof(double) * kGradSlots * f->N, L.st));
+        FCUDA(cudaMemsetAsync(L.grad32, 0, sizeof(float) * kGradSlots * f->N, L.st));
         FCUDA(cudaMemsetAsync(L.dscal, 0, sizeof(double) * 2, L.st));
     }
     FCUDA(cudaMemsetAsync(f->dgsrc, 0, sizeof(double) * f->nshots, f->lanes[0].st));
@@ -1052,19 +1090,20 @@ int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
         const size_t N = f->N;
         FwiLane& L0 = f->lanes[0];
         for (size_t l = 1; l < f->lanes.size(); ++l) {
-            add_grad<<<4 * 152, 256, 0, L0.st>>>(L0.grad, f->lanes[l].grad, 8 * N);
+            add_grad<<<4 * 152, 256, 0, L0.st>>>(L0.grad, f->lanes[l].grad, (size_t)f->ng() * N);
             ++f->launches;
         }
         FCUDA(cudaGetLastError());
         FCUDA(cudaStreamSynchronize(L0.st));
-        std::vector<double> g(8 * N), gsrc(f->nshots);
-        FCUDA(cudaMemcpy(g.data(), L0.grad, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+        std::vector<double> g((size_t)f->ng() * N), gsrc(f->nshots);
+        FCUDA(cudaMemcpy(g.data(), L0.grad, sizeof(double) * f->ng() * N, cudaMemcpyDeviceToHost));
         FCUDA(cudaMemcpy(gsrc.data(), f->dgsrc, sizeof(double) * f->nshots, cudaMemcpyDeviceToHost));
         if (f->family == SEIDART_ELECTROMAG2) {
             em_chain(f, g, gsrc, grad);
             return SEIDART_OK;
         }
         memcpy(grad, g.data(), sizeof(double) * 4 * N);
+        if (f->full) memcpy(grad + 5 * N, g.data() + 8 * N, sizeof(double) * 2 * N);  // c15, c35 after rho
         // chain the face buoyancies B = 1/mean(rho_a, rho_b) to rho (FP32 forward values)
         std::vector<float> rho(N);
         FCUDA(cudaMemcpy(rho.data(), L0.a.m[S2_RHO], sizeof(float) * N, cudaMemcpyDeviceToHost));
@@ -1159,6 +1198,20 @@ int seidart_fwi_forward_step_host(SeidartFwi* f, float* x) {
 }
 
 long long seidart_fwi_launches(const SeidartFwi* f) { return f ? f->launches : -1; }
+
+int seidart_fwi_set_full_tensor(SeidartFwi* f, int on) {
+    if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
+    if (f->family != SEIDART_SEISMIC2) return ferr(SEIDART_ERR_ARG, "the full-tensor gradient is for seismic2");
+    if (f->full != (on != 0)) {
+        f->full = on != 0;
+        // the flag is baked into the captured segment graphs: capture again
+        for (auto& L : f->lanes) {
+            FCUDA(cudaStreamSynchronize(L.st));
+            L.graphs = false;
+        }
+    }
+    return SEIDART_OK;
+}
 int seidart_fwi_checkpointing(const SeidartFwi* f, int* every, int* count) {
     if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
     if (every) *every = f->K;

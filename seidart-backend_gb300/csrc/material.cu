@@ -20,10 +20,12 @@
 // the image holds 1-based row numbers of the material table (the reference
 // reads mlist(im(i,j), col)); tables are row-major [nmat][ncol] as a NumPy
 // caller holds them.
+#include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <complex>
 #include <string>
 #include <vector>
@@ -226,9 +228,227 @@ const char* kEpsNames[6] = {"eps11.dat", "eps12.dat", "eps13.dat", "eps22.dat", 
 const char* kSigNames[6] = {"sig11.dat", "sig12.dat", "sig13.dat", "sig22.dat", "sig23.dat", "sig33.dat"};
 const char* kGamNames[3] = {"gamma_x.dat", "gamma_y.dat", "gamma_z.dat"};
 
+// ------------------------------------------------------------ device pass
+// The same expansion as device kernels writing the padded FP64 grids in
+// device memory: one fill kernel (interior from the table, the CPML at its
+// initial value), then per carry iteration i = 1..P+1 a row phase and a
+// column phase.  Within a phase every statement reads a row (column) that no
+// statement of the phase writes, except no-op self copies (i = P+1), so the
+// statements of a phase run in parallel and the phases keep the reference's
+// order.  Per-material values that need arithmetic (|eps| for complex
+// permittivity) are formed on the host over the small table, so the device
+// result equals the host pass bit for bit.
+enum { K_PLAIN = 0, K_SIG12 = 1, K_SIG13 = 2, K_SIG23 = 3 };  // carry kinds (permittivity quirks)
+
+struct DevPass {
+    double* out[22];  // device grids (complex ones as interleaved pairs)
+    int kind[22];     // K_* carry role of each array
+    int narr;
+    int cplx[22];     // 1: complex grid (two doubles per cell)
+    int NX, NZ, P, nx, nz;
+};
+
+// interior fill: out[a](i, j) = tab[row(im)][a] (complex: two doubles), and
+// optionally times the density gradient; CPML cells get `edge`
+__global__ void mat_fill(DevPass D, const int* __restrict__ im, const double* __restrict__ tab, int tstride,
+                         const double* __restrict__ grad, int grad_arr, double edge) {
+    const size_t cells = (size_t)D.NX * D.NZ;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < cells * D.narr;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / cells);
+        const size_t c = q - (size_t)a * cells;
+        const int i = (int)(c % D.NX), j = (int)(c / D.NX);  // 0-based padded
+        const int ii = i - D.P, jj = j - D.P;
+        const bool in = ii >= 0 && ii < D.nx && jj >= 0 && jj < D.nz;
+        if (D.cplx[a]) {
+            double re = edge, imv = 0.0;
+            if (in) {
+                const int r = im[(size_t)ii + (size_t)D.nx * jj] - 1;
+                re = tab[(size_t)r * tstride + 2 * a];
+                imv = tab[(size_t)r * tstride + 2 * a + 1];
+            }
+            D.out[a][2 * c] = re;
+            D.out[a][2 * c + 1] = imv;
+        } else {
+            double v = edge;
+            if (in) {
+                const int r = im[(size_t)ii + (size_t)D.nx * jj] - 1;
+                v = tab[(size_t)r * tstride + (D.cplx[0] ? 2 * a : a)];
+                if (grad && a == grad_arr) v = v * grad[(size_t)ii + (size_t)D.nx * jj];
+            }
+            D.out[a][c] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void cp_cell(const DevPass& D, int dst_a, size_t dc, int src_a, size_t sc) {
+    if (D.cplx[dst_a]) {
+        const double re = D.out[src_a][2 * sc], imv = D.out[src_a][2 * sc + 1];
+        D.out[dst_a][2 * dc] = re;
+        D.out[dst_a][2 * dc + 1] = imv;
+    } else {
+        D.out[dst_a][dc] = D.out[src_a][sc];
+    }
+}
+
+// row phase of iteration i (1-based): rows i <- P+1 and nx+P-1+i <- nx+P-1;
+// the sig12 array is not carried to high x (its statement writes sig13,
+// which the sig13 statement overwrites with its own carry)
+__global__ void mat_rows(DevPass D, int i) {
+    const int NX = D.NX, NZ = D.NZ;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)D.narr * NZ * 2;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / (2 * (size_t)NZ));
+        const int r = (int)(q - (size_t)a * 2 * NZ);
+        const int j = r % NZ, hi = r / NZ;  // 0-based column, 0 low / 1 high
+        const int dst = hi ? (D.nx + D.P - 1 + i) - 1 : i - 1, src = hi ? (D.nx + D.P - 1) - 1 : D.P;
+        if (dst == src) continue;
+        if (hi && D.kind[a] == K_SIG12) continue;
+        cp_cell(D, a, (size_t)dst + (size_t)NX * j, a, (size_t)src + (size_t)NX * j);
+    }
+}
+
+// column phase of iteration i: cols i <- P+1 and nz+P-1+i <- nz+P-1; at
+// low z sig12 takes sig11's column and sig23 takes sig33's column
+__global__ void mat_cols(DevPass D, int i, int sig11, int sig33) {
+    const int NX = D.NX;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)D.narr * NX * 2;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / (2 * (size_t)NX));
+        const int r = (int)(q - (size_t)a * 2 * NX);
+        const int row = r % NX, hi = r / NX;
+        const int dst = hi ? (D.nz + D.P - 1 + i) - 1 : i - 1, src = hi ? (D.nz + D.P - 1) - 1 : D.P;
+        int from = a;
+        if (!hi && D.kind[a] == K_SIG12) from = sig11;
+        if (!hi && D.kind[a] == K_SIG23) from = sig33;
+        if (dst == src && from == a) continue;
+        cp_cell(D, a, (size_t)row + (size_t)NX * dst, from, (size_t)row + (size_t)NX * src);
+    }
+}
+
+// Upload the image (and the gradient), run fill + carry on `st`, free the
+// scratch.  tab: host table already reduced to the output columns (tstride
+// doubles per material row).  carry = false: attenuation (the CPML keeps
+// `edge`).
+int run_dev_pass(DevPass D, const int* im, const std::vector<double>& tab, int tstride, const double* grad,
+                 int grad_arr, double edge, bool carry, int sig11, int sig33, cudaStream_t st) {
+    int* dim = nullptr;
+    double* dtab = nullptr;
+    double* dgrad = nullptr;
+    const size_t ncell = (size_t)D.nx * D.nz;
+    auto fail = [&](const char* what) {
+        cudaGetLastError();
+        if (dim) cudaFree(dim);
+        if (dtab) cudaFree(dtab);
+        if (dgrad) cudaFree(dgrad);
+        return merr(SEIDART_ERR_CUDA, std::string("device material pre-pass: ") + what);
+    };
+    if (cudaMalloc((void**)&dim, ncell * sizeof(int)) != cudaSuccess ||
+        cudaMalloc((void**)&dtab, tab.size() * sizeof(double)) != cudaSuccess ||
+        (grad && cudaMalloc((void**)&dgrad, ncell * sizeof(double)) != cudaSuccess))
+        return fail("scratch allocation");
+    if (cudaMemcpyAsync(dim, im, ncell * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (grad && cudaMemcpyAsync(dgrad, grad, ncell * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess))
+        return fail("upload");
+    mat_fill<<<4 * 152, 256, 0, st>>>(D, dim, dtab, tstride, dgrad, grad_arr, edge);
+    if (carry)
+        for (int i = 1; i <= D.P + 1; ++i) {
+            mat_rows<<<(unsigned)std::min<size_t>(4 * 152, ((size_t)D.narr * D.NZ * 2 + 255) / 256), 256, 0, st>>>(D, i);
+            mat_cols<<<(unsigned)std::min<size_t>(4 * 152, ((size_t)D.narr * D.NX * 2 + 255) / 256), 256, 0, st>>>(
+                D, i, sig11, sig33);
+        }
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) return fail("kernels");
+    cudaFree(dim);
+    cudaFree(dtab);
+    if (dgrad) cudaFree(dgrad);
+    return SEIDART_OK;
+}
+
+// host table reduced to the output columns: row r holds `count` values
+// starting at 1-based column col0 (complex tables: interleaved pairs)
+std::vector<double> table_cols(const double* t, int nmat, int ncol, int col0, int count, bool cplx) {
+    const int w = cplx ? 2 : 1;
+    std::vector<double> out((size_t)nmat * count * w);
+    for (int r = 0; r < nmat; ++r)
+        for (int a = 0; a < count; ++a)
+            for (int c = 0; c < w; ++c) out[((size_t)r * count + a) * w + c] = t[((size_t)r * ncol + col0 - 1 + a) * w + c];
+    return out;
+}
+
+DevPass dev_pass(double* const* out, int narr, int nx, int nz, int P) {
+    DevPass D{};
+    D.narr = narr;
+    D.nx = nx; D.nz = nz; D.P = P;
+    D.NX = nx + 2 * P; D.NZ = nz + 2 * P;
+    for (int a = 0; a < narr; ++a) { D.out[a] = out[a]; D.kind[a] = K_PLAIN; D.cplx[a] = 0; }
+    return D;
+}
+
 }  // namespace
 
 extern "C" {
+
+int seidart_stiffness_arrays_dev(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                                 const double* gradient, double* const* dev_out, void* stream) {
+    int rc = check_inputs(im, nx, nz, mlist, nmat, ncol, 23, npml);
+    if (rc != SEIDART_OK) return rc;
+    if (!dev_out) return merr(SEIDART_ERR_ARG, "dev_out must not be NULL");
+    for (int a = 0; a < 22; ++a)
+        if (!dev_out[a]) return merr(SEIDART_ERR_ARG, "every stiffness output grid is needed (the carry reads them)");
+    DevPass D = dev_pass(dev_out, 22, nx, nz, npml);
+    return run_dev_pass(D, im, table_cols(mlist, nmat, ncol, 2, 22, false), 22, gradient, 21, 0.0, true, -1, -1,
+                        (cudaStream_t)stream);
+}
+
+int seidart_permittivity_arrays_dev(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
+                                    double* const* dev_out, void* stream) {
+    int rc = check_inputs(im, nx, nz, mlist, nmat, ncol, 13, npml);
+    if (rc != SEIDART_OK) return rc;
+    if (!dev_out) return merr(SEIDART_ERR_ARG, "dev_out must not be NULL");
+    for (int a = 0; a < 12; ++a)
+        if (!dev_out[a]) return merr(SEIDART_ERR_ARG, "every permittivity output grid is needed (the carry reads them)");
+    // eps11 12 13 22 23 33 (cols 2..7), sig11 12 13 22 23 33 (cols 8..13)
+    DevPass D = dev_pass(dev_out, 12, nx, nz, npml);
+    D.kind[7] = K_SIG12; D.kind[8] = K_SIG13; D.kind[10] = K_SIG23;
+    return run_dev_pass(D, im, table_cols(mlist, nmat, ncol, 2, 12, false), 12, nullptr, -1, 0.0, true, 6, 11,
+                        (cudaStream_t)stream);
+}
+
+int seidart_permittivity_arrays_c_dev(const int* im, int nx, int nz, const double* mlist_c, int nmat, int ncol,
+                                      int npml, double* const* dev_out, void* stream) {
+    int rc = check_inputs(im, nx, nz, mlist_c, nmat, ncol, 13, npml);
+    if (rc != SEIDART_OK) return rc;
+    if (!dev_out) return merr(SEIDART_ERR_ARG, "dev_out must not be NULL");
+    for (int a = 0; a < 12; ++a)
+        if (!dev_out[a]) return merr(SEIDART_ERR_ARG, "every permittivity output grid is needed (the carry reads them)");
+    // complex eps (interleaved pairs) and sigma = |table value| formed here,
+    // with the C library's hypot as the host pass uses; table rows of 12
+    // complex slots, the sigma slots holding (|z|, 0)
+    std::vector<double> tab = table_cols(mlist_c, nmat, ncol, 2, 12, true);
+    for (int r = 0; r < nmat; ++r)
+        for (int a = 6; a < 12; ++a) {
+            double* z = &tab[((size_t)r * 12 + a) * 2];
+            z[0] = hypot(z[0], z[1]);
+            z[1] = 0.0;
+        }
+    DevPass D = dev_pass(dev_out, 12, nx, nz, npml);
+    for (int a = 0; a < 6; ++a) D.cplx[a] = 1;
+    D.kind[7] = K_SIG12; D.kind[8] = K_SIG13; D.kind[10] = K_SIG23;
+    return run_dev_pass(D, im, tab, 24, nullptr, -1, 0.0, true, 6, 11, (cudaStream_t)stream);
+}
+
+int seidart_attenuation_arrays_dev(const int* im, int nx, int nz, const double* alist, int nmat, int ncol, int npml,
+                                   double cpmlvalue, double* const* dev_out, void* stream) {
+    int rc = check_inputs(im, nx, nz, alist, nmat, ncol, 3, npml);
+    if (rc != SEIDART_OK) return rc;
+    if (!dev_out) return merr(SEIDART_ERR_ARG, "dev_out must not be NULL");
+    for (int a = 0; a < 3; ++a)
+        if (!dev_out[a]) return merr(SEIDART_ERR_ARG, "every attenuation output grid is needed");
+    DevPass D = dev_pass(dev_out, 3, nx, nz, npml);
+    return run_dev_pass(D, im, table_cols(alist, nmat, ncol, 1, 3, false), 3, nullptr, -1, cpmlvalue, false, -1, -1,
+                        (cudaStream_t)stream);
+}
 
 int seidart_stiffness_arrays(const int* im, int nx, int nz, const double* mlist, int nmat, int ncol, int npml,
                              const double* gradient, double* const* out) {

@@ -310,9 +310,32 @@ int download_f32_pinned(SeidartSolver& s, double* h, const float* d, size_t n) {
     return SEIDART_OK;
 }
 
+// true when p is device memory (a model grid produced on the device, e.g. by
+// the device material pre-pass); such arrays are copied or converted device
+// to device
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice;
+}
+
 template <typename T>
 int upload(SeidartSolver& s, void* d, const double* h, size_t n, int mode = 0) {
     cudaStream_t st = s.stream;
+    if (h && is_device_ptr(h)) {
+        if (sizeof(T) == sizeof(double)) {
+            CUDA_TRY(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            if (mode != 0 && n > 0) derive_f64<<<4 * 152, 256, 0, st>>>((double*)d, n, mode, s.src.dt);
+        } else if (n > 0) {
+            convert_to_f32<<<4 * 152, 256, 0, st>>>((float*)d, h, n, mode, s.src.dt);
+        }
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return SEIDART_OK;
+    }
     if (sizeof(T) == sizeof(double)) {
         CUDA_TRY(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, st));
         if (mode != 0 && n > 0) {
@@ -810,6 +833,18 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         return set_err(SEIDART_ERR_ARG, "source index (%d,%d,%d)+cpml outside the padded grid", src->xind, src->yind, src->zind);
     for (int q = 0; q < L.nmodel; ++q)
         if (!model[q]) return set_err(SEIDART_ERR_ARG, "model array %d is NULL", q);
+    // device-resident model grids: the stiffness, density and attenuation
+    // slots of seismic2 and seismic3 (their set-up only copies or converts
+    // them); every other array is read on the host during set-up
+    {
+        const bool dev_ok = family == SEIDART_SEISMIC2 || family == SEIDART_SEISMIC3;
+        const int first_cpml = cpml_slot(family);
+        for (int q = 0; q < L.nmodel; ++q)
+            if (is_device_ptr(model[q]) && (!dev_ok || q >= first_cpml))
+                return set_err(SEIDART_ERR_ARG,
+                               "model array %d is device memory: only the stiffness, density and attenuation grids "
+                               "of seismic2 and seismic3 may be", q);
+    }
     const size_t N = (size_t)nx * ny * nz;
     for (int r = 0; r < nrec; ++r)
         if (!rec_cells || rec_cells[r] < 0 || (size_t)rec_cells[r] >= N)

@@ -180,6 +180,44 @@ class Problem:
         return i + self.nx * k
 
 
+def _is_device_grid(a) -> bool:
+    return hasattr(a, "data_ptr") and bool(getattr(a, "is_cuda", False))
+
+
+class _DevicePtr:
+    """A CUDA tensor standing in a model slot: ptr_array passes its address."""
+
+    def __init__(self, t, ncell: int, name: str):
+        import torch
+        if t.dtype != torch.float64 or t.numel() != ncell or not t.is_contiguous():
+            raise ValueError(f"device model grid {name} must be a contiguous float64 CUDA tensor of {ncell} cells "
+                             "(row-major (nz, nx) / (nz, ny, nx), the Fortran layout)")
+        self.t = t
+        self.ctypes = type("_P", (), {"data": t.data_ptr()})()
+
+
+def _model_arrays(problem: Problem) -> list:
+    """The model slots for seidart_solver_create: host FP64 grids, or for
+    seismic2 / seismic3 CUDA FP64 tensors (the device material pre-pass's
+    output) in the stiffness, density and attenuation slots."""
+    names = MODEL_SLOTS[problem.family]
+    if not any(_is_device_grid(problem.model[n]) for n in names):
+        return problem.model_list()
+    if problem.plane_wave:
+        raise ValueError("plane-wave set-up reads the stiffness on the host: pass host model grids")
+    out = []
+    for n in names:
+        a = problem.model[n]
+        if _is_device_grid(a):
+            out.append(_DevicePtr(a, problem.ncell, n))
+        else:
+            a = np.asfortranarray(a, dtype=np.float64)
+            if a.shape != problem.shape:
+                raise ValueError(f"model array {n} has shape {a.shape}, expected {problem.shape}")
+            out.append(a)
+    return out
+
+
 class Solver:
     """Device copy of a Problem, advanced on the GPU."""
 
@@ -187,7 +225,7 @@ class Solver:
         self.problem = problem
         self.precision = precision
         self.lay = layout(problem.family)
-        self._model = problem.model_list()      # keep alive during create
+        self._model = _model_arrays(problem)    # keep alive during create
         self._src = problem.src_list()
         rec = problem.receiver_array()
         self._rec = rec

@@ -73,18 +73,18 @@ def allreduce_sum(arrays: dict) -> dict:
 
 
 def sharded_gradient(problem, shots: list, observed: list, rank: int, world: int,
-                     gradient: Callable | None = None) -> tuple[float, dict]:
+                     gradient: Callable | None = None, full_tensor: bool = False) -> tuple[float, dict]:
     """Misfit and gradient over all shots with each rank computing its share.
 
     ``gradient(problem, shots, observed) -> (loss, {name: array})`` defaults
     to the GPU adjoint (:class:`seidart_gpu.fwi.Fwi`).  The per-rank losses and
     gradients are summed over ranks, so every rank returns the full-batch
-    result."""
+    result.  ``full_tensor`` (seismic2) adds dL/dc15 and dL/dc35."""
     if gradient is None:
         from .fwi import Fwi
 
         def gradient(p, s, o):
-            with Fwi(p, s, o) as f:
+            with Fwi(p, s, o, full_tensor=full_tensor) as f:
                 return f.gradient()
 
     idx = shard(list(range(len(shots))), rank, world)
@@ -94,7 +94,7 @@ def sharded_gradient(problem, shots: list, observed: list, rank: int, world: int
         # a rank without shots still joins every collective: it sends zeros
         # under the same keys the busy ranks send for this problem family
         from .fwi import grad_keys
-        loss, g = 0.0, {k: np.zeros(problem.shape, order="F") for k in grad_keys(problem.family)}
+        loss, g = 0.0, {k: np.zeros(problem.shape, order="F") for k in grad_keys(problem.family, full_tensor)}
     arrays = {k: np.asarray(v, dtype=np.float64) for k, v in g.items()}
     arrays["__loss__"] = np.array([loss], dtype=np.float64)
     tot = allreduce_sum(arrays)

@@ -31,13 +31,16 @@ from ._lib import ELECTROMAG2, SEISMIC2, SeidartError, UnstableError, lib, ptr_a
 from .api import Problem
 
 GRAD_KEYS = ("c11", "c13", "c33", "c55", "rho")
+GRAD_KEYS_FULL = GRAD_KEYS + ("c15", "c35")  # seismic2 with the full 2D tensor
 GRAD_KEYS_EM = ("e11", "e13", "e33", "s11", "s13", "s33")
 NSTATE = 17     # vx vz sigmaxx sigmazz sigmaxz + 12 memory arrays
 NSTATE_EM = 7   # Ex Ez Hy + 4 memory arrays
 
 
-def grad_keys(family: int) -> tuple:
-    return GRAD_KEYS_EM if family == ELECTROMAG2 else GRAD_KEYS
+def grad_keys(family: int, full_tensor: bool = False) -> tuple:
+    if family == ELECTROMAG2:
+        return GRAD_KEYS_EM
+    return GRAD_KEYS_FULL if full_tensor else GRAD_KEYS
 
 _DECL = False
 
@@ -56,6 +59,7 @@ def _declare():
         "seidart_fwi_forward_step_host": (i, [vp, vp]),
         "seidart_fwi_adjoint_step_host": (i, [vp, vp, vp, vp]),
         "seidart_fwi_launches": (C.c_longlong, [vp]),
+        "seidart_fwi_set_full_tensor": (i, [vp, i]),
         "seidart_fwi_checkpointing": (i, [vp, C.POINTER(i), C.POINTER(i)]),
         "seidart_fwi_destroy": (i, [vp]),
         "seidart_fwi_last_error": (C.c_char_p, []),
@@ -85,7 +89,8 @@ class Fwi:
     """Misfit and gradient of one 2D model (seismic2 or electromag2) over
     several shots."""
 
-    def __init__(self, problem: Problem, shots: list[Shot], observed=None, checkpoint_every: int = 0):
+    def __init__(self, problem: Problem, shots: list[Shot], observed=None, checkpoint_every: int = 0,
+                 full_tensor: bool = False):
         if problem.family not in (SEISMIC2, ELECTROMAG2):
             raise ValueError("the adjoint covers the 2D solvers seismic2 and electromag2")
         _declare()
@@ -109,13 +114,17 @@ class Fwi:
         xs = np.array([s.xind for s in shots], dtype=np.int32)
         zs = np.array([s.zind for s in shots], dtype=np.int32)
         h = C.c_void_p()
-        self.keys = grad_keys(problem.family)
+        if full_tensor and problem.family != SEISMIC2:
+            raise ValueError("full_tensor is for seismic2 (dL/dc15 and dL/dc35)")
+        self.keys = grad_keys(problem.family, full_tensor)
         self.nstate = NSTATE_EM if problem.family == ELECTROMAG2 else NSTATE
         _check(lib().seidart_fwi_create_family(
             C.byref(h), problem.family, C.byref(problem.domain()), C.byref(problem.source()), problem.density_code(),
             ptr_array(self._model), self.nshots, xs.ctypes.data, zs.ctypes.data, ptr_array(self._src),
             self.nrec, rec.ctypes.data if self.nrec else None, ptr_array(self._obs), int(checkpoint_every)))
         self.handle = h
+        if full_tensor:
+            _check(lib().seidart_fwi_set_full_tensor(h, 1))
 
     # ---------------------------------------------------------------- compute
     def gradient(self) -> tuple[float, dict]:

@@ -41,6 +41,10 @@ def _declare():
         "seidart_permittivity_write_c": [C.c_char_p, vp, i, i, vp, i, i, i],
         "seidart_attenuation_arrays": [vp, i, i, vp, i, i, i, d, vp],
         "seidart_attenuation_write": [C.c_char_p, vp, i, i, vp, i, i, i, d],
+        "seidart_stiffness_arrays_dev": [vp, i, i, vp, i, i, i, vp, vp, vp],
+        "seidart_permittivity_arrays_dev": [vp, i, i, vp, i, i, i, vp, vp],
+        "seidart_permittivity_arrays_c_dev": [vp, i, i, vp, i, i, i, vp, vp],
+        "seidart_attenuation_arrays_dev": [vp, i, i, vp, i, i, i, d, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -127,3 +131,63 @@ def attenuation_write(directory, im, alist, npml: int, cpmlvalue: float) -> None
     _check(lib().seidart_attenuation_write(str(Path(directory)).encode(), im.ctypes.data, im.shape[0], im.shape[1],
                                            alist.ctypes.data, alist.shape[0], alist.shape[1], int(npml),
                                            float(cpmlvalue)))
+
+
+# ------------------------------------------------------------ on the device
+def _device_grids(n, nx, nz, npml, complex_valued=False):
+    import torch
+    dt = torch.complex128 if complex_valued else torch.float64
+    # row-major (NZ, NX) is the Fortran (NX, NZ) layout the solvers read
+    return [torch.empty((nz + 2 * npml, nx + 2 * npml), dtype=dt, device="cuda") for _ in range(n)]
+
+
+def _stream_ptr(stream):
+    import torch
+    return (stream or torch.cuda.current_stream()).cuda_stream
+
+
+def stiffness_arrays_device(im, mlist, npml: int, gradient=None, stream=None) -> dict:
+    """The stiffness pre-pass run on the device: {c11 .. c66, rho} as CUDA
+    FP64 tensors of shape (nz + 2 npml, nx + 2 npml) -- row-major, so the
+    memory is the Fortran (nx, nz) grid the solvers read; ``fortran(t)``
+    gives the NumPy view.  Bit-identical to :func:`stiffness_arrays`."""
+    im, mlist = _inputs(im, mlist)
+    nx, nz = im.shape
+    out = _device_grids(22, nx, nz, npml)
+    g = None if gradient is None else np.asfortranarray(gradient, dtype=np.float64)
+    ptrs = (C.c_void_p * 22)(*[t.data_ptr() for t in out])
+    _check(lib().seidart_stiffness_arrays_dev(im.ctypes.data, nx, nz, mlist.ctypes.data, mlist.shape[0],
+                                              mlist.shape[1], int(npml), None if g is None else g.ctypes.data, ptrs,
+                                              _stream_ptr(stream)))
+    return dict(zip(STIFFNESS_NAMES, out))
+
+
+def permittivity_arrays_device(im, mlist, npml: int, complex_valued: bool = False, stream=None) -> dict:
+    """The permittivity pre-pass on the device (see stiffness_arrays_device)."""
+    im, mlist = _inputs(im, mlist, np.complex128 if complex_valued else np.float64)
+    nx, nz = im.shape
+    eps = _device_grids(6, nx, nz, npml, complex_valued)
+    sig = _device_grids(6, nx, nz, npml)
+    ptrs = (C.c_void_p * 12)(*[t.data_ptr() for t in eps + sig])
+    fn = lib().seidart_permittivity_arrays_c_dev if complex_valued else lib().seidart_permittivity_arrays_dev
+    _check(fn(im.ctypes.data, nx, nz, mlist.ctypes.data, mlist.shape[0], mlist.shape[1], int(npml), ptrs,
+              _stream_ptr(stream)))
+    return dict(zip(EPS_NAMES + SIG_NAMES, eps + sig))
+
+
+def attenuation_arrays_device(im, alist, npml: int, cpmlvalue: float, stream=None) -> dict:
+    """The attenuation pre-pass on the device (see stiffness_arrays_device)."""
+    im, alist = _inputs(im, alist)
+    nx, nz = im.shape
+    out = _device_grids(3, nx, nz, npml)
+    ptrs = (C.c_void_p * 3)(*[t.data_ptr() for t in out])
+    _check(lib().seidart_attenuation_arrays_dev(im.ctypes.data, nx, nz, alist.ctypes.data, alist.shape[0],
+                                                alist.shape[1], int(npml), float(cpmlvalue), ptrs,
+                                                _stream_ptr(stream)))
+    return dict(zip(GAMMA_NAMES, out))
+
+
+def fortran(t) -> np.ndarray:
+    """A device grid of the *_device functions as a host (nx, nz) array in
+    Fortran order."""
+    return t.cpu().numpy().T

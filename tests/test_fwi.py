@@ -194,3 +194,71 @@ def test_model_traces_match_solver():
     for s, shot in enumerate(shots):
         ref = sg.run(_shot_problem(start, shot), sg.FP32)["traces"]
         assert np.array_equal(tr[s], ref)
+
+
+# ------------------------------------------------ full 2D tensor: c15, c35
+FULL_KEYS = ("c11", "c13", "c33", "c55", "rho", "c15", "c35")
+
+
+def _tilted(p):
+    """The model with c15 = 0.05 c11 and c35 = -0.04 c33 everywhere, so the
+    off-diagonal terms of both stress updates are live."""
+    from seidart_gpu.fwi import with_model
+    return with_model(p, c15=0.05 * p.model["c11"], c35=-0.04 * p.model["c33"])
+
+
+@pytest.fixture(scope="module")
+def fwi64_full(oracle):
+    pytest.importorskip("torch")
+    from oracle import grad_torch
+    start, true, shots = _case()
+    start, true = _tilted(start), _tilted(true)
+    obs = _oracle_observed(oracle, true, shots)
+    loss, g = grad_torch.misfit_and_gradient(start, shots, obs, 3, keys=FULL_KEYS)
+    return start, shots, obs, loss, g
+
+
+@pytest.mark.gpu
+def test_full_tensor_gradient_matches_fp64_oracle_gradient(fwi64_full):
+    """dL/dc15 and dL/dc35 (cpmlfdtd.f08:342-351, :380-383) with the other
+    five, against the FP64 autograd gradient of the restatement; turning the
+    full tensor on leaves the five others unchanged bit for bit."""
+    from seidart_gpu.fwi import Fwi
+    start, shots, obs, loss64, g64 = fwi64_full
+    with Fwi(start, shots, obs, full_tensor=True) as f:
+        loss, g = f.gradient()
+    assert sorted(g) == sorted(FULL_KEYS)
+    assert abs(loss - loss64) <= 1e-3 * loss64
+    for k in FULL_KEYS:
+        assert np.max(np.abs(g64[k])) > 0, k
+        assert _rel(g[k], g64[k]) <= GRAD_TOL, (k, _rel(g[k], g64[k]))
+    with Fwi(start, shots, obs) as f:
+        _, g5 = f.gradient()
+    assert sorted(g5) == sorted(FULL_KEYS[:5])
+    for k in FULL_KEYS[:5]:
+        assert np.array_equal(g5[k], g[k]), k
+
+
+@pytest.mark.gpu
+def test_full_tensor_gradient_matches_finite_differences(fwi64_full, oracle):
+    from seidart_gpu.fwi import Fwi, with_model
+    start, shots, obs, _, _ = fwi64_full
+    with Fwi(start, shots, obs, full_tensor=True) as f:
+        _, g = f.gradient()
+    rng = np.random.default_rng(12)
+    checked = 0
+    for key in ("c15", "c35"):
+        a = np.abs(g[key])
+        strong = np.argwhere(a >= 0.2 * a.max())
+        for cell in strong[rng.choice(len(strong), size=2, replace=False)]:
+            cell = tuple(cell)
+            base = start.model[key]
+            h = 1e-4 * abs(base[cell])
+            plus, minus = base.copy(order="F"), base.copy(order="F")
+            plus[cell] += h
+            minus[cell] -= h
+            fd = (_oracle_loss(oracle, with_model(start, **{key: plus}), shots, obs)
+                  - _oracle_loss(oracle, with_model(start, **{key: minus}), shots, obs)) / (2 * h)
+            assert abs(g[key][cell] - fd) <= GRAD_TOL * abs(fd), (key, cell, g[key][cell], fd)
+            checked += 1
+    assert checked == 4
