@@ -242,6 +242,8 @@ struct S3Args {
     int wave_n;            // ints of wave_ctl the epilogue clears
     int wave_ctas;         // CTAs of the persistent fused step (resident slots)
     int wave_lag;          // planes between the fused step's stress and velocity fronts (0: default)
+    int l2_hint;           // FP32 staged stress: 1 = read-once copies with an L2 evict-first policy
+    int v_reverse;         // FP32 velocity kernels: 1 = walk the planes from nz-1 down to 0
 };
 // layout of S3Args::wave_ctl
 constexpr int WAVE_DONE0 = 32;

@@ -111,6 +111,30 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
         : "memory");
 }
 
+// L2 eviction policy for read-once streams: lines they bring in go first,
+// so data another CTA reads again (velocity planes) stays longer
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                              uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(saddr(dst)),
+        "l"(src), "r"(bytes), "r"(saddr(bar)), "l"(pol)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load3_hint(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                               unsigned long long* bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+        "%3, %4}], [%5], %6;" ::"r"(saddr(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(saddr(bar)), "l"(pol)
+        : "memory");
+}
+
 // ------------------------------------------------------ L2 prefetch
 __device__ __forceinline__ void pf_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 

@@ -311,7 +311,12 @@ __device__ __forceinline__ void stress_copies(const S3Args<float>& A, const S3XM
     }
     __syncthreads();
     if (tid < 22) {
-        if (tid == 0) {
+        if (A.l2_hint && tid <= 6) {
+            // the coefficient block and the old stresses are read once
+            const uint64_t pol = policy_evict_first();
+            if (tid == 0) bulk_g2s_hint(sm, A.packed + lin * (NCOEF * NT), TILE_BYTES, bar, pol);
+            else tma_load3_hint(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, bar, pol);
+        } else if (tid == 0) {
             bulk_g2s(sm, A.packed + lin * (NCOEF * NT), TILE_BYTES, bar);
         } else if (tid <= 6) {
             tma_load3(sm + XS_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, bar);

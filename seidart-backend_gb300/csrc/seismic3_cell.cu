@@ -251,6 +251,7 @@ __device__ __forceinline__ bool lean_tile_p(const S3Args<float>& A, int x0, int 
 __device__ __forceinline__ void s3p_velocity_prefetch(const S3Args<float>& A, int tid) {
     int tx, ty, k;
     if (!tile_ahead(A.pfp_d, tx, ty, k)) return;
+    if (A.v_reverse) k = A.nz - 1 - k;  // the plane that launch position will update
     for (int half = 0; half < 2; ++half) {
         const int ty8 = 2 * ty + half;  // the two 32 x 8 row blocks of the tile
         pf_tile_rows(A.f, 9, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
@@ -269,7 +270,10 @@ __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, St
     const int tid = threadIdx.y * PX + threadIdx.x;
     if (A.prefetch_v > 0) s3p_velocity_prefetch(A, tid);
     const int it = *si.step;
-    const int x0 = blockIdx.x * TPX + 2 * threadIdx.x, gy = blockIdx.y * TPY + threadIdx.y, k = blockIdx.z;
+    // v_reverse: the planes are walked from the top, where the stress
+    // kernel that just ran finished, so its last stresses are still in L2
+    const int k = A.v_reverse ? A.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
+    const int x0 = blockIdx.x * TPX + 2 * threadIdx.x, gy = blockIdx.y * TPY + threadIdx.y;
     const int nx = A.nx, ny = A.ny;
     float vsq = 0.f, ssq = 0.f;
     if (lean_tile_p(A, blockIdx.x * TPX, blockIdx.y * TPY, k)) {
