@@ -544,6 +544,8 @@ def main():
                     help="run a small ragged batch (16 models of the batch workload's distribution, 40 steps in "
                          "launches of 20, the autotuned kernel) and exit: the case the batch profile in profiles/ "
                          "is captured on")
+    ap.add_argument("--s3-profile-precision", default="fp32", choices=["fp32", "fp64", "fp64fast"],
+                    help="precision of --s3-profile-case")
     ap.add_argument("--s3-profile-case", action="store_true",
                     help="run 4 FP32 steps of the 3D workload at --grid (e.g. 192: 224^3 padded cells) through "
                          "the default kernels and exit: the case the 3D kernel profiles in profiles/ are captured on")
@@ -578,7 +580,8 @@ def main():
     if args.s3_profile_case:
         import seidart_gpu as sg
         p = make_problem(nt=4)
-        with sg.Solver(p, sg.FP32) as s:
+        prec = {"fp32": sg.FP32, "fp64": sg.FP64, "fp64fast": sg.FP64_FAST}[args.s3_profile_precision]
+        with sg.Solver(p, prec) as s:
             s.step(4)
             s.sync()
             tr, _ = s.traces()
