@@ -25,26 +25,59 @@ __device__ __forceinline__ float cpml_apply(float* m, size_t c, const CpmlC& p, 
     m[c] = mv;
     return d * p.k + mv;
 }
-// C-PML correction of the nine derivatives of stress loop L (1: normal
-// stresses, 2: sigma_xy, 3: sigma_xz, 4: sigma_yz); memory slots 9(L-1)..
+// The C-PML step of stress loop L (1: normal stresses, 2: sigma_xy,
+// 3: sigma_xz, 4: sigma_yz; memory slots 9(L-1)..9L-1) in three parts, so a
+// kernel can issue the loads of two loops before the stores of either:
+// cpml_load reads the nine memories, cpml_update advances them and rescales
+// the loop's nine derivatives, cpml_store writes them back.
+struct CpmlPair {
+    CpmlC h, f;  // half-grid and full-grid coefficient triples of the cell
+};
+__device__ __forceinline__ CpmlPair cpml_both(const S3Args<float>& A, size_t c) {
+    return CpmlPair{cpml_at(A, c, true), cpml_at(A, c, false)};
+}
+template <int L>
+__device__ __forceinline__ void cpml_load(const S3Args<float>& A, size_t c, float (&m)[9]) {
+    float* const* M = A.mem + 9 * (L - 1);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m[q] = M[q][c];
+}
+template <int L>
+__device__ __forceinline__ void cpml_store(const S3Args<float>& A, size_t c, const float (&m)[9]) {
+    float* const* M = A.mem + 9 * (L - 1);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) M[q][c] = m[q];
+}
+template <int L>
+__device__ __forceinline__ void cpml_update(const CpmlPair& P, float (&m)[9], float (&gx)[3], float (&gy)[3],
+                                            float (&gz)[3]) {
+    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
+    const CpmlC px = xh ? P.h : P.f, py = yh ? P.h : P.f, pz = zh ? P.h : P.f;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        m[3 * f] = px.b * m[3 * f] + px.a * gx[f];
+        gx[f] = gx[f] * px.k + m[3 * f];
+        m[3 * f + 1] = py.b * m[3 * f + 1] + py.a * gy[f];
+        gy[f] = gy[f] * py.k + m[3 * f + 1];
+        // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
+        // (reference quirk, cpmlfdtd.f08:1855-1866)
+        m[3 * f + 2] = pz.b * m[3 * f + 2] + pz.a * gz[f];
+        if (!(L == 2 && f == 0)) gz[f] = gz[f] * pz.k + m[3 * f + 2];
+    }
+}
+
+// C-PML correction of the nine derivatives of stress loop L, loads first
 template <int L>
 __device__ __forceinline__ void loop_cpml(const S3Args<float>& A, size_t c, float (&gx)[3], float (&gy)[3],
                                           float (&gz)[3]) {
-    constexpr bool xh = (L == 1 || L == 4), yh = (L == 2 || L == 4), zh = (L != 1);
-    const CpmlC px = cpml_at(A, c, xh), py = cpml_at(A, c, yh), pz = cpml_at(A, c, zh);
-    float* const* M = A.mem + 9 * (L - 1);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-        gx[f] = cpml_apply(M[3 * f], c, px, gx[f]);
-        gy[f] = cpml_apply(M[3 * f + 1], c, py, gy[f]);
-        if (L == 2 && f == 0) {
-            // loop 2 advances memory_dvx_dz2 but sigma_xy uses the raw dvx_dz
-            // (reference quirk, cpmlfdtd.f08:1855-1866)
-            M[2][c] = pz.b * M[2][c] + pz.a * gz[0];
-        } else {
-            gz[f] = cpml_apply(M[3 * f + 2], c, pz, gz[f]);
-        }
-    }
+    const CpmlPair P = cpml_both(A, c);
+    // all nine memories are loaded before the first store: a store to one
+    // memory array would otherwise hold the next array's load behind it (the
+    // compiler cannot rule out aliasing), one DRAM round trip per memory
+    float m[9];
+    cpml_load<L>(A, c, m);
+    cpml_update<L>(P, m, gx, gy, gz);
+    cpml_store<L>(A, c, m);
 }
 
 // sigma_new = (sigma_old + dt * sum_j C_ij e_j) / (1 + gamma dt); C read

@@ -58,42 +58,58 @@ __device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, in
     const int code = A.density_code;
     const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
                                 k < A.box.k1);
+    const bool ux = LEAN || (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2);
+    const bool uy = LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 1 && gy <= ny - 3 && k >= 2 && k <= nz - 2);
+    const bool uz = LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 2 && gy <= ny - 2 && k >= 1 && k <= nz - 3);
+    // shell cells: the two coefficient triples and the nine memories
+    // (slots 36..44: x y z derivative memories of vx, vy, vz) are all loaded
+    // before the first store, so they cost one DRAM round trip, not nine
+    CpmlC ph{0.f, 0.f, 0.f}, pf{0.f, 0.f, 0.f};
+    float m[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (pml) {
+        ph = cpml_at(A, c, true);
+        pf = cpml_at(A, c, false);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = A.mem[36 + q][c];
+    }
     const float byy = inv_mean_f(r0, r0, code);
-    if (LEAN || (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2)) {  // vx
+    if (ux) {  // vx
         float d1 = (27.0f * (sxx0 - sxxm1) + sxxm2) * hx;
         float d2 = (27.0f * (sxy0 - sxyym1) + sxyym2) * hy;
         float d3 = (27.0f * (sxz0 - sxzzm1) + sxzzm2) * hz;
         if (pml) {
-            const CpmlC p = cpml_at(A, c, true);
-            d1 = cpml_apply(A.mem[36], c, p, d1);
-            d2 = cpml_apply(A.mem[40], c, p, d2);
-            d3 = cpml_apply(A.mem[42], c, p, d3);
+            m[0] = ph.b * m[0] + ph.a * d1; d1 = d1 * ph.k + m[0];
+            m[4] = ph.b * m[4] + ph.a * d2; d2 = d2 * ph.k + m[4];
+            m[6] = ph.b * m[6] + ph.a * d3; d3 = d3 * ph.k + m[6];
         }
         vx = vx + (d1 * inv_mean_f(r0, rxm, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
     }
-    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 1 && gy <= ny - 3 && k >= 2 && k <= nz - 2)) {  // vy
+    if (uy) {  // vy
         float d1 = (27.0f * (sxyp1 - sxy0) - sxyp2) * hx;
         float d2 = (27.0f * (syyp1 - syy0) - syyp2) * hy;
         float d3 = (27.0f * (syz0 - syzzm1) + syzzm2) * hz;
         if (pml) {
-            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
-            d1 = cpml_apply(A.mem[39], c, ph, d1);
-            d2 = cpml_apply(A.mem[37], c, ph, d2);
-            d3 = cpml_apply(A.mem[44], c, pf, d3);
+            m[3] = ph.b * m[3] + ph.a * d1; d1 = d1 * ph.k + m[3];
+            m[1] = ph.b * m[1] + ph.a * d2; d2 = d2 * ph.k + m[1];
+            m[8] = pf.b * m[8] + pf.a * d3; d3 = d3 * pf.k + m[8];
         }
         vy = vy + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzm, code)) * dt;
     }
-    if (LEAN || (gx >= 1 && gx <= nx - 3 && gy >= 2 && gy <= ny - 2 && k >= 1 && k <= nz - 3)) {  // vz
+    if (uz) {  // vz
         float d1 = (27.0f * (sxzp1 - sxz0) - sxzp2) * hx;
         float d2 = (27.0f * (syz0 - syzym1) + syzym2) * hy;
         float d3 = (27.0f * (szzp1 - szz0) - szzp2) * hz;
         if (pml) {
-            const CpmlC ph = cpml_at(A, c, true), pf = cpml_at(A, c, false);
-            d1 = cpml_apply(A.mem[41], c, ph, d1);
-            d2 = cpml_apply(A.mem[43], c, pf, d2);
-            d3 = cpml_apply(A.mem[38], c, ph, d3);
+            m[5] = ph.b * m[5] + ph.a * d1; d1 = d1 * ph.k + m[5];
+            m[7] = pf.b * m[7] + pf.a * d2; d2 = d2 * pf.k + m[7];
+            m[2] = ph.b * m[2] + ph.a * d3; d3 = d3 * ph.k + m[2];
         }
         vz = vz + (d1 * inv_mean_f(r0, rxp, code) + d2 * byy + d3 * inv_mean_f(r0, rzp, code)) * dt;
+    }
+    if (pml) {  // each memory written only by the update that advanced it
+        if (ux) { A.mem[36][c] = m[0]; A.mem[40][c] = m[4]; A.mem[42][c] = m[6]; }
+        if (uy) { A.mem[39][c] = m[3]; A.mem[37][c] = m[1]; A.mem[44][c] = m[8]; }
+        if (uz) { A.mem[41][c] = m[5]; A.mem[43][c] = m[7]; A.mem[38][c] = m[2]; }
     }
     bool src_cell = false;
     if (!LEAN) {

@@ -256,26 +256,52 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
     // C index: 0 c11 1 c12 2 c13 3 c14 4 c15 5 c16 6 c22 7 c23 8 c24 9 c25 10 c26
     //          11 c33 12 c34 13 c35 14 c36 15 c44 16 c45 17 c46 18 c55 19 c56 20 c66
     // old stress order: xx xy xz yy yz zz ; gamma order: x y z xy yz xz
+    // shell cells: the memories of loops 1 and 2 are loaded together, and
+    // those of loops 3 and 4 together after the first pair's stores, so a
+    // cell waits for two DRAM round trips instead of four
+    CpmlPair P{};
+    float ma[9], mb[9];
+    if (pml) {
+        P = cpml_both(A, c);
+        if (L1) cpml_load<1>(A, c, ma);
+        if (L2) cpml_load<2>(A, c, mb);
+    }
     if (L1) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
-        if (pml) loop_cpml<1>(A, c, ex, ey, ez);
+        if (pml) {
+            cpml_update<1>(P, ma, ex, ey, ez);
+            cpml_store<1>(A, c, ma);
+        }
         st_sig<STREAM>(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
         st_sig<STREAM>(A.f[6] + c, stress_new(CR, so[3 * NT], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
         st_sig<STREAM>(A.f[8] + c, stress_new(CR, so[5 * NT], GM(2), 2, 7, 11, 12, 13, 14, dt, ex, ey, ez));
     }
     if (L2) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
-        if (pml) loop_cpml<2>(A, c, ex, ey, ez);
+        if (pml) {
+            cpml_update<2>(P, mb, ex, ey, ez);
+            cpml_store<2>(A, c, mb);
+        }
         st_sig<STREAM>(A.f[4] + c, stress_new(CR, so[NT], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+    }
+    if (pml) {
+        if (L3) cpml_load<3>(A, c, ma);
+        if (L4) cpml_load<4>(A, c, mb);
     }
     if (L3) {
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
-        if (pml) loop_cpml<3>(A, c, ex, ey, ez);
+        if (pml) {
+            cpml_update<3>(P, ma, ex, ey, ez);
+            cpml_store<3>(A, c, ma);
+        }
         st_sig<STREAM>(A.f[5] + c, stress_new(CR, so[2 * NT], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
     }
     if (L4) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
-        if (pml) loop_cpml<4>(A, c, ex, ey, ez);
+        if (pml) {
+            cpml_update<4>(P, mb, ex, ey, ez);
+            cpml_store<4>(A, c, mb);
+        }
         st_sig<STREAM>(A.f[7] + c, stress_new(CR, so[4 * NT], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
     }
 }
