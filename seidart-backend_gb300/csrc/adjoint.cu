@@ -120,7 +120,10 @@ __device__ __forceinline__ void gather_sT(const AdjArgs& A, int i, int k, float&
 }
 
 // Starts the adjoint of step n: completes lambda_v(n) (gather of S^T from
-// step n+1, receiver residuals of step n), then D^T and V^T.
+// step n+1, receiver residuals of step n), then D^T and V^T.  Every load
+// precedes the first store: a store to one array would otherwise hold every
+// later load behind it (the compiler cannot rule out aliasing between the
+// slices of lam, grad and scr), one DRAM round trip each.
 __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
     const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
     const int nx = A.nx, nz = A.nz;
@@ -141,16 +144,15 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
         lvx = 0.f;
         lvz = 0.f;
     }
-    lam[c] = lvx;
-    lam[N + c] = lvz;
-    if (i == A.isrc && k == A.jsrc && A.srcz) *A.gsrc += (double)lvz * (double)(float)A.srcz[*A.base + A.j - 1];
     const float* xc = A.xc;
     const float *sxx = xc + 2 * N, *szz = xc + 3 * N, *sxz = xc + 4 * N;
     const float* rho = A.m[6];
     const bool pml = !(i >= A.box.i0 && i < A.box.i1 && k >= A.box.k0 && k < A.box.k1);
     const float dt = A.dt, hx = A.hx, hz = A.hz;
+    const bool ix = inX(i, k, nx, nz), iz = inZ(i, k, nx, nz);
     float lf1 = 0.f, lf2 = 0.f, lf3 = 0.f, lf4 = 0.f;
-    if (inX(i, k, nx, nz)) {
+    float l8 = 0.f, l11 = 0.f, l10 = 0.f, l9 = 0.f, g4 = 0.f, g5 = 0.f, g6 = 0.f, g7 = 0.f;
+    if (ix) {
         const float bxx = inv_mean_f(rho[c], rho[c - 1], A.density_code);
         const float bzx = inv_mean_f(rho[c], rho[c - nx], A.density_code);
         float F1 = (27.0f * (sxx[c] - sxx[c - 1]) + sxx[c - 2]) * hx;
@@ -160,20 +162,19 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
             const float ik = A.m[10][c], a = A.m[12][c], b = A.m[14][c];
             F1 = F1 * ik + xc[(5 + 8) * N + c];
             F2 = F2 * ik + xc[(5 + 11) * N + c];
-            float* l8 = lam + (5 + 8) * N + c;
-            float* l11 = lam + (5 + 11) * N + c;
-            lf1 = (ik + a) * p1 + a * *l8;
-            *l8 = b * (p1 + *l8);
-            lf2 = (ik + a) * p2 + a * *l11;
-            *l11 = b * (p2 + *l11);
+            const float o8 = lam[(5 + 8) * N + c], o11 = lam[(5 + 11) * N + c];
+            lf1 = (ik + a) * p1 + a * o8;
+            l8 = b * (p1 + o8);
+            lf2 = (ik + a) * p2 + a * o11;
+            l11 = b * (p2 + o11);
         } else {
             lf1 = p1;
             lf2 = p2;
         }
-        A.grad[4 * N + c] += lvx * dt * F1;
-        A.grad[5 * N + c] += lvx * dt * F2;
+        g4 = A.grad[4 * N + c] + lvx * dt * F1;
+        g5 = A.grad[5 * N + c] + lvx * dt * F2;
     }
-    if (inZ(i, k, nx, nz)) {
+    if (iz) {
         const float bxz = inv_mean_f(rho[c], rho[c + 1], A.density_code);
         const float bzz = inv_mean_f(rho[c], rho[c + nx], A.density_code);
         float F3 = (27.0f * (sxz[c + 1] - sxz[c]) - sxz[c + 2]) * hx;
@@ -183,18 +184,39 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
             const float ikh = A.m[11][c], ah = A.m[13][c], bh = A.m[15][c];
             F3 = F3 * ikh + xc[(5 + 10) * N + c];
             F4 = F4 * ikh + xc[(5 + 9) * N + c];
-            float* l10 = lam + (5 + 10) * N + c;
-            float* l9 = lam + (5 + 9) * N + c;
-            lf3 = (ikh + ah) * p3 + ah * *l10;
-            *l10 = bh * (p3 + *l10);
-            lf4 = (ikh + ah) * p4 + ah * *l9;
-            *l9 = bh * (p4 + *l9);
+            const float o10 = lam[(5 + 10) * N + c], o9 = lam[(5 + 9) * N + c];
+            lf3 = (ikh + ah) * p3 + ah * o10;
+            l10 = bh * (p3 + o10);
+            lf4 = (ikh + ah) * p4 + ah * o9;
+            l9 = bh * (p4 + o9);
         } else {
             lf3 = p3;
             lf4 = p4;
         }
-        A.grad[6 * N + c] += lvz * dt * F3;
-        A.grad[7 * N + c] += lvz * dt * F4;
+        g6 = A.grad[6 * N + c] + lvz * dt * F3;
+        g7 = A.grad[7 * N + c] + lvz * dt * F4;
+    }
+    const bool src = i == A.isrc && k == A.jsrc && A.srcz;
+    const double fsrc = src ? (double)(float)A.srcz[*A.base + A.j - 1] : 0.0;
+    // ---- stores
+    lam[c] = lvx;
+    lam[N + c] = lvz;
+    if (src) *A.gsrc += (double)lvz * fsrc;
+    if (ix) {
+        if (pml) {
+            lam[(5 + 8) * N + c] = l8;
+            lam[(5 + 11) * N + c] = l11;
+        }
+        A.grad[4 * N + c] = g4;
+        A.grad[5 * N + c] = g5;
+    }
+    if (iz) {
+        if (pml) {
+            lam[(5 + 10) * N + c] = l10;
+            lam[(5 + 9) * N + c] = l9;
+        }
+        A.grad[6 * N + c] = g6;
+        A.grad[7 * N + c] = g7;
     }
     A.scr[c] = lf1;
     A.scr[N + c] = lf2;
@@ -203,6 +225,7 @@ __global__ void __launch_bounds__(BX* BY) adj_velocity(AdjArgs A) {
 }
 
 // ------------------------------------------------- gather of V^T, then S^T
+// All loads first, then all stores (as in adj_velocity).
 __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
     const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
     const int nx = A.nx, nz = A.nz;
@@ -224,9 +247,15 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
     const float* vz = A.xp + N;
     const float* xc = A.xc;
     float* lam = A.lam;
+    const bool in_n = inN(i, k, nx, nz), in_s = inS(i, k, nx, nz);
     float ld1 = 0.f, ld2 = 0.f, ld3 = 0.f, ld4 = 0.f, le1 = 0.f, le2 = 0.f, le3 = 0.f, le4 = 0.f;
     float nsxx = lsxx, nszz = lszz, nsxz = lsxz;
-    if (inN(i, k, nx, nz)) {
+    float l0 = 0.f, l1 = 0.f, l2 = 0.f, l3 = 0.f, l4 = 0.f, l5 = 0.f, l6 = 0.f, l7 = 0.f;  // new memory adjoints
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;  // new gradient sums
+    // dL/dc15, dL/dc35 collect a term from each loop, normal loop first
+    const bool full = A.full && (in_n || in_s);
+    float g8 = full ? A.grad[8 * N + c] : 0.f, g9 = full ? A.grad[9 * N + c] : 0.f;
+    if (in_n) {
         const float gx = m[7][c], gz = m[8][c];
         const float px = dt * gx * lsxx, pz = dt * gz * lszz;
         nsxx = gx * lsxx;
@@ -240,27 +269,27 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
             const float ik = m[10][c], ikh = m[11][c], a = m[12][c], ah = m[13][c], b = m[14][c], bh = m[15][c];
             D1 = D1 * ikh + xc[(5 + 0) * N + c];
             D2 = D2 * ik + xc[(5 + 3) * N + c];
-            float* l0 = lam + (5 + 0) * N + c;  // dvx_dx1 (half)
-            float* l1 = lam + (5 + 1) * N + c;  // dvx_dz1 (half)
-            float* l3 = lam + (5 + 3) * N + c;  // dvz_dz1 (full)
-            float* l2 = lam + (5 + 2) * N + c;  // dvz_dx1 (full)
-            ld1 = (ikh + ah) * lD1 + ah * *l0;
-            *l0 = bh * (lD1 + *l0);
-            ld4 = (ikh + ah) * lD3 + ah * *l1;
-            *l1 = bh * (lD3 + *l1);
-            ld2 = (ik + a) * lD2 + a * *l3;
-            *l3 = b * (lD2 + *l3);
-            ld3 = (ik + a) * lD3 + a * *l2;
-            *l2 = b * (lD3 + *l2);
+            const float o0 = lam[(5 + 0) * N + c];  // dvx_dx1 (half)
+            const float o1 = lam[(5 + 1) * N + c];  // dvx_dz1 (half)
+            const float o3 = lam[(5 + 3) * N + c];  // dvz_dz1 (full)
+            const float o2 = lam[(5 + 2) * N + c];  // dvz_dx1 (full)
+            ld1 = (ikh + ah) * lD1 + ah * o0;
+            l0 = bh * (lD1 + o0);
+            ld4 = (ikh + ah) * lD3 + ah * o1;
+            l1 = bh * (lD3 + o1);
+            ld2 = (ik + a) * lD2 + a * o3;
+            l3 = b * (lD2 + o3);
+            ld3 = (ik + a) * lD3 + a * o2;
+            l2 = b * (lD3 + o2);
         } else {
             ld1 = lD1;
             ld2 = lD2;
             ld3 = lD3;
             ld4 = lD3;
         }
-        A.grad[c] += px * D1;
-        A.grad[N + c] += px * D2 + pz * D1;
-        A.grad[2 * N + c] += pz * D2;
+        g0 = A.grad[c] + px * D1;
+        g1 = A.grad[N + c] + (px * D2 + pz * D1);
+        g2 = A.grad[2 * N + c] + pz * D2;
         if (A.full) {
             // c15 and c35 multiply dvz_dx + dvx_dz of the normal-stress loop
             // (cpmlfdtd.f08:342-351): forward x (full coefficients) and
@@ -271,11 +300,11 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
                 D3 = D3 * m[10][c] + xc[(5 + 2) * N + c];
                 D4 = D4 * m[11][c] + xc[(5 + 1) * N + c];
             }
-            A.grad[8 * N + c] += px * (D3 + D4);
-            A.grad[9 * N + c] += pz * (D3 + D4);
+            g8 = g8 + px * (D3 + D4);
+            g9 = g9 + pz * (D3 + D4);
         }
     }
-    if (inS(i, k, nx, nz)) {
+    if (in_s) {
         const float gxz = m[9][c];
         const float pxz = dt * gxz * lsxz;
         nsxz = gxz * lsxz;
@@ -286,25 +315,25 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
             const float ikh = m[11][c], ah = m[13][c], bh = m[15][c];
             E3 = E3 * ikh + xc[(5 + 6) * N + c];
             E4 = E4 * ikh + xc[(5 + 5) * N + c];
-            float* l4 = lam + (5 + 4) * N + c;  // dvx_dx2
-            float* l5 = lam + (5 + 5) * N + c;  // dvx_dz2
-            float* l6 = lam + (5 + 6) * N + c;  // dvz_dx2
-            float* l7 = lam + (5 + 7) * N + c;  // dvz_dz2
-            le1 = (ikh + ah) * lE1 + ah * *l4;
-            *l4 = bh * (lE1 + *l4);
-            le4 = (ikh + ah) * lE34 + ah * *l5;
-            *l5 = bh * (lE34 + *l5);
-            le3 = (ikh + ah) * lE34 + ah * *l6;
-            *l6 = bh * (lE34 + *l6);
-            le2 = (ikh + ah) * lE2 + ah * *l7;
-            *l7 = bh * (lE2 + *l7);
+            const float o4 = lam[(5 + 4) * N + c];  // dvx_dx2
+            const float o5 = lam[(5 + 5) * N + c];  // dvx_dz2
+            const float o6 = lam[(5 + 6) * N + c];  // dvz_dx2
+            const float o7 = lam[(5 + 7) * N + c];  // dvz_dz2
+            le1 = (ikh + ah) * lE1 + ah * o4;
+            l4 = bh * (lE1 + o4);
+            le4 = (ikh + ah) * lE34 + ah * o5;
+            l5 = bh * (lE34 + o5);
+            le3 = (ikh + ah) * lE34 + ah * o6;
+            l6 = bh * (lE34 + o6);
+            le2 = (ikh + ah) * lE2 + ah * o7;
+            l7 = bh * (lE2 + o7);
         } else {
             le1 = lE1;
             le2 = lE2;
             le3 = lE34;
             le4 = lE34;
         }
-        A.grad[3 * N + c] += pxz * (E3 + E4);
+        g3 = A.grad[3 * N + c] + pxz * (E3 + E4);
         if (A.full) {
             // sigma_xz's c15 dvx_dx (backward x) and c35 dvz_dz (forward z),
             // half coefficients (cpmlfdtd.f08:380-383)
@@ -315,13 +344,38 @@ __global__ void __launch_bounds__(BX* BY) adj_stress(AdjArgs A) {
                 E1 = E1 * ikh + xc[(5 + 4) * N + c];
                 E2 = E2 * ikh + xc[(5 + 7) * N + c];
             }
-            A.grad[8 * N + c] += pxz * E1;
-            A.grad[9 * N + c] += pxz * E2;
+            g8 = g8 + pxz * E1;
+            g9 = g9 + pxz * E2;
         }
     }
+    // ---- stores
     lam[2 * N + c] = nsxx;
     lam[3 * N + c] = nszz;
     lam[4 * N + c] = nsxz;
+    if (in_n) {
+        if (pml) {
+            lam[(5 + 0) * N + c] = l0;
+            lam[(5 + 1) * N + c] = l1;
+            lam[(5 + 3) * N + c] = l3;
+            lam[(5 + 2) * N + c] = l2;
+        }
+        A.grad[c] = g0;
+        A.grad[N + c] = g1;
+        A.grad[2 * N + c] = g2;
+    }
+    if (in_s) {
+        if (pml) {
+            lam[(5 + 4) * N + c] = l4;
+            lam[(5 + 5) * N + c] = l5;
+            lam[(5 + 6) * N + c] = l6;
+            lam[(5 + 7) * N + c] = l7;
+        }
+        A.grad[3 * N + c] = g3;
+    }
+    if (full) {
+        A.grad[8 * N + c] = g8;
+        A.grad[9 * N + c] = g9;
+    }
     float* s = A.scr + 4 * N;
     s[c] = ld1; s[N + c] = ld2; s[2 * N + c] = ld3; s[3 * N + c] = ld4;
     s[4 * N + c] = le1; s[5 * N + c] = le2; s[6 * N + c] = le3; s[7 * N + c] = le4;
@@ -397,6 +451,8 @@ struct OopArgs {
 
 #define D4F(p1, p0, p2, m1, h) ((27.0f * ((p1) - (p0)) - ((p2) - (m1))) * (h))
 
+// Both recompute kernels issue every load before the first store (the
+// slices of `in` and `out` could alias as far as the compiler knows).
 __global__ void __launch_bounds__(BX* BY) oop_stress(OopArgs O) {
     const int i = blockIdx.x * BX + threadIdx.x, k = blockIdx.y * BY + threadIdx.y;
     const S2Args<float>& a = O.a;
@@ -407,15 +463,11 @@ __global__ void __launch_bounds__(BX* BY) oop_stress(OopArgs O) {
     const float* mi = O.in + 5 * N;
     float* mo = O.out + 5 * N;
     const bool normal = inN(i, k, nx, nz), shear = inS(i, k, nx, nz);
-    if (!normal) {
-        O.out[2 * N + c] = O.in[2 * N + c];
-        O.out[3 * N + c] = O.in[3 * N + c];
-    }
-    if (!shear) O.out[4 * N + c] = O.in[4 * N + c];
-    if (!normal && !shear) return;
     const bool pml = !(i >= a.box.i0 && i < a.box.i1 && k >= a.box.k0 && k < a.box.k1);
     const float dt = a.dt;
     const float hx = 1.0f / (24.0f * a.dx), hz = 1.0f / (24.0f * a.dz);
+    float sxx = O.in[2 * N + c], szz = O.in[3 * N + c], sxz = O.in[4 * N + c];
+    float M0 = 0.f, M1 = 0.f, M2 = 0.f, M3 = 0.f, M4 = 0.f, M5 = 0.f, M6 = 0.f, M7 = 0.f;
     if (normal) {
         float dvx_dx = D4F(vx[c + 1], vx[c], vx[c + 2], vx[c - 1], hx);
         float dvz_dz = D4F(vz[c], vz[c - nx], vz[c + nx], vz[c - 2 * nx], hz);
@@ -423,19 +475,18 @@ __global__ void __launch_bounds__(BX* BY) oop_stress(OopArgs O) {
         float dvx_dz = D4F(vx[c], vx[c - nx], vx[c + nx], vx[c - 2 * nx], hz);
         if (pml) {
             const float bh = a.m[15][c], ah = a.m[13][c], b = a.m[14][c], aa = a.m[12][c];
-            const float M0 = bh * mi[c] + ah * dvx_dx;
-            const float M1 = bh * mi[N + c] + ah * dvx_dz;
-            const float M3 = b * mi[3 * N + c] + aa * dvz_dz;
-            const float M2 = b * mi[2 * N + c] + aa * dvz_dx;
-            mo[c] = M0; mo[N + c] = M1; mo[2 * N + c] = M2; mo[3 * N + c] = M3;
+            M0 = bh * mi[c] + ah * dvx_dx;
+            M1 = bh * mi[N + c] + ah * dvx_dz;
+            M3 = b * mi[3 * N + c] + aa * dvz_dz;
+            M2 = b * mi[2 * N + c] + aa * dvz_dx;
             dvx_dx = dvx_dx * a.m[11][c] + M0;
             dvx_dz = dvx_dz * a.m[11][c] + M1;
             dvz_dz = dvz_dz * a.m[10][c] + M3;
             dvz_dx = dvz_dx * a.m[10][c] + M2;
         }
         const float c11 = a.m[0][c], c13 = a.m[1][c], c15 = a.m[2][c], c33 = a.m[3][c], c35 = a.m[4][c];
-        O.out[2 * N + c] = (O.in[2 * N + c] + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * a.m[7][c];
-        O.out[3 * N + c] = (O.in[3 * N + c] + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * a.m[8][c];
+        sxx = (sxx + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * a.m[7][c];
+        szz = (szz + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * a.m[8][c];
     }
     if (shear) {
         float dvx_dx = D4F(vx[c], vx[c - 1], vx[c + 1], vx[c - 2], hx);
@@ -444,19 +495,24 @@ __global__ void __launch_bounds__(BX* BY) oop_stress(OopArgs O) {
         float dvx_dz = D4F(vx[c + nx], vx[c], vx[c + 2 * nx], vx[c - nx], hz);
         if (pml) {
             const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
-            const float M4 = bh * mi[4 * N + c] + ah * dvx_dx;
-            const float M5 = bh * mi[5 * N + c] + ah * dvx_dz;
-            const float M7 = bh * mi[7 * N + c] + ah * dvz_dz;
-            const float M6 = bh * mi[6 * N + c] + ah * dvz_dx;
-            mo[4 * N + c] = M4; mo[5 * N + c] = M5; mo[6 * N + c] = M6; mo[7 * N + c] = M7;
+            M4 = bh * mi[4 * N + c] + ah * dvx_dx;
+            M5 = bh * mi[5 * N + c] + ah * dvx_dz;
+            M7 = bh * mi[7 * N + c] + ah * dvz_dz;
+            M6 = bh * mi[6 * N + c] + ah * dvz_dx;
             dvx_dx = dvx_dx * kh + M4;
             dvx_dz = dvx_dz * kh + M5;
             dvz_dz = dvz_dz * kh + M7;
             dvz_dx = dvz_dx * kh + M6;
         }
         const float c15 = a.m[2][c], c35 = a.m[4][c], c55 = a.m[5][c];
-        O.out[4 * N + c] = (O.in[4 * N + c] + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * a.m[9][c];
+        sxz = (sxz + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * a.m[9][c];
     }
+    // ---- stores (fields outside the loops are copied through)
+    O.out[2 * N + c] = sxx;
+    O.out[3 * N + c] = szz;
+    O.out[4 * N + c] = sxz;
+    if (pml && normal) { mo[c] = M0; mo[N + c] = M1; mo[2 * N + c] = M2; mo[3 * N + c] = M3; }
+    if (pml && shear) { mo[4 * N + c] = M4; mo[5 * N + c] = M5; mo[6 * N + c] = M6; mo[7 * N + c] = M7; }
 }
 
 __global__ void __launch_bounds__(BX* BY) oop_velocity(OopArgs O) {
@@ -472,32 +528,32 @@ __global__ void __launch_bounds__(BX* BY) oop_velocity(OopArgs O) {
     const bool pml = !(i >= a.box.i0 && i < a.box.i1 && k >= a.box.k0 && k < a.box.k1);
     const float dt = a.dt;
     const float hx = 1.0f / (24.0f * a.dx), hz = 1.0f / (24.0f * a.dz);
+    const bool ix = inX(i, k, nx, nz), iz = inZ(i, k, nx, nz);
     float vx = O.in[c], vz = O.in[N + c];
-    if (inX(i, k, nx, nz)) {
+    float M8 = 0.f, M11 = 0.f, M10 = 0.f, M9 = 0.f;
+    if (ix) {
         const float bxx = inv_mean_f(rho[c], rho[c - 1], a.density_code);
         const float bzx = inv_mean_f(rho[c], rho[c - nx], a.density_code);
         float dsxx_dx = (27.0f * (sxx[c] - sxx[c - 1]) + sxx[c - 2]) * hx;
         float dsxz_dz = (27.0f * (sxz[c] - sxz[c - nx]) + sxz[c - 2 * nx]) * hz;
         if (pml) {
             const float b = a.m[14][c], aa = a.m[12][c], kk = a.m[10][c];
-            const float M8 = b * mi[8 * N + c] + aa * dsxx_dx;
-            const float M11 = b * mi[11 * N + c] + aa * dsxz_dz;
-            mo[8 * N + c] = M8; mo[11 * N + c] = M11;
+            M8 = b * mi[8 * N + c] + aa * dsxx_dx;
+            M11 = b * mi[11 * N + c] + aa * dsxz_dz;
             dsxx_dx = dsxx_dx * kk + M8;
             dsxz_dz = dsxz_dz * kk + M11;
         }
         vx = vx + dt * (dsxx_dx * bxx + dsxz_dz * bzx);
     }
-    if (inZ(i, k, nx, nz)) {
+    if (iz) {
         const float bxz = inv_mean_f(rho[c], rho[c + 1], a.density_code);
         const float bzz = inv_mean_f(rho[c], rho[c + nx], a.density_code);
         float dsxz_dx = (27.0f * (sxz[c + 1] - sxz[c]) - sxz[c + 2]) * hx;
         float dszz_dz = (27.0f * (szz[c + nx] - szz[c]) - szz[c + 2 * nx]) * hz;
         if (pml) {
             const float bh = a.m[15][c], ah = a.m[13][c], kh = a.m[11][c];
-            const float M10 = bh * mi[10 * N + c] + ah * dsxz_dx;
-            const float M9 = bh * mi[9 * N + c] + ah * dszz_dz;
-            mo[10 * N + c] = M10; mo[9 * N + c] = M9;
+            M10 = bh * mi[10 * N + c] + ah * dsxz_dx;
+            M9 = bh * mi[9 * N + c] + ah * dszz_dz;
             dsxz_dx = dsxz_dx * kh + M10;
             dszz_dz = dszz_dz * kh + M9;
         }
@@ -505,6 +561,9 @@ __global__ void __launch_bounds__(BX* BY) oop_velocity(OopArgs O) {
     }
     if (i == a.isrc && k == a.jsrc && O.srcz) vz = vz + (float)O.srcz[*O.base + O.j - 1] / rho[c];
     if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { vx = 0.f; vz = 0.f; }
+    // ---- stores
+    if (pml && ix) { mo[8 * N + c] = M8; mo[11 * N + c] = M11; }
+    if (pml && iz) { mo[10 * N + c] = M10; mo[9 * N + c] = M9; }
     O.out[c] = vx;
     O.out[N + c] = vz;
 }

@@ -64,9 +64,17 @@ __global__ void __launch_bounds__(BX* BY) em_adj_e(EmAdjArgs A) {
     }
     const bool ring = i == 0 || i == nx - 1 || k == 0 || k == nz - 1;
     if (ring) { lex = 0.f; lez = 0.f; }
-    if (i == a.isrc && k == a.jsrc && A.srcz) *A.gsrc += (double)lez * (double)(float)A.srcz[*A.base + A.j - 1];
+    // every load precedes the first store (a store would hold later loads
+    // behind it: the compiler cannot rule out aliasing between the slices)
+    const bool src = i == a.isrc && k == a.jsrc && A.srcz;
+    const double fsrc = src ? (double)(float)A.srcz[*A.base + A.j - 1] : 0.0;
+    const double lez_src = (double)lez;
     float sz = 0.f, sx = 0.f;
-    if (i >= 1 && k >= 1) {
+    const bool upd = i >= 1 && k >= 1;
+    const bool pml = !in_box(a.box, i, k);
+    float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float m3 = 0.f, m2 = 0.f;
+    if (upd) {
         const float dt = a.dt;
         const float* xp = A.xp;
         const float* xc = A.xc;
@@ -74,33 +82,30 @@ __global__ void __launch_bounds__(BX* BY) em_adj_e(EmAdjArgs A) {
         const float* hy = xc + 2 * N;
         float DHz = (hy[c] - hy[c - nx]) * a.dz;
         float DHx = (hy[c] - hy[c - 1]) * a.dx;
-        const bool pml = !in_box(a.box, i, k);
         if (pml) {
             DHz = DHz * a.cpml[0][c] + xc[6 * N + c];
             DHx = DHx * a.cpml[1][c] + xc[5 * N + c];
         }
         const float aEx = a.c[0][c], bEx = a.c[1][c], dEx = a.c[2][c], eEx = a.c[3][c];
         const float aEz = a.c[4][c], bEz = a.c[5][c], dEz = a.c[6][c], eEz = a.c[7][c];
-        float* g = A.grad;
-        g[c] -= lex * dt * DHz;
-        g[N + c] += lex * dt * DHx;
-        g[2 * N + c] -= lex * dt * exo;
-        g[3 * N + c] -= lex * dt * ezo;
-        g[4 * N + c] -= lez * dt * DHz;
-        g[5 * N + c] += lez * dt * DHx;
-        g[6 * N + c] -= lez * dt * exo;
-        g[7 * N + c] -= lez * dt * ezo;
+        const float* G = A.grad;
+        g[0] = G[c] - lex * dt * DHz;
+        g[1] = G[N + c] + lex * dt * DHx;
+        g[2] = G[2 * N + c] - lex * dt * exo;
+        g[3] = G[3 * N + c] - lex * dt * ezo;
+        g[4] = G[4 * N + c] - lez * dt * DHz;
+        g[5] = G[5 * N + c] + lez * dt * DHx;
+        g[6] = G[6 * N + c] - lez * dt * exo;
+        g[7] = G[7 * N + c] - lez * dt * ezo;
         const float lDHz = -dt * (aEx * lex + aEz * lez);
         const float lDHx = dt * (bEx * lex + bEz * lez);
         float lrz = lDHz, lrx = lDHx;
         if (pml) {
-            float* l3 = lam + 6 * N + c;
-            float* l2 = lam + 5 * N + c;
-            const float M3 = *l3 + lDHz, M2 = *l2 + lDHx;
+            const float M3 = lam[6 * N + c] + lDHz, M2 = lam[5 * N + c] + lDHx;
             lrz = a.cpml[0][c] * lDHz + a.cpml[2][c] * M3;
             lrx = a.cpml[1][c] * lDHx + a.cpml[3][c] * M2;
-            *l3 = a.cpml[4][c] * M3;
-            *l2 = a.cpml[5][c] * M2;
+            m3 = a.cpml[4][c] * M3;
+            m2 = a.cpml[5][c] * M2;
         }
         sz = lrz * a.dz;
         sx = lrx * a.dx;
@@ -108,6 +113,16 @@ __global__ void __launch_bounds__(BX* BY) em_adj_e(EmAdjArgs A) {
         const float nlez = lez - dt * (eEx * lex + eEz * lez);
         lex = nlex;
         lez = nlez;
+    }
+    // ---- stores
+    if (src) *A.gsrc += lez_src * fsrc;
+    if (upd) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) A.grad[q * N + c] = g[q];
+        if (pml) {
+            lam[6 * N + c] = m3;
+            lam[5 * N + c] = m2;
+        }
     }
     lam[c] = lex;
     lam[N + c] = lez;
@@ -136,8 +151,9 @@ __global__ void __launch_bounds__(BX* BY) em_adj_h(EmAdjArgs A) {
             const float M0 = *l0 - lD, M1 = *l1 + lD;
             lrz = a.cpml[0][c] * (-lD) + a.cpml[2][c] * M0;
             lrx = a.cpml[1][c] * lD + a.cpml[3][c] * M1;
-            *l0 = a.cpml[4][c] * M0;
-            *l1 = a.cpml[5][c] * M1;
+            const float n0 = a.cpml[4][c] * M0, n1 = a.cpml[5][c] * M1;  // both loads before the stores
+            *l0 = n0;
+            *l1 = n1;
         }
         q0 = lrz * a.dz;
         q1 = lrx * a.dx;
@@ -180,15 +196,19 @@ __global__ void __launch_bounds__(BX* BY) em_oop_h(EmOopArgs O) {
     const float *Ex = in, *Ez = in + N;
     float dEx_dz = (Ex[c + nx] - Ex[c]) * a.dz;
     float dEz_dx = (Ez[c + 1] - Ez[c]) * a.dx;
+    float M0 = 0.f, M1 = 0.f;
     if (pml) {
-        const float M0 = a.cpml[4][c] * in[3 * N + c] + a.cpml[2][c] * dEx_dz;
-        const float M1 = a.cpml[5][c] * in[4 * N + c] + a.cpml[3][c] * dEz_dx;
-        out[3 * N + c] = M0;
-        out[4 * N + c] = M1;
+        M0 = a.cpml[4][c] * in[3 * N + c] + a.cpml[2][c] * dEx_dz;
+        M1 = a.cpml[5][c] * in[4 * N + c] + a.cpml[3][c] * dEz_dx;
         dEz_dx = dEz_dx * a.cpml[1][c] + M1;
         dEx_dz = dEx_dz * a.cpml[0][c] + M0;
     }
     const float hy = (i == 0 || k == 0) ? 0.f : in[2 * N + c];
+    // stores after every load
+    if (pml) {
+        out[3 * N + c] = M0;
+        out[4 * N + c] = M1;
+    }
     out[2 * N + c] = hy + a.dbHy * (dEz_dx - dEx_dz);
 }
 
@@ -202,15 +222,14 @@ __global__ void __launch_bounds__(BX* BY) em_oop_e(EmOopArgs O) {
     float* out = O.out;
     const bool pml = !in_box(a.box, i, k);
     float ex = in[c], ez = in[N + c];
+    float M2 = 0.f, M3 = 0.f;  // stored after every load
     if (i >= 1 && k >= 1) {
         const float* Hy = out + 2 * N;
         float dHy_dz = (Hy[c] - Hy[c - nx]) * a.dz;
         float dHy_dx = (Hy[c] - Hy[c - 1]) * a.dx;
         if (pml) {
-            const float M2 = a.cpml[5][c] * in[5 * N + c] + a.cpml[3][c] * dHy_dx;
-            const float M3 = a.cpml[4][c] * in[6 * N + c] + a.cpml[2][c] * dHy_dz;
-            out[5 * N + c] = M2;
-            out[6 * N + c] = M3;
+            M2 = a.cpml[5][c] * in[5 * N + c] + a.cpml[3][c] * dHy_dx;
+            M3 = a.cpml[4][c] * in[6 * N + c] + a.cpml[2][c] * dHy_dz;
             dHy_dz = dHy_dz * a.cpml[0][c] + M3;
             dHy_dx = dHy_dx * a.cpml[1][c] + M2;
         }
@@ -220,11 +239,15 @@ __global__ void __launch_bounds__(BX* BY) em_oop_e(EmOopArgs O) {
         ez = ezo + (-(aEz * dHy_dz) + bEz * dHy_dx - dEz * exo - eEz * ezo) * a.dt;
         ex = exo + (-(aEx * dHy_dz) + bEx * dHy_dx - dEx * exo - eEx * ezo) * a.dt;
     } else if (pml) {
-        out[5 * N + c] = in[5 * N + c];
-        out[6 * N + c] = in[6 * N + c];
+        M2 = in[5 * N + c];
+        M3 = in[6 * N + c];
     }
     if (i == a.isrc && k == a.jsrc && O.srcz) ez = ez + (float)O.srcz[*O.base + O.j - 1] * a.dt / a.c[9][c];
     if (i == 0 || i == nx - 1 || k == 0 || k == nz - 1) { ex = 0.f; ez = 0.f; }
+    if (pml) {
+        out[5 * N + c] = M2;
+        out[6 * N + c] = M3;
+    }
     out[c] = ex;
     out[N + c] = ez;
 }

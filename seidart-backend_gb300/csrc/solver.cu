@@ -978,12 +978,14 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         // the pair kernel holds two cells per thread: 4 CTAs per SM (352^3: 0.995 ms
         // against 1.14 ms at 5 and 1.015 ms for the one-cell kernel at 6)
         if (s->s3f.velocity_pair && !getenv("SEIDART_S3_VEL_MINB")) s->s3f.velocity_minb = 4;
-        // read-once stress copies with an L2 evict-first policy, and the
-        // velocity kernel walking down from the planes the stress kernel
-        // finished on: bit-identical, 3.215 -> 3.196 ms at 352^3
-        // (SEIDART_S3_L2HINT=0 / SEIDART_S3_VREV=0 turn them off)
+        // the velocity kernel walks down from the planes the stress kernel
+        // finished on (bit-identical; SEIDART_S3_VREV=0 turns it off).  The
+        // stress kernel's read-once copies take an L2 evict-first policy only
+        // on request (SEIDART_S3_L2HINT=1): it paid while the stress kernel
+        // waited on its C-PML memories (2.200 -> 2.187 ms at 352^3) and costs
+        // since their loads are batched (1.684 -> 1.758 ms)
         t = getenv("SEIDART_S3_L2HINT");
-        s->s3f.l2_hint = (t && *t == '0') ? 0 : 1;
+        s->s3f.l2_hint = (t && *t == '1') ? 1 : 0;
         t = getenv("SEIDART_S3_VREV");
         s->s3f.v_reverse = (t && *t == '0') ? 0 : 1;
         t = getenv("SEIDART_S3_PFP");
