@@ -136,7 +136,7 @@ def make_problem(nt=None):
 # full-size launch is too large for a multi-pass capture), divided by that
 # launch's algorithmic bytes; the bench scales it to its own launch by the
 # algorithmic bytes.
-TRAFFIC_RATIO = {"s3x_stress": 1.121, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.205}
+TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.153}
 
 
 def kernel_bytes(p, box_cells: int) -> dict:
