@@ -329,6 +329,29 @@ def bench_families() -> dict:
     return out
 
 
+def bench_plane_wave_3d(nt: int = 200) -> dict:
+    """The 3D workload (352^3 cells) with a plane-wave source in place of the
+    point force: FP32 on the fast kernels (tiles that meet an injection face
+    take the per-cell path, the faces are injected after each velocity
+    update) and fast FP64, with the FP32 error on the final fields."""
+    import seidart_gpu as sg
+    p = make_problem(nt=nt)
+    p = dataclasses.replace(p, src={}, plane_wave={"kind": "pw", "wavelet": "gaus1", "frequency": 40.0,
+                                                   "x_z_rotation": 20.0, "x_y_rotation": 30.0})
+    r = {"grid": list(p.shape), "cells": p.ncell, "steps": p.time_steps,
+         "source": "plane wave (gaus1, 40 Hz, rotations x-z 20, x-y 30 degrees)"}
+    runs = {}
+    for prec, key in ((sg.FP32, "fp32"), (sg.FP64_FAST, "fp64_fast")):
+        t = _timed_run(p, prec, want_fields=True)
+        runs[key] = t
+        r[key] = {"value": p.ncell * t["steps"] / (t["ms"] / 1e3) / 1e9, "unit": UNIT,
+                  "ms_per_step": t["ms"] / t["steps"], "gpu_launches": t["launches"]}
+    got = np.concatenate([np.asarray(f).ravel() for f in runs["fp32"]["fields"]])
+    ref = np.concatenate([np.asarray(f).ravel() for f in runs["fp64_fast"]["fields"]])
+    r["fp32_vs_fp64_fast_fields_rel_l2"] = float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300))
+    return r
+
+
 def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
     """Ragged batch: all models advance together; rate over the timed steps."""
     import torch
@@ -764,6 +787,7 @@ def main():
     if not args.no_2d and rank == 0:
         legs["configs_2d"] = bench_2d_configs()
         legs["families"] = bench_families()
+        legs["plane_wave_3d"] = bench_plane_wave_3d()
     if not args.no_batch and rank == 0:
         legs["batched"] = bench_batch()
     if not args.no_fwi and rank == 0:

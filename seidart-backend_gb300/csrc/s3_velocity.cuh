@@ -132,6 +132,26 @@ __device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, in
         w[3] = sxx0; w[4] = syy0; w[5] = szz0; w[6] = sxy0; w[7] = syz0; w[8] = sxz0;
         ssq = w[3] * w[3] + w[4] * w[4] + w[5] * w[5] + 2.0f * (w[6] * w[6] + w[7] * w[7] + w[8] * w[8]);
     }
+    // plane-wave face cells: their norms are taken after the injection
+    if (!LEAN && A.pw.on && pw_cell(A.pw, gx, gy, k)) {
+        vsq = 0.f;
+        ssq = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) w[q] = 0.f;
+    }
+}
+
+// true when the TW x TH tile of plane k (x0.., y0..) meets a plane-wave
+// injection face (such tiles take the per-cell path, which leaves face
+// cells out of the norms)
+__device__ __forceinline__ bool pw_tile(const PwDev& pw, int x0, int y0, int k, int tw, int th) {
+    for (int f = 0; f < pw.nface; ++f) {
+        const PwFace& F = pw.face[f];
+        if (k >= F.lo[2] && k <= F.hi[2] && x0 <= F.hi[0] && x0 + tw - 1 >= F.lo[0] && y0 <= F.hi[1] &&
+            y0 + th - 1 >= F.lo[1])
+            return true;
+    }
+    return false;
 }
 
 // true when the whole TW x TH tile of plane k qualifies for the lean path
@@ -146,6 +166,7 @@ __device__ __forceinline__ bool lean_tile(const S3Args<float>& A, int x0, int y0
         const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
         if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + TW && js + 1 >= y0 && js < y0 + TH) return false;
     }
+    if (A.pw.on && pw_tile(A.pw, x0, y0, k, TW, TH)) return false;
     return true;
 }
 

@@ -244,6 +244,7 @@ __device__ __forceinline__ bool lean_tile_p(const S3Args<float>& A, int x0, int 
         return false;
     const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
     if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + TPX && js + 1 >= y0 && js < y0 + TPY) return false;
+    if (A.pw.on && pw_tile(A.pw, x0, y0, k, TPX, TPY)) return false;
     return true;
 }
 
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, St
         if (gy >= ny) return m;
         for (int q = 0; q < 2; ++q) {
             if (x0 + q >= nx) break;
+            if (A.pw.on && pw_cell(A.pw, x0 + q, gy, k)) continue;  // taken after the injection
             const size_t c = (size_t)(x0 + q) + (size_t)nx * ((size_t)gy + (size_t)ny * k);
             double n;
             if (!stress) {

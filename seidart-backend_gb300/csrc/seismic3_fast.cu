@@ -376,8 +376,9 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
     if (A.wave_ctl)
         for (int q = threadIdx.x; q < A.wave_n; q += blockDim.x) A.wave_ctl[q] = 0;
     if (threadIdx.x == 0) {
-        A.norms[it - 1] = v;
-        A.norms[A.nt + it - 1] = w;
+        // plane waves: the face cells' norms were written by the injection
+        A.norms[it - 1] = A.pw.on ? nanmax(A.norms[it - 1], v) : v;
+        A.norms[A.nt + it - 1] = A.pw.on ? nanmax(A.norms[A.nt + it - 1], w) : w;
         *s.step = it + 1;
     }
 }
@@ -387,7 +388,7 @@ __global__ void s3f_epilogue(S3Args<float> A, StepInfo s) {
 void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_t st, const LaunchHook* h,
                           const S3Maps* maps, int stress_kind, int velocity_kind) {
     const dim3 blk(TX, TY), grd((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + ZCH - 1) / ZCH);
-    if (a.wave_ctl && a.staged) {
+    if (a.wave_ctl && a.staged && !a.pw.on) {
         // both half-steps in one launch
         launch_seismic3_wave(a, *(const S3XMaps*)a.staged, s, st);
         if (h) h->fn(h->ctx, 0, "s3w_step");
@@ -415,10 +416,12 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
         launch_seismic3_cell_stress(a, st);
         if (h) h->fn(h->ctx, 0, "s3c_stress");
     }
-    if (velocity_kind == S3K_CELL && a.staged_v) {
+    // plane waves need the kernels that leave face cells out of the norms:
+    // the cell-pair or one-cell velocity kernel
+    if (velocity_kind == S3K_CELL && a.staged_v && !a.pw.on) {
         launch_seismic3_staged_velocity(a, *(const S3XMaps*)a.staged_v, s, st);
         if (h) h->fn(h->ctx, 1, "s3x_velocity");
-    } else if (velocity_kind == S3K_ZMARCH) {
+    } else if (velocity_kind == S3K_ZMARCH && !a.pw.on) {
         s3f_velocity<<<grd, blk, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 1, "s3f_velocity");
     } else if (a.velocity_pair) {
@@ -431,6 +434,10 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
     if (a.stress_src) {
         s3f_stress_source<<<1, 1, 0, st>>>(a, s);
         if (h) h->fn(h->ctx, 2, "s3f_stress_source");
+    }
+    if (a.pw.on) {
+        pw_seismic3<float>(a, s, st);  // face injection and the face cells' norms
+        if (h) h->fn(h->ctx, 5, "pw_faces");
     }
     s3f_epilogue<<<1, 256, 0, st>>>(a, s);
     if (h) h->fn(h->ctx, 3, "s3f_epilogue");

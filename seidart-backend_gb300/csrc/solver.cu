@@ -735,7 +735,6 @@ void launch_one_step(SeidartSolver& s, cudaStream_t st, const LaunchHook* h = nu
     case SEIDART_ELECTROMAG3: f32 ? launch_electromag3_f32(s.e3f, si, st, h) : SD_F64(electromag3, s.e3d); break;
     case SEIDART_SEISMIC3:
         if (!f32) SD_F64(seismic3, s.s3d);
-        else if (s.s3f.pw.on) launch_seismic3_f32(s.s3f, si, st, h);  // plane waves: the one-cell kernels
         else launch_seismic3_fast(s.s3f, si, st, h, s.s3_tma ? &s.s3_maps : nullptr, s.s3_stress_kind,
                                   s.s3_velocity_kind);
         break;

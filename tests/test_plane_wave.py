@@ -119,6 +119,11 @@ def _pw_cases():
     s3 = models.seismic3_layers(n=20, cpml=4, nt=40, nlayers=2, nrec_side=3, rec_z=3, src_z=5)
     s3 = replace(s3, src={}, plane_wave={"kind": "pw", "wavelet": "gaus1", "frequency": 1500.0,
                                          "x_z_rotation": 30.0, "x_y_rotation": 40.0, "y_z_rotation": 15.0})
+    # 104^3 cells: the FP32 fast kernels' lean tiles exist, and the
+    # injection faces cross some of them
+    s3l = models.seismic3_layers(n=88, cpml=8, nt=40, nlayers=3, nrec_side=4, rec_z=3, src_z=10)
+    s3l = replace(s3l, src={}, plane_wave={"kind": "pw", "wavelet": "gaus1", "frequency": 400.0,
+                                           "x_z_rotation": 25.0, "x_y_rotation": 35.0, "y_z_rotation": 10.0})
     e2 = models.electromag2_blocks(n=40, cpml=6, nt=80, src=(20, 8), nrec=6, rec_z=5, nblocks=3)
     e2.model["e13"][:] = 0.5
     e2 = replace(e2, src={}, plane_wave={"kind": "pw", "wavelet": "gaus1", "frequency": 1.0e9,
@@ -126,8 +131,8 @@ def _pw_cases():
     e3 = models.electromag3_blocks(n=20, cpml=4, nt=50, nblocks=2, nrec_side=3)
     e3 = replace(e3, src={}, plane_wave={"kind": "pw", "wavelet": "gaus0", "frequency": 1.5e9,
                                          "x_z_rotation": -30.0, "x_y_rotation": 20.0, "y_z_rotation": 25.0})
-    return {"seismic2": s2, "seismic2_p": s2p, "seismic25": s25, "seismic3": s3, "electromag2": e2,
-            "electromag3": e3}
+    return {"seismic2": s2, "seismic2_p": s2p, "seismic25": s25, "seismic3": s3, "seismic3_lean": s3l,
+            "electromag2": e2, "electromag3": e3}
 
 
 PW = _pw_cases() if _lib.LIB_PATH.exists() else {}
