@@ -344,6 +344,10 @@ long long seidart_batch_launches(const SeidartBatch* b);
 long long seidart_batch_graph_launches(const SeidartBatch* b);
 int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid);
 int seidart_batch_num_variants(void);
+/* How kernel variant `variant` walks the flattened tile list: "strided"
+ * (CTA b of G takes tiles b, b+G, ...) or "chunked" (a contiguous range per
+ * CTA); NULL outside 0 .. seidart_batch_num_variants()-1. */
+const char* seidart_batch_variant_walk(int variant);
 int seidart_batch_destroy(SeidartBatch* b);
 const char* seidart_batch_last_error(void);
 

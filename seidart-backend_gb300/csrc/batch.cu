@@ -236,6 +236,27 @@ __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, in
     return vx * vx + vz * vz;
 }
 
+// phase 3 of a step: per model, the stress source (non-'ac' sources, added
+// after the velocity update as the reference does) and the receiver gather
+__device__ __forceinline__ void model_tail(const BatchArgs& B, int it, int tid, int nthreads) {
+    for (int m = blockIdx.x; m < B.nmodels; m += gridDim.x) {
+        const BModel& a = B.models[m];
+        if (a.stress_src && tid == 0) {
+            const int nx = a.nx;
+            const size_t c = IXM(a.isrc + 1, a.jsrc + 1), c1 = IXM(a.isrc + 2, a.jsrc + 2);
+            const float* rho = a.m[6];
+            if (a.src[2]) a.f[2][c] = a.f[2][c] + (float)a.src[2][it - 1] / rho[c];
+            if (a.src[3]) a.f[4][c1] = a.f[4][c1] + (float)a.src[3][it - 1] / rho[c1];
+            if (a.src[4]) a.f[3][c] = a.f[3][c] + (float)a.src[4][it - 1] / rho[c];
+        }
+        for (int r = tid; r < a.nrec; r += nthreads) {
+            const size_t base = (size_t)(it - 1) * 2 * a.nrec;
+            a.traces[base + r] = a.f[0][a.rec[r]];
+            a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
+        }
+    }
+}
+
 // MINB CTAs per SM bound the registers: 1024 threads per SM leave 64
 // registers per thread (capping them lower, 32 or 40, with 6 or 8 CTAs of
 // 256 threads, measured slower on the 64-model batch: spills)
@@ -266,23 +287,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_persistent(BatchArgs B, int 
         }
         if (!grid_barrier(B)) return;
         // phase 3: per-model stress source and receivers
-        for (int m = blockIdx.x; m < B.nmodels; m += gridDim.x) {
-            const BModel& a = B.models[m];
-            const int tid = threadIdx.x + TX * threadIdx.y;
-            if (a.stress_src && tid == 0) {
-                const int nx = a.nx;
-                const size_t c = IXM(a.isrc + 1, a.jsrc + 1), c1 = IXM(a.isrc + 2, a.jsrc + 2);
-                const float* rho = a.m[6];
-                if (a.src[2]) a.f[2][c] = a.f[2][c] + (float)a.src[2][it - 1] / rho[c];
-                if (a.src[3]) a.f[4][c1] = a.f[4][c1] + (float)a.src[3][it - 1] / rho[c1];
-                if (a.src[4]) a.f[3][c] = a.f[3][c] + (float)a.src[4][it - 1] / rho[c];
-            }
-            for (int r = tid; r < a.nrec; r += TX * TY) {
-                const size_t base = (size_t)(it - 1) * 2 * a.nrec;
-                a.traces[base + r] = a.f[0][a.rec[r]];
-                a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
-            }
-        }
+        model_tail(B, it, threadIdx.x + TX * threadIdx.y, TX * TY);
         if (!grid_barrier(B)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) *B.step = it0 + nsteps;
@@ -392,22 +397,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nst
         wn.flush(B, it, lane);
         if (!grid_barrier(B)) return;
         // phase 3: per-model stress source and receivers
-        for (int m = blockIdx.x; m < B.nmodels; m += gridDim.x) {
-            const BModel& a = B.models[m];
-            if (a.stress_src && tid == 0) {
-                const int nx = a.nx;
-                const size_t c = IXM(a.isrc + 1, a.jsrc + 1), c1 = IXM(a.isrc + 2, a.jsrc + 2);
-                const float* rho = a.m[6];
-                if (a.src[2]) a.f[2][c] = a.f[2][c] + (float)a.src[2][it - 1] / rho[c];
-                if (a.src[3]) a.f[4][c1] = a.f[4][c1] + (float)a.src[3][it - 1] / rho[c1];
-                if (a.src[4]) a.f[3][c] = a.f[3][c] + (float)a.src[4][it - 1] / rho[c];
-            }
-            for (int r = tid; r < a.nrec; r += TX * TY) {
-                const size_t base = (size_t)(it - 1) * 2 * a.nrec;
-                a.traces[base + r] = a.f[0][a.rec[r]];
-                a.traces[base + a.nrec + r] = a.f[1][a.rec[r]];
-            }
-        }
+        model_tail(B, it, tid, TX * TY);
         for (int t = t0; t < t0 + PD && t < t1; ++t) tile_prefetch<TX, TY, 1>(B, t, tid);
         if (!grid_barrier(B)) return;
     }
@@ -786,6 +776,9 @@ int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int*
     return SEIDART_OK;
 }
 int seidart_batch_num_variants(void) { return kNumVariants; }
+const char* seidart_batch_variant_walk(int variant) {
+    return variant >= 0 && variant < kNumVariants ? kVariants[variant].walk : nullptr;
+}
 int seidart_batch_set_stream_sync(SeidartBatch* b) {
     return b ? (cudaStreamSynchronize(b->stream) == cudaSuccess ? SEIDART_OK : SEIDART_ERR_CUDA) : SEIDART_ERR_ARG;
 }

@@ -39,6 +39,7 @@ def _declare():
         "seidart_batch_graph_launches": (ll, [vp]),
         "seidart_batch_config": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "seidart_batch_num_variants": (i, []),
+        "seidart_batch_variant_walk": (C.c_char_p, [i]),
         "seidart_batch_destroy": (i, [vp]),
         "seidart_batch_last_error": (C.c_char_p, []),
     }
@@ -85,10 +86,12 @@ class Batch:
                                       C.addressof(mptrs), C.addressof(sptrs), C.addressof(nrec), C.addressof(rptrs)))
         self.handle = h
         self.tuning = None
+        self.variant = 1  # the library's default until autotuned or set
         if autotune:
             v, b = C.c_int(), C.c_int()
             _check(L.seidart_batch_autotune(self.handle, min(trial_steps, problems[0].time_steps),
                                             C.byref(v), C.byref(b)))
+            self.variant = v.value
             self.tuning = self._tuning_table()
         for m, p in enumerate(problems):
             self._set_fields(m, p.field_list())
@@ -101,20 +104,24 @@ class Batch:
             bps = (C.c_int * 2)()
             ms = (C.c_double * 2)()
             _check(L.seidart_batch_tuning(self.handle, v, C.byref(tx), C.byref(ty), C.addressof(bps), C.addressof(ms)))
+            walk = L.seidart_batch_variant_walk(v).decode()
             for q in range(2):
                 if ms[q] >= 0:
-                    out.append({"variant": v, "tile": [tx.value, ty.value], "ctas_per_sm": bps[q], "ms": ms[q]})
+                    out.append({"variant": v, "walk": walk, "tile": [tx.value, ty.value], "ctas_per_sm": bps[q],
+                                "ms": ms[q]})
         return out
 
     def config(self) -> dict:
         tx, ty, bps, grid = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         _check(lib().seidart_batch_config(self.handle, C.byref(tx), C.byref(ty), C.byref(bps), C.byref(grid)))
-        return {"tile": [tx.value, ty.value], "ctas_per_sm": bps.value, "grid": grid.value}
+        return {"variant": self.variant, "walk": lib().seidart_batch_variant_walk(self.variant).decode(),
+                "tile": [tx.value, ty.value], "ctas_per_sm": bps.value, "grid": grid.value}
 
     def set_config(self, variant: int, ctas_per_sm: int) -> None:
         """Use kernel variant ``variant`` (0 .. num_variants-1) with the given
         CTAs per SM instead of the autotuned choice."""
         _check(lib().seidart_batch_set_config(self.handle, int(variant), int(ctas_per_sm)))
+        self.variant = int(variant)
 
     @staticmethod
     def num_variants() -> int:
