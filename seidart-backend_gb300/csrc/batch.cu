@@ -34,6 +34,8 @@ struct BModel {
     const float* m[16];  // S2_* slots; gamma -> 1/(1+gamma dt), kappa -> 1/kappa
     float* f[5];
     float* mem[12];
+    float* f2[5];     // second state set of the fused step (double buffering)
+    float* mem2[12];
     const double* src[5];
     const int* rec;
     float* traces;   // [nt][2][nrec]
@@ -51,6 +53,8 @@ struct BatchArgs {
     int* status;            // 0 ok, 1 barrier timeout
     long long spin_limit;   // barrier spin budget (iterations)
     int force_timeout;      // test hook: expect one more arrival than exists
+    const int* tile_rec_off;  // fused step: receivers of tile t are tile_rec[off[t] .. off[t+1])
+    const int* tile_rec;      //   (model-local receiver numbers)
 };
 
 // Grid-wide barrier for a cooperative (co-resident) grid with a bounded wait.
@@ -404,10 +408,303 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nst
     if (blockIdx.x == 0 && tid == 0) *B.step = it0 + nsteps;
 }
 
+// ------------------------------------------------------------ fused step
+// One pass over the tiles per step.  A CTA stages the velocities of its
+// TX x TY tile plus a 4-cell halo in shared memory, recomputes the new
+// stresses on the tile plus a 2-cell halo (the halo cells are its
+// neighbours' work too: the same arithmetic gives the same values), then
+// updates the tile's velocities from those stresses, so the new stresses
+// never make a round trip through HBM between the half-steps and a step has
+// one grid barrier instead of three.  A halo reads old values that the
+// neighbouring tiles overwrite in the same pass, so the state is double
+// buffered: step s of a launch reads set s & 1 (0 = the solver's arrays, 1 =
+// the batch's second set) and writes the other; fields are written for every
+// cell (copied where no loop updates them), memories where the loops update
+// them, which are the only cells where they are read.  A launch of an odd
+// number of steps ends by copying the second set back, so every launch
+// starts and ends with the state in the solver's arrays.  The stress source
+// is added to the stored stresses of the source cells after the velocity
+// update has used them, and the receivers of a tile are read back after its
+// velocities are stored, as the three-phase walk does.
+template <int TX, int TY>
+struct FusedTile {
+    static constexpr int VW = TX + 8, VH = TY + 8;  // velocities: x0-4 .. x0+TX+3, z0-4 .. z0+TY+3
+    static constexpr int SW = TX + 4, SH = TY + 4;  // new stresses: x0-2 .. x0+TX+1, z0-2 .. z0+TY+1
+};
+
+// new stresses of cell (i, j) (Fortran indices) from the staged velocities
+// VX, VZ (row pitch W) -- cell_stress's arithmetic; an owner cell also
+// stores its stresses (plus the stress source) and updated memories
+__device__ __forceinline__ void fused_stress_cell(const BModel& a, int i, int j, const float* VX, const float* VZ,
+                                                  int W, float* const* fr, float* const* fw, float* const* mr,
+                                                  float* const* mw, bool own, int it, float (&o)[3]) {
+    const int nx = a.nx, nz = a.nz;
+    const bool normal = (j >= 3 && j <= nz - 1 && i >= 2 && i <= nx - 2);
+    const bool shear = (j >= 2 && j <= nz - 2 && i >= 3 && i <= nx - 1);
+    const size_t c = IXM(i, j);
+    float sxx = fr[2][c], szz = fr[3][c], sxz = fr[4][c];
+    if (normal || shear) {
+        const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
+        const float x0 = VX[0], xa = VX[-2], xb = VX[-1], xc = VX[1], xd = VX[2];
+        const float xe = VX[-2 * W], xf = VX[-W], xg = VX[W], xh = VX[2 * W];
+        const float z0 = VZ[0], za = VZ[-2], zb = VZ[-1], zc = VZ[1], zd = VZ[2];
+        const float ze = VZ[-2 * W], zf = VZ[-W], zg = VZ[W], zh = VZ[2 * W];
+        const float c11 = __ldg(a.m[0] + c), c13 = __ldg(a.m[1] + c), c15 = __ldg(a.m[2] + c);
+        const float c33 = __ldg(a.m[3] + c), c35 = __ldg(a.m[4] + c), c55 = __ldg(a.m[5] + c);
+        const float gx = __ldg(a.m[7] + c), gz = __ldg(a.m[8] + c), gxz = __ldg(a.m[9] + c);
+        float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (pml) {
+            kap = __ldg(a.m[10] + c); kaph = __ldg(a.m[11] + c); aa = __ldg(a.m[12] + c);
+            ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) m[q] = mr[q][c];
+        }
+        const float dt = a.dt, hx = a.hx, hz = a.hz;
+#define D4(p1, p0, p2, m1, h) ((27.0f * ((p1) - (p0)) - ((p2) - (m1))) * (h))
+        if (normal) {
+            float dvx_dx = D4(xc, x0, xd, xb, hx);
+            float dvz_dz = D4(z0, zf, zg, ze, hz);
+            float dvz_dx = D4(zc, z0, zd, zb, hx);
+            float dvx_dz = D4(x0, xf, xg, xe, hz);
+            if (pml) {
+                const float M0 = bh * m[0] + ah * dvx_dx, M1 = bh * m[1] + ah * dvx_dz;
+                const float M3 = b * m[3] + aa * dvz_dz, M2 = b * m[2] + aa * dvz_dx;
+                if (own) { mw[0][c] = M0; mw[1][c] = M1; mw[2][c] = M2; mw[3][c] = M3; }
+                dvx_dx = dvx_dx * kaph + M0;
+                dvx_dz = dvx_dz * kaph + M1;
+                dvz_dz = dvz_dz * kap + M3;
+                dvz_dx = dvz_dx * kap + M2;
+            }
+            sxx = (sxx + (c11 * dvx_dx + c13 * dvz_dz + c15 * (dvz_dx + dvx_dz)) * dt) * gx;
+            szz = (szz + (c13 * dvx_dx + c33 * dvz_dz + c35 * (dvz_dx + dvx_dz)) * dt) * gz;
+        }
+        if (shear) {
+            float dvx_dx = D4(x0, xb, xc, xa, hx);
+            float dvz_dz = D4(zg, z0, zh, zf, hz);
+            float dvz_dx = D4(z0, zb, zc, za, hx);
+            float dvx_dz = D4(xg, x0, xh, xf, hz);
+            if (pml) {
+                const float M4 = bh * m[4] + ah * dvx_dx, M5 = bh * m[5] + ah * dvx_dz;
+                const float M7 = bh * m[7] + ah * dvz_dz, M6 = bh * m[6] + ah * dvz_dx;
+                if (own) { mw[4][c] = M4; mw[5][c] = M5; mw[6][c] = M6; mw[7][c] = M7; }
+                dvx_dx = dvx_dx * kaph + M4;
+                dvx_dz = dvx_dz * kaph + M5;
+                dvz_dz = dvz_dz * kaph + M7;
+                dvz_dx = dvz_dx * kaph + M6;
+            }
+            sxz = (sxz + (c15 * dvx_dx + c35 * dvz_dz + c55 * (dvz_dx + dvx_dz)) * dt) * gxz;
+        }
+#undef D4
+    }
+    o[0] = sxx;
+    o[1] = szz;
+    o[2] = sxz;
+    if (own) {
+        if (a.stress_src && i - 1 == a.isrc && j - 1 == a.jsrc) {
+            const float r = a.m[6][c];
+            if (a.src[2]) sxx = sxx + (float)a.src[2][it - 1] / r;
+            if (a.src[4]) szz = szz + (float)a.src[4][it - 1] / r;
+        }
+        if (a.stress_src && a.src[3] && i - 2 == a.isrc && j - 2 == a.jsrc)
+            sxz = sxz + (float)a.src[3][it - 1] / a.m[6][c];
+        fw[2][c] = sxx;
+        fw[3][c] = szz;
+        fw[4][c] = sxz;
+    }
+}
+
+// velocity update of owner cell (i, j) from the staged new stresses (row
+// pitch SW) and old velocities (row pitch VW) -- cell_velocity's arithmetic
+__device__ __forceinline__ float fused_velocity_cell(const BModel& a, int i, int j, int it, const float* SXX,
+                                                     const float* SZZ, const float* SXZ, int SW, float vx, float vz,
+                                                     float* const* fw, float* const* mr, float* const* mw,
+                                                     float (&vo)[2]) {
+    const int nx = a.nx, nz = a.nz;
+    const size_t c = IXM(i, j);
+    const bool pml = !(i - 1 >= a.box.i0 && i - 1 < a.box.i1 && j - 1 >= a.box.k0 && j - 1 < a.box.k1);
+    const bool ux = (j >= 3 && j <= nz - 1 && i >= 3 && i <= nx - 1);
+    const bool uz = (j >= 2 && j <= nz - 2 && i >= 2 && i <= nx - 2);
+    const long xm1 = (long)max(i - 1, 1) - i, xp1 = (long)min(i + 1, nx) - i;
+    const long zm1 = ((long)max(j - 1, 1) - j) * nx, zp1 = ((long)min(j + 1, nz) - j) * nx;
+    const float s0 = SXX[0], sm1 = SXX[-1], sm2 = SXX[-2];
+    const float q0 = SXZ[0], qm1 = SXZ[-SW], qm2 = SXZ[-2 * SW], qp1 = SXZ[1], qp2 = SXZ[2];
+    const float w0 = SZZ[0], wp1 = SZZ[SW], wp2 = SZZ[2 * SW];
+    const float* R = a.m[6] + c;
+    const float r0 = __ldg(R), rxm = __ldg(R + xm1), rzm = __ldg(R + zm1), rxp = __ldg(R + xp1), rzp = __ldg(R + zp1);
+    float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m8 = 0.f, m9 = 0.f, m10 = 0.f, m11 = 0.f;
+    if (pml) {
+        kap = __ldg(a.m[10] + c); kaph = __ldg(a.m[11] + c); aa = __ldg(a.m[12] + c);
+        ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
+        m8 = mr[8][c]; m9 = mr[9][c]; m10 = mr[10][c]; m11 = mr[11][c];
+    }
+    const float dt = a.dt, hx = a.hx, hz = a.hz;
+    if (ux) {
+        const float bxx = inv_mean_f(r0, rxm, a.density_code);
+        const float bzx = inv_mean_f(r0, rzm, a.density_code);
+        float d1 = (27.0f * (s0 - sm1) + sm2) * hx;
+        float d2 = (27.0f * (q0 - qm1) + qm2) * hz;
+        if (pml) {
+            const float M8 = b * m8 + aa * d1, M11 = b * m11 + aa * d2;
+            mw[8][c] = M8; mw[11][c] = M11;
+            d1 = d1 * kap + M8;
+            d2 = d2 * kap + M11;
+        }
+        vx = vx + dt * (d1 * bxx + d2 * bzx);
+    }
+    if (uz) {
+        const float bxz = inv_mean_f(r0, rxp, a.density_code);
+        const float bzz = inv_mean_f(r0, rzp, a.density_code);
+        float d1 = (27.0f * (qp1 - q0) - qp2) * hx;
+        float d2 = (27.0f * (wp1 - w0) - wp2) * hz;
+        if (pml) {
+            const float M10 = bh * m10 + ah * d1, M9 = bh * m9 + ah * d2;
+            mw[10][c] = M10; mw[9][c] = M9;
+            d1 = d1 * kaph + M10;
+            d2 = d2 * kaph + M9;
+        }
+        vz = vz + dt * (d1 * bxz + d2 * bzz);
+    }
+    if (i - 1 == a.isrc && j - 1 == a.jsrc) {
+        if (a.src[0]) vx = vx + (float)a.src[0][it - 1] / r0;
+        if (a.src[1]) vz = vz + (float)a.src[1][it - 1] / r0;
+    }
+    if (i == 1 || i == nx || j == 1 || j == nz) { vx = 0.f; vz = 0.f; }
+    fw[0][c] = vx;
+    fw[1][c] = vz;
+    vo[0] = vx;
+    vo[1] = vz;
+    return vx * vx + vz * vz;
+}
+
+// L2 prefetch of the rows of tile t in read set rd: fields, the ten model
+// arrays a step reads, and outside the inert box the memories and the C-PML
+// coefficients
+template <int TX, int TY, int NT>
+__device__ __forceinline__ void fused_prefetch(const BatchArgs& B, int t, int rd, int tid) {
+    const BModel& M = B.models[B.tile_model[t]];
+    const int lt = t - M.tile0, x0 = (lt % M.tiles_x) * TX, z0 = (lt / M.tiles_x) * TY;
+    const int x1 = min(x0 + TX, M.nx) - 1, z1 = min(z0 + TY, M.nz);
+    const bool shell = !(x0 >= M.box.i0 && x1 < M.box.i1 && z0 >= M.box.k0 && z1 <= M.box.k1);
+    const int narr = shell ? 33 : 15;
+    for (int q = tid; q < narr * TY; q += NT) {
+        const int a = q / TY, y = z0 + q % TY;
+        if (y >= z1) continue;
+        const float* base = a < 5 ? (rd ? M.f2[a] : M.f[a])                     // fields
+                          : a < 15 ? M.m[a - 5]                                   // c11 .. gxz (rho among them)
+                          : a < 27 ? (rd ? M.mem2[a - 15] : M.mem[a - 15])        // memories
+                          : M.m[10 + a - 27];                                     // C-PML coefficients
+        const float* row = base + (size_t)y * M.nx;
+#pragma unroll
+        for (int xo = 0; xo < TX; xo += 32)
+            if (x0 + xo <= x1) pf_l2(row + x0 + xo);
+        pf_l2(row + x1);
+    }
+}
+
+template <int TX, int TY, int NT, int MINB = 1024 / NT>
+__global__ void __launch_bounds__(NT, MINB) s2b_fused(BatchArgs B, int nsteps) {
+    using T = FusedTile<TX, TY>;
+    constexpr int VW = T::VW, VH = T::VH, SW = T::SW, SH = T::SH;
+    __shared__ float sv[2][VH * VW];
+    __shared__ float ss[3][SH * SW];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int t0 = (int)((long long)B.ntiles * blockIdx.x / gridDim.x);
+    const int t1 = (int)((long long)B.ntiles * (blockIdx.x + 1) / gridDim.x);
+    const int it0 = *B.step;
+    for (int s = 0; s < nsteps; ++s) {
+        const int it = it0 + s, rd = s & 1;
+        WarpNorm wn;
+        for (int t = t0; t < t1; ++t) {
+            if (t + 1 < t1) fused_prefetch<TX, TY, NT>(B, t + 1, rd, tid);
+            const int mi = B.tile_model[t];
+            const BModel& a = B.models[mi];
+            if (mi != wn.model) {
+                wn.flush(B, it, lane);
+                wn.model = mi;
+            }
+            const int nx = a.nx, nz = a.nz, lt = t - a.tile0;
+            const int x0 = (lt % a.tiles_x) * TX, z0 = (lt / a.tiles_x) * TY;  // 0-based tile origin
+            float* const* fr = rd ? a.f2 : a.f;
+            float* const* fw = rd ? a.f : a.f2;
+            float* const* mr = rd ? a.mem2 : a.mem;
+            float* const* mw = rd ? a.mem : a.mem2;
+            // velocities of the tile and a 4-cell halo (zero outside the grid);
+            // the loop is unrolled so that every load is in flight at once
+#pragma unroll
+            for (int q0 = 0; q0 < VH * VW; q0 += NT) {
+                const int q = q0 + tid;
+                if (q >= VH * VW) break;
+                const int x = x0 - 4 + q % VW, z = z0 - 4 + q / VW;
+                const bool in = x >= 0 && x < nx && z >= 0 && z < nz;
+                const size_t c = (size_t)(in ? x : 0) + (size_t)nx * (in ? z : 0);
+                const float u = fr[0][c], w = fr[1][c];
+                sv[0][q] = in ? u : 0.f;
+                sv[1][q] = in ? w : 0.f;
+            }
+            __syncthreads();
+            // new stresses of the tile and a 2-cell halo
+            for (int q = tid; q < SH * SW; q += NT) {
+                const int lx = q % SW, lz = q / SW, x = x0 - 2 + lx, z = z0 - 2 + lz;
+                float o[3] = {0.f, 0.f, 0.f};
+                if (x >= 0 && x < nx && z >= 0 && z < nz) {
+                    const bool own = lx >= 2 && lx < TX + 2 && lz >= 2 && lz < TY + 2;
+                    const int v = (lz + 2) * VW + lx + 2;
+                    fused_stress_cell(a, x + 1, z + 1, &sv[0][v], &sv[1][v], VW, fr, fw, mr, mw, own, it, o);
+                }
+                ss[0][q] = o[0];
+                ss[1][q] = o[1];
+                ss[2][q] = o[2];
+            }
+            __syncthreads();
+            // velocities of the tile (every thread takes part in the warp norms)
+            for (int q0 = 0; q0 < TX * TY; q0 += NT) {
+                const int q = q0 + tid;
+                const int lx = q % TX, lz = q / TX, x = x0 + lx, z = z0 + lz;
+                float sq = 0.f, vo[2] = {0.f, 0.f};
+                if (q < TX * TY && x < nx && z < nz) {
+                    const int sc = (lz + 2) * SW + lx + 2, vc = (lz + 4) * VW + lx + 4;
+                    sq = fused_velocity_cell(a, x + 1, z + 1, it, &ss[0][sc], &ss[1][sc], &ss[2][sc], SW, sv[0][vc],
+                                             sv[1][vc], fw, mr, mw, vo);
+                }
+                wn.add(sq, vo);
+            }
+            __syncthreads();
+            // receivers of the tile, from the velocities just stored
+            const size_t base = (size_t)(it - 1) * 2 * a.nrec;
+            for (int q = B.tile_rec_off[t] + tid; q < B.tile_rec_off[t + 1]; q += NT) {
+                const int r = B.tile_rec[q];
+                a.traces[base + r] = fw[0][a.rec[r]];
+                a.traces[base + a.nrec + r] = fw[1][a.rec[r]];
+            }
+        }
+        wn.flush(B, it, lane);
+        if (!grid_barrier(B)) return;
+    }
+    if (nsteps & 1) {
+        // the last step wrote the second set: copy it back tile by tile
+        for (int t = t0; t < t1; ++t) {
+            const BModel& a = B.models[B.tile_model[t]];
+            const int lt = t - a.tile0, x0 = (lt % a.tiles_x) * TX, z0 = (lt / a.tiles_x) * TY;
+            for (int q = tid; q < TX * TY; q += NT) {
+                const int x = x0 + q % TX, z = z0 + q / TX;
+                if (x >= a.nx || z >= a.nz) continue;
+                const size_t c = (size_t)x + (size_t)a.nx * z;
+#pragma unroll
+                for (int f = 0; f < 5; ++f) a.f[f][c] = a.f2[f][c];
+#pragma unroll
+                for (int f = 0; f < 12; ++f) a.mem[f][c] = a.mem2[f][c];
+            }
+        }
+    }
+    if (blockIdx.x == 0 && tid == 0) *B.step = it0 + nsteps;
+}
+
 struct Variant {
     int tx, ty;
     const void* fn;
-    const char* walk;  // "strided": tile b, b+G, ...; "chunked": a contiguous range per CTA
+    const char* walk;  // "strided": tile b, b+G, ...; "chunked": a contiguous range per CTA;
+                       // "fused": chunked, both half-steps in one pass (one barrier per step)
+    int threads;       // CTA size of a 1D block (fused step); 0: a tx x ty block, one thread per cell
 };
 const Variant kVariants[] = {
     {32, 4, (const void*)s2b_persistent<32, 4>, "strided"},
@@ -422,7 +719,13 @@ const Variant kVariants[] = {
     {32, 16, (const void*)s2b_chunked<32, 16, 1>, "chunked"},
     {32, 16, (const void*)s2b_chunked<32, 16, 2>, "chunked"},
     {64, 8, (const void*)s2b_chunked<64, 8, 1>, "chunked"},
+    // the fused step in its two fastest shapes (measured on the 64-model
+    // batch: 34 and 38 ms per 24 steps against 23.6 for the 64 x 8 chunked
+    // walk; 32 x 8, 32 x 16, 28 x 28 and 28 x 12 tiles were slower still)
+    {64, 8, (const void*)s2b_fused<64, 8, 256>, "fused", 256},
+    {64, 16, (const void*)s2b_fused<64, 16, 512>, "fused", 512},
 };
+__host__ __device__ constexpr int block_threads(const Variant& V) { return V.threads ? V.threads : V.tx * V.ty; }
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 }  // namespace
@@ -437,6 +740,9 @@ struct SeidartBatch {
     std::vector<SeidartSolver*> solvers;  // each model's arena and state
     BModel* dev_models[kNumVariants] = {nullptr};  // descriptors per tile-shape variant
     int* dev_tile_model[kNumVariants] = {nullptr};
+    int* dev_tile_rec_off[kNumVariants] = {nullptr};  // fused variants: receivers per tile
+    int* dev_tile_rec[kNumVariants] = {nullptr};
+    std::vector<float*> second;  // per model: the fused step's second state set, 17 arrays
     int ntiles[kNumVariants] = {0};
     int* ctl = nullptr;  // step, barrier count, barrier generation, status
     cudaStream_t stream = nullptr;
@@ -465,7 +771,7 @@ int berr(int code, const std::string& m) {
 int max_bps(int var) {
     int n = 0;
     const Variant& V = kVariants[var];
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, V.fn, V.tx * V.ty, 0) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, V.fn, block_threads(V), 0) != cudaSuccess) return 0;
     return n;
 }
 
@@ -481,9 +787,11 @@ int launch_chunk(SeidartBatch* b, int var, int bps, int nsteps, int force_timeou
     A.status = b->ctl + 3;
     A.spin_limit = b->spin_limit;
     A.force_timeout = force_timeout;
+    A.tile_rec_off = b->dev_tile_rec_off[var];
+    A.tile_rec = b->dev_tile_rec[var];
     const Variant& V = kVariants[var];
     if (bps < 1 || bps > max_bps(var)) return berr(SEIDART_ERR_ARG, "CTAs per SM outside the occupancy limit");
-    dim3 blk(V.tx, V.ty), grd(b->nsm * bps);
+    dim3 blk = V.threads ? dim3(V.threads) : dim3(V.tx, V.ty), grd(b->nsm * bps);
     void* args[] = {&A, &nsteps};
     const cudaError_t e = cudaLaunchCooperativeKernel(V.fn, grd, blk, args, 0, b->stream);
     if (e != cudaSuccess) return berr(SEIDART_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
@@ -543,9 +851,12 @@ int seidart_batch_destroy(SeidartBatch* b) {
     if (!b) return SEIDART_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto* s : b->solvers) seidart_solver_destroy(s);
+    for (float* p : b->second) cudaFree(p);
     for (int v = 0; v < kNumVariants; ++v) {
         if (b->dev_models[v]) cudaFree(b->dev_models[v]);
         if (b->dev_tile_model[v]) cudaFree(b->dev_tile_model[v]);
+        if (b->dev_tile_rec_off[v]) cudaFree(b->dev_tile_rec_off[v]);
+        if (b->dev_tile_rec[v]) cudaFree(b->dev_tile_rec[v]);
     }
     for (int q = 0; q < 2; ++q)
         if (b->gexec[q]) cudaGraphExecDestroy(b->gexec[q]);
@@ -607,6 +918,20 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
     }
     const int ctl0[4] = {1, 0, 0, 0};
     cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    // the fused step's second state set: 5 fields and 12 memories per model,
+    // zeroed once (cells no loop updates are never written in either set)
+    for (int m = 0; m < nmodels; ++m) {
+        const size_t n = (size_t)hm[m].nx * hm[m].nz;
+        float* p = nullptr;
+        if (cudaMalloc((void**)&p, sizeof(float) * 17 * n) != cudaSuccess) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_NOMEM, "second state set allocation failed");
+        }
+        b->second.push_back(p);
+        cudaMemset(p, 0, sizeof(float) * 17 * n);
+        for (int q = 0; q < 5; ++q) hm[m].f2[q] = p + (size_t)q * n;
+        for (int q = 0; q < 12; ++q) hm[m].mem2[q] = p + (size_t)(5 + q) * n;
+    }
     for (int v = 0; v < kNumVariants; ++v) {
         std::vector<int> tm;
         std::vector<BModel> mv = hm;
@@ -625,6 +950,31 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
         }
         cudaMemcpy(b->dev_tile_model[v], tm.data(), sizeof(int) * tm.size(), cudaMemcpyHostToDevice);
         cudaMemcpy(b->dev_models[v], mv.data(), sizeof(BModel) * nmodels, cudaMemcpyHostToDevice);
+        if (kVariants[v].threads) {
+            // receivers listed per tile (counting sort by the tile holding the cell)
+            // (the solvers have checked every cell index against their grids)
+            const int nt = (int)tm.size();
+            std::vector<int> off(nt + 1, 0), tile_of;
+            for (int m = 0; m < nmodels; ++m)
+                for (int r = 0; r < (nrec && rec_cells ? nrec[m] : 0); ++r) {
+                    const int c = rec_cells[m][r], x = c % mv[m].nx, z = c / mv[m].nx;
+                    const int t = mv[m].tile0 + x / kVariants[v].tx + mv[m].tiles_x * (z / kVariants[v].ty);
+                    tile_of.push_back(t);
+                    ++off[t + 1];
+                }
+            for (int t = 0; t < nt; ++t) off[t + 1] += off[t];
+            std::vector<int> list(std::max<size_t>(tile_of.size(), 1)), fill(off.begin(), off.end() - 1);
+            size_t k = 0;
+            for (int m = 0; m < nmodels; ++m)
+                for (int r = 0; r < (nrec && rec_cells ? nrec[m] : 0); ++r) list[fill[tile_of[k++]]++] = r;
+            if (cudaMalloc((void**)&b->dev_tile_rec_off[v], sizeof(int) * off.size()) != cudaSuccess ||
+                cudaMalloc((void**)&b->dev_tile_rec[v], sizeof(int) * list.size()) != cudaSuccess) {
+                seidart_batch_destroy(b);
+                return berr(SEIDART_ERR_NOMEM, "receiver table allocation failed");
+            }
+            cudaMemcpy(b->dev_tile_rec_off[v], off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(b->dev_tile_rec[v], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice);
+        }
     }
     b->variant = 1;
     b->bps = std::max(1, max_bps(1));

@@ -42,7 +42,7 @@ def test_batch_matches_single_model_runs(oracle):
             assert rel_l2(nrm, o["norms"]) <= 1e-4
 
 
-@pytest.mark.parametrize("variant", range(12))
+@pytest.mark.parametrize("variant", range(14))
 def test_every_kernel_variant_matches_single_runs(variant):
     if variant >= Batch.num_variants():
         pytest.skip("variant not built")
@@ -58,6 +58,11 @@ def test_every_kernel_variant_matches_single_runs(variant):
             tr, nrm = b.traces(m)
             assert rel_l2(tr, single["traces"]) <= 1e-6, (variant, m)
             assert rel_l2(nrm, single["norms"]) <= 1e-6, (variant, m)
+            # final state in the solver's arrays (the fused walk double buffers
+            # it and copies an odd-length launch's result back)
+            f = b.fields(m)
+            for q in range(5):
+                assert rel_l2(f[q], single["fields"][q]) <= 1e-6, (variant, m, q)
 
 
 def test_bounded_barrier_timeout_reports_status():
