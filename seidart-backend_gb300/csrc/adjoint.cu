@@ -40,6 +40,7 @@
 extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
 extern "C" int seidart_solver_internal_e2f(SeidartSolver* s, E2Args<float>* out, const int** rec);
 extern "C" int seidart_solver_internal_reset(SeidartSolver* s);
+extern "C" int seidart_solver_internal_share_model(SeidartSolver* dst, const SeidartSolver* src);
 extern "C" int seidart_solver_internal_advance(SeidartSolver* s, int nsteps);
 extern "C" int seidart_solver_internal_set_step(SeidartSolver* s, int steps_done);
 extern "C" int seidart_solver_internal_set_source(SeidartSolver* s, int isrc, int jsrc, const double* dev_srcx,
@@ -1070,6 +1071,9 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
         s0.zind = shot_zind[l];
         int rc = seidart_solver_create(&L.s, family, SEIDART_FP32, dom, &s0, density_code, model, srcs, nrec,
                                        rec_cells);
+        // every shot runs on one model: the lanes read lane 0's copy, so the
+        // concurrent shots keep one model in L2 instead of one each
+        if (rc == SEIDART_OK && l > 0) rc = seidart_solver_internal_share_model(L.s, f->lanes[0].s);
         if (rc != SEIDART_OK) { std::string e = seidart_last_error(); seidart_fwi_destroy(f); return ferr(rc, e); }
         lane_args(f, L, &L.rec);
         L.st = seidart_solver_internal_stream(L.s);

@@ -1287,6 +1287,34 @@ int seidart_solver_internal_e2f(SeidartSolver* s, E2Args<float>* out, const int*
     return SEIDART_OK;
 }
 
+// Point dst's read-only model arrays (coefficients, density, attenuation,
+// C-PML profiles) at src's, so solvers of one model (the concurrent shots of
+// a misfit gradient) read one copy and keep it in L2 together.  Both must be
+// FP32 solvers of the same family, grid and model; dst's cached graphs are
+// dropped (they hold the launch arguments by value).  dst's own copy stays
+// allocated but unused.
+int seidart_solver_internal_share_model(SeidartSolver* dst, const SeidartSolver* src) {
+    if (!dst || !src || dst->family != src->family || dst->precision != SEIDART_FP32 ||
+        src->precision != SEIDART_FP32 || dst->ncell != src->ncell)
+        return set_err(SEIDART_ERR_ARG, "model sharing needs two FP32 solvers of one family and grid");
+    if (dst->family == SEIDART_SEISMIC2) {
+        for (int q = 0; q < 16; ++q) dst->s2f.m[q] = src->s2f.m[q];
+    } else if (dst->family == SEIDART_ELECTROMAG2) {
+        for (int q = 0; q < 10; ++q) dst->e2f.c[q] = src->e2f.c[q];
+        for (int q = 0; q < 6; ++q) dst->e2f.cpml[q] = src->e2f.cpml[q];
+    } else {
+        return set_err(SEIDART_ERR_UNSUPPORTED, "model sharing covers seismic2 and electromag2");
+    }
+    CUDA_TRY(cudaStreamSynchronize(dst->stream));
+    for (int q = 0; q < 2; ++q)
+        if (dst->graph_exec[q]) {
+            cudaGraphExecDestroy(dst->graph_exec[q]);
+            dst->graph_exec[q] = nullptr;
+            dst->graph_len[q] = 0;
+        }
+    return SEIDART_OK;
+}
+
 // zero fields, memories, traces and norms; back to step 1
 int seidart_solver_internal_reset(SeidartSolver* s) {
     if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
