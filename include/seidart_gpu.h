@@ -475,7 +475,8 @@ int seidart_attenuation_arrays_dev(const int* im, int nx, int nz, const double* 
  * (cudaGetSymbolAddress with that device current, which may load the
  * module); make that first call before any stream capture begins.  Every
  * call waits for `stream` to finish before it returns, because it copies
- * the results into host memory.  The looked-up address is kept for the life
+ * the results into host memory, so it must not be issued on a stream that
+ * is being captured into a CUDA graph.  The looked-up address is kept for the life
  * of the process, so cudaDeviceReset between calls is not supported.  Calls
  * that overlap on one device share the scratch and race: serialise them. */
 #define SEIDART_NOALLOC_MAX_TRACES 8192
