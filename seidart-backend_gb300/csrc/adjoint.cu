@@ -1057,10 +1057,11 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const size_t per = lane_bytes(f->N, f->ns, f->K, f->G, f->nt, nrec);
-    const size_t want = std::max<size_t>(1, (size_t)(1.2e6 / (double)f->N + 0.5));
-    int nl = (int)std::min<size_t>(std::min<size_t>((size_t)nshots, want), std::max<size_t>(1, (free_b / 4 * 3) / per));
+    // (SEIDART_FWI_LANES sets the number instead, within the shots and memory)
+    size_t want = std::max<size_t>(1, (size_t)(1.2e6 / (double)f->N + 0.5));
     const char* env = getenv("SEIDART_FWI_LANES");
-    if (env && atoi(env) > 0) nl = std::min(nl, atoi(env));
+    if (env && atoi(env) > 0) want = (size_t)atoi(env);
+    const int nl = (int)std::min<size_t>(std::min<size_t>((size_t)nshots, want), std::max<size_t>(1, (free_b / 4 * 3) / per));
     f->lanes.resize(nl);
     for (int l = 0; l < nl; ++l) {
         FwiLane& L = f->lanes[l];
