@@ -12,6 +12,9 @@ grid (stress half-step + velocity half-step, source, Dirichlet faces, norms,
             model upload + conversion, a full 1500-step run, copy-back of the
             final fields and traces)
   roofline  dominant kernel: algorithmic bytes per launch / its CUDA-event time
+            (the layered model runs the material-indexed stress kernel: one
+            byte per cell instead of 27 coefficient words, counted as such;
+            per_cell_layout times the per-cell arrays on the same steps)
   cpu_baseline  the CPU restatement (reference production flags, OpenMP) on a
             bounded sample of the same workload
   configs_2d  the two 2D workloads at full length: seismic2 256^2 + 20 CPML
@@ -136,16 +139,21 @@ def make_problem(nt=None):
 # full-size launch is too large for a multi-pass capture), divided by that
 # launch's algorithmic bytes; the bench scales it to its own launch by the
 # algorithmic bytes.
-TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.153}
+TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.153,
+                 "s3x_stress/indexed": 1.118}
 
 
-def kernel_bytes(p, box_cells: int) -> dict:
+def kernel_bytes(p, box_cells: int, indexed: bool = False) -> dict:
     """Algorithmic bytes per launch (FP32): every array the kernel must touch,
     read or written once; CPML memories and coefficients only on the CPML
-    shell (outside the inert interior box)."""
+    shell (outside the inert interior box).  `indexed`: the stress kernel
+    reads the material-indexed layout -- one byte per cell instead of the
+    21 C_ij and 6 attenuation factors (the table of tuples is a few KB)."""
     n = p.ncell
     shell = n - box_cells
     stress = WORD * (42 * n + 78 * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12; shell: 36 memories R+W + 6 coefficients
+    if indexed:
+        stress = WORD * (15 * n + 78 * shell) + n  # v 3 + sigma R+W 12 + one material byte
     velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
     # the fused step does both half-steps: the whole step's algorithmic bytes
     return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3p_velocity": velocity,
@@ -154,11 +162,15 @@ def kernel_bytes(p, box_cells: int) -> dict:
             "s3w_step": step_bytes(p, box_cells)}
 
 
-def step_bytes(p, box_cells: int) -> int:
+def step_bytes(p, box_cells: int, indexed: bool = False) -> int:
     """Per-step algorithmic bytes of the whole leapfrog step: 9 fields read and
     written once, 21 C_ij + rho + 6 gamma read once (46 words), plus 45
-    memories R+W and 6 CPML coefficients on shell cells (96 words)."""
+    memories R+W and 6 CPML coefficients on shell cells (96 words).
+    `indexed`: one material byte per cell in place of the 27 coefficient
+    words (19 words + 1 byte per cell)."""
     shell = p.ncell - box_cells
+    if indexed:
+        return WORD * (19 * p.ncell + 96 * shell) + p.ncell
     return WORD * (46 * p.ncell + 96 * shell)
 
 
@@ -670,6 +682,7 @@ def main():
     box_cells = interior_box_cells(p)
     stream = torch.cuda.Stream()
     s = sg.Solver(p, sg.FP32)
+    nmat = s.material_count()  # > 0: the stress kernel reads the material-indexed layout
     s.set_stream(stream.cuda_stream)
     s.step(args.warmup)
     s.sync()
@@ -691,12 +704,13 @@ def main():
         ms_total = float(t.item())
     value = world * p.ncell * args.steps / (ms_total / 1e3) / 1e9
     hbm, peak_kind = peaks()
-    kb = kernel_bytes(p, box_cells)
+    kb = kernel_bytes(p, box_cells, indexed=nmat > 0)
     kernels = prof["kernels"]
     dom = max((k for k in kernels if k in kb), key=lambda k: kernels[k]["ms"])
     avg_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
     achieved = kb[dom] / (avg_ms / 1e3) / 1e9
-    sb = step_bytes(p, box_cells)
+    traffic_key = dom + "/indexed" if nmat > 0 and dom == "s3x_stress" else dom
+    sb = step_bytes(p, box_cells, indexed=nmat > 0)
     step_gbs = sb * args.steps / (ms_total / 1e3) / 1e9
     launches = sum(v["launches"] for v in kernels.values())
     s.close()
@@ -780,6 +794,27 @@ def main():
         extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
         extra["fp32_speedup_vs_fp64_fast"] = value / world / extra["fp64_fast"]["value"]
 
+    if nmat > 0 and rank == 0:
+        # the same steps with the per-cell coefficient arrays (27 words per
+        # cell instead of one material byte), on the per-cell byte count
+        os.environ["SEIDART_S3_MATIDX"] = "0"
+        try:
+            sp = sg.Solver(p, sg.FP32)
+            sp.step(args.warmup)
+            sp.sync()
+            prp = sp.profile(args.steps)
+            sp.sync()
+            sp.close()
+        finally:
+            del os.environ["SEIDART_S3_MATIDX"]
+        msp = prp["total_ms"] / args.steps
+        sbp = step_bytes(p, box_cells)
+        extra["per_cell_layout"] = {
+            "value": p.ncell / (msp / 1e3) / 1e9, "unit": UNIT, "ms_per_step": msp,
+            "step_roofline": {"frac": sbp / (msp / 1e3) / 1e9 / hbm, "bytes_per_step": sbp},
+            "kernels_ms": {k: v["ms"] / v["launches"] for k, v in prp["kernels"].items()},
+            "note": "the staged stress kernel reading the 21 C_ij and 6 attenuation arrays per cell"}
+
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline_sample(p)
@@ -807,10 +842,14 @@ def main():
             "cpu_baseline": cpu,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "traffic": TRAFFIC_RATIO[dom] * kb[dom] if dom in TRAFFIC_RATIO else None,
+                         "traffic": TRAFFIC_RATIO[traffic_key] * kb[dom] if traffic_key in TRAFFIC_RATIO else None,
                          "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
                          "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms},
             "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb},
+            "model_layout": {"materials": nmat,
+                             "stress_coefficients": ("material-indexed: one byte per cell and a table of "
+                                                     f"{nmat} FP32 (C_ij, gamma) tuples")
+                             if nmat > 0 else "per-cell arrays (21 C_ij + 6 attenuation factors)"},
             **extra,
             "kernels": kernels,
             "wall_s_timed": wall,

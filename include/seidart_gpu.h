@@ -237,6 +237,14 @@ int seidart_solver_sync(SeidartSolver* s);
 /* Copy traces / norms of steps [0, steps_done) to the host. */
 int seidart_solver_traces(SeidartSolver* s, double* traces, double* norms);
 int seidart_solver_steps_done(const SeidartSolver* s);
+/* Materials of an FP32 seismic3 solver's material-indexed coefficient
+ * layout: when the 21 stiffness and 6 attenuation arrays hold at most 32
+ * distinct tuples (as a model expanded from a material image does), the
+ * stress kernel reads one byte per cell and a table instead of 27 arrays,
+ * with the same FP32 values (the index is found on the device at set-up).
+ * 0 = per-cell arrays (too many tuples, nx not a multiple of 4, another
+ * family or precision, or SEIDART_S3_MATIDX=0). */
+int seidart_solver_material_count(const SeidartSolver* s);
 /* Device pointer of field slot `slot` (FP64 or FP32 per precision). */
 void* seidart_solver_field_ptr(SeidartSolver* s, int slot);
 /* Advance nsteps steps launching kernels one by one (no CUDA graph) with a

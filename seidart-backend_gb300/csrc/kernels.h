@@ -244,7 +244,23 @@ struct S3Args {
     int wave_lag;          // planes between the fused step's stress and velocity fronts (0: default)
     int l2_hint;           // FP32 staged stress: 1 = read-once copies with an L2 evict-first policy
     int v_reverse;         // FP32 velocity kernels: 1 = walk the planes from nz-1 down to 0
+    // FP32 staged stress kernel, material-indexed model: when the 21 C_ij and
+    // 6 attenuation factors take at most S3_MAXMAT distinct tuples, mat_ids
+    // holds one byte per cell (tile-packed like `packed`: [tile][8][32]) and
+    // mat_tab the tuples ([S3_MAXMAT][27] floats); NULL = per-cell arrays
+    const unsigned char* mat_ids;
+    const float* mat_tab;
+    int mat_tab_bytes;     // bytes of mat_tab a tile copies (a multiple of 16)
+    int mat_minb;          // CTAs per SM the indexed stress kernel is compiled for (4 .. 6)
 };
+constexpr int S3_MAXMAT = 32;
+// The material index of an FP32 3D solver's coefficient arrays, found on the
+// device (matidx.cu): on success the tile-packed material bytes and the
+// [S3_MAXMAT][27] FP32 table (both cudaMalloc'd, the caller frees them) and
+// the number of materials, returned too; 0 when the model holds more than
+// S3_MAXMAT distinct tuples (or on an allocation failure).
+int seismic3_material_index(const S3Args<float>& a, int nx, int ny, int nz, unsigned char** ids, float** tab,
+                            int* nmat, cudaStream_t st);
 // layout of S3Args::wave_ctl
 constexpr int WAVE_DONE0 = 32;
 // TMA tensor maps of the staged FP32 3D stress kernel: old stresses (32 x 8

@@ -78,7 +78,11 @@ __device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, i
     if (!tile_ahead(A.pf_d, tx, ty, k)) return;
     if (k < 1 || k > A.nz - 2) return;
     const size_t lin = (size_t)tx + (size_t)gridDim.x * ((size_t)ty + (size_t)gridDim.y * k);
-    if (tid < NCOEF * NT / 32) pf_l2(A.packed + lin * (NCOEF * NT) + tid * 32);
+    if (A.mat_ids) {
+        if (tid < NT / 128) pf_l2(A.mat_ids + lin * NT + tid * 128);  // the tile's material bytes
+    } else if (tid < NCOEF * NT / 32) {
+        pf_l2(A.packed + lin * (NCOEF * NT) + tid * 32);
+    }
     pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, NT);
     if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {
         pf_tile_rows(A.mem, 36, tx, ty, k, A.nx, A.ny, tid, NT);
@@ -212,10 +216,22 @@ constexpr int XS_VH = XS_SIG + 6 * NT;          // [3][VHH][VHW]
 constexpr int XS_VZ = XS_VH + 3 * VHW * VHH;    // [3][4][NT]: z = k-2, k-1, k+1, k+2
 constexpr int XS_TOTAL = XS_VZ + 12 * NT;
 constexpr unsigned XS_BYTES = XS_TOTAL * sizeof(float);  // 51,840
+// Material-indexed model: the coefficient block is replaced by the material
+// table ([S3_MAXMAT][27] floats) and the tile's material bytes ([NT]); the
+// stresses and velocities follow at a 128-byte aligned offset.
+constexpr int XI_TAB = 0;
+constexpr int XI_ID = S3_MAXMAT * NCOEF;                 // 864 floats
+constexpr int XI_SIG = XI_ID + NT / 4;                   // 928 floats (3,712 bytes)
+constexpr int XI_TOTAL = XI_SIG + (XS_TOTAL - XS_SIG);
+constexpr unsigned XI_BYTES = XI_TOTAL * sizeof(float);  // 27,904
+constexpr unsigned XS_FIELD_BYTES = XS_BYTES - TILE_BYTES;  // stresses and velocities of a tile
+static_assert((XI_SIG * sizeof(float)) % 128 == 0, "tensor-copy destinations need 128-byte alignment");
 
-template <bool LEAN, bool STREAM = true>
+// IDX: the material-indexed layout (coefficients from the material table)
+template <bool LEAN, bool STREAM = true, bool IDX = false>
 __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float* sm, unsigned long long* bar, int tid,
                                             int x0, int y0, int k, int probe, unsigned parity = 0) {
+    constexpr int SIG = IDX ? XI_SIG : XS_SIG, VH = SIG + 6 * NT, VZ = VH + 3 * VHW * VHH;
     const int nx = A.nx, ny = A.ny, nz = A.nz;
     const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
     bool L1 = true, L2 = true, L3 = true, L4 = true, active = true;
@@ -234,8 +250,8 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
     const int hc = (threadIdx.y + 2) * VHW + threadIdx.x + 4;
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-        const float* H = sm + XS_VH + f * VHW * VHH + hc;
-        const float* Z = sm + XS_VZ + f * 4 * NT + tid;
+        const float* H = sm + VH + f * VHW * VHH + hc;
+        const float* Z = sm + VZ + f * 4 * NT + tid;
         const float a0 = H[0];
         const float xm2 = H[-2], xm1 = H[-1], xp1 = H[1], xp2 = H[2];
         const float ym2 = H[-2 * VHW], ym1 = H[-VHW], yp1 = H[VHW], yp2 = H[2 * VHW];
@@ -247,9 +263,13 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
         fz[f] = (27.0f * (zp1 - a0) - (zp2 - zm1)) * hz;
         bz[f] = (27.0f * (a0 - zm1) - (zp1 - zm2)) * hz;
     }
-    const float* so = sm + XS_SIG + tid;  // old stress q at so[q * NT]
-    const auto CR = [&](int q) { return sm[q * NT + tid]; };
-    const auto GM = [&](int q) { return sm[(21 + q) * NT + tid]; };
+    const float* so = sm + SIG + tid;  // old stress q at so[q * NT]
+    // coefficient q of this cell: its slot of the tile block, or of its
+    // material's row of the table (the same FP32 values)
+    const float* cf = IDX ? sm + XI_TAB + NCOEF * reinterpret_cast<const unsigned char*>(sm + XI_ID)[tid] : sm + tid;
+    constexpr int CS = IDX ? 1 : NT;
+    const auto CR = [&](int q) { return cf[q * CS]; };
+    const auto GM = [&](int q) { return cf[(21 + q) * CS]; };
     const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 &&
                                 A.box.k0 <= k && k < A.box.k1);
     const float dt = A.dt;
@@ -328,14 +348,33 @@ __device__ __forceinline__ void stress_copies_issue(const S3Args<float>& A, cons
     }
 }
 
+template <bool IDX = false>
 __device__ __forceinline__ void stress_copies(const S3Args<float>& A, const S3XMaps& M, float* sm,
                                               unsigned long long* bar, int tid, int x0, int y0, int k, size_t lin,
                                               int probe) {
     if (tid == 0) {
         mbar_init(bar, 1);
-        mbar_expect_tx(bar, XS_BYTES + (unsigned)probe);
+        mbar_expect_tx(bar, (IDX ? (unsigned)A.mat_tab_bytes + NT + XS_FIELD_BYTES : XS_BYTES) + (unsigned)probe);
     }
     __syncthreads();
+    if (IDX) {
+        // the material table (lane 0), the tile's material bytes (lane 22),
+        // the stresses and velocities (lanes 1..21) as in the block layout
+        if (tid == 0) {
+            bulk_g2s(sm + XI_TAB, A.mat_tab, (unsigned)A.mat_tab_bytes, bar);
+        } else if (tid == 22) {
+            bulk_g2s(sm + XI_ID, A.mat_ids + lin * NT, NT, bar);
+        } else if (tid <= 6) {
+            tma_load3(sm + XI_SIG + (tid - 1) * NT, &M.sig[tid - 1], x0, y0, k, bar);
+        } else if (tid <= 9) {
+            tma_load3(sm + XI_SIG + 6 * NT + (tid - 7) * VHW * VHH, &M.vh[tid - 7], x0 - 4, y0 - 2, k, bar);
+        } else if (tid < 22) {
+            const int q = tid - 10, f = q >> 2, zi = q & 3;
+            const int dz = zi < 2 ? zi - 2 : zi - 1;
+            tma_load3(sm + XI_SIG + 6 * NT + 3 * VHW * VHH + q * NT, &M.vp[f], x0, y0, k + dz, bar);
+        }
+        return;
+    }
     if (tid < 22) {
         if (A.l2_hint && tid <= 6) {
             // the coefficient block and the old stresses are read once
@@ -368,7 +407,7 @@ __device__ __forceinline__ int probe_bytes(const S3Args<float>& A, int tx, int t
     return (A.wait_probe > 0 && tx == 0 && ty == 0 && k == 2) ? A.wait_probe : 0;
 }
 
-template <int MINB>
+template <int MINB, bool IDX = false>
 __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __grid_constant__ S3XMaps M) {
     extern __shared__ __align__(128) float sm[];
     __shared__ __align__(8) unsigned long long bar;
@@ -378,10 +417,10 @@ __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __
     if (k < 1 || k > nz - 2) return;  // planes 0 and nz-1 hold no stress update
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     const int probe = probe_bytes(A, blockIdx.x, blockIdx.y, k);
-    stress_copies(A, M, sm, &bar, tid, x0, y0, k, blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k),
-                  probe);
-    if (lean_stress_tile(A, x0, y0, k)) staged_tile<true>(A, sm, &bar, tid, x0, y0, k, probe);
-    else staged_tile<false>(A, sm, &bar, tid, x0, y0, k, probe);
+    stress_copies<IDX>(A, M, sm, &bar, tid, x0, y0, k,
+                       blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k), probe);
+    if (lean_stress_tile(A, x0, y0, k)) staged_tile<true, true, IDX>(A, sm, &bar, tid, x0, y0, k, probe);
+    else staged_tile<false, true, IDX>(A, sm, &bar, tid, x0, y0, k, probe);
 }
 
 // ------------------------------------------------ fused step (wavefront)
@@ -683,7 +722,17 @@ bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* m) {
 }
 
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st) {
-    s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
+    if (a.mat_ids) {
+        // the indexed layout's 27.9 KB of shared memory leave room for more
+        // CTAs per SM than the block layout's 51.8 KB
+        switch (a.mat_minb) {
+        case 5: s3x_stress<5, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
+        case 6: s3x_stress<6, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
+        default: s3x_stress<4, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
+        }
+    } else {
+        s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
+    }
 }
 
 int seismic3_wave_prepare(const S3Args<float>& a) {

@@ -158,6 +158,9 @@ struct SeidartSolver {
     float* pin = nullptr;        // pinned host double buffer of FP32 read-backs (2 x kPinChunk floats)
     cudaEvent_t pin_ev[2] = {nullptr, nullptr};
     S3XMaps s3_staged{};         // tensor maps of the staged stress kernel (when s3f.staged is set)
+    unsigned char* s3_mat_ids = nullptr;  // material-indexed model: one byte per cell, tile-packed
+    float* s3_mat_tab = nullptr;          // and the [S3_MAXMAT][27] table of FP32 coefficient tuples
+    int s3_nmat = 0;                      // materials of the indexed layout (0: per-cell arrays)
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
@@ -1012,6 +1015,18 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         // grid allows it; SEIDART_S3_STAGED=0 keeps the bulk kernel
         const char* st = getenv("SEIDART_S3_STAGED");
         if (!(st && *st == '0') && seismic3_staged_prepare(s->s3f, &s->s3_staged)) s->s3f.staged = &s->s3_staged;
+        // material-indexed coefficients for the staged kernel when the model
+        // allows them (SEIDART_S3_MATIDX=0 keeps the per-cell blocks)
+        const char* mi = getenv("SEIDART_S3_MATIDX");
+        if (s->s3f.staged && !(mi && *mi == '0') &&
+            seismic3_material_index(s->s3f, s->dom.nx, s->dom.ny, s->dom.nz, &s->s3_mat_ids, &s->s3_mat_tab,
+                                    &s->s3_nmat, s->stream) > 0) {
+            s->s3f.mat_ids = s->s3_mat_ids;
+            s->s3f.mat_tab = s->s3_mat_tab;
+            s->s3f.mat_tab_bytes = (s->s3_nmat * 27 * (int)sizeof(float) + 15) / 16 * 16;
+        }
+        const char* mb = getenv("SEIDART_S3_IDX_MINB");
+        s->s3f.mat_minb = (mb && *mb >= '4' && *mb <= '6') ? atoi(mb) : 4;
         // staged velocity kernel: bit-identical but measured slower at 352^3
         // (1.55 ms against 1.19 ms), so only on request
         const char* sv = getenv("SEIDART_S3_STAGED_V");
@@ -1225,6 +1240,8 @@ int seidart_solver_profile(SeidartSolver* s, int nsteps, double* total_ms, doubl
 
 int seidart_solver_steps_done(const SeidartSolver* s) { return s ? s->steps_done : -1; }
 
+int seidart_solver_material_count(const SeidartSolver* s) { return s ? s->s3_nmat : -1; }
+
 int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex, int* is_fp32,
                                    size_t* ncell, void** stream) {
     if (!s || slot < 0 || slot >= (int)s->fields.size()) return set_err(SEIDART_ERR_ARG, "bad field slot");
@@ -1263,6 +1280,8 @@ int seidart_solver_destroy(SeidartSolver* s) {
         if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
     if (s->arena) cudaFree(s->arena);
     if (s->s3_packed) cudaFree(s->s3_packed);
+    if (s->s3_mat_ids) cudaFree(s->s3_mat_ids);
+    if (s->s3_mat_tab) cudaFree(s->s3_mat_tab);
     if (s->stage) cudaFree(s->stage);
     if (s->pin) cudaFreeHost(s->pin);
     for (int b = 0; b < 2; ++b)

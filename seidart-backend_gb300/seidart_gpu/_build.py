@@ -28,7 +28,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", str(INCLUDE)]
 # (source, precision) pairs; precision None = compiled once
 DUAL = ["seismic2.cu", "electromag2.cu", "seismic25.cu", "electromag25.cu", "seismic3.cu", "electromag3.cu"]
-SINGLE = ["solver.cu", "seismic3_fast.cu", "seismic3_tma.cu", "seismic3_cell.cu", "seismic3_bulk.cu", "fileio.cu", "batch.cu", "adjoint.cu", "adjoint_em.cu", "noalloc.cu", "material.cu", "planewave.cu"]
+SINGLE = ["solver.cu", "seismic3_fast.cu", "seismic3_tma.cu", "seismic3_cell.cu", "seismic3_bulk.cu", "fileio.cu", "batch.cu", "adjoint.cu", "adjoint_em.cu", "noalloc.cu", "material.cu", "planewave.cu", "matidx.cu"]
 
 
 def _nvcc() -> str:

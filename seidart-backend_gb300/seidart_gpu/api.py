@@ -283,6 +283,11 @@ class Solver:
     def steps_done(self) -> int:
         return lib().seidart_solver_steps_done(self.handle)
 
+    def material_count(self) -> int:
+        """Materials of the FP32 3D material-indexed coefficient layout (0:
+        the per-cell arrays are used)."""
+        return lib().seidart_solver_material_count(self.handle)
+
     @property
     def launches(self) -> int:
         return lib().seidart_solver_launches(self.handle)
