@@ -385,7 +385,22 @@ def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
     cfg = b.config()
     launches = b.launches
     graph_launches = b.graph_launches
+    mats = [b.material_count(m) for m in range(len(ps))]
     b.close()
+    # the same timed steps with the per-cell coefficient arrays
+    os.environ["SEIDART_BATCH_MATIDX"] = "0"
+    try:
+        bp = Batch(ps, autotune=True)
+        bp.step(warm)
+        bp.sync()
+        t0 = time.perf_counter()
+        bp.step(nt - warm, chunk=500)
+        bp.sync()
+        dtp = time.perf_counter() - t0
+        cfgp = bp.config()
+        bp.close()
+    finally:
+        del os.environ["SEIDART_BATCH_MATIDX"]
     # the same models one by one (single-model FP32 solver), a bounded sample
     seq_cells, seq_t = 0, 0.0
     for p in ps[:8]:
@@ -399,11 +414,24 @@ def bench_batch(nmodels: int = 64, nt: int = 3000, warm: int = 20) -> dict:
             seq_t += time.perf_counter() - t1
             seq_cells += q.ncell * 280
     # algorithmic bytes per step: 20 words per cell + 30 per CPML cell (FP32)
+    # with per-cell coefficient arrays; an indexed model reads one material
+    # byte per cell instead of its nine stress coefficient words
     hbm, _ = peaks()
-    step_b = sum(4 * (20 * p.ncell + 30 * (p.ncell - (p.nx - 2 * p.cpml) * (p.nz - 2 * p.cpml))) for p in ps)
+
+    def shell(p):
+        return p.ncell - (p.nx - 2 * p.cpml) * (p.nz - 2 * p.cpml)
+
+    step_cell = sum(4 * (20 * p.ncell + 30 * shell(p)) for p in ps)
+    step_b = sum((4 * (11 * p.ncell + 30 * shell(p)) + p.ncell) if m > 0 else 4 * (20 * p.ncell + 30 * shell(p))
+                 for p, m in zip(ps, mats))
     gbs = step_b * (nt - warm) / dt / 1e9
+    gbs_cell = step_cell * (nt - warm) / dtp / 1e9
     return {"value": cells * (nt - warm) / dt / 1e9, "unit": UNIT, "models": nmodels, "cells": cells,
             "algorithmic_gbs": gbs, "frac_of_measured_hbm": gbs / hbm, "bytes_per_step": step_b,
+            "materials_per_model": {"min": min(mats), "max": max(mats)},
+            "per_cell_layout": {"value": cells * (nt - warm) / dtp / 1e9, "unit": UNIT, "seconds": dtp,
+                                "frac_of_measured_hbm": gbs_cell / hbm, "bytes_per_step": step_cell,
+                                "tuned": cfgp},
             "steps_timed": nt - warm, "seconds": dt, "setup_s": setup, "tuned": cfg, "gpu_launches": launches,
             "graph_replays": graph_launches,
             "one_by_one": {"value": seq_cells / seq_t / 1e9, "unit": UNIT,

@@ -352,6 +352,12 @@ long long seidart_batch_launches(const SeidartBatch* b);
 long long seidart_batch_graph_launches(const SeidartBatch* b);
 int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int* grid);
 int seidart_batch_num_variants(void);
+/* Materials of model m's indexed stress coefficients: a model whose nine
+ * stress coefficients (c11 c13 c15 c33 c35 c55, three attenuation factors)
+ * hold at most 32 distinct tuples is walked with one byte per cell and a
+ * table of the tuples (found on the device at creation, the same FP32
+ * values); 0 = per-cell arrays (or SEIDART_BATCH_MATIDX=0), -1 = bad m. */
+int seidart_batch_material_count(const SeidartBatch* b, int m);
 /* How kernel variant `variant` walks the flattened tile list: "strided"
  * (CTA b of G takes tiles b, b+G, ...) or "chunked" (a contiguous range per
  * CTA); NULL outside 0 .. seidart_batch_num_variants()-1. */

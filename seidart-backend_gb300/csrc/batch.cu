@@ -36,6 +36,11 @@ struct BModel {
     float* mem[12];
     float* f2[5];     // second state set of the fused step (double buffering)
     float* mem2[12];
+    // material-indexed stress coefficients (NULL: the per-cell arrays m[0..5],
+    // m[7..9]): one byte per cell in grid order and a [32][9] table of
+    // c11 c13 c15 c33 c35 c55 and the three attenuation factors
+    const unsigned char* ids;
+    const float* tab;
     const double* src[5];
     const int* rec;
     float* traces;   // [nt][2][nrec]
@@ -103,6 +108,21 @@ __device__ __forceinline__ bool tile_cell(const BatchArgs& B, int t, const BMode
 
 #define IXM(fi, fk) ((size_t)((fi) - 1) + (size_t)nx * (size_t)((fk) - 1))
 
+// the nine stress coefficients of cell c: from the material table when the
+// model is indexed (the same FP32 values), else from the per-cell arrays
+__device__ __forceinline__ void stress_coefs(const BModel& a, size_t c, float& c11, float& c13, float& c15,
+                                             float& c33, float& c35, float& c55, float& gx, float& gz, float& gxz) {
+    if (a.ids) {
+        const float* T = a.tab + 9 * __ldg(a.ids + c);
+        c11 = __ldg(T); c13 = __ldg(T + 1); c15 = __ldg(T + 2); c33 = __ldg(T + 3); c35 = __ldg(T + 4);
+        c55 = __ldg(T + 5); gx = __ldg(T + 6); gz = __ldg(T + 7); gxz = __ldg(T + 8);
+    } else {
+        c11 = __ldg(a.m[0] + c); c13 = __ldg(a.m[1] + c); c15 = __ldg(a.m[2] + c);
+        c33 = __ldg(a.m[3] + c); c35 = __ldg(a.m[4] + c); c55 = __ldg(a.m[5] + c);
+        gx = __ldg(a.m[7] + c); gz = __ldg(a.m[8] + c); gxz = __ldg(a.m[9] + c);
+    }
+}
+
 // stress half-step of one cell (seismic2.cu FP32 arithmetic).  Every load
 // is issued before any arithmetic: the velocity stencil with clamped
 // (always valid) indices, the coefficients and old stresses, and on shell
@@ -128,9 +148,8 @@ __device__ __forceinline__ void cell_stress(const BModel& a, int i, int j) {
     const float xe = VX[zm2], xf = VX[zm1], xg = VX[zp1], xh = VX[zp2];
     const float z0 = VZ[0], za = VZ[xm2], zb = VZ[xm1], zc = VZ[xp1], zd = VZ[xp2];
     const float ze = VZ[zm2], zf = VZ[zm1], zg = VZ[zp1], zh = VZ[zp2];
-    const float c11 = __ldg(a.m[0] + c), c13 = __ldg(a.m[1] + c), c15 = __ldg(a.m[2] + c);
-    const float c33 = __ldg(a.m[3] + c), c35 = __ldg(a.m[4] + c), c55 = __ldg(a.m[5] + c);
-    const float gx = __ldg(a.m[7] + c), gz = __ldg(a.m[8] + c), gxz = __ldg(a.m[9] + c);
+    float c11, c13, c15, c33, c35, c55, gx, gz, gxz;
+    stress_coefs(a, c, c11, c13, c15, c33, c35, c55, gx, gz, gxz);
     const float sxx = a.f[2][c], szz = a.f[3][c], sxz = a.f[4][c];
     float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (pml) {
@@ -329,6 +348,14 @@ __device__ __forceinline__ void tile_prefetch(const BatchArgs& B, int t, int tid
     for (int q = tid; q < narr * TY; q += TX * TY) {
         const int a = q / TY, y = z0 + q % TY;
         if (y >= z1) continue;
+        if (PHASE == 1 && M.ids && a >= 5 && a < 14) {
+            // indexed model: the row's material bytes stand for the nine coefficient rows
+            if (a == 5) {
+                pf_l2(M.ids + (size_t)y * M.nx + x0);
+                pf_l2(M.ids + (size_t)y * M.nx + x1);
+            }
+            continue;
+        }
         const float* row = pf_array<PHASE>(M, a) + (size_t)y * M.nx;
 #pragma unroll
         for (int xo = 0; xo < TX; xo += 32)
@@ -449,9 +476,8 @@ __device__ __forceinline__ void fused_stress_cell(const BModel& a, int i, int j,
         const float xe = VX[-2 * W], xf = VX[-W], xg = VX[W], xh = VX[2 * W];
         const float z0 = VZ[0], za = VZ[-2], zb = VZ[-1], zc = VZ[1], zd = VZ[2];
         const float ze = VZ[-2 * W], zf = VZ[-W], zg = VZ[W], zh = VZ[2 * W];
-        const float c11 = __ldg(a.m[0] + c), c13 = __ldg(a.m[1] + c), c15 = __ldg(a.m[2] + c);
-        const float c33 = __ldg(a.m[3] + c), c35 = __ldg(a.m[4] + c), c55 = __ldg(a.m[5] + c);
-        const float gx = __ldg(a.m[7] + c), gz = __ldg(a.m[8] + c), gxz = __ldg(a.m[9] + c);
+        float c11, c13, c15, c33, c35, c55, gx, gz, gxz;
+        stress_coefs(a, c, c11, c13, c15, c33, c35, c55, gx, gz, gxz);
         float kap = 1.f, kaph = 1.f, aa = 0.f, ah = 0.f, b = 0.f, bh = 0.f, m[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (pml) {
             kap = __ldg(a.m[10] + c); kaph = __ldg(a.m[11] + c); aa = __ldg(a.m[12] + c);
@@ -589,6 +615,14 @@ __device__ __forceinline__ void fused_prefetch(const BatchArgs& B, int t, int rd
     for (int q = tid; q < narr * TY; q += NT) {
         const int a = q / TY, y = z0 + q % TY;
         if (y >= z1) continue;
+        if (M.ids && a >= 5 && a < 15 && a != 11) {
+            // indexed model: the material bytes stand for the nine coefficient rows (rho, a = 11, stays)
+            if (a == 5) {
+                pf_l2(M.ids + (size_t)y * M.nx + x0);
+                pf_l2(M.ids + (size_t)y * M.nx + x1);
+            }
+            continue;
+        }
         const float* base = a < 5 ? (rd ? M.f2[a] : M.f[a])                     // fields
                           : a < 15 ? M.m[a - 5]                                   // c11 .. gxz (rho among them)
                           : a < 27 ? (rd ? M.mem2[a - 15] : M.mem[a - 15])        // memories
@@ -743,6 +777,8 @@ struct SeidartBatch {
     int* dev_tile_rec_off[kNumVariants] = {nullptr};  // fused variants: receivers per tile
     int* dev_tile_rec[kNumVariants] = {nullptr};
     std::vector<float*> second;  // per model: the fused step's second state set, 17 arrays
+    std::vector<void*> owned;    // material bytes and tables of indexed models
+    std::vector<int> nmat;       // materials of each model's indexed layout (0: per-cell arrays)
     int ntiles[kNumVariants] = {0};
     int* ctl = nullptr;  // step, barrier count, barrier generation, status
     cudaStream_t stream = nullptr;
@@ -852,6 +888,7 @@ int seidart_batch_destroy(SeidartBatch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto* s : b->solvers) seidart_solver_destroy(s);
     for (float* p : b->second) cudaFree(p);
+    for (void* p : b->owned) cudaFree(p);
     for (int v = 0; v < kNumVariants; ++v) {
         if (b->dev_models[v]) cudaFree(b->dev_models[v]);
         if (b->dev_tile_model[v]) cudaFree(b->dev_tile_model[v]);
@@ -918,6 +955,31 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
     }
     const int ctl0[4] = {1, 0, 0, 0};
     cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    // material-indexed stress coefficients per model where the model allows
+    // them (SEIDART_BATCH_MATIDX=0 keeps the per-cell arrays)
+    const char* mi = getenv("SEIDART_BATCH_MATIDX");
+    if (!(mi && *mi == '0')) {
+        if (cudaDeviceSynchronize() != cudaSuccess) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_CUDA, "device synchronisation before the material index failed");
+        }
+        for (int m = 0; m < nmodels; ++m) {
+            const float* coef[9] = {hm[m].m[0], hm[m].m[1], hm[m].m[2], hm[m].m[3], hm[m].m[4],
+                                    hm[m].m[5], hm[m].m[7], hm[m].m[8], hm[m].m[9]};
+            unsigned char* ids = nullptr;
+            float* tab = nullptr;
+            int nmat = 0;
+            if (seismic2_material_index(coef, (size_t)hm[m].nx * hm[m].nz, &ids, &tab, &nmat, b->stream) > 0) {
+                hm[m].ids = ids;
+                hm[m].tab = tab;
+                b->owned.push_back(ids);
+                b->owned.push_back(tab);
+            }
+            b->nmat.push_back(nmat);
+        }
+    } else {
+        b->nmat.assign(nmodels, 0);
+    }
     // the fused step's second state set: 5 fields and 12 memories per model,
     // zeroed once (cells no loop updates are never written in either set)
     for (int m = 0; m < nmodels; ++m) {
@@ -1126,6 +1188,9 @@ int seidart_batch_config(const SeidartBatch* b, int* tx, int* ty, int* bps, int*
     return SEIDART_OK;
 }
 int seidart_batch_num_variants(void) { return kNumVariants; }
+int seidart_batch_material_count(const SeidartBatch* b, int m) {
+    return (b && m >= 0 && m < (int)b->nmat.size()) ? b->nmat[m] : -1;
+}
 const char* seidart_batch_variant_walk(int variant) {
     return variant >= 0 && variant < kNumVariants ? kVariants[variant].walk : nullptr;
 }

@@ -261,6 +261,11 @@ constexpr int S3_MAXMAT = 32;
 // S3_MAXMAT distinct tuples (or on an allocation failure).
 int seismic3_material_index(const S3Args<float>& a, int nx, int ny, int nz, unsigned char** ids, float** tab,
                             int* nmat, cudaStream_t st);
+// The same for the nine stress coefficients of an FP32 seismic2 model
+// (c11 c13 c15 c33 c35 c55 and the three attenuation factors, in that order
+// in `coef`): one byte per cell in grid order and a [S3_MAXMAT][9] table.
+int seismic2_material_index(const float* const* coef, size_t ncell, unsigned char** ids, float** tab, int* nmat,
+                            cudaStream_t st);
 // layout of S3Args::wave_ctl
 constexpr int WAVE_DONE0 = 32;
 // TMA tensor maps of the staged FP32 3D stress kernel: old stresses (32 x 8

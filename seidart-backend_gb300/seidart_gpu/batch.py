@@ -40,6 +40,7 @@ def _declare():
         "seidart_batch_config": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "seidart_batch_num_variants": (i, []),
         "seidart_batch_variant_walk": (C.c_char_p, [i]),
+        "seidart_batch_material_count": (i, [vp, i]),
         "seidart_batch_destroy": (i, [vp]),
         "seidart_batch_last_error": (C.c_char_p, []),
     }
@@ -122,6 +123,10 @@ class Batch:
         CTAs per SM instead of the autotuned choice."""
         _check(lib().seidart_batch_set_config(self.handle, int(variant), int(ctas_per_sm)))
         self.variant = int(variant)
+
+    def material_count(self, m: int) -> int:
+        """Materials of model m's indexed stress coefficients (0: per-cell arrays)."""
+        return lib().seidart_batch_material_count(self.handle, int(m))
 
     @staticmethod
     def num_variants() -> int:

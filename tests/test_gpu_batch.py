@@ -95,3 +95,32 @@ def test_sharded_batch_covers_every_model_once():
                 assert rel_l2(tr, single["traces"]) <= 1e-6, m
                 seen.append(m)
     assert sorted(seen) == list(range(len(probs)))
+
+
+def test_material_indexed_batch_is_bit_identical(monkeypatch):
+    """Layered models walk with one material byte per cell and a table of
+    their stress-coefficient tuples; the traces, norms and fields equal the
+    walk over per-cell arrays (SEIDART_BATCH_MATIDX=0) bit for bit, for the
+    two-phase and the fused walks."""
+    probs = small_batch(nt=40)
+    probs[1].src["zz"] = 0.25 * probs[1].src["z"]
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("SEIDART_BATCH_MATIDX", flag)
+        for variant in (11, Batch.num_variants() - 1):
+            with Batch(probs, autotune=False) as b:
+                mats = [b.material_count(m) for m in range(len(probs))]
+                b.set_config(variant, 1)
+                b.step(15, chunk=7)
+                b.step(probs[0].time_steps - 15)
+                b.sync()
+                out[flag, variant] = (mats, [b.traces(m) for m in range(len(probs))],
+                                      [b.fields(m) for m in range(len(probs))])
+    for variant in (11, Batch.num_variants() - 1):
+        mi, tri, fi = out["1", variant]
+        mp, trp, fp = out["0", variant]
+        assert all(m > 0 for m in mi) and all(m == 0 for m in mp)
+        for m in range(len(probs)):
+            assert np.array_equal(tri[m][0], trp[m][0]) and np.array_equal(tri[m][1], trp[m][1])
+            for q in range(5):
+                assert np.array_equal(fi[m][q], fp[m][q]), (variant, m, q)
