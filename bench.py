@@ -872,8 +872,15 @@ def main():
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": TRAFFIC_RATIO[traffic_key] * kb[dom] if traffic_key in TRAFFIC_RATIO else None,
                          "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
-                         "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms},
-            "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb},
+                         "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms,
+                         "bytes_basis": ("the layout the kernel reads: material-indexed (15 words + 1 byte per "
+                                         "cell, 78 words per shell cell); with per-cell coefficient arrays (42 + 78 "
+                                         f"words) a launch moves {kernel_bytes(p, box_cells)[dom] / 1e9:.2f} GB")
+                         if nmat > 0 and dom == "s3x_stress" else "per-cell coefficient arrays"},
+            "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb,
+                              "bytes_basis": ("material-indexed: 19 words + 1 byte per cell, 96 words per shell "
+                                              f"cell; per-cell arrays: {step_bytes(p, box_cells) / 1e9:.2f} GB per step")
+                              if nmat > 0 else "per-cell arrays: 46 words per cell, 96 per shell cell"},
             "model_layout": {"materials": nmat,
                              "stress_coefficients": ("material-indexed: one byte per cell and a table of "
                                                      f"{nmat} FP32 (C_ij, gamma) tuples")
