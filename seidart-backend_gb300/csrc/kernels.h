@@ -251,7 +251,8 @@ struct S3Args {
     const unsigned char* mat_ids;
     const float* mat_tab;
     int mat_tab_bytes;     // bytes of mat_tab a tile copies (a multiple of 16)
-    int mat_minb;          // CTAs per SM the indexed stress kernel is compiled for (4 .. 6)
+    int mem_merged;        // FP32 staged stress kernel: 1 = the 36 stress-loop C-PML memories held as 21
+                           // (derivatives two loops share advance one memory; slots 0..17 and 20, 23, 26)
 };
 constexpr int S3_MAXMAT = 32;
 // The material index of an FP32 3D solver's coefficient arrays, found on the

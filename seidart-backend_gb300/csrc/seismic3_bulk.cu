@@ -228,7 +228,7 @@ constexpr unsigned XS_FIELD_BYTES = XS_BYTES - TILE_BYTES;  // stresses and velo
 static_assert((XI_SIG * sizeof(float)) % 128 == 0, "tensor-copy destinations need 128-byte alignment");
 
 // IDX: the material-indexed layout (coefficients from the material table)
-template <bool LEAN, bool STREAM = true, bool IDX = false>
+template <bool LEAN, bool STREAM = true, bool IDX = false, bool MERGED = false>
 __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float* sm, unsigned long long* bar, int tid,
                                             int x0, int y0, int k, int probe, unsigned parity = 0) {
     constexpr int SIG = IDX ? XI_SIG : XS_SIG, VH = SIG + 6 * NT, VZ = VH + 3 * VHW * VHH;
@@ -278,19 +278,40 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
     // old stress order: xx xy xz yy yz zz ; gamma order: x y z xy yz xz
     // shell cells: the memories of loops 1 and 2 are loaded together, and
     // those of loops 3 and 4 together after the first pair's stores, so a
-    // cell waits for two DRAM round trips instead of four
+    // cell waits for two DRAM round trips instead of four.
+    // MERGED: the derivatives two loops share -- the same stencil with the
+    // same C-PML coefficients -- advance one memory instead of two: forward x
+    // with the half-grid coefficients (loops 1 and 4), backward x full (2 and
+    // 3), backward y full (1 and 3), forward y half (2 and 4), forward z half
+    // (3 and 4).  Where both loops of a pair update a cell their two memories
+    // start at zero and advance with the same values, so they stay equal; the
+    // first loop of the pair that applies at the cell advances the shared
+    // memory and the other reads the advanced value.  Loop 1's nine slots,
+    // loop 2's nine and loop 3's three z slots hold the 21 memories, all
+    // loaded at once (one round trip); seidart_solver_get_memory rebuilds the
+    // reference's 36 arrays from them.
     CpmlPair P{};
-    float ma[9], mb[9];
+    float ma[9], mb[9], mz[3];
     if (pml) {
         P = cpml_both(A, c);
-        if (L1) cpml_load<1>(A, c, ma);
-        if (L2) cpml_load<2>(A, c, mb);
+        if (MERGED) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                ma[q] = A.mem[q][c];
+                mb[q] = A.mem[9 + q][c];
+            }
+#pragma unroll
+            for (int f = 0; f < 3; ++f) mz[f] = A.mem[18 + 3 * f + 2][c];
+        } else {
+            if (L1) cpml_load<1>(A, c, ma);
+            if (L2) cpml_load<2>(A, c, mb);
+        }
     }
     if (L1) {
         float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) {
             cpml_update<1>(P, ma, ex, ey, ez);
-            cpml_store<1>(A, c, ma);
+            if (!MERGED) cpml_store<1>(A, c, ma);
         }
         st_sig<STREAM>(A.f[3] + c, stress_new(CR, so[0], GM(0), 0, 1, 2, 3, 4, 5, dt, ex, ey, ez));
         st_sig<STREAM>(A.f[6] + c, stress_new(CR, so[3 * NT], GM(1), 1, 6, 7, 8, 9, 10, dt, ex, ey, ez));
@@ -300,9 +321,51 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
         float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {bz[0], bz[1], bz[2]};
         if (pml) {
             cpml_update<2>(P, mb, ex, ey, ez);
-            cpml_store<2>(A, c, mb);
+            if (!MERGED) cpml_store<2>(A, c, mb);
         }
         st_sig<STREAM>(A.f[4] + c, stress_new(CR, so[NT], GM(3), 5, 10, 14, 17, 19, 20, dt, ex, ey, ez));
+    }
+    if (MERGED) {
+        // advance memory m with coefficient triple p unless the pair's other
+        // loop already did (done), then rescale the derivative
+        const auto adv = [](float& m, const CpmlC& p, float& g, bool done) {
+            if (!done) m = p.b * m + p.a * g;
+            g = g * p.k + m;
+        };
+        if (L3) {
+            float ex[3] = {bx[0], bx[1], bx[2]}, ey[3] = {by[0], by[1], by[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+            if (pml) {
+#pragma unroll
+                for (int f = 0; f < 3; ++f) {
+                    adv(mb[3 * f], P.f, ex[f], L2);      // backward x, full: loop 2's memory
+                    adv(ma[3 * f + 1], P.f, ey[f], L1);  // backward y, full: loop 1's memory
+                    adv(mz[f], P.h, ez[f], false);       // forward z, half: loop 3's own
+                }
+            }
+            st_sig<STREAM>(A.f[5] + c, stress_new(CR, so[2 * NT], GM(5), 4, 9, 13, 16, 18, 19, dt, ex, ey, ez));
+        }
+        if (L4) {
+            float ex[3] = {fx[0], fx[1], fx[2]}, ey[3] = {fy[0], fy[1], fy[2]}, ez[3] = {fz[0], fz[1], fz[2]};
+            if (pml) {
+#pragma unroll
+                for (int f = 0; f < 3; ++f) {
+                    adv(ma[3 * f], P.h, ex[f], L1);      // forward x, half: loop 1's memory
+                    adv(mb[3 * f + 1], P.h, ey[f], L2);  // forward y, half: loop 2's memory
+                    adv(mz[f], P.h, ez[f], L3);          // forward z, half: loop 3's memory
+                }
+            }
+            st_sig<STREAM>(A.f[7] + c, stress_new(CR, so[4 * NT], GM(4), 3, 8, 12, 15, 16, 17, dt, ex, ey, ez));
+        }
+        if (pml) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                A.mem[q][c] = ma[q];
+                A.mem[9 + q][c] = mb[q];
+            }
+#pragma unroll
+            for (int f = 0; f < 3; ++f) A.mem[18 + 3 * f + 2][c] = mz[f];
+        }
+        return;
     }
     if (pml) {
         if (L3) cpml_load<3>(A, c, ma);
@@ -407,7 +470,7 @@ __device__ __forceinline__ int probe_bytes(const S3Args<float>& A, int tx, int t
     return (A.wait_probe > 0 && tx == 0 && ty == 0 && k == 2) ? A.wait_probe : 0;
 }
 
-template <int MINB, bool IDX = false>
+template <int MINB, bool IDX = false, bool MERGED = false>
 __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __grid_constant__ S3XMaps M) {
     extern __shared__ __align__(128) float sm[];
     __shared__ __align__(8) unsigned long long bar;
@@ -419,8 +482,8 @@ __global__ void __launch_bounds__(NT, MINB) s3x_stress(S3Args<float> A, const __
     const int probe = probe_bytes(A, blockIdx.x, blockIdx.y, k);
     stress_copies<IDX>(A, M, sm, &bar, tid, x0, y0, k,
                        blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * k), probe);
-    if (lean_stress_tile(A, x0, y0, k)) staged_tile<true, true, IDX>(A, sm, &bar, tid, x0, y0, k, probe);
-    else staged_tile<false, true, IDX>(A, sm, &bar, tid, x0, y0, k, probe);
+    if (lean_stress_tile(A, x0, y0, k)) staged_tile<true, true, IDX, MERGED>(A, sm, &bar, tid, x0, y0, k, probe);
+    else staged_tile<false, true, IDX, MERGED>(A, sm, &bar, tid, x0, y0, k, probe);
 }
 
 // ------------------------------------------------ fused step (wavefront)
@@ -713,26 +776,21 @@ bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* m) {
         if (!seismic3_make_map(&m->vh[f], a.f[f], a.nx, a.ny, a.nz, VHW, VHH)) return false;
         if (!seismic3_make_map(&m->vp[f], a.f[f], a.nx, a.ny, a.nz, BX, BY)) return false;
     }
-    if (cudaFuncSetAttribute((const void*)s3x_stress<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_BYTES) !=
-        cudaSuccess) {
-        cudaGetLastError();
-        return false;
+    for (const void* fn : {(const void*)s3x_stress<4>, (const void*)s3x_stress<4, false, true>}) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)XS_BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
     }
     return true;
 }
 
 void launch_seismic3_staged_stress(const S3Args<float>& a, const S3XMaps& maps, cudaStream_t st) {
-    if (a.mat_ids) {
-        // the indexed layout's 27.9 KB of shared memory leave room for more
-        // CTAs per SM than the block layout's 51.8 KB
-        switch (a.mat_minb) {
-        case 5: s3x_stress<5, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
-        case 6: s3x_stress<6, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
-        default: s3x_stress<4, true><<<tile_grid(a), dim3(BX, BY), XI_BYTES, st>>>(a, maps); break;
-        }
-    } else {
-        s3x_stress<4><<<tile_grid(a), dim3(BX, BY), XS_BYTES, st>>>(a, maps);
-    }
+    const dim3 grd = tile_grid(a), blk(BX, BY);
+    if (a.mat_ids && a.mem_merged) s3x_stress<4, true, true><<<grd, blk, XI_BYTES, st>>>(a, maps);
+    else if (a.mat_ids) s3x_stress<4, true><<<grd, blk, XI_BYTES, st>>>(a, maps);
+    else if (a.mem_merged) s3x_stress<4, false, true><<<grd, blk, XS_BYTES, st>>>(a, maps);
+    else s3x_stress<4><<<grd, blk, XS_BYTES, st>>>(a, maps);
 }
 
 int seismic3_wave_prepare(const S3Args<float>& a) {

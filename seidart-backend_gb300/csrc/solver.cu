@@ -213,6 +213,33 @@ __global__ void derive_f64(double* __restrict__ d, size_t n, int mode, double dt
         d[q] = mode == 1 ? __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(x, dt))) : __ddiv_rn(1.0, x);
     }
 }
+// The reference's memory q (0..35) of stress loop L = q / 9 + 1 from the
+// merged layout of the FP32 staged stress kernel: the slot that holds it
+// (its own, or the one the loop shares with another loop for the same
+// stencil and coefficients) where loop L updates the cell, zero elsewhere --
+// the reference never advances a loop's memory outside the loop's range.
+__global__ void s3_unmerge(S3Args<float> a, int q, float* __restrict__ out) {
+    const int L = q / 9 + 1, f = (q % 9) / 3, d = q % 3;
+    int slot = q;
+    if (L == 3 && d == 0) slot = 9 + 3 * f;       // backward x, full: loop 2's
+    if (L == 3 && d == 1) slot = 3 * f + 1;       // backward y, full: loop 1's
+    if (L == 4 && d == 0) slot = 3 * f;           // forward x, half: loop 1's
+    if (L == 4 && d == 1) slot = 9 + 3 * f + 1;   // forward y, half: loop 2's
+    if (L == 4 && d == 2) slot = 18 + 3 * f + 2;  // forward z, half: loop 3's
+    const float* src = a.mem[slot];
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const size_t n = (size_t)nx * ny * nz;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((size_t)nx * ny));
+        const bool x14 = i >= 1 && i <= nx - 3, x23 = i >= 2 && i <= nx - 2;
+        const bool y13 = j >= 2 && j <= ny - 2, y24 = j >= 1 && j <= ny - 3;
+        const bool z12 = k >= 2 && k <= nz - 2, z34 = k >= 1 && k <= nz - 3;
+        const bool in = L == 1 ? (x14 && y13 && z12) : L == 2 ? (x23 && y24 && z12)
+                      : L == 3 ? (x23 && y13 && z34) : (x14 && y24 && z34);
+        out[c] = in ? src[c] : 0.0f;
+    }
+}
+
 __global__ void convert_to_f64(double* __restrict__ d, const float* __restrict__ s, size_t n) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         d[q] = (double)s[q];
@@ -1025,8 +1052,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.mat_tab = s->s3_mat_tab;
             s->s3f.mat_tab_bytes = (s->s3_nmat * 27 * (int)sizeof(float) + 15) / 16 * 16;
         }
-        const char* mb = getenv("SEIDART_S3_IDX_MINB");
-        s->s3f.mat_minb = (mb && *mb >= '4' && *mb <= '6') ? atoi(mb) : 4;
+
         // staged velocity kernel: bit-identical but measured slower at 352^3
         // (1.55 ms against 1.19 ms), so only on request
         const char* sv = getenv("SEIDART_S3_STAGED_V");
@@ -1050,6 +1076,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
                 s->s3f.wave_n = 0;
             }
         }
+        // the staged stress kernel holds the 36 stress-loop C-PML memories as
+        // 21 (SEIDART_S3_MERGE=0 keeps all 36); the fused step keeps 36
+        const char* mg = getenv("SEIDART_S3_MERGE");
+        s->s3f.mem_merged = (s->s3f.staged && !s->s3f.wave_ctl && !(mg && *mg == '0')) ? 1 : 0;
     }
     *out = s;
     return SEIDART_OK;
@@ -1118,12 +1148,26 @@ int seidart_solver_get_fields(SeidartSolver* s, double* const* fields) {
 int seidart_solver_get_memory(SeidartSolver* s, double* const* mem) {
     if (!s || !mem) return set_err(SEIDART_ERR_ARG, "NULL argument");
     const size_t n = s->ncell * (s->L.cplx ? 2 : 1);
+    float* tmp = nullptr;  // a rebuilt stress-loop memory of the merged layout
     for (int q = 0; q < s->L.nmem; ++q) {
         if (!mem[q]) continue;
-        const int rc = s->precision == SEIDART_FP32 ? download<float>(*s, mem[q], s->mem[q], n)
-                                                    : download<double>(*s, mem[q], s->mem[q], n);
-        if (rc != SEIDART_OK) return rc;
+        const void* src = s->mem[q];
+        if (s->family == SEIDART_SEISMIC3 && s->precision == SEIDART_FP32 && s->s3f.mem_merged && q < 36) {
+            if (!tmp && cudaMalloc((void**)&tmp, n * sizeof(float)) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(SEIDART_ERR_NOMEM, "no device memory to rebuild the C-PML memories");
+            }
+            s3_unmerge<<<4 * 152, 256, 0, s->stream>>>(s->s3f, q, tmp);
+            src = tmp;
+        }
+        const int rc = s->precision == SEIDART_FP32 ? download<float>(*s, mem[q], src, n)
+                                                    : download<double>(*s, mem[q], src, n);
+        if (rc != SEIDART_OK) {
+            if (tmp) cudaFree(tmp);
+            return rc;
+        }
     }
+    if (tmp) cudaFree(tmp);
     return SEIDART_OK;
 }
 

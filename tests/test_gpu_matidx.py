@@ -1,9 +1,17 @@
-"""Material-indexed coefficients of the FP32 3D stress kernel: a model whose
-21 C_ij and 6 attenuation arrays hold few distinct tuples (layers, or any
-model expanded from a material image) runs with one byte per cell and a
-table of FP32 tuples; fields, memories, traces and norms equal the per-cell
-layout (SEIDART_S3_MATIDX=0) bit for bit.  A model with a distinct tuple per
-cell, or more than 32 tuples, keeps the per-cell layout."""
+"""Layouts of the FP32 3D stress kernel that change what it reads, not what
+it computes.
+
+Material-indexed coefficients: a model whose 21 C_ij and 6 attenuation
+arrays hold few distinct tuples (layers, or any model expanded from a
+material image) runs with one byte per cell and a table of FP32 tuples;
+fields, memories, traces and norms equal the per-cell layout
+(SEIDART_S3_MATIDX=0) bit for bit.  A model with a distinct tuple per cell,
+or more than 32 tuples, keeps the per-cell layout.
+
+Merged C-PML memories: the stress loops' 36 memories held as 21 (the loops
+that share a derivative stencil and its coefficients share the memory);
+the results and the 36 memories rebuilt on read-back equal the 36-array
+layout (SEIDART_S3_MERGE=0) bit for bit."""
 import dataclasses
 
 import numpy as np
@@ -15,8 +23,9 @@ from seidart_gpu import models
 pytestmark = pytest.mark.gpu
 
 
-def _run(p, indexed, monkeypatch, memory=True):
+def _run(p, indexed, monkeypatch, memory=True, merged=True):
     monkeypatch.setenv("SEIDART_S3_MATIDX", "1" if indexed else "0")
+    monkeypatch.setenv("SEIDART_S3_MERGE", "1" if merged else "0")
     with sg.Solver(p, sg.FP32) as s:
         nmat = s.material_count()
         s.step(p.time_steps)
@@ -82,3 +91,16 @@ def test_full_size_indexed_matches_per_cell(monkeypatch):
     base = _run(p, False, monkeypatch, memory=False)
     assert got["nmat"] == 5
     _same(got, base, memory=False)
+
+
+@pytest.mark.parametrize("indexed", [True, False])
+def test_merged_memories_equal_the_36_array_layout(indexed, monkeypatch):
+    """A grid small enough that every cell is a C-PML cell near some face, a
+    stress source, and all four loops' boundary rows: fields, traces, norms
+    and the 36 stress-loop memories (rebuilt from the 21 merged ones)."""
+    p = models.seismic3_layers(n=24, cpml=8, nt=40, nlayers=2, nrec_side=4, rec_z=3, src_z=6)
+    p = dataclasses.replace(p, src={"xx": 1e6 * p.src["z"], "yz": -5e5 * p.src["z"], "z": p.src["z"]})
+    got = _run(p, indexed, monkeypatch, merged=True)
+    base = _run(p, indexed, monkeypatch, merged=False)
+    _same(got, base)
+    assert max(np.max(np.abs(m)) for m in base["memory"][:36]) > 0
