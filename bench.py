@@ -140,20 +140,23 @@ def make_problem(nt=None):
 # launch's algorithmic bytes; the bench scales it to its own launch by the
 # algorithmic bytes.
 TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.153,
-                 "s3x_stress/indexed": 1.118}
+                 "s3x_stress/indexed-merged": 1.088}
 
 
-def kernel_bytes(p, box_cells: int, indexed: bool = False) -> dict:
+def kernel_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36) -> dict:
     """Algorithmic bytes per launch (FP32): every array the kernel must touch,
     read or written once; CPML memories and coefficients only on the CPML
     shell (outside the inert interior box).  `indexed`: the stress kernel
     reads the material-indexed layout -- one byte per cell instead of the
-    21 C_ij and 6 attenuation factors (the table of tuples is a few KB)."""
+    21 C_ij and 6 attenuation factors (the table of tuples is a few KB).
+    `mems`: stress-loop memories it advances (36, or 21 when the loops that
+    share a derivative stencil and its coefficients share the memory)."""
     n = p.ncell
     shell = n - box_cells
-    stress = WORD * (42 * n + 78 * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12; shell: 36 memories R+W + 6 coefficients
+    sh = 2 * mems + 6  # shell: memories R+W + 6 C-PML coefficients
+    stress = WORD * (42 * n + sh * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12
     if indexed:
-        stress = WORD * (15 * n + 78 * shell) + n  # v 3 + sigma R+W 12 + one material byte
+        stress = WORD * (15 * n + sh * shell) + n  # v 3 + sigma R+W 12 + one material byte
     velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
     # the fused step does both half-steps: the whole step's algorithmic bytes
     return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3p_velocity": velocity,
@@ -162,16 +165,18 @@ def kernel_bytes(p, box_cells: int, indexed: bool = False) -> dict:
             "s3w_step": step_bytes(p, box_cells)}
 
 
-def step_bytes(p, box_cells: int, indexed: bool = False) -> int:
+def step_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36) -> int:
     """Per-step algorithmic bytes of the whole leapfrog step: 9 fields read and
     written once, 21 C_ij + rho + 6 gamma read once (46 words), plus 45
     memories R+W and 6 CPML coefficients on shell cells (96 words).
     `indexed`: one material byte per cell in place of the 27 coefficient
-    words (19 words + 1 byte per cell)."""
+    words (19 words + 1 byte per cell); `mems` = 21: the stress loops' 36
+    memories held as 21 (30 memories R+W + 6 coefficients = 66 words)."""
     shell = p.ncell - box_cells
+    sh = 2 * (mems + 9) + 6
     if indexed:
-        return WORD * (19 * p.ncell + 96 * shell) + p.ncell
-    return WORD * (46 * p.ncell + 96 * shell)
+        return WORD * (19 * p.ncell + sh * shell) + p.ncell
+    return WORD * (46 * p.ncell + sh * shell)
 
 
 def interior_box_cells(p) -> int:
@@ -711,6 +716,7 @@ def main():
     stream = torch.cuda.Stream()
     s = sg.Solver(p, sg.FP32)
     nmat = s.material_count()  # > 0: the stress kernel reads the material-indexed layout
+    mems = s.stress_memory_arrays()  # 21: merged stress-loop memories
     s.set_stream(stream.cuda_stream)
     s.step(args.warmup)
     s.sync()
@@ -732,13 +738,15 @@ def main():
         ms_total = float(t.item())
     value = world * p.ncell * args.steps / (ms_total / 1e3) / 1e9
     hbm, peak_kind = peaks()
-    kb = kernel_bytes(p, box_cells, indexed=nmat > 0)
+    kb = kernel_bytes(p, box_cells, indexed=nmat > 0, mems=mems)
     kernels = prof["kernels"]
     dom = max((k for k in kernels if k in kb), key=lambda k: kernels[k]["ms"])
     avg_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
     achieved = kb[dom] / (avg_ms / 1e3) / 1e9
-    traffic_key = dom + "/indexed" if nmat > 0 and dom == "s3x_stress" else dom
-    sb = step_bytes(p, box_cells, indexed=nmat > 0)
+    # the capture behind each ratio was of the layout the default solver ran
+    # then; a layout without one reports no traffic figure
+    traffic_key = dom if (nmat == 0 and mems == 36) or dom != "s3x_stress" else dom + "/indexed-merged"
+    sb = step_bytes(p, box_cells, indexed=nmat > 0, mems=mems)
     step_gbs = sb * args.steps / (ms_total / 1e3) / 1e9
     launches = sum(v["launches"] for v in kernels.values())
     s.close()
@@ -822,10 +830,13 @@ def main():
         extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
         extra["fp32_speedup_vs_fp64_fast"] = value / world / extra["fp64_fast"]["value"]
 
-    if nmat > 0 and rank == 0:
-        # the same steps with the per-cell coefficient arrays (27 words per
-        # cell instead of one material byte), on the per-cell byte count
+    if (nmat > 0 or mems == 21) and rank == 0:
+        # the same steps on the reference's data layout -- per-cell
+        # coefficient arrays (27 words per cell instead of one material
+        # byte) and all 36 stress-loop memories -- on that layout's count
+        keep = {k: os.environ.get(k) for k in ("SEIDART_S3_MATIDX", "SEIDART_S3_MERGE")}
         os.environ["SEIDART_S3_MATIDX"] = "0"
+        os.environ["SEIDART_S3_MERGE"] = "0"
         try:
             sp = sg.Solver(p, sg.FP32)
             sp.step(args.warmup)
@@ -834,14 +845,19 @@ def main():
             sp.sync()
             sp.close()
         finally:
-            del os.environ["SEIDART_S3_MATIDX"]
+            for k, v in keep.items():
+                if v is None:
+                    del os.environ[k]
+                else:
+                    os.environ[k] = v
         msp = prp["total_ms"] / args.steps
         sbp = step_bytes(p, box_cells)
         extra["per_cell_layout"] = {
             "value": p.ncell / (msp / 1e3) / 1e9, "unit": UNIT, "ms_per_step": msp,
             "step_roofline": {"frac": sbp / (msp / 1e3) / 1e9 / hbm, "bytes_per_step": sbp},
             "kernels_ms": {k: v["ms"] / v["launches"] for k, v in prp["kernels"].items()},
-            "note": "the staged stress kernel reading the 21 C_ij and 6 attenuation arrays per cell"}
+            "note": "the staged stress kernel reading the 21 C_ij and 6 attenuation arrays per cell and "
+                    "advancing all 36 stress-loop memories"}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
@@ -873,15 +889,16 @@ def main():
                          "traffic": TRAFFIC_RATIO[traffic_key] * kb[dom] if traffic_key in TRAFFIC_RATIO else None,
                          "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
                          "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms,
-                         "bytes_basis": ("the layout the kernel reads: material-indexed (15 words + 1 byte per "
-                                         "cell, 78 words per shell cell); with per-cell coefficient arrays (42 + 78 "
-                                         f"words) a launch moves {kernel_bytes(p, box_cells)[dom] / 1e9:.2f} GB")
-                         if nmat > 0 and dom == "s3x_stress" else "per-cell coefficient arrays"},
+                         "bytes_basis": (f"the layout the kernel reads: {'material-indexed (15 words + 1 byte' if nmat > 0 else 'per-cell coefficient arrays (42 words'} per cell), "
+                                         f"{mems} stress-loop memories ({2 * mems + 6} words per shell cell); the "
+                                         "reference's layout (42 + 78 words) is "
+                                         f"{kernel_bytes(p, box_cells)[dom] / 1e9:.2f} GB per launch")
+                         if dom == "s3x_stress" else "per-cell arrays"},
             "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb,
-                              "bytes_basis": ("material-indexed: 19 words + 1 byte per cell, 96 words per shell "
-                                              f"cell; per-cell arrays: {step_bytes(p, box_cells) / 1e9:.2f} GB per step")
-                              if nmat > 0 else "per-cell arrays: 46 words per cell, 96 per shell cell"},
-            "model_layout": {"materials": nmat,
+                              "bytes_basis": (f"{'material-indexed: 19 words + 1 byte' if nmat > 0 else 'per-cell arrays: 46 words'} per cell, "
+                                              f"{2 * (mems + 9) + 6} words per shell cell; the reference's layout "
+                                              f"(46 + 96 words): {step_bytes(p, box_cells) / 1e9:.2f} GB per step")},
+            "model_layout": {"materials": nmat, "stress_memory_arrays": mems,
                              "stress_coefficients": ("material-indexed: one byte per cell and a table of "
                                                      f"{nmat} FP32 (C_ij, gamma) tuples")
                              if nmat > 0 else "per-cell arrays (21 C_ij + 6 attenuation factors)"},

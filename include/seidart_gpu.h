@@ -245,6 +245,12 @@ int seidart_solver_steps_done(const SeidartSolver* s);
  * 0 = per-cell arrays (too many tuples, nx not a multiple of 4, another
  * family or precision, or SEIDART_S3_MATIDX=0). */
 int seidart_solver_material_count(const SeidartSolver* s);
+/* Stress-loop C-PML memory arrays a seismic3 solver advances: 21 when the
+ * FP32 staged stress kernel shares one memory between the two loops that
+ * apply the same derivative stencil with the same coefficients (the default;
+ * SEIDART_S3_MERGE=0 keeps 36), else 36; 0 for other families.
+ * seidart_solver_get_memory returns the reference's 36 either way. */
+int seidart_solver_stress_memory_arrays(const SeidartSolver* s);
 /* Device pointer of field slot `slot` (FP64 or FP32 per precision). */
 void* seidart_solver_field_ptr(SeidartSolver* s, int slot);
 /* Advance nsteps steps launching kernels one by one (no CUDA graph) with a

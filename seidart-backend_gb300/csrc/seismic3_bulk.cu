@@ -85,7 +85,13 @@ __device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, i
     }
     pf_tile_rows(A.f, 9, tx, ty, k, A.nx, A.ny, tid, NT);
     if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {
-        pf_tile_rows(A.mem, 36, tx, ty, k, A.nx, A.ny, tid, NT);
+        if (A.mem_merged) {
+            // the 21 memories the merged layout advances: slots 0..17, 20, 23, 26
+            pf_tile_rows(A.mem, 18, tx, ty, k, A.nx, A.ny, tid, NT);
+            for (int f = 0; f < 3; ++f) pf_tile_rows(A.mem + 20 + 3 * f, 1, tx, ty, k, A.nx, A.ny, tid, NT);
+        } else {
+            pf_tile_rows(A.mem, 36, tx, ty, k, A.nx, A.ny, tid, NT);
+        }
         pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, NT);
     }
 }

@@ -1286,6 +1286,12 @@ int seidart_solver_steps_done(const SeidartSolver* s) { return s ? s->steps_done
 
 int seidart_solver_material_count(const SeidartSolver* s) { return s ? s->s3_nmat : -1; }
 
+int seidart_solver_stress_memory_arrays(const SeidartSolver* s) {
+    if (!s) return -1;
+    if (s->family != SEIDART_SEISMIC3) return 0;
+    return (s->precision == SEIDART_FP32 && s->s3f.mem_merged) ? 21 : 36;
+}
+
 int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex, int* is_fp32,
                                    size_t* ncell, void** stream) {
     if (!s || slot < 0 || slot >= (int)s->fields.size()) return set_err(SEIDART_ERR_ARG, "bad field slot");

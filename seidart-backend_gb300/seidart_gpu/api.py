@@ -288,6 +288,11 @@ class Solver:
         the per-cell arrays are used)."""
         return lib().seidart_solver_material_count(self.handle)
 
+    def stress_memory_arrays(self) -> int:
+        """Stress-loop C-PML memory arrays a seismic3 solver advances (21
+        merged or 36); get_memory returns the 36 either way."""
+        return lib().seidart_solver_stress_memory_arrays(self.handle)
+
     @property
     def launches(self) -> int:
         return lib().seidart_solver_launches(self.handle)
