@@ -143,21 +143,25 @@ TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146
                  "s3x_stress/indexed-merged": 1.088}
 
 
-def kernel_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36) -> dict:
+def kernel_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36, cpmlidx: bool = False) -> dict:
     """Algorithmic bytes per launch (FP32): every array the kernel must touch,
     read or written once; CPML memories and coefficients only on the CPML
     shell (outside the inert interior box).  `indexed`: the stress kernel
     reads the material-indexed layout -- one byte per cell instead of the
     21 C_ij and 6 attenuation factors (the table of tuples is a few KB).
     `mems`: stress-loop memories it advances (36, or 21 when the loops that
-    share a derivative stencil and its coefficients share the memory)."""
+    share a derivative stencil and its coefficients share the memory).
+    `cpmlidx`: shell cells read one C-PML byte instead of the six C-PML
+    coefficient grids."""
     n = p.ncell
     shell = n - box_cells
-    sh = 2 * mems + 6  # shell: memories R+W + 6 C-PML coefficients
-    stress = WORD * (42 * n + sh * shell)   # v 3 + C 21 + gamma 6 + sigma R+W 12
+    cp_w, cp_b = (0, 1) if cpmlidx else (6, 0)  # C-PML coefficients per shell cell: words, bytes
+    sh = 2 * mems + cp_w  # shell: memories R+W + the C-PML coefficients
+    stress = WORD * (42 * n + sh * shell) + cp_b * shell   # v 3 + C 21 + gamma 6 + sigma R+W 12
     if indexed:
-        stress = WORD * (15 * n + sh * shell) + n  # v 3 + sigma R+W 12 + one material byte
-    velocity = WORD * (13 * n + 24 * shell)  # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + 6 coefficients
+        stress = WORD * (15 * n + sh * shell) + n + cp_b * shell  # v 3 + sigma R+W 12 + one material byte
+    # sigma 6 + rho 1 + v R+W 6; shell: 9 memories R+W + the C-PML coefficients
+    velocity = WORD * (13 * n + (18 + cp_w) * shell) + cp_b * shell
     # the fused step does both half-steps: the whole step's algorithmic bytes
     return {"s3c_stress": stress, "s3c_velocity": velocity, "s3x_velocity": velocity, "s3p_velocity": velocity,
             "s3f_stress": stress, "s3f_velocity": velocity,
@@ -165,18 +169,21 @@ def kernel_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36) -> di
             "s3w_step": step_bytes(p, box_cells)}
 
 
-def step_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36) -> int:
+def step_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36, cpmlidx: bool = False) -> int:
     """Per-step algorithmic bytes of the whole leapfrog step: 9 fields read and
     written once, 21 C_ij + rho + 6 gamma read once (46 words), plus 45
     memories R+W and 6 CPML coefficients on shell cells (96 words).
     `indexed`: one material byte per cell in place of the 27 coefficient
     words (19 words + 1 byte per cell); `mems` = 21: the stress loops' 36
-    memories held as 21 (30 memories R+W + 6 coefficients = 66 words)."""
+    memories held as 21 (30 memories R+W + 6 coefficients = 66 words);
+    `cpmlidx`: one C-PML byte per shell cell instead of the six coefficient
+    words."""
     shell = p.ncell - box_cells
-    sh = 2 * (mems + 9) + 6
+    sh = 2 * (mems + 9) + (0 if cpmlidx else 6)
+    extra = shell if cpmlidx else 0
     if indexed:
-        return WORD * (19 * p.ncell + sh * shell) + p.ncell
-    return WORD * (46 * p.ncell + sh * shell)
+        return WORD * (19 * p.ncell + sh * shell) + p.ncell + extra
+    return WORD * (46 * p.ncell + sh * shell) + extra
 
 
 def interior_box_cells(p) -> int:
@@ -717,6 +724,7 @@ def main():
     s = sg.Solver(p, sg.FP32)
     nmat = s.material_count()  # > 0: the stress kernel reads the material-indexed layout
     mems = s.stress_memory_arrays()  # 21: merged stress-loop memories
+    ncpml = s.cpml_tuples()  # > 0: indexed C-PML coefficients
     s.set_stream(stream.cuda_stream)
     s.step(args.warmup)
     s.sync()
@@ -738,15 +746,16 @@ def main():
         ms_total = float(t.item())
     value = world * p.ncell * args.steps / (ms_total / 1e3) / 1e9
     hbm, peak_kind = peaks()
-    kb = kernel_bytes(p, box_cells, indexed=nmat > 0, mems=mems)
+    kb = kernel_bytes(p, box_cells, indexed=nmat > 0, mems=mems, cpmlidx=ncpml > 0)
     kernels = prof["kernels"]
     dom = max((k for k in kernels if k in kb), key=lambda k: kernels[k]["ms"])
     avg_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
     achieved = kb[dom] / (avg_ms / 1e3) / 1e9
     # the capture behind each ratio was of the layout the default solver ran
     # then; a layout without one reports no traffic figure
-    traffic_key = dom if (nmat == 0 and mems == 36) or dom != "s3x_stress" else dom + "/indexed-merged"
-    sb = step_bytes(p, box_cells, indexed=nmat > 0, mems=mems)
+    traffic_key = (dom if (nmat == 0 and mems == 36 and ncpml == 0) or dom != "s3x_stress"
+                   else dom + "/indexed-merged" + ("-cpml" if ncpml > 0 else ""))
+    sb = step_bytes(p, box_cells, indexed=nmat > 0, mems=mems, cpmlidx=ncpml > 0)
     step_gbs = sb * args.steps / (ms_total / 1e3) / 1e9
     launches = sum(v["launches"] for v in kernels.values())
     s.close()
@@ -830,13 +839,13 @@ def main():
         extra["fp32_speedup_vs_fp64"] = value / world / extra["fp64_plain"]["value"]
         extra["fp32_speedup_vs_fp64_fast"] = value / world / extra["fp64_fast"]["value"]
 
-    if (nmat > 0 or mems == 21) and rank == 0:
+    if (nmat > 0 or mems == 21 or ncpml > 0) and rank == 0:
         # the same steps on the reference's data layout -- per-cell
         # coefficient arrays (27 words per cell instead of one material
         # byte) and all 36 stress-loop memories -- on that layout's count
-        keep = {k: os.environ.get(k) for k in ("SEIDART_S3_MATIDX", "SEIDART_S3_MERGE")}
-        os.environ["SEIDART_S3_MATIDX"] = "0"
-        os.environ["SEIDART_S3_MERGE"] = "0"
+        keep = {k: os.environ.get(k) for k in ("SEIDART_S3_MATIDX", "SEIDART_S3_MERGE", "SEIDART_S3_CPMLIDX")}
+        for k in keep:
+            os.environ[k] = "0"
         try:
             sp = sg.Solver(p, sg.FP32)
             sp.step(args.warmup)
@@ -890,15 +899,15 @@ def main():
                          "traffic_source": "ncu dram__bytes_read+write of the 224^3 case, scaled by algorithmic bytes",
                          "algorithmic_bytes_per_launch": kb[dom], "avg_launch_ms": avg_ms,
                          "bytes_basis": (f"the layout the kernel reads: {'material-indexed (15 words + 1 byte' if nmat > 0 else 'per-cell coefficient arrays (42 words'} per cell), "
-                                         f"{mems} stress-loop memories ({2 * mems + 6} words per shell cell); the "
+                                         f"{mems} stress-loop memories and {'one C-PML byte' if ncpml > 0 else 'six C-PML words'} per shell cell; the "
                                          "reference's layout (42 + 78 words) is "
                                          f"{kernel_bytes(p, box_cells)[dom] / 1e9:.2f} GB per launch")
                          if dom == "s3x_stress" else "per-cell arrays"},
             "step_roofline": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_step": sb,
                               "bytes_basis": (f"{'material-indexed: 19 words + 1 byte' if nmat > 0 else 'per-cell arrays: 46 words'} per cell, "
-                                              f"{2 * (mems + 9) + 6} words per shell cell; the reference's layout "
+                                              f"{2 * (mems + 9) + (0 if ncpml > 0 else 6)} words{' + 1 byte' if ncpml > 0 else ''} per shell cell; the reference's layout "
                                               f"(46 + 96 words): {step_bytes(p, box_cells) / 1e9:.2f} GB per step")},
-            "model_layout": {"materials": nmat, "stress_memory_arrays": mems,
+            "model_layout": {"materials": nmat, "stress_memory_arrays": mems, "cpml_tuples": ncpml,
                              "stress_coefficients": ("material-indexed: one byte per cell and a table of "
                                                      f"{nmat} FP32 (C_ij, gamma) tuples")
                              if nmat > 0 else "per-cell arrays (21 C_ij + 6 attenuation factors)"},

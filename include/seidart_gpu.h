@@ -251,6 +251,13 @@ int seidart_solver_material_count(const SeidartSolver* s);
  * SEIDART_S3_MERGE=0 keeps 36), else 36; 0 for other families.
  * seidart_solver_get_memory returns the reference's 36 either way. */
 int seidart_solver_stress_memory_arrays(const SeidartSolver* s);
+/* Tuples of an FP32 seismic3 solver's indexed C-PML coefficients: when the
+ * six C-PML grids hold at most 64 distinct tuples (grids built from 1D
+ * damping profiles do), the stress and velocity kernels read one byte per
+ * cell and a table instead of six grids, with the same FP32 values.  0 =
+ * the grids (too many tuples, nx not a multiple of 4, or
+ * SEIDART_S3_CPMLIDX=0). */
+int seidart_solver_cpml_tuples(const SeidartSolver* s);
 /* Device pointer of field slot `slot` (FP64 or FP32 per precision). */
 void* seidart_solver_field_ptr(SeidartSolver* s, int slot);
 /* Advance nsteps steps launching kernels one by one (no CUDA graph) with a

@@ -251,10 +251,16 @@ struct S3Args {
     const unsigned char* mat_ids;
     const float* mat_tab;
     int mat_tab_bytes;     // bytes of mat_tab a tile copies (a multiple of 16)
+    // indexed C-PML coefficients (FP32 staged stress and pair velocity
+    // kernels): one byte per cell, tile-packed like mat_ids, and a
+    // [S3_MAXCPML][6] table of the six grids' values; NULL = per-cell grids
+    const unsigned char* cpml_ids;
+    const float* cpml_tab;
     int mem_merged;        // FP32 staged stress kernel: 1 = the 36 stress-loop C-PML memories held as 21
                            // (derivatives two loops share advance one memory; slots 0..17 and 20, 23, 26)
 };
 constexpr int S3_MAXMAT = 32;
+constexpr int S3_MAXCPML = 64;  // C-PML coefficient tuples of the indexed C-PML layout
 // The material index of an FP32 3D solver's coefficient arrays, found on the
 // device (matidx.cu): on success the tile-packed material bytes and the
 // [S3_MAXMAT][27] FP32 table (both cudaMalloc'd, the caller frees them) and
@@ -262,6 +268,11 @@ constexpr int S3_MAXMAT = 32;
 // S3_MAXMAT distinct tuples (or on an allocation failure).
 int seismic3_material_index(const S3Args<float>& a, int nx, int ny, int nz, unsigned char** ids, float** tab,
                             int* nmat, cudaStream_t st);
+// The same for the six C-PML coefficient grids (1/kappa, 1/kappa_half, a,
+// a_half, b, b_half as stored for FP32): tile-packed bytes and a
+// [S3_MAXCPML][6] table, 0 when they hold more than S3_MAXCPML tuples.
+int seismic3_cpml_index(const S3Args<float>& a, int nx, int ny, int nz, unsigned char** ids, float** tab, int* ntup,
+                        cudaStream_t st);
 // The same for the nine stress coefficients of an FP32 seismic2 model
 // (c11 c13 c15 c33 c35 c55 and the three attenuation factors, in that order
 // in `coef`): one byte per cell in grid order and a [S3_MAXMAT][9] table.

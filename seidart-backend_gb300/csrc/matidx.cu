@@ -30,14 +30,14 @@
 
 namespace {
 
-constexpr int NSLOT = 64;
+constexpr int NSLOT = 128;
 
 struct HashTable {
     unsigned long long key[NSLOT];  // 0 = empty
     unsigned long long rep[NSLOT];  // smallest cell holding the tuple
     int count;                      // claimed slots
     int collision;                  // a cell's tuple differs from its slot's representative
-    int slot_id[NSLOT];             // material number of each claimed slot (set by the host)
+    int slot_id[NSLOT];             // tuple number of each claimed slot (set by the host)
 };
 
 // the coefficient arrays of one model (27 for seismic3, 9 for seismic2)
@@ -133,9 +133,9 @@ namespace {
 // Hash, number, assign and tabulate (steps 1-4 above).  tiled: the 3D
 // tile-packed byte layout on an nx x ny x nz grid; else one byte per cell in
 // grid order.  Returns the number of materials, 0 when they are more than
-// S3_MAXMAT (or on an allocation failure).
+// max_tuples (or on an allocation failure).
 int build_index(const Arr& A, size_t ncell, bool tiled, int nx, int ny, int nz, unsigned char** ids_out,
-                float** tab_out, cudaStream_t st) {
+                float** tab_out, cudaStream_t st, int max_tuples = S3_MAXMAT) {
     *ids_out = nullptr;
     *tab_out = nullptr;
     HashTable* T = nullptr;
@@ -157,7 +157,7 @@ int build_index(const Arr& A, size_t ncell, bool tiled, int nx, int ny, int nz, 
     if (cudaMemcpyAsync(&h, T, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return fail(true);
-    if (h.count < 1 || h.count > S3_MAXMAT) return fail(false);
+    if (h.count < 1 || h.count > max_tuples) return fail(false);
     // number the tuples by their first cell
     std::vector<std::pair<unsigned long long, int>> order;
     for (int s = 0; s < NSLOT; ++s)
@@ -171,8 +171,8 @@ int build_index(const Arr& A, size_t ncell, bool tiled, int nx, int ny, int nz, 
     int* dev_collision = (int*)((char*)T + offsetof(HashTable, collision));
     if (cudaMemcpyAsync(dev_slot_id, h.slot_id, sizeof h.slot_id, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMalloc((void**)&ids, nbytes) != cudaSuccess ||
-        cudaMalloc((void**)&tab, sizeof(float) * S3_MAXMAT * A.n) != cudaSuccess ||
-        cudaMemsetAsync(tab, 0, sizeof(float) * S3_MAXMAT * A.n, st) != cudaSuccess)
+        cudaMalloc((void**)&tab, sizeof(float) * max_tuples * A.n) != cudaSuccess ||
+        cudaMemsetAsync(tab, 0, sizeof(float) * max_tuples * A.n, st) != cudaSuccess)
         return fail(true);
     if (tiled) matidx_assign_tiled<<<dim3(gx, gy, nz), dim3(32, 8), 0, st>>>(A, nx, ny, nz, T, ids);
     else matidx_assign_linear<<<4 * 152, 256, 0, st>>>(A, ncell, T, ids);
@@ -207,4 +207,13 @@ int seismic2_material_index(const float* const* coef, size_t ncell, unsigned cha
     A.n = 9;
     *nmat_out = build_index(A, ncell, false, 0, 0, 0, ids_out, tab_out, st);
     return *nmat_out;
+}
+
+int seismic3_cpml_index(const S3Args<float>& a, int nx, int ny, int nz, unsigned char** ids_out, float** tab_out,
+                        int* ntup_out, cudaStream_t st) {
+    Arr A{};
+    for (int q = 0; q < 6; ++q) A.p[q] = a.cpml[q];
+    A.n = 6;
+    *ntup_out = build_index(A, (size_t)nx * ny * nz, true, nx, ny, nz, ids_out, tab_out, st, S3_MAXCPML);
+    return *ntup_out;
 }

@@ -36,6 +36,24 @@ struct CpmlPair {
 __device__ __forceinline__ CpmlPair cpml_both(const S3Args<float>& A, size_t c) {
     return CpmlPair{cpml_at(A, c, true), cpml_at(A, c, false)};
 }
+// place of cell (x, y, k) in the tile-packed byte layouts: tile (x/32, y/8,
+// k) of the 32 x 8 tile grid, then (y % 8) * 32 + x % 32 within the tile
+__device__ __forceinline__ size_t tile_byte(int nx, int ny, int x, int y, int k) {
+    const int gx = (nx + 31) >> 5, gy = (ny + 7) >> 3;
+    return (((size_t)k * gy + (y >> 3)) * gx + (x >> 5)) * 256 + ((y & 7) << 5) + (x & 31);
+}
+// both C-PML coefficient triples of cell c = (x, y, k): from the indexed
+// table when the solver found one (the same FP32 values), else the grids
+__device__ __forceinline__ CpmlPair cpml_pair_at(const S3Args<float>& A, size_t c, int x, int y, int k) {
+    if (A.cpml_ids) {
+        const float* T = A.cpml_tab + 6 * __ldg(A.cpml_ids + tile_byte(A.nx, A.ny, x, y, k));
+        return CpmlPair{CpmlC{__ldg(T + 5), __ldg(T + 3), __ldg(T + 1)}, CpmlC{__ldg(T + 4), __ldg(T + 2), __ldg(T)}};
+    }
+    return cpml_both(A, c);
+}
+// L2 prefetch of the C-PML coefficients of tile (tx, ty, k) of the 32 x 8
+// grid: its 256 index bytes, or the six grids' rows
+__device__ __forceinline__ void pf_cpml_tile(const S3Args<float>& A, int tx, int ty, int k, int tid, int nthreads);
 template <int L>
 __device__ __forceinline__ void cpml_load(const S3Args<float>& A, size_t c, float (&m)[9]) {
     float* const* M = A.mem + 9 * (L - 1);
@@ -184,6 +202,15 @@ __device__ __forceinline__ void pf_tile_rows(const float* const* arr, int narr, 
         const float* row = arr[q >> 3] + ((size_t)k * ny + y) * nx;
         pf_l2(row + x0);
         pf_l2(row + x1);
+    }
+}
+
+__device__ __forceinline__ void pf_cpml_tile(const S3Args<float>& A, int tx, int ty, int k, int tid, int nthreads) {
+    if (A.cpml_ids) {
+        const int gx = (A.nx + 31) >> 5, gy = (A.ny + 7) >> 3;
+        if (tid < 2) pf_l2(A.cpml_ids + (((size_t)k * gy + ty) * gx + tx) * 256 + tid * 128);
+    } else {
+        pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, nthreads);
     }
 }
 

@@ -67,8 +67,9 @@ __device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, in
     CpmlC ph{0.f, 0.f, 0.f}, pf{0.f, 0.f, 0.f};
     float m[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (pml) {
-        ph = cpml_at(A, c, true);
-        pf = cpml_at(A, c, false);
+        const CpmlPair P = cpml_pair_at(A, c, gx, gy, k);
+        ph = P.h;
+        pf = P.f;
 #pragma unroll
         for (int q = 0; q < 9; ++q) m[q] = A.mem[36 + q][c];
     }

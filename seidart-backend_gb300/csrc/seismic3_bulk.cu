@@ -92,7 +92,7 @@ __device__ __forceinline__ void s3b_prefetch(const S3Args<float>& A, int dist, i
         } else {
             pf_tile_rows(A.mem, 36, tx, ty, k, A.nx, A.ny, tid, NT);
         }
-        pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, NT);
+        pf_cpml_tile(A, tx, ty, k, tid, NT);
     }
 }
 
@@ -299,7 +299,7 @@ __device__ __forceinline__ void staged_tile(const S3Args<float>& A, const float*
     CpmlPair P{};
     float ma[9], mb[9], mz[3];
     if (pml) {
-        P = cpml_both(A, c);
+        P = cpml_pair_at(A, c, gx, gy, k);
         if (MERGED) {
 #pragma unroll
             for (int q = 0; q < 9; ++q) {

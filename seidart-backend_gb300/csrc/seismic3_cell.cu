@@ -117,7 +117,7 @@ __device__ __forceinline__ void s3c_velocity_prefetch(const S3Args<float>& A, in
     pf_tile_rows(&A.rho, 1, tx, ty, k, A.nx, A.ny, tid, BX * BY);
     if (!tile_in_box(A.box, tx, ty, k, A.nx, A.ny)) {
         pf_tile_rows(A.mem + 36, 9, tx, ty, k, A.nx, A.ny, tid, BX * BY);
-        pf_tile_rows(A.cpml, 6, tx, ty, k, A.nx, A.ny, tid, BX * BY);
+        pf_cpml_tile(A, tx, ty, k, tid, BX * BY);
     }
 }
 
@@ -259,7 +259,7 @@ __device__ __forceinline__ void s3p_velocity_prefetch(const S3Args<float>& A, in
         pf_tile_rows(&A.rho, 1, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
         if (!tile_in_box(A.box, tx, ty8, k, A.nx, A.ny)) {
             pf_tile_rows(A.mem + 36, 9, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
-            pf_tile_rows(A.cpml, 6, tx, ty8, k, A.nx, A.ny, tid, PX * PY);
+            pf_cpml_tile(A, tx, ty8, k, tid, PX * PY);
         }
     }
 }

@@ -161,6 +161,9 @@ struct SeidartSolver {
     unsigned char* s3_mat_ids = nullptr;  // material-indexed model: one byte per cell, tile-packed
     float* s3_mat_tab = nullptr;          // and the [S3_MAXMAT][27] table of FP32 coefficient tuples
     int s3_nmat = 0;                      // materials of the indexed layout (0: per-cell arrays)
+    unsigned char* s3_cpml_ids = nullptr; // indexed C-PML coefficients: one byte per cell, tile-packed
+    float* s3_cpml_tab = nullptr;         // and the [S3_MAXCPML][6] table
+    int s3_ncpml = 0;                     // C-PML tuples of the indexed layout (0: the six grids)
     bool s3_tma = false;  // TMA-fed stress kernel prepared (grid meets the TMA rules)
     int s3_tma_variant = 0;
     S3Maps s3_maps;       // its tensor maps
@@ -1052,6 +1055,15 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.mat_tab = s->s3_mat_tab;
             s->s3f.mat_tab_bytes = (s->s3_nmat * 27 * (int)sizeof(float) + 15) / 16 * 16;
         }
+        // the six C-PML grids indexed the same way (a grid built from 1D
+        // profiles holds a few dozen tuples; SEIDART_S3_CPMLIDX=0 keeps them)
+        const char* ci = getenv("SEIDART_S3_CPMLIDX");
+        if (s->s3f.staged && !(ci && *ci == '0') &&
+            seismic3_cpml_index(s->s3f, s->dom.nx, s->dom.ny, s->dom.nz, &s->s3_cpml_ids, &s->s3_cpml_tab,
+                                &s->s3_ncpml, s->stream) > 0) {
+            s->s3f.cpml_ids = s->s3_cpml_ids;
+            s->s3f.cpml_tab = s->s3_cpml_tab;
+        }
 
         // staged velocity kernel: bit-identical but measured slower at 352^3
         // (1.55 ms against 1.19 ms), so only on request
@@ -1286,6 +1298,8 @@ int seidart_solver_steps_done(const SeidartSolver* s) { return s ? s->steps_done
 
 int seidart_solver_material_count(const SeidartSolver* s) { return s ? s->s3_nmat : -1; }
 
+int seidart_solver_cpml_tuples(const SeidartSolver* s) { return s ? s->s3_ncpml : -1; }
+
 int seidart_solver_stress_memory_arrays(const SeidartSolver* s) {
     if (!s) return -1;
     if (s->family != SEIDART_SEISMIC3) return 0;
@@ -1332,6 +1346,8 @@ int seidart_solver_destroy(SeidartSolver* s) {
     if (s->s3_packed) cudaFree(s->s3_packed);
     if (s->s3_mat_ids) cudaFree(s->s3_mat_ids);
     if (s->s3_mat_tab) cudaFree(s->s3_mat_tab);
+    if (s->s3_cpml_ids) cudaFree(s->s3_cpml_ids);
+    if (s->s3_cpml_tab) cudaFree(s->s3_cpml_tab);
     if (s->stage) cudaFree(s->stage);
     if (s->pin) cudaFreeHost(s->pin);
     for (int b = 0; b < 2; ++b)

@@ -77,6 +77,7 @@ _SIGS = {
     "seidart_solver_steps_done": (C.c_int, [C.c_void_p]),
     "seidart_solver_material_count": (C.c_int, [C.c_void_p]),
     "seidart_solver_stress_memory_arrays": (C.c_int, [C.c_void_p]),
+    "seidart_solver_cpml_tuples": (C.c_int, [C.c_void_p]),
     "seidart_solver_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_int]),
     "seidart_solver_field_ptr": (C.c_void_p, [C.c_void_p, C.c_int]),

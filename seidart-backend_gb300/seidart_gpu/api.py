@@ -293,6 +293,10 @@ class Solver:
         merged or 36); get_memory returns the 36 either way."""
         return lib().seidart_solver_stress_memory_arrays(self.handle)
 
+    def cpml_tuples(self) -> int:
+        """Tuples of the FP32 3D indexed C-PML coefficients (0: the grids)."""
+        return lib().seidart_solver_cpml_tuples(self.handle)
+
     @property
     def launches(self) -> int:
         return lib().seidart_solver_launches(self.handle)

@@ -11,7 +11,11 @@ or more than 32 tuples, keeps the per-cell layout.
 Merged C-PML memories: the stress loops' 36 memories held as 21 (the loops
 that share a derivative stencil and its coefficients share the memory);
 the results and the 36 memories rebuilt on read-back equal the 36-array
-layout (SEIDART_S3_MERGE=0) bit for bit."""
+layout (SEIDART_S3_MERGE=0) bit for bit.
+
+Indexed C-PML coefficients: the six C-PML grids read as one byte per cell
+and a table when they hold at most 64 tuples; bit for bit the grids
+(SEIDART_S3_CPMLIDX=0), which more tuples keep."""
 import dataclasses
 
 import numpy as np
@@ -23,15 +27,17 @@ from seidart_gpu import models
 pytestmark = pytest.mark.gpu
 
 
-def _run(p, indexed, monkeypatch, memory=True, merged=True):
+def _run(p, indexed, monkeypatch, memory=True, merged=True, cpmlidx=True):
     monkeypatch.setenv("SEIDART_S3_MATIDX", "1" if indexed else "0")
     monkeypatch.setenv("SEIDART_S3_MERGE", "1" if merged else "0")
+    monkeypatch.setenv("SEIDART_S3_CPMLIDX", "1" if cpmlidx else "0")
     with sg.Solver(p, sg.FP32) as s:
         nmat = s.material_count()
+        ncpml = s.cpml_tuples()
         s.step(p.time_steps)
         s.sync()
         tr, nrm = s.traces()
-        out = {"fields": s.get_fields(), "traces": tr, "norms": nrm, "nmat": nmat}
+        out = {"fields": s.get_fields(), "traces": tr, "norms": nrm, "nmat": nmat, "ncpml": ncpml}
         if memory:
             out["memory"] = s.get_memory()
         return out
@@ -104,3 +110,22 @@ def test_merged_memories_equal_the_36_array_layout(indexed, monkeypatch):
     base = _run(p, indexed, monkeypatch, merged=False)
     _same(got, base)
     assert max(np.max(np.abs(m)) for m in base["memory"][:36]) > 0
+
+
+def test_cpml_index_is_bit_identical(monkeypatch):
+    p = models.seismic3_layers(n=40, cpml=8, nt=40, nlayers=2, nrec_side=4, rec_z=3, src_z=6)
+    got = _run(p, True, monkeypatch, cpmlidx=True)
+    base = _run(p, True, monkeypatch, cpmlidx=False)
+    assert got["ncpml"] > 0 and base["ncpml"] == 0
+    _same(got, base)
+
+
+def test_many_cpml_tuples_keep_the_grids(monkeypatch):
+    p = models.seismic3_layers(n=40, cpml=8, nt=10, nlayers=2, nrec_side=4, rec_z=3, src_z=6)
+    rng = np.random.default_rng(3)
+    model = {k: v.copy() for k, v in p.model.items()}
+    a = model["acoef"]
+    model["acoef"] = np.asfortranarray(np.where(a != 0, a * (1.0 + 1e-3 * rng.random(a.shape)), a))
+    q = dataclasses.replace(p, model=model)
+    got = _run(q, True, monkeypatch, memory=False)
+    assert got["ncpml"] == 0
