@@ -140,7 +140,7 @@ def make_problem(nt=None):
 # launch's algorithmic bytes; the bench scales it to its own launch by the
 # algorithmic bytes.
 TRAFFIC_RATIO = {"s3x_stress": 1.081, "s3b_stress": 1.113, "s3c_velocity": 1.146, "s3p_velocity": 1.153,
-                 "s3x_stress/indexed-merged": 1.088}
+                 "s3x_stress/indexed-merged": 1.088, "s3x_stress/indexed-merged-cpml": 1.066}
 
 
 def kernel_bytes(p, box_cells: int, indexed: bool = False, mems: int = 36, cpmlidx: bool = False) -> dict:
