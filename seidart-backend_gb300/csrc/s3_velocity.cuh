@@ -22,7 +22,9 @@ __device__ __forceinline__ float ldv(const float* p) {
 // inside the inert interior box, at least two cells from every face and away
 // from the source cells, so every update applies, no index needs clamping and
 // no CPML, source or Dirichlet test is made.
-template <bool LEAN, int LD = LD_NC>
+// CODE: the density rule as a compile-time constant (1..4), or 0 to read
+// A.density_code at run time
+template <bool LEAN, int LD = LD_NC, int CODE = 0>
 __device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, int gx, int gy, int k, float& vsq,
                                               float& ssq, float (&w)[9]) {
     const int nx = A.nx, ny = A.ny, nz = A.nz;
@@ -55,7 +57,7 @@ __device__ __forceinline__ void velocity_cell(const S3Args<float>& A, int it, in
     float vx = A.f[0][c], vy = A.f[1][c], vz = A.f[2][c];
     const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
     const float dt = A.dt;
-    const int code = A.density_code;
+    const int code = CODE ? CODE : A.density_code;
     const bool pml = !LEAN && !(A.box.i0 <= gx && gx < A.box.i1 && A.box.j0 <= gy && gy < A.box.j1 && A.box.k0 <= k &&
                                 k < A.box.k1);
     const bool ux = LEAN || (gx >= 2 && gx <= nx - 2 && gy >= 2 && gy <= ny - 2 && k >= 2 && k <= nz - 2);

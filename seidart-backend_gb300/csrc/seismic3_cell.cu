@@ -196,6 +196,7 @@ __device__ __forceinline__ void vel_lean_cell(float sxx0, float sxxm1, float sxx
     ssq = sxx0 * sxx0 + syy0 * syy0 + szz0 * szz0 + 2.0f * (sxy0 * sxy0 + syz0 * syz0 + sxz0 * sxz0);
 }
 
+template <int CODE = 0>
 __device__ __forceinline__ void velocity_pair_lean(const S3Args<float>& A, int gx, int gy, int k, float& vsq,
                                                    float& ssq) {
     const long sy = A.nx, sz = (long)A.nx * A.ny;
@@ -216,7 +217,7 @@ __device__ __forceinline__ void velocity_pair_lean(const S3Args<float>& A, int g
     float2 vx = *V0, vy = *V1, vz = *V2;
     const float hx = 1.0f / (24.0f * A.dx), hy = 1.0f / (24.0f * A.dy), hz = 1.0f / (24.0f * A.dz);
     const float dt = A.dt;
-    const int code = A.density_code;
+    const int code = CODE ? CODE : A.density_code;
     float vs0, ss0, vs1, ss1;
     // cell x: x-2, x-1 from the pair below, x+1, x+2 from this pair and the next
     vel_lean_cell(sxx_0.x, sxx_m.y, sxx_m.x, sxy_0.x, sxy_y1.x, sxy_y2.x, sxy_0.y, sxy_p.x, syy_0.x, syy_y1.x,
@@ -264,7 +265,9 @@ __device__ __forceinline__ void s3p_velocity_prefetch(const S3Args<float>& A, in
     }
 }
 
-template <int MINB>
+// CODE: the density rule compiled in (1..4; the face buoyancies then fold to
+// one expression each), 0 = read at run time
+template <int MINB, int CODE = 0>
 __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, StepInfo si) {
     __shared__ unsigned redu[2 * PX * PY / 32];
     __shared__ double redd[2][PX * PY / 32];
@@ -278,13 +281,13 @@ __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, St
     const int nx = A.nx, ny = A.ny;
     float vsq = 0.f, ssq = 0.f;
     if (lean_tile_p(A, blockIdx.x * TPX, blockIdx.y * TPY, k)) {
-        velocity_pair_lean(A, x0, gy, k, vsq, ssq);
+        velocity_pair_lean<CODE>(A, x0, gy, k, vsq, ssq);
     } else if (gy < ny) {
         float w[9];
         for (int q = 0; q < 2; ++q) {
             if (x0 + q >= nx) break;
             float vs = 0.f, ss = 0.f;
-            velocity_cell<false>(A, it, x0 + q, gy, k, vs, ss, w);
+            velocity_cell<false, LD_NC, CODE>(A, it, x0 + q, gy, k, vs, ss, w);
             vsq = fmax_bits(vsq, vs);
             ssq = fmax_bits(ssq, ss);
         }
@@ -517,7 +520,15 @@ void launch_seismic3_pair_velocity(const S3Args<float>& a, const StepInfo& s, cu
     case 6: s3p_velocity<6><<<grd, blk, 0, st>>>(a, s); break;
     case 7: s3p_velocity<7><<<grd, blk, 0, st>>>(a, s); break;
     case 8: s3p_velocity<8><<<grd, blk, 0, st>>>(a, s); break;
-    default: s3p_velocity<4><<<grd, blk, 0, st>>>(a, s); break;
+    default:
+        switch (a.density_code) {
+        case 1: s3p_velocity<4, 1><<<grd, blk, 0, st>>>(a, s); break;
+        case 2: s3p_velocity<4, 2><<<grd, blk, 0, st>>>(a, s); break;
+        case 3: s3p_velocity<4, 3><<<grd, blk, 0, st>>>(a, s); break;
+        case 4: s3p_velocity<4, 4><<<grd, blk, 0, st>>>(a, s); break;
+        default: s3p_velocity<4><<<grd, blk, 0, st>>>(a, s); break;
+        }
+        break;
     }
 }
 
