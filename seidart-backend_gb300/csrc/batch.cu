@@ -198,6 +198,8 @@ __device__ __forceinline__ void cell_stress(const BModel& a, int i, int j) {
 
 // velocity half-step, force source, Dirichlet ring; returns the cell's |v|^2.
 // Loads first, as in cell_stress.
+// CODE: the density rule compiled in (1..4), 0 = the model's at run time
+template <int CODE = 0>
 __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, int it, float (&vo)[2]) {
     const int nx = a.nx, nz = a.nz;
     const size_t c = IXM(i, j);
@@ -220,10 +222,11 @@ __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, in
         ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
         m8 = a.mem[8][c]; m9 = a.mem[9][c]; m10 = a.mem[10][c]; m11 = a.mem[11][c];
     }
+    const int code = CODE ? CODE : a.density_code;
     const float dt = a.dt, hx = a.hx, hz = a.hz;
     if (ux) {
-        const float bxx = inv_mean_f(r0, rxm, a.density_code);
-        const float bzx = inv_mean_f(r0, rzm, a.density_code);
+        const float bxx = inv_mean_f(r0, rxm, code);
+        const float bzx = inv_mean_f(r0, rzm, code);
         float d1 = (27.0f * (s0 - sm1) + sm2) * hx;
         float d2 = (27.0f * (q0 - qm1) + qm2) * hz;
         if (pml) {
@@ -235,8 +238,8 @@ __device__ __forceinline__ float cell_velocity(const BModel& a, int i, int j, in
         vx = vx + dt * (d1 * bxx + d2 * bzx);
     }
     if (uz) {
-        const float bxz = inv_mean_f(r0, rxp, a.density_code);
-        const float bzz = inv_mean_f(r0, rzp, a.density_code);
+        const float bxz = inv_mean_f(r0, rxp, code);
+        const float bzz = inv_mean_f(r0, rzp, code);
         float d1 = (27.0f * (qp1 - q0) - qp2) * hx;
         float d2 = (27.0f * (wp1 - w0) - wp2) * hz;
         if (pml) {
@@ -283,7 +286,7 @@ __device__ __forceinline__ void model_tail(const BatchArgs& B, int it, int tid, 
 // MINB CTAs per SM bound the registers: 1024 threads per SM leave 64
 // registers per thread (capping them lower, 32 or 40, with 6 or 8 CTAs of
 // 256 threads, measured slower on the 64-model batch: spills)
-template <int TX, int TY, int MINB = 1024 / (TX * TY)>
+template <int TX, int TY, int CODE = 0, int MINB = 1024 / (TX * TY)>
 __global__ void __launch_bounds__(TX* TY, MINB) s2b_persistent(BatchArgs B, int nsteps) {
     __shared__ double red[TX * TY / 32];
     __shared__ float redf[TX * TY / 32];
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_persistent(BatchArgs B, int 
             const BModel* M;
             int i, j;
             float sq = 0.f, vo[2] = {0.f, 0.f};
-            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity(*M, i, j, it, vo);
+            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity<CODE>(*M, i, j, it, vo);
             const double n = block_norm_f32<TX * TY / 32>(
                 sq, [&] { return sqrt((double)vo[0] * vo[0] + (double)vo[1] * vo[1]); }, redf, red);
             if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&M->norms[it - 1], n);
@@ -393,7 +396,7 @@ struct WarpNorm {
 // its tiles mostly share one model (descriptor stays in L1) and neighbouring
 // tile rows stay in L2; the rows of tile t+PD are prefetched while tile t
 // computes.
-template <int TX, int TY, int PD, int MINB = 1024 / (TX * TY)>
+template <int TX, int TY, int PD, int CODE = 0, int MINB = 1024 / (TX * TY)>
 __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nsteps) {
     const int tid = threadIdx.x + TX * threadIdx.y, lane = tid & 31;
     const int t0 = (int)((long long)B.ntiles * blockIdx.x / gridDim.x);
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(TX* TY, MINB) s2b_chunked(BatchArgs B, int nst
             const BModel* M;
             int i, j;
             float sq = 0.f, vo[2] = {0.f, 0.f};
-            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity(*M, i, j, it, vo);
+            if (tile_cell<TX, TY>(B, t, M, i, j)) sq = cell_velocity<CODE>(*M, i, j, it, vo);
             wn.add(sq, vo);
         }
         wn.flush(B, it, lane);
@@ -541,6 +544,7 @@ __device__ __forceinline__ void fused_stress_cell(const BModel& a, int i, int j,
 
 // velocity update of owner cell (i, j) from the staged new stresses (row
 // pitch SW) and old velocities (row pitch VW) -- cell_velocity's arithmetic
+template <int CODE = 0>
 __device__ __forceinline__ float fused_velocity_cell(const BModel& a, int i, int j, int it, const float* SXX,
                                                      const float* SZZ, const float* SXZ, int SW, float vx, float vz,
                                                      float* const* fw, float* const* mr, float* const* mw,
@@ -563,10 +567,11 @@ __device__ __forceinline__ float fused_velocity_cell(const BModel& a, int i, int
         ah = __ldg(a.m[13] + c); b = __ldg(a.m[14] + c); bh = __ldg(a.m[15] + c);
         m8 = mr[8][c]; m9 = mr[9][c]; m10 = mr[10][c]; m11 = mr[11][c];
     }
+    const int code = CODE ? CODE : a.density_code;
     const float dt = a.dt, hx = a.hx, hz = a.hz;
     if (ux) {
-        const float bxx = inv_mean_f(r0, rxm, a.density_code);
-        const float bzx = inv_mean_f(r0, rzm, a.density_code);
+        const float bxx = inv_mean_f(r0, rxm, code);
+        const float bzx = inv_mean_f(r0, rzm, code);
         float d1 = (27.0f * (s0 - sm1) + sm2) * hx;
         float d2 = (27.0f * (q0 - qm1) + qm2) * hz;
         if (pml) {
@@ -578,8 +583,8 @@ __device__ __forceinline__ float fused_velocity_cell(const BModel& a, int i, int
         vx = vx + dt * (d1 * bxx + d2 * bzx);
     }
     if (uz) {
-        const float bxz = inv_mean_f(r0, rxp, a.density_code);
-        const float bzz = inv_mean_f(r0, rzp, a.density_code);
+        const float bxz = inv_mean_f(r0, rxp, code);
+        const float bzz = inv_mean_f(r0, rzp, code);
         float d1 = (27.0f * (qp1 - q0) - qp2) * hx;
         float d2 = (27.0f * (wp1 - w0) - wp2) * hz;
         if (pml) {
@@ -635,7 +640,7 @@ __device__ __forceinline__ void fused_prefetch(const BatchArgs& B, int t, int rd
     }
 }
 
-template <int TX, int TY, int NT, int MINB = 1024 / NT>
+template <int TX, int TY, int NT, int CODE = 0, int MINB = 1024 / NT>
 __global__ void __launch_bounds__(NT, MINB) s2b_fused(BatchArgs B, int nsteps) {
     using T = FusedTile<TX, TY>;
     constexpr int VW = T::VW, VH = T::VH, SW = T::SW, SH = T::SH;
@@ -697,7 +702,7 @@ __global__ void __launch_bounds__(NT, MINB) s2b_fused(BatchArgs B, int nsteps) {
                 float sq = 0.f, vo[2] = {0.f, 0.f};
                 if (q < TX * TY && x < nx && z < nz) {
                     const int sc = (lz + 2) * SW + lx + 2, vc = (lz + 4) * VW + lx + 4;
-                    sq = fused_velocity_cell(a, x + 1, z + 1, it, &ss[0][sc], &ss[1][sc], &ss[2][sc], SW, sv[0][vc],
+                    sq = fused_velocity_cell<CODE>(a, x + 1, z + 1, it, &ss[0][sc], &ss[1][sc], &ss[2][sc], SW, sv[0][vc],
                                              sv[1][vc], fw, mr, mw, vo);
                 }
                 wn.add(sq, vo);
@@ -759,8 +764,27 @@ const Variant kVariants[] = {
     {64, 8, (const void*)s2b_fused<64, 8, 256>, "fused", 256},
     {64, 16, (const void*)s2b_fused<64, 16, 512>, "fused", 512},
 };
+// the same variants compiled for the arithmetic-mean density rule (the
+// reference CLI's default), used when every model of a batch takes it
+const Variant kVariantsArith[] = {
+    {32, 4, (const void*)s2b_persistent<32, 4, 3>, "strided"},
+    {32, 8, (const void*)s2b_persistent<32, 8, 3>, "strided"},
+    {64, 4, (const void*)s2b_persistent<64, 4, 3>, "strided"},
+    {32, 16, (const void*)s2b_persistent<32, 16, 3>, "strided"},
+    {64, 8, (const void*)s2b_persistent<64, 8, 3>, "strided"},
+    {32, 8, (const void*)s2b_chunked<32, 8, 1, 3>, "chunked"},
+    {32, 8, (const void*)s2b_chunked<32, 8, 2, 3>, "chunked"},
+    {64, 4, (const void*)s2b_chunked<64, 4, 2, 3>, "chunked"},
+    {32, 4, (const void*)s2b_chunked<32, 4, 2, 3>, "chunked"},
+    {32, 16, (const void*)s2b_chunked<32, 16, 1, 3>, "chunked"},
+    {32, 16, (const void*)s2b_chunked<32, 16, 2, 3>, "chunked"},
+    {64, 8, (const void*)s2b_chunked<64, 8, 1, 3>, "chunked"},
+    {64, 8, (const void*)s2b_fused<64, 8, 256, 3>, "fused", 256},
+    {64, 16, (const void*)s2b_fused<64, 16, 512, 3>, "fused", 512},
+};
 __host__ __device__ constexpr int block_threads(const Variant& V) { return V.threads ? V.threads : V.tx * V.ty; }
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+static_assert(sizeof(kVariantsArith) == sizeof(kVariants), "one arithmetic-rule kernel per variant");
 
 }  // namespace
 
@@ -779,6 +803,7 @@ struct SeidartBatch {
     std::vector<float*> second;  // per model: the fused step's second state set, 17 arrays
     std::vector<void*> owned;    // material bytes and tables of indexed models
     std::vector<int> nmat;       // materials of each model's indexed layout (0: per-cell arrays)
+    const Variant* table = kVariants;  // kVariantsArith when every model takes the arithmetic mean
     int ntiles[kNumVariants] = {0};
     int* ctl = nullptr;  // step, barrier count, barrier generation, status
     cudaStream_t stream = nullptr;
@@ -804,9 +829,9 @@ int berr(int code, const std::string& m) {
     return code;
 }
 
-int max_bps(int var) {
+int max_bps(const SeidartBatch* b, int var) {
     int n = 0;
-    const Variant& V = kVariants[var];
+    const Variant& V = b->table[var];
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, V.fn, block_threads(V), 0) != cudaSuccess) return 0;
     return n;
 }
@@ -825,8 +850,8 @@ int launch_chunk(SeidartBatch* b, int var, int bps, int nsteps, int force_timeou
     A.force_timeout = force_timeout;
     A.tile_rec_off = b->dev_tile_rec_off[var];
     A.tile_rec = b->dev_tile_rec[var];
-    const Variant& V = kVariants[var];
-    if (bps < 1 || bps > max_bps(var)) return berr(SEIDART_ERR_ARG, "CTAs per SM outside the occupancy limit");
+    const Variant& V = b->table[var];
+    if (bps < 1 || bps > max_bps(b, var)) return berr(SEIDART_ERR_ARG, "CTAs per SM outside the occupancy limit");
     dim3 blk = V.threads ? dim3(V.threads) : dim3(V.tx, V.ty), grd(b->nsm * bps);
     void* args[] = {&A, &nsteps};
     const cudaError_t e = cudaLaunchCooperativeKernel(V.fn, grd, blk, args, 0, b->stream);
@@ -955,6 +980,10 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
     }
     const int ctl0[4] = {1, 0, 0, 0};
     cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    // one density rule for every model: the kernels compiled for it
+    bool arith = true;
+    for (int m = 0; m < nmodels; ++m) arith = arith && hm[m].density_code == SEIDART_DENSITY_ARITHMETIC;
+    if (arith) b->table = kVariantsArith;
     // material-indexed stress coefficients per model where the model allows
     // them (SEIDART_BATCH_MATIDX=0 keeps the per-cell arrays)
     const char* mi = getenv("SEIDART_BATCH_MATIDX");
@@ -1039,7 +1068,7 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
         }
     }
     b->variant = 1;
-    b->bps = std::max(1, max_bps(1));
+    b->bps = std::max(1, max_bps(b, 1));
     *out = b;
     return SEIDART_OK;
 }
@@ -1054,7 +1083,7 @@ int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, 
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     for (int v = 0; v < kNumVariants; ++v) {
-        const int mx = max_bps(v);
+        const int mx = max_bps(b, v);
         const int cand[2] = {mx, std::max(1, mx / 2)};
         for (int q = 0; q < 2; ++q) {
             const int bps = cand[q];
@@ -1104,7 +1133,7 @@ int seidart_batch_tuning(const SeidartBatch* b, int variant, int* tx, int* ty, i
 }
 
 int seidart_batch_set_config(SeidartBatch* b, int variant, int bps) {
-    if (!b || variant < 0 || variant >= kNumVariants || bps < 1 || bps > max_bps(variant))
+    if (!b || variant < 0 || variant >= kNumVariants || bps < 1 || bps > max_bps(b, variant))
         return berr(SEIDART_ERR_ARG, "bad batch configuration");
     b->variant = variant;
     b->bps = bps;

@@ -124,3 +124,23 @@ def test_material_indexed_batch_is_bit_identical(monkeypatch):
             assert np.array_equal(tri[m][0], trp[m][0]) and np.array_equal(tri[m][1], trp[m][1])
             for q in range(5):
                 assert np.array_equal(fi[m][q], fp[m][q]), (variant, m, q)
+
+
+@pytest.mark.parametrize("variant", [1, 11, 12])
+def test_mixed_density_rules_use_the_generic_kernels(variant):
+    """A batch whose models average density differently runs the kernels that
+    read each model's rule at run time (a batch of one rule runs kernels
+    compiled for it); both match single-model runs."""
+    import dataclasses
+    probs = small_batch(nt=30)
+    probs = [dataclasses.replace(p, density=rule) for p, rule in
+             zip(probs, ("harmonic", "arithmetic", "geometric", "none", "arithmetic"))]
+    with Batch(probs, autotune=False) as b:
+        b.set_config(variant, 1)
+        b.step(probs[0].time_steps)
+        b.sync()
+        for m, p in enumerate(probs):
+            single = sg.run(p, sg.FP32)
+            tr, nrm = b.traces(m)
+            assert rel_l2(tr, single["traces"]) <= 1e-6, (variant, m)
+            assert rel_l2(nrm, single["norms"]) <= 1e-6, (variant, m)
