@@ -233,6 +233,7 @@ struct S3Args {
     int pfv_d[3];        // the same for `prefetch_v`
     int pfp_d[3];        // the pair velocity kernel's prefetch distance on its 32 x 16 x 1 tile grid
     int velocity_pair;   // FP32: 1 = the cell-pair velocity kernel (nx even)
+    int velocity_sub;    // pair velocity kernel: 1 = each warp makes the lean test for its own two rows
     const void* staged;  // host pointer to S3XMaps when the staged stress kernel is set up, else NULL
     const void* staged_v;  // the same for the staged velocity kernel
     int velocity_minb;     // FP32: CTAs per SM the cell velocity kernel is compiled for (4 .. 8)

@@ -155,8 +155,15 @@ __global__ void __launch_bounds__(BX* BY, MINB) s3c_velocity(S3Args<float> A, St
 // arithmetic per pair instead of 64 -- and the arithmetic per cell is the
 // one-cell kernel's; other tiles run the one-cell path for each cell.
 // Needs nx even (every pair then starts 8 bytes aligned).
+// Warp parts (SUB): warp w (rows 2w, 2w + 1 of the tile) makes the lean test
+// for its own 32 x 2 part; the grid's inert box rarely ends on a 16-row
+// boundary (its high faces lie one cell short of one, where the half-grid
+// C-PML profile reaches), so fewer cells take the one-cell path.  (Parts of
+// 16 x 4, 8 pairs x 4 rows per warp, made the x granularity finer too but
+// cost more in split rows than they saved: 0.881 against 0.790 ms at 352^3.)
 constexpr int PX = 16, PY = 16;     // threads per CTA
 constexpr int TPX = 32, TPY = 16;   // cells per tile
+constexpr int SPY = 2;              // rows per warp part (SUB)
 
 __device__ __forceinline__ float fmax_bits(float a, float b) {
     // non-negative floats order like their bit patterns; NaN wins
@@ -236,16 +243,17 @@ __device__ __forceinline__ void velocity_pair_lean(const S3Args<float>& A, int g
     ssq = fmax_bits(ss0, ss1);
 }
 
-// lean test of a 32 x 16 pair tile (the same rules as lean_tile)
+// lean test of a TW x TH part of a pair tile (the same rules as lean_tile)
+template <int TW, int TH>
 __device__ __forceinline__ bool lean_tile_p(const S3Args<float>& A, int x0, int y0, int k) {
     const int nx = A.nx, ny = A.ny, nz = A.nz;
-    if (!(x0 >= 2 && x0 + TPX - 1 <= nx - 3 && y0 >= 2 && y0 + TPY - 1 <= ny - 3 && k >= 2 && k <= nz - 3)) return false;
-    if (!(x0 >= A.box.i0 && x0 + TPX <= A.box.i1 && y0 >= A.box.j0 && y0 + TPY <= A.box.j1 && k >= A.box.k0 &&
+    if (!(x0 >= 2 && x0 + TW - 1 <= nx - 3 && y0 >= 2 && y0 + TH - 1 <= ny - 3 && k >= 2 && k <= nz - 3)) return false;
+    if (!(x0 >= A.box.i0 && x0 + TW <= A.box.i1 && y0 >= A.box.j0 && y0 + TH <= A.box.j1 && k >= A.box.k0 &&
           k < A.box.k1))
         return false;
     const int is = A.isrc, js = A.jsrc, ks = A.ksrc;
-    if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + TPX && js + 1 >= y0 && js < y0 + TPY) return false;
-    if (A.pw.on && pw_tile(A.pw, x0, y0, k, TPX, TPY)) return false;
+    if (k >= ks && k <= ks + 1 && is + 1 >= x0 && is < x0 + TW && js + 1 >= y0 && js < y0 + TH) return false;
+    if (A.pw.on && pw_tile(A.pw, x0, y0, k, TW, TH)) return false;
     return true;
 }
 
@@ -267,7 +275,7 @@ __device__ __forceinline__ void s3p_velocity_prefetch(const S3Args<float>& A, in
 
 // CODE: the density rule compiled in (1..4; the face buoyancies then fold to
 // one expression each), 0 = read at run time
-template <int MINB, int CODE = 0>
+template <int MINB, int CODE = 0, bool SUB = false>
 __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, StepInfo si) {
     __shared__ unsigned redu[2 * PX * PY / 32];
     __shared__ double redd[2][PX * PY / 32];
@@ -280,7 +288,10 @@ __global__ void __launch_bounds__(PX* PY, MINB) s3p_velocity(S3Args<float> A, St
     const int x0 = blockIdx.x * TPX + 2 * threadIdx.x, gy = blockIdx.y * TPY + threadIdx.y;
     const int nx = A.nx, ny = A.ny;
     float vsq = 0.f, ssq = 0.f;
-    if (lean_tile_p(A, blockIdx.x * TPX, blockIdx.y * TPY, k)) {
+    static_assert(PX * SPY == 32, "a warp part is one warp's rows");
+    const bool lean = SUB ? lean_tile_p<TPX, SPY>(A, blockIdx.x * TPX, blockIdx.y * TPY + SPY * (tid >> 5), k)
+                          : lean_tile_p<TPX, TPY>(A, blockIdx.x * TPX, blockIdx.y * TPY, k);
+    if (lean) {
         velocity_pair_lean<CODE>(A, x0, gy, k, vsq, ssq);
     } else if (gy < ny) {
         float w[9];
@@ -521,6 +532,16 @@ void launch_seismic3_pair_velocity(const S3Args<float>& a, const StepInfo& s, cu
     case 7: s3p_velocity<7><<<grd, blk, 0, st>>>(a, s); break;
     case 8: s3p_velocity<8><<<grd, blk, 0, st>>>(a, s); break;
     default:
+        if (a.velocity_sub) {
+            switch (a.density_code) {
+            case 1: s3p_velocity<4, 1, true><<<grd, blk, 0, st>>>(a, s); break;
+            case 2: s3p_velocity<4, 2, true><<<grd, blk, 0, st>>>(a, s); break;
+            case 3: s3p_velocity<4, 3, true><<<grd, blk, 0, st>>>(a, s); break;
+            case 4: s3p_velocity<4, 4, true><<<grd, blk, 0, st>>>(a, s); break;
+            default: s3p_velocity<4, 0, true><<<grd, blk, 0, st>>>(a, s); break;
+            }
+            break;
+        }
         switch (a.density_code) {
         case 1: s3p_velocity<4, 1><<<grd, blk, 0, st>>>(a, s); break;
         case 2: s3p_velocity<4, 2><<<grd, blk, 0, st>>>(a, s); break;

@@ -1010,6 +1010,10 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         // the pair kernel holds two cells per thread: 4 CTAs per SM (352^3: 0.995 ms
         // against 1.14 ms at 5 and 1.015 ms for the one-cell kernel at 6)
         if (s->s3f.velocity_pair && !getenv("SEIDART_S3_VEL_MINB")) s->s3f.velocity_minb = 4;
+        // warps make the lean test for their own two rows of the pair tile
+        // (SEIDART_S3_VSUB=0: one test per 32 x 16 tile)
+        t = getenv("SEIDART_S3_VSUB");
+        s->s3f.velocity_sub = (t && *t == '0') ? 0 : 1;
         // the velocity kernel walks down from the planes the stress kernel
         // finished on (bit-identical; SEIDART_S3_VREV=0 turns it off).  The
         // stress kernel's read-once copies take an L2 evict-first policy only

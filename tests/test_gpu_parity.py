@@ -180,6 +180,38 @@ def test_seismic3_fp32_velocity_pair_kernel(oracle, monkeypatch):
         assert rel_l2(out["1"]["fields"][q], o["fields"][q]) <= FP32_TOL, q
 
 
+def test_seismic3_fp32_velocity_warp_parts(oracle, monkeypatch):
+    """The pair velocity kernel's lean test per warp (32 x 2 cells) against
+    one test per 32 x 16 tile, on a grid with a ragged y tail, a force and a
+    stress source and C-PML faces that cut through tiles: more cells take the
+    lean path, whose expressions are the one-cell path's (within 1e-6, as the
+    one-cell kernel), and the result stays within FP32_TOL of the oracle."""
+    p = models.seismic3_layers(n=84, cpml=10, nt=40, nlayers=3, nrec_side=4, rec_z=3, src_z=12, ny=70)
+    p.src["x"] = 0.5 * p.src["z"]
+    p.src["xx"] = 1e6 * p.src["z"]
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("SEIDART_S3_VSUB", flag)
+        with sg.Solver(p, sg.FP32) as s:
+            s.step(p.time_steps)
+            s.sync()
+            tr, nrm = s.traces()
+            out[flag] = (s.get_fields(), s.get_memory(), tr, nrm)
+    a, b = out["0"], out["1"]
+    assert np.max(np.abs(a[2])) > 0 and max(np.max(np.abs(a[1][q])) for q in range(36, 45)) > 0
+    errs = {"traces": rel_l2(b[2], a[2]), "norms": rel_l2(b[3], a[3])}
+    for q in range(9):
+        errs[f"field {q}"] = rel_l2(b[0][q], a[0][q])
+    for q in range(36, 45):
+        errs[f"memory {q}"] = rel_l2(b[1][q], a[1][q])
+    print({k: float(v) for k, v in errs.items()})
+    assert max(errs.values()) <= 1e-6, errs
+    o = oracle.run_oracle(p)
+    assert rel_l2(b[2], o["traces"]) <= FP32_TOL
+    for q in range(9):
+        assert rel_l2(b[0][q], o["fields"][q]) <= FP32_TOL, q
+
+
 def test_seismic3_fp32_odd_sizes(oracle):
     """Odd nx and ny: the staged stress and the cell-pair velocity kernels
     need nx % 4 == 0 and nx even, so the bulk-copy stress and the one-cell
