@@ -775,7 +775,7 @@ cudaError_t seismic3_bulk_pack(const S3Args<float>& a, float* packed, cudaStream
 // tensor-copy rules (row pitch a multiple of 16 bytes) or the driver entry
 // point is missing, in which case the caller keeps the bulk kernel.
 bool seismic3_staged_prepare(const S3Args<float>& a, S3XMaps* m) {
-    if (a.nx % 4 != 0 || !a.packed) return false;
+    if (a.nx % 4 != 0) return false;
     for (int q = 0; q < 6; ++q)
         if (!seismic3_make_map(&m->sig[q], a.f[3 + q], a.nx, a.ny, a.nz, BX, BY)) return false;
     for (int f = 0; f < 3; ++f) {

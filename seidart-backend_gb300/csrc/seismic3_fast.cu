@@ -400,7 +400,7 @@ void launch_seismic3_fast(const S3Args<float>& a, const StepInfo& s, cudaStream_
         if (h) h->fn(h->ctx, 3, "s3f_epilogue");
         return;
     }
-    if (stress_kind == S3K_BULK && a.packed && a.staged) {
+    if (stress_kind == S3K_BULK && (a.packed || a.mat_ids) && a.staged) {
         launch_seismic3_staged_stress(a, *(const S3XMaps*)a.staged, st);
         if (h) h->fn(h->ctx, 0, "s3x_stress");
     } else if (stress_kind == S3K_BULK && a.packed) {

@@ -1033,18 +1033,6 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         const char* t = getenv("SEIDART_S3_BULK");
         s->s3f.bulk_variant = (t && *t >= '0' && *t <= '9') ? atoi(t) : 2;
         if (s->s3f.bulk_variant >= seismic3_bulk_variants()) s->s3f.bulk_variant = 0;
-        const size_t bytes = seismic3_bulk_bytes(s->dom.nx, s->dom.ny, s->dom.nz);
-        if (cudaMalloc((void**)&s->s3_packed, bytes) != cudaSuccess) {
-            cudaGetLastError();
-            seidart_solver_destroy(s);
-            return set_err(SEIDART_ERR_NOMEM, "cannot allocate %zu bytes for the packed 3D coefficients", bytes);
-        }
-        if (seismic3_bulk_pack(s->s3f, s->s3_packed, s->stream) != cudaSuccess ||
-            cudaStreamSynchronize(s->stream) != cudaSuccess) {
-            seidart_solver_destroy(s);
-            return set_err(SEIDART_ERR_CUDA, "coefficient packing failed: %s", cudaGetErrorString(cudaGetLastError()));
-        }
-        s->s3f.packed = s->s3_packed;
         // fully staged variant (TMA tiles for stresses and velocities) when the
         // grid allows it; SEIDART_S3_STAGED=0 keeps the bulk kernel
         const char* st = getenv("SEIDART_S3_STAGED");
@@ -1058,6 +1046,26 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.mat_ids = s->s3_mat_ids;
             s->s3f.mat_tab = s->s3_mat_tab;
             s->s3f.mat_tab_bytes = (s->s3_nmat * 27 * (int)sizeof(float) + 15) / 16 * 16;
+        }
+        // the tile-packed per-cell coefficient block (27 words per cell, 4.7 GB
+        // at 352^3) only where a kernel reads it: the per-cell layout, the bulk
+        // kernel, and the fused step (its tiles read the block)
+        const char* wv = getenv("SEIDART_S3_WAVE");
+        const bool want_wave = wv && *wv == '1';
+        if (!s->s3f.mat_ids || want_wave) {
+            const size_t bytes = seismic3_bulk_bytes(s->dom.nx, s->dom.ny, s->dom.nz);
+            if (cudaMalloc((void**)&s->s3_packed, bytes) != cudaSuccess) {
+                cudaGetLastError();
+                seidart_solver_destroy(s);
+                return set_err(SEIDART_ERR_NOMEM, "cannot allocate %zu bytes for the packed 3D coefficients", bytes);
+            }
+            if (seismic3_bulk_pack(s->s3f, s->s3_packed, s->stream) != cudaSuccess ||
+                cudaStreamSynchronize(s->stream) != cudaSuccess) {
+                seidart_solver_destroy(s);
+                return set_err(SEIDART_ERR_CUDA, "coefficient packing failed: %s",
+                               cudaGetErrorString(cudaGetLastError()));
+            }
+            s->s3f.packed = s->s3_packed;
         }
         // the six C-PML grids indexed the same way (a grid built from 1D
         // profiles holds a few dozen tuples; SEIDART_S3_CPMLIDX=0 keeps them)
@@ -1077,9 +1085,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.staged_v = &s->s3_staged;
         // fused step (both half-steps in one wavefront launch) on top of the
         // staged stress tiles, on request (SEIDART_S3_WAVE=1)
-        const char* wv = getenv("SEIDART_S3_WAVE");
-        if (s->s3f.staged && !s->s3f.staged_v && (wv && *wv == '1') && s->s3_velocity_kind == S3K_CELL &&
-            s->wave_ctl) {
+        if (s->s3f.staged && !s->s3f.staged_v && want_wave && s->s3_velocity_kind == S3K_CELL && s->wave_ctl) {
             s->s3f.wave_ctl = s->wave_ctl;
             s->s3f.wave_n = s->wave_n;
             s->s3f.wave_ctas = seismic3_wave_prepare(s->s3f);
