@@ -9,7 +9,7 @@
 // the table holds exactly the values the per-cell layout would read:
 //   1. matidx_hash: every cell hashes its 27 FP32 bit patterns; the lanes of
 //      a warp with equal hashes elect one, which inserts the hash into a
-//      64-slot open-addressing table (atomicCAS) and lowers the slot's
+//      128-slot open-addressing table (atomicCAS) and lowers the slot's
 //      representative cell (atomicMin); a claimed slot is counted.
 //   2. the host reads the table back, numbers the claimed slots by their
 //      representative cell (a deterministic order) and uploads the numbers.
