@@ -21,11 +21,13 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "../../include/seidart_gpu.h"
+#include "host_pool.h"
 #include "kernels.h"
 
 // plane-wave set-up (planewave.cu)
@@ -280,16 +282,7 @@ int ensure_pin(SeidartSolver& s) {
     return SEIDART_OK;
 }
 
-// run body(lo, hi) over [0, m) on up to 16 host threads
-template <typename F>
-void host_parallel(size_t m, F body) {
-    const unsigned hw = std::thread::hardware_concurrency();
-    const size_t nth = std::max<size_t>(1, std::min<size_t>(std::min(hw, 16u), m >> 18));
-    std::vector<std::thread> pool;
-    for (size_t w = 1; w < nth; ++w) pool.emplace_back([&, w] { body(m * w / nth, m * (w + 1) / nth); });
-    body(0, m / nth);
-    for (auto& t : pool) t.join();
-}
+using seidart_host::host_parallel;  // body(lo, hi) over [0, m) on the host thread pool
 
 void widen(double* dst, const float* src, size_t m) {
     host_parallel(m, [&](size_t lo, size_t hi) {
@@ -463,19 +456,15 @@ BoxH interior_box(const SeidartSolver& s, const double* const* model) {
     if (!nonempty()) return empty;
     // cell-by-cell verification, z planes shared out over host threads (on
     // the 352^3 grid one thread takes 84 ms)
-    const unsigned hw = std::thread::hardware_concurrency();
-    const int nth = (int)std::min<long>(std::max(1u, std::min(hw, 16u)), (long)(b.k1 - b.k0));
+    seidart_host::HostPool& pool = seidart_host::HostPool::get();
+    const int nth = (int)std::min<long>(pool.size(), (long)(b.k1 - b.k0));
     std::atomic<bool> bad{false};
-    auto verify = [&](int w) {
+    pool.run(nth, [&](int w) {
         for (int k = b.k0 + w; k < b.k1 && !bad.load(std::memory_order_relaxed); k += nth)
             for (int j = b.j0; j < b.j1; ++j)
                 for (int i = b.i0; i < b.i1; ++i)
                     if (active(i, j, k)) { bad = true; return; }
-    };
-    std::vector<std::thread> pool;
-    for (int w = 1; w < nth; ++w) pool.emplace_back(verify, w);
-    verify(0);
-    for (auto& t : pool) t.join();
+    });
     return bad ? empty : b;
 }
 
@@ -841,11 +830,34 @@ int seidart_layout(int family, int* nmodel, int* nsrc, int* nfield, int* nmem, i
     return SEIDART_OK;
 }
 
+namespace {
+// Set-up stage times on stderr when SEIDART_TRACE_SETUP=1; each mark first
+// waits for the solver's stream, so a stage's device work counts in it.
+struct SetupTrace {
+    bool on;
+    std::chrono::steady_clock::time_point last;
+    SetupTrace() {
+        const char* t = getenv("SEIDART_TRACE_SETUP");
+        on = t && *t == '1';
+        last = std::chrono::steady_clock::now();
+    }
+    void mark(const char* stage, cudaStream_t st = nullptr) {
+        if (!on) return;
+        if (st) cudaStreamSynchronize(st);
+        const auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "seidart set-up: %-24s %9.2f ms\n", stage,
+                std::chrono::duration<double, std::milli>(t - last).count());
+        last = t;
+    }
+};
+}  // namespace
+
 int seidart_solver_create(SeidartSolver** out, int family, int precision, const SeidartDomain* dom,
                           const SeidartSource* src, int density_code, const double* const* model,
                           const double* const* srcfn, int nrec, const int* rec_cells) {
     if (!out || !dom || !src || !model) return set_err(SEIDART_ERR_ARG, "NULL argument");
     *out = nullptr;
+    SetupTrace trace;
     Layout L;
     if (!layout_of(family, &L)) return set_err(SEIDART_ERR_ARG, "unknown solver family %d", family);
     if (precision != SEIDART_FP64 && precision != SEIDART_FP32 && precision != SEIDART_FP64_FAST)
@@ -905,7 +917,9 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         s->s3_stress_kind = kind("SEIDART_S3_STRESS", s->s3_stress_kind);
         s->s3_velocity_kind = kind("SEIDART_S3_VELOCITY", s->s3_velocity_kind);
     }
+    trace.mark("checks");
     s->box = interior_box(*s, model);
+    trace.mark("interior box");
     for (int q = 0; q < L.nsrc; ++q) {
         // stress-source series are every slot after the force components
         const int first_stress = (family == SEIDART_SEISMIC2) ? S2_SRCXX : ((family == SEIDART_SEISMIC3 || family == SEIDART_SEISMIC25) ? S3_SRCXX : 1 << 20);
@@ -958,6 +972,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
                 delete s;
                 return set_err(SEIDART_ERR_NOMEM, "device allocation of %zu MiB failed: %s", mb, cudaGetErrorString(e));
             }
+            trace.mark("arena sizing + allocation");
         } else {
             int rc = SEIDART_OK;
             if (cudaMemsetAsync(s->arena, 0, s->arena_bytes, s->stream) != cudaSuccess) rc = SEIDART_ERR_CUDA;
@@ -972,6 +987,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             if (rc == SEIDART_OK && cudaMemcpyAsync(s->step_dev, &one, sizeof(int), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
                 rc = SEIDART_ERR_CUDA;
             if (rc == SEIDART_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = SEIDART_ERR_CUDA;
+            trace.mark("zero state, sources");
             derived.clear();
             if (rc == SEIDART_OK)
                 rc = precision == SEIDART_FP32 ? setup_model<float>(*s, model, srcfn, dsrc, derived)
@@ -982,6 +998,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             }
         }
     }
+    trace.mark("model upload", s->stream);
     if (precision == SEIDART_FP32) finish_args<float>(*s); else finish_args<double>(*s);
     if (family == SEIDART_SEISMIC3 && precision == SEIDART_FP32 && s->s3_stress_kind == S3K_TMA) {
         const char* t = getenv("SEIDART_S3_TMA");
@@ -1037,6 +1054,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         // grid allows it; SEIDART_S3_STAGED=0 keeps the bulk kernel
         const char* st = getenv("SEIDART_S3_STAGED");
         if (!(st && *st == '0') && seismic3_staged_prepare(s->s3f, &s->s3_staged)) s->s3f.staged = &s->s3_staged;
+        trace.mark("staged kernel maps", s->stream);
         // material-indexed coefficients for the staged kernel when the model
         // allows them (SEIDART_S3_MATIDX=0 keeps the per-cell blocks)
         const char* mi = getenv("SEIDART_S3_MATIDX");
@@ -1047,6 +1065,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.mat_tab = s->s3_mat_tab;
             s->s3f.mat_tab_bytes = (s->s3_nmat * 27 * (int)sizeof(float) + 15) / 16 * 16;
         }
+        trace.mark("material index", s->stream);
         // the tile-packed per-cell coefficient block (27 words per cell, 4.7 GB
         // at 352^3) only where a kernel reads it: the per-cell layout, the bulk
         // kernel, and the fused step (its tiles read the block)
@@ -1067,6 +1086,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             }
             s->s3f.packed = s->s3_packed;
         }
+        trace.mark("per-cell coefficient block", s->stream);
         // the six C-PML grids indexed the same way (a grid built from 1D
         // profiles holds a few dozen tuples; SEIDART_S3_CPMLIDX=0 keeps them)
         const char* ci = getenv("SEIDART_S3_CPMLIDX");
@@ -1077,6 +1097,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
             s->s3f.cpml_tab = s->s3_cpml_tab;
         }
 
+        trace.mark("C-PML index", s->stream);
         // staged velocity kernel: bit-identical but measured slower at 352^3
         // (1.55 ms against 1.19 ms), so only on request
         const char* sv = getenv("SEIDART_S3_STAGED_V");
@@ -1103,6 +1124,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
         const char* mg = getenv("SEIDART_S3_MERGE");
         s->s3f.mem_merged = (s->s3f.staged && !s->s3f.wave_ctl && !(mg && *mg == '0')) ? 1 : 0;
     }
+    trace.mark("kernel set-up", s->stream);
     *out = s;
     return SEIDART_OK;
 }
