@@ -979,7 +979,10 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
         return berr(SEIDART_ERR_NOMEM, "batch control allocation failed");
     }
     const int ctl0[4] = {1, 0, 0, 0};
-    cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    if (cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice) != cudaSuccess) {
+        seidart_batch_destroy(b);
+        return berr(SEIDART_ERR_CUDA, std::string("batch control upload failed: ") + cudaGetErrorString(cudaGetLastError()));
+    }
     // one density rule for every model: the kernels compiled for it
     bool arith = true;
     for (int m = 0; m < nmodels; ++m) arith = arith && hm[m].density_code == SEIDART_DENSITY_ARITHMETIC;
@@ -1024,11 +1027,12 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
         for (int q = 0; q < 12; ++q) hm[m].mem2[q] = p + (size_t)(5 + q) * n;
     }
     for (int v = 0; v < kNumVariants; ++v) {
+        const Variant& V = b->table[v];
         std::vector<int> tm;
         std::vector<BModel> mv = hm;
         for (int m = 0; m < nmodels; ++m) {
-            mv[m].tiles_x = (mv[m].nx + kVariants[v].tx - 1) / kVariants[v].tx;
-            const int tz = (mv[m].nz + kVariants[v].ty - 1) / kVariants[v].ty;
+            mv[m].tiles_x = (mv[m].nx + V.tx - 1) / V.tx;
+            const int tz = (mv[m].nz + V.ty - 1) / V.ty;
             mv[m].tile0 = (int)tm.size();
             mv[m].tiles = mv[m].tiles_x * tz;
             for (int q = 0; q < mv[m].tiles; ++q) tm.push_back(m);
@@ -1039,9 +1043,12 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
             seidart_batch_destroy(b);
             return berr(SEIDART_ERR_NOMEM, "tile table allocation failed");
         }
-        cudaMemcpy(b->dev_tile_model[v], tm.data(), sizeof(int) * tm.size(), cudaMemcpyHostToDevice);
-        cudaMemcpy(b->dev_models[v], mv.data(), sizeof(BModel) * nmodels, cudaMemcpyHostToDevice);
-        if (kVariants[v].threads) {
+        if (cudaMemcpy(b->dev_tile_model[v], tm.data(), sizeof(int) * tm.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->dev_models[v], mv.data(), sizeof(BModel) * nmodels, cudaMemcpyHostToDevice) != cudaSuccess) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_CUDA, std::string("tile table upload failed: ") + cudaGetErrorString(cudaGetLastError()));
+        }
+        if (V.threads) {
             // receivers listed per tile (counting sort by the tile holding the cell)
             // (the solvers have checked every cell index against their grids)
             const int nt = (int)tm.size();
@@ -1049,7 +1056,7 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
             for (int m = 0; m < nmodels; ++m)
                 for (int r = 0; r < (nrec && rec_cells ? nrec[m] : 0); ++r) {
                     const int c = rec_cells[m][r], x = c % mv[m].nx, z = c / mv[m].nx;
-                    const int t = mv[m].tile0 + x / kVariants[v].tx + mv[m].tiles_x * (z / kVariants[v].ty);
+                    const int t = mv[m].tile0 + x / V.tx + mv[m].tiles_x * (z / V.ty);
                     tile_of.push_back(t);
                     ++off[t + 1];
                 }
@@ -1063,8 +1070,14 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
                 seidart_batch_destroy(b);
                 return berr(SEIDART_ERR_NOMEM, "receiver table allocation failed");
             }
-            cudaMemcpy(b->dev_tile_rec_off[v], off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice);
-            cudaMemcpy(b->dev_tile_rec[v], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice);
+            if (cudaMemcpy(b->dev_tile_rec_off[v], off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice) !=
+                    cudaSuccess ||
+                cudaMemcpy(b->dev_tile_rec[v], list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice) !=
+                    cudaSuccess) {
+                seidart_batch_destroy(b);
+                return berr(SEIDART_ERR_CUDA,
+                            std::string("receiver table upload failed: ") + cudaGetErrorString(cudaGetLastError()));
+            }
         }
     }
     b->variant = 1;
@@ -1114,7 +1127,8 @@ int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, 
         if (rc != SEIDART_OK) return berr(rc, seidart_last_error());
     }
     const int ctl0[4] = {1, 0, 0, 0};
-    cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice);
+    if (cudaMemcpy(b->ctl, ctl0, sizeof ctl0, cudaMemcpyHostToDevice) != cudaSuccess)
+        return berr(SEIDART_ERR_CUDA, std::string("batch control reset failed: ") + cudaGetErrorString(cudaGetLastError()));
     b->steps_done = 0;
     if (best_variant) *best_variant = b->variant;
     if (best_bps) *best_bps = b->bps;
@@ -1198,7 +1212,8 @@ int seidart_batch_force_timeout(SeidartBatch* b, long long spin_limit) {
     if (rc != SEIDART_OK) return rc;
     // clear the status and barrier words for later use
     const int ctl_clear[3] = {0, 0, 0};
-    cudaMemcpy(b->ctl + 1, ctl_clear, sizeof ctl_clear, cudaMemcpyHostToDevice);
+    if (cudaMemcpy(b->ctl + 1, ctl_clear, sizeof ctl_clear, cudaMemcpyHostToDevice) != cudaSuccess)
+        return berr(SEIDART_ERR_CUDA, std::string("batch control reset failed: ") + cudaGetErrorString(cudaGetLastError()));
     return st != 0 ? SEIDART_ERR_TIMEOUT : SEIDART_OK;
 }
 
