@@ -1021,7 +1021,15 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
         seidart_fwi_destroy(f);
         return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
     }
-    cudaMemcpy(f->dsrc, f->srch.data(), sizeof(double) * nshots * f->nt, cudaMemcpyHostToDevice);
+    // a failed upload of the sources, receiver chains or observed traces
+    // ends the set-up with the CUDA error
+    auto upload_failed = [&]() {
+        const std::string m = std::string("FWI upload failed: ") + cudaGetErrorString(cudaGetLastError());
+        seidart_fwi_destroy(f);
+        return ferr(SEIDART_ERR_CUDA, m);
+    };
+    if (cudaMemcpy(f->dsrc, f->srch.data(), sizeof(double) * nshots * f->nt, cudaMemcpyHostToDevice) != cudaSuccess)
+        return upload_failed();
     {   // receiver chains per cell (several receivers may share a cell)
         std::vector<int> first(f->N, -1), next(nrec > 0 ? nrec : 1, -1);
         for (int r = nrec - 1; r >= 0; --r) {
@@ -1039,8 +1047,9 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
             seidart_fwi_destroy(f);
             return ferr(SEIDART_ERR_NOMEM, "FWI buffer allocation failed");
         }
-        cudaMemcpy(f->rfirst, first.data(), sizeof(int) * f->N, cudaMemcpyHostToDevice);
-        cudaMemcpy(f->rnext, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice);
+        if (cudaMemcpy(f->rfirst, first.data(), sizeof(int) * f->N, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(f->rnext, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return upload_failed();
     }
     std::vector<float> tmp(nobs);
     for (int sh = 0; sh < nshots && nobs; ++sh) {
@@ -1049,7 +1058,9 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
         } else {
             for (size_t q = 0; q < nobs; ++q) tmp[q] = (float)observed[sh][q];
         }
-        cudaMemcpy(f->dobs + (size_t)sh * nobs, tmp.data(), sizeof(float) * nobs, cudaMemcpyHostToDevice);
+        if (cudaMemcpy(f->dobs + (size_t)sh * nobs, tmp.data(), sizeof(float) * nobs, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            return upload_failed();
     }
     // lanes: enough concurrent shots for about 1.2 M cells in flight (on a
     // 552^2 grid 4 lanes measured 2.57 s per 16-shot gradient, 16 lanes

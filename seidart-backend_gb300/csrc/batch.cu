@@ -1022,7 +1022,11 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
             return berr(SEIDART_ERR_NOMEM, "second state set allocation failed");
         }
         b->second.push_back(p);
-        cudaMemset(p, 0, sizeof(float) * 17 * n);
+        if (cudaMemset(p, 0, sizeof(float) * 17 * n) != cudaSuccess) {
+            seidart_batch_destroy(b);
+            return berr(SEIDART_ERR_CUDA, std::string("second state set clear failed: ") +
+                                              cudaGetErrorString(cudaGetLastError()));
+        }
         for (int q = 0; q < 5; ++q) hm[m].f2[q] = p + (size_t)q * n;
         for (int q = 0; q < 12; ++q) hm[m].mem2[q] = p + (size_t)(5 + q) * n;
     }
