@@ -371,10 +371,11 @@ struct SnapshotPipe {
             else snap_copy<double, double><<<blocks, 256, 0, comp>>>((const double*)dev, (double*)dst, n, stride);
         }
         if (cudaGetLastError() != cudaSuccess) return io_err(SEIDART_ERR_CUDA, "snapshot kernel launch failed");
-        cudaEventRecord(ready[r], comp);
-        cudaStreamWaitEvent(copy, ready[r], 0);
-        cudaMemcpyAsync(hring[r], dring[r], slots.size() * bytes1, cudaMemcpyDeviceToHost, copy);
-        cudaEventRecord(copied[r], copy);
+        if (cudaEventRecord(ready[r], comp) != cudaSuccess || cudaStreamWaitEvent(copy, ready[r], 0) != cudaSuccess ||
+            cudaMemcpyAsync(hring[r], dring[r], slots.size() * bytes1, cudaMemcpyDeviceToHost, copy) != cudaSuccess ||
+            cudaEventRecord(copied[r], copy) != cudaSuccess)
+            return io_err(SEIDART_ERR_CUDA, std::string("snapshot copy could not be issued: ") +
+                                                cudaGetErrorString(cudaGetLastError()));
         pending_step[r] = it;
         // writer: wait for this slot's copy, then write one file per channel
         cudaEvent_t ev = copied[r];
@@ -480,15 +481,18 @@ struct BlockPipe {
         snprintf(name, sizeof name, "%06d-%06d.%d.%d.%d.blk.zst", ii, jj, xind, yind, zind);
         return prefix + name;
     }
-    // hand the current block to the copy stream and the writer
-    void flush() {
-        if (in_block == 0) return;
+    // hand the current block to the copy stream and the writer; false (and
+    // the reason in err) when the copy could not be issued
+    bool flush(std::string& err) {
+        if (in_block == 0) return true;
         const int b = cur;
         const size_t bytes = 3 * slab * (size_t)in_block * sizeof(float);
-        cudaEventRecord(full[b], comp);
-        cudaStreamWaitEvent(copy, full[b], 0);
-        cudaMemcpyAsync(hblk[b], dblk[b], bytes, cudaMemcpyDeviceToHost, copy);
-        cudaEventRecord(copied[b], copy);
+        if (cudaEventRecord(full[b], comp) != cudaSuccess || cudaStreamWaitEvent(copy, full[b], 0) != cudaSuccess ||
+            cudaMemcpyAsync(hblk[b], dblk[b], bytes, cudaMemcpyDeviceToHost, copy) != cudaSuccess ||
+            cudaEventRecord(copied[b], copy) != cudaSuccess) {
+            err = std::string("block copy could not be issued: ") + cudaGetErrorString(cudaGetLastError());
+            return false;
+        }
         busy[b] = true;
         const std::string path = block_name();
         cudaEvent_t ev = copied[b];
@@ -501,6 +505,7 @@ struct BlockPipe {
         });
         cur ^= 1;
         in_block = 0;
+        return true;
     }
     int capture(int it) {
         (void)it;
@@ -518,11 +523,13 @@ struct BlockPipe {
         if (f32) block_gather<float><<<4 * 152, 256, 0, comp>>>((const float*)dev[0], (const float*)dev[1], (const float*)dev[2], out, nx, cpml, onx, onz, stride);
         else block_gather<double><<<4 * 152, 256, 0, comp>>>((const double*)dev[0], (const double*)dev[1], (const double*)dev[2], out, nx, cpml, onx, onz, stride);
         if (cudaGetLastError() != cudaSuccess) return io_err(SEIDART_ERR_CUDA, "block gather launch failed");
-        if (++in_block == spb) flush();
+        std::string err;
+        if (++in_block == spb && !flush(err)) return io_err(SEIDART_ERR_CUDA, err);
         return SEIDART_OK;
     }
     int finish() {
-        flush();
+        std::string err;
+        if (!flush(err)) return io_err(SEIDART_ERR_CUDA, err);
         if (copy) cudaStreamSynchronize(copy);
         writer.drain();
         if (writer.failed) return io_err(SEIDART_ERR_IO, why.empty() ? "zstd block write failed" : why);
