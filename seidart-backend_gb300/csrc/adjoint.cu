@@ -36,6 +36,7 @@
 #include "../../include/seidart_gpu.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "trace.h"
 
 extern "C" int seidart_solver_internal_s2f(SeidartSolver* s, S2Args<float>* out, const int** rec);
 extern "C" int seidart_solver_internal_e2f(SeidartSolver* s, E2Args<float>* out, const int** rec);
@@ -986,6 +987,7 @@ int seidart_fwi_create_family(SeidartFwi** out, int family, const SeidartDomain*
                               int density_code, const double* const* model, int nshots, const int* shot_xind,
                               const int* shot_zind, const double* const* shot_srcz, int nrec, const int* rec_cells,
                               const double* const* observed, int checkpoint_every) {
+    seidart_trace::Range nvtx("seidart_fwi_create");
     if (!out || !dom || !src || !model || nshots < 1 || !shot_xind || !shot_zind || !shot_srcz)
         return ferr(SEIDART_ERR_ARG, "bad arguments");
     if (family != SEIDART_SEISMIC2 && family != SEIDART_ELECTROMAG2)
@@ -1139,6 +1141,7 @@ int seidart_fwi_create(SeidartFwi** out, const SeidartDomain* dom, const Seidart
 // electromag2 [6][ncell] dL/deps11, dL/deps13, dL/deps33 (relative
 // permittivities, as in e11.dat ...), dL/dsig11, dL/dsig13, dL/dsig33.
 int seidart_fwi_gradient(SeidartFwi* f, double* loss, double* grad) {
+    seidart_trace::Range nvtx("seidart_fwi_gradient");
     if (!f) return ferr(SEIDART_ERR_ARG, "NULL");
     f->launches = 0;
     for (auto& L : f->lanes) {

@@ -24,6 +24,7 @@
 #include "../../include/seidart_gpu.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "trace.h"
 
 namespace {
 
@@ -931,6 +932,7 @@ int seidart_batch_destroy(SeidartBatch* b) {
 int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* doms, const SeidartSource* srcs,
                          const int* density_codes, const double* const* const* models,
                          const double* const* const* srcfn, const int* nrec, const int* const* rec_cells) {
+    seidart_trace::Range nvtx("seidart_batch_create");
     if (!out || nmodels < 1 || !doms || !srcs || !models) return berr(SEIDART_ERR_ARG, "bad arguments");
     *out = nullptr;
     SeidartBatch* b = new SeidartBatch();
@@ -1094,6 +1096,7 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
 // the batch itself, keep the fastest, then reset every model to zero state
 // and step 1 (set the initial fields afterwards).
 int seidart_batch_autotune(SeidartBatch* b, int trial_steps, int* best_variant, int* best_bps) {
+    seidart_trace::Range nvtx("seidart_batch_autotune");
     if (!b || trial_steps < 1 || trial_steps > b->time_steps) return berr(SEIDART_ERR_ARG, "bad trial length");
     double best = 1e300;
     cudaEvent_t e0, e1;
@@ -1162,6 +1165,7 @@ int seidart_batch_set_config(SeidartBatch* b, int variant, int bps) {
 // chunk of steps, each launch captured once in a CUDA graph and replayed
 // (the device step counter lets one graph serve any starting step).
 int seidart_batch_step(SeidartBatch* b, int nsteps, int chunk) {
+    seidart_trace::Range nvtx("seidart_batch_step");
     if (!b || nsteps < 0 || b->steps_done + nsteps > b->time_steps) return berr(SEIDART_ERR_ARG, "steps exceed time_steps");
     if (chunk < 1) chunk = nsteps > 0 ? nsteps : 1;
     b->launches = 0;

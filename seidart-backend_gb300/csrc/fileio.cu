@@ -53,6 +53,7 @@
 #include <vector>
 
 #include "../../include/seidart_gpu.h"
+#include "trace.h"
 
 // solver internals used here (defined in solver.cu)
 extern "C" int seidart_solver_snapshot_source(SeidartSolver* s, int slot, void** dev, int* is_complex,
@@ -606,6 +607,7 @@ int seidart_run_files(const char* dir_c, int family, int precision, const Seidar
 int seidart_run_files_pw(const char* dir_c, int family, int precision, const SeidartDomain* dom,
                          const SeidartSource* src, int density_code, const char* source_type, int single_output,
                          int write_snapshots, const SeidartPlaneWave* pw_in) {
+    seidart_trace::Range nvtx("seidart_run_files");
     if (!dom || !src) return io_err(SEIDART_ERR_ARG, "NULL domain/source");
     const std::string dir = dir_c && *dir_c ? dir_c : ".";
     const std::string stype = source_type ? trim(source_type) : std::string("ac");

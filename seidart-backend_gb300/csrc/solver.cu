@@ -28,6 +28,7 @@
 
 #include "../../include/seidart_gpu.h"
 #include "host_pool.h"
+#include "trace.h"
 #include "kernels.h"
 
 // plane-wave set-up (planewave.cu)
@@ -858,6 +859,7 @@ int seidart_solver_create(SeidartSolver** out, int family, int precision, const 
     if (!out || !dom || !src || !model) return set_err(SEIDART_ERR_ARG, "NULL argument");
     *out = nullptr;
     SetupTrace trace;
+    seidart_trace::Range nvtx("seidart_solver_create");
     Layout L;
     if (!layout_of(family, &L)) return set_err(SEIDART_ERR_ARG, "unknown solver family %d", family);
     if (precision != SEIDART_FP64 && precision != SEIDART_FP32 && precision != SEIDART_FP64_FAST)
@@ -1216,6 +1218,7 @@ int seidart_solver_get_memory(SeidartSolver* s, double* const* mem) {
 }
 
 int seidart_solver_step(SeidartSolver* s, int nsteps) {
+    seidart_trace::Range nvtx("seidart_solver_step");
     if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
     if (nsteps < 0 || s->steps_done + nsteps > s->src.time_steps)
         return set_err(SEIDART_ERR_ARG, "stepping %d steps from step %d exceeds time_steps = %d", nsteps,
@@ -1242,6 +1245,7 @@ int seidart_solver_step(SeidartSolver* s, int nsteps) {
 }
 
 int seidart_solver_sync(SeidartSolver* s) {
+    seidart_trace::Range nvtx("seidart_solver_sync");
     if (!s) return set_err(SEIDART_ERR_ARG, "NULL solver");
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     CUDA_TRY(cudaGetLastError());
