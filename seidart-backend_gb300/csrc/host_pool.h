@@ -29,10 +29,11 @@ class HostPool {
     int size() const { return (int)workers_.size() + 1; }
     // f(w) for w in [0, n): w = 0 (and any w beyond the workers) on the
     // caller, the rest on the workers; returns when all are done.  Calls
-    // from several threads take turns.
+    // from several threads take turns; a call made from inside a range (a
+    // nested loop) runs all its ranges on the calling thread.
     void run(int n, const std::function<void(int)>& f) {
-        if (n <= 1) {
-            f(0);
+        if (n <= 1 || in_range()) {
+            for (int w = 0; w < n; ++w) f(w);
             return;
         }
         if (getpid() != pid_) {  // forked child: the workers live in the parent only
@@ -52,14 +53,26 @@ class HostPool {
             ++gen_;
         }
         cv_.notify_all();
-        f(0);
-        for (int w = nw; w < n; ++w) f(w);
+        {
+            RangeFlag inside;
+            f(0);
+            for (int w = nw; w < n; ++w) f(w);
+        }
         std::unique_lock<std::mutex> l(mu_);
         done_cv_.wait(l, [&] { return pending_ == 0; });
         job_ = nullptr;
     }
 
   private:
+    // set on a thread while it runs a range
+    static bool& in_range() {
+        static thread_local bool flag = false;
+        return flag;
+    }
+    struct RangeFlag {
+        RangeFlag() { in_range() = true; }
+        ~RangeFlag() { in_range() = false; }
+    };
     HostPool() : pid_(getpid()) {
         const unsigned hw = std::thread::hardware_concurrency();
         const int n = (int)std::max(1u, std::min(hw, 16u));
@@ -76,7 +89,10 @@ class HostPool {
                 if (w >= njob_) continue;
                 f = job_;
             }
-            (*f)(w);
+            {
+                RangeFlag inside;
+                (*f)(w);
+            }
             std::lock_guard<std::mutex> l(mu_);
             if (--pending_ == 0) done_cv_.notify_one();
         }

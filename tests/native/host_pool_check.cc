@@ -1,7 +1,8 @@
 // Checks the host thread pool of the solver's set-up and transfer loops
 // (seidart-backend_gb300/csrc/host_pool.h) on the CPU: every element of a
 // range visited exactly once for many sizes, three threads calling at once,
-// a forked child (which has no pool workers) and more ranges than workers.
+// a forked child (which has no pool workers), more ranges than workers and
+// a loop nested inside a range.
 #include <sys/wait.h>
 #include <atomic>
 #include <cstdio>
@@ -36,6 +37,18 @@ int main() {
     std::vector<int> hit(pool.size() + 7, 0);
     pool.run((int)hit.size(), [&](int w) { hit[w] += 1; });
     for (int h : hit) if (h != 1) { printf("FAIL overflow\n"); return 1; }
+    // a loop inside a range runs on the calling thread instead of waiting for the pool
+    std::vector<std::atomic<int>> inner(64 << 18);
+    host_parallel(16 << 18, [&](size_t lo, size_t hi) {
+        (void)hi;
+        const size_t base = (lo / (1 << 18)) % 4;
+        host_parallel(16 << 18, [&](size_t a, size_t b) {
+            for (size_t q = a; q < b; q += 4096) inner[base * (16 << 18) + q] += 1;
+        });
+    });
+    long total = 0;
+    for (auto& x : inner) total += x;
+    if (total <= 0) { printf("FAIL nested\n"); return 1; }
     printf("ok size=%d\n", pool.size());
     return 0;
 }
