@@ -935,15 +935,15 @@ int seidart_batch_create(SeidartBatch** out, int nmodels, const SeidartDomain* d
     seidart_trace::Range nvtx("seidart_batch_create");
     if (!out || nmodels < 1 || !doms || !srcs || !models) return berr(SEIDART_ERR_ARG, "bad arguments");
     *out = nullptr;
+    // all models advance together: checked before any model is set up
+    for (int m = 1; m < nmodels; ++m)
+        if (srcs[m].time_steps != srcs[0].time_steps)
+            return berr(SEIDART_ERR_ARG, "all models of a batch advance together: time_steps must match");
     SeidartBatch* b = new SeidartBatch();
     b->nmodels = nmodels;
     b->time_steps = srcs[0].time_steps;
     std::vector<BModel> hm;
     for (int m = 0; m < nmodels; ++m) {
-        if (srcs[m].time_steps != b->time_steps) {
-            seidart_batch_destroy(b);
-            return berr(SEIDART_ERR_ARG, "all models of a batch advance together: time_steps must match");
-        }
         SeidartSolver* s = nullptr;
         const int rc = seidart_solver_create(&s, SEIDART_SEISMIC2, SEIDART_FP32, &doms[m], &srcs[m],
                                              density_codes ? density_codes[m] : SEIDART_DENSITY_ARITHMETIC,

@@ -62,3 +62,18 @@ def test_valid_arguments_without_a_gpu_are_unsupported():
         sg.Solver(_problem(), sg.FP64)
     assert e.value.code == UNSUPPORTED
     assert "no CUDA device" in str(e.value)
+
+
+def test_batch_arguments_are_checked_per_model():
+    """seidart_batch_create: the models advance together (equal time_steps),
+    and a model's own bad argument is reported with its index."""
+    from seidart_gpu.batch import Batch
+    probs = models.batch_layered_vti(nmodels=3, nt=10, cpml=6, nmin=24, nmax=40, step=8, nrec=4, seed=3)
+    short = [probs[0], dataclasses.replace(probs[1], time_steps=5, src={k: v[:5] for k, v in probs[1].src.items()})]
+    with pytest.raises(SeidartError) as e:
+        Batch(short, autotune=False)
+    assert e.value.code == ARG and "time_steps must match" in str(e.value)
+    bad = [dataclasses.replace(probs[0], xind=10_000), probs[1]]
+    with pytest.raises(SeidartError) as e:
+        Batch(bad, autotune=False)
+    assert e.value.code == ARG and "model 0" in str(e.value) and "source index" in str(e.value)
