@@ -77,3 +77,19 @@ def test_batch_arguments_are_checked_per_model():
     with pytest.raises(SeidartError) as e:
         Batch(bad, autotune=False)
     assert e.value.code == ARG and "model 0" in str(e.value) and "source index" in str(e.value)
+
+
+def test_gradient_arguments_are_checked():
+    """seidart_fwi_create_family refuses a shot whose source lies outside
+    the grid; the Python layer refuses families without an adjoint before
+    it reaches the ABI (which would answer SEIDART_ERR_UNSUPPORTED)."""
+    from seidart_gpu.fwi import Fwi, Shot
+    p = _problem()
+    shot = Shot(xind=12, zind=6, srcz=np.asarray(p.src["z"], dtype=np.float64))
+    far = Shot(xind=10_000, zind=6, srcz=shot.srcz)
+    with pytest.raises(SeidartError) as e:
+        Fwi(p, [shot, far])
+    assert e.value.code == ARG and "shot source outside the grid" in str(e.value)
+    p3 = models.seismic3_layers(n=16, cpml=4, nt=10, nlayers=2, nrec_side=2, rec_z=2, src_z=4)
+    with pytest.raises(ValueError, match="seismic2 and electromag2"):
+        Fwi(p3, [Shot(xind=8, zind=4, srcz=np.asarray(p3.src["z"], dtype=np.float64))])
